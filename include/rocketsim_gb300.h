@@ -1,0 +1,291 @@
+/*
+ * rocketsim_gb300.h -- C ABI of the GB300-native RocketSim arena tick.
+ *
+ * Every entry point replaces one call of RocketSim's C++ Arena/Car/Ball API
+ * (ZealanL/RocketSim v2.2); the reference interface each one stands in for is
+ * cited beside it as <file>:<line> relative to the RocketSim source tree.
+ *
+ * Rules of the ABI:
+ *  - plain C types only (no torch, no C++ classes); all structs are POD with
+ *    explicit padding so that ctypes / cgo / JNI mirrors can be written by hand;
+ *  - every function returns int status (RSG_OK == 0) or a pointer (NULL on
+ *    error); the message of the last error on the calling thread is returned
+ *    by rsg_get_last_error().  Nothing throws across this boundary
+ *    (the reference throws std::runtime_error, src/Framework.h:67-72);
+ *  - state crosses the boundary in Unreal units (uu) exactly like
+ *    Car::GetState / Car::SetState (src/Sim/Car/Car.cpp:10-36) and
+ *    Ball::GetState / Ball::SetState (src/Sim/Ball/Ball.cpp:27-51); inside the
+ *    library it is kept in Bullet units (uu / 50) as the reference does;
+ *  - a batch owns many independent arenas that live in device memory as
+ *    structure-of-arrays; calls on one batch must be externally serialised
+ *    (the reference arena is not thread-safe either, src/Sim/Arena/Arena.h).
+ */
+#ifndef ROCKETSIM_GB300_H
+#define ROCKETSIM_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSG_OK 0
+#define RSG_ERR_ARG (-1)        /* bad argument (index, size, null pointer) */
+#define RSG_ERR_STATE (-2)      /* call not valid in the current state */
+#define RSG_ERR_CUDA (-3)       /* a CUDA runtime call failed */
+#define RSG_ERR_MESH (-4)       /* collision mesh file rejected */
+#define RSG_ERR_DEVICE (-5)     /* a kernel reported a device-side error flag */
+
+/* Game modes: src/Sim/GameMode.h:6-17. Only SOCCAR and THE_VOID are simulated. */
+#define RSG_GAMEMODE_SOCCAR 0
+#define RSG_GAMEMODE_THE_VOID 5
+
+/* Teams: src/Sim/Car/Car.h:130-133 */
+#define RSG_TEAM_BLUE 0
+#define RSG_TEAM_ORANGE 1
+
+/* Car hitbox presets: src/Sim/Car/CarConfig/CarConfig.cpp:94-100 */
+#define RSG_CAR_OCTANE 0
+#define RSG_CAR_DOMINUS 1
+#define RSG_CAR_PLANK 2
+#define RSG_CAR_BREAKOUT 3
+#define RSG_CAR_HYBRID 4
+#define RSG_CAR_MERC 5
+
+#define RSG_MAX_CARS_PER_ARENA 8
+#define RSG_NUM_BOOST_PADS 34
+
+typedef struct rsg_vec3 {
+    float x, y, z;
+} rsg_vec3;
+
+/* Column vectors forward/right/up, src/Math/MathTypes/MathTypes.h:169-176 */
+typedef struct rsg_rotmat {
+    rsg_vec3 forward, right, up;
+} rsg_rotmat;
+
+/* CarControls, src/Sim/CarControls.h:7-33 (bools stored as uint8_t) */
+typedef struct rsg_car_controls {
+    float throttle, steer, pitch, yaw, roll;
+    uint8_t jump, boost, handbrake, _pad0;
+} rsg_car_controls;
+
+/* BallHitInfo, src/Sim/BallHitInfo/BallHitInfo.h:9-26 */
+typedef struct rsg_ball_hit_info {
+    uint8_t is_valid;
+    uint8_t _pad0[3];
+    rsg_vec3 relative_pos_on_ball;
+    rsg_vec3 ball_pos;
+    rsg_vec3 extra_hit_vel;
+    uint64_t tick_count_when_hit;
+    uint64_t tick_count_when_extra_impulse_applied;
+} rsg_ball_hit_info;
+
+/* CarState, src/Sim/Car/Car.h:17-120, field for field */
+typedef struct rsg_car_state {
+    rsg_vec3 pos;
+    rsg_rotmat rot_mat;
+    rsg_vec3 vel;
+    rsg_vec3 ang_vel;
+    uint64_t tick_count_since_update;
+    uint8_t is_on_ground;
+    uint8_t wheels_with_contact[4];
+    uint8_t has_jumped;
+    uint8_t has_double_jumped;
+    uint8_t has_flipped;
+    rsg_vec3 flip_rel_torque;
+    float jump_time;
+    float flip_time;
+    uint8_t is_flipping;
+    uint8_t is_jumping;
+    uint8_t _pad0[2];
+    float air_time;
+    float air_time_since_jump;
+    float boost;
+    float time_since_boosted;
+    uint8_t is_boosting;
+    uint8_t _pad1[3];
+    float boosting_time;
+    uint8_t is_supersonic;
+    uint8_t _pad2[3];
+    float supersonic_time;
+    float handbrake_val;
+    uint8_t is_auto_flipping;
+    uint8_t _pad3[3];
+    float auto_flip_timer;
+    float auto_flip_torque_scale;
+    uint8_t world_contact_has_contact;
+    uint8_t _pad4[3];
+    rsg_vec3 world_contact_normal;
+    uint32_t car_contact_other_car_id;
+    float car_contact_cooldown_timer;
+    uint8_t is_demoed;
+    uint8_t _pad5[3];
+    float demo_respawn_timer;
+    rsg_ball_hit_info ball_hit_info;
+    rsg_car_controls last_controls;
+} rsg_car_state;
+
+/* BallState, src/Sim/Ball/Ball.h:18-57 (soccar part) */
+typedef struct rsg_ball_state {
+    rsg_vec3 pos;
+    rsg_rotmat rot_mat;
+    rsg_vec3 vel;
+    rsg_vec3 ang_vel;
+    uint64_t tick_count_since_update;
+} rsg_ball_state;
+
+/* BoostPadState, src/Sim/BoostPad/BoostPad.h:23-35 */
+typedef struct rsg_pad_state {
+    uint8_t is_active;
+    uint8_t _pad0[3];
+    float cooldown;
+    uint32_t cur_locked_car_id;
+    uint32_t prev_locked_car_id;
+} rsg_pad_state;
+
+/* WheelPairConfig / CarConfig, src/Sim/Car/CarConfig/CarConfig.h:5-40 */
+typedef struct rsg_wheel_pair_config {
+    float wheel_radius;
+    float suspension_rest_length;
+    rsg_vec3 connection_point_offset;
+} rsg_wheel_pair_config;
+
+typedef struct rsg_car_config {
+    rsg_vec3 hitbox_size;
+    rsg_vec3 hitbox_pos_offset;
+    rsg_wheel_pair_config front_wheels;
+    rsg_wheel_pair_config back_wheels;
+    uint8_t three_wheels;
+    uint8_t _pad0[3];
+    float dodge_deadzone;
+} rsg_car_config;
+
+/* Event kinds delivered to the callbacks after a step completes. */
+#define RSG_EVENT_GOAL 1      /* a = scoring team (Arena.cpp:748-752) */
+#define RSG_EVENT_BUMP 2      /* a = bumper id, b = victim id, flag = is_demo (Arena.cpp:399-400) */
+#define RSG_EVENT_BALL_HIT 3  /* a = car id; the reference records it in CarState::ballHitInfo (Ball.cpp:251-259) */
+
+typedef struct rsg_event {
+    uint32_t arena;
+    uint32_t kind;
+    uint64_t tick;
+    uint32_t a;
+    uint32_t b;
+    uint32_t flag;
+    uint32_t _pad0;
+} rsg_event;
+
+typedef struct rsg_batch rsg_batch;
+
+/* Arena::GoalScoreEventFn (src/Sim/Arena/Arena.h:24) and CarBumpEventFn (Arena.h:25)
+ * become one event callback each; they run on the host after the step's device work. */
+typedef void (*rsg_goal_fn)(rsg_batch* batch, uint32_t arena, int scoring_team, void* user);
+typedef void (*rsg_bump_fn)(rsg_batch* batch, uint32_t arena, uint32_t bumper_id, uint32_t victim_id,
+                            int is_demo, void* user);
+typedef void (*rsg_ball_hit_fn)(rsg_batch* batch, uint32_t arena, uint32_t car_id, uint64_t tick, void* user);
+
+/* ---- lifecycle ------------------------------------------------------------ */
+
+/* RocketSim::InitFromMem (src/RocketSim.h:27-32, src/RocketSim.cpp:98-185):
+ * loads .cmf collision meshes (src/CollisionMeshFile/CollisionMeshFile.cpp:11-61)
+ * for one game mode and builds the shared BVH used by every batch.
+ * Idempotent per game mode like the reference (RocketSim.cpp:100-105). */
+int rsg_init_from_mem(int game_mode, const uint8_t* const* mesh_files, const uint64_t* mesh_sizes,
+                      int n_files);
+
+/* Message of the last failing call on this thread (replaces RS_ERR_CLOSE). */
+int rsg_get_last_error(char* buf, uint64_t buf_len);
+
+/* Car preset lookup, CAR_CONFIG_* constants (CarConfig.cpp:94-100). */
+int rsg_get_car_config_preset(int preset, rsg_car_config* out);
+
+/* Arena::Create (src/Sim/Arena/Arena.h:111, Arena.cpp:416-544), batched:
+ * n_arenas independent arenas of one game mode, each holding up to
+ * max_cars_per_arena cars.  tick_rate must be 15..120 (Arena.cpp:419).
+ * Allocates all device memory of the batch. */
+rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate);
+void rsg_batch_destroy(rsg_batch* batch);
+int rsg_batch_num_arenas(const rsg_batch* batch, uint32_t* out);
+
+/* ---- cars ----------------------------------------------------------------- */
+
+/* Arena::AddCar (Arena.h:71, Arena.cpp:50-62).  The car is placed with
+ * Car::Respawn's state (Car.cpp:43-56) at respawn location `respawn_index`
+ * (0..3); the reference draws that index from a time-seeded RNG, so callers
+ * that need reproducibility pass it explicitly (or -1 for index 0). */
+int rsg_add_car(rsg_batch* batch, uint32_t arena, int team, const rsg_car_config* config,
+                int respawn_index, uint32_t* out_car_id);
+/* Arena::RemoveCar(id) (Arena.h:74-80, Arena.cpp:80-94) */
+int rsg_remove_car(rsg_batch* batch, uint32_t arena, uint32_t car_id);
+/* Arena::GetCars (Arena.h:66): ids in the order per-car updates run. */
+int rsg_get_car_ids(const rsg_batch* batch, uint32_t arena, uint32_t* out_ids, uint32_t cap, uint32_t* out_n);
+/* The reference iterates its cars in std::unordered_set<Car*> order
+ * (Arena.h:35, Arena.cpp:706,720), which depends on heap addresses.  This sets
+ * the per-car update order explicitly (a permutation of the arena's car ids). */
+int rsg_set_car_update_order(rsg_batch* batch, uint32_t arena, const uint32_t* ids, uint32_t n);
+
+/* Writing Car::controls (Car.h:149); the reference has no setter. */
+int rsg_set_car_controls(rsg_batch* batch, uint32_t arena, uint32_t car_id, const rsg_car_controls* controls);
+/* Controls of every car slot of every arena from host memory, layout [arena][slot]
+ * with max_cars_per_arena slots per arena (slot order == rsg_get_car_ids order). */
+int rsg_set_controls_all(rsg_batch* batch, const rsg_car_controls* controls, uint64_t count);
+
+/* Car::GetState / Car::SetState (Car.cpp:10-36) */
+int rsg_get_car_state(rsg_batch* batch, uint32_t arena, uint32_t car_id, rsg_car_state* out);
+int rsg_set_car_state(rsg_batch* batch, uint32_t arena, uint32_t car_id, const rsg_car_state* state);
+/* Car::Demolish (Car.cpp:38-41) */
+int rsg_demolish_car(rsg_batch* batch, uint32_t arena, uint32_t car_id, float respawn_delay);
+
+/* ---- ball, pads, arena ---------------------------------------------------- */
+
+/* Ball::GetState / Ball::SetState (Ball.cpp:27-51) */
+int rsg_get_ball_state(rsg_batch* batch, uint32_t arena, rsg_ball_state* out);
+int rsg_set_ball_state(rsg_batch* batch, uint32_t arena, const rsg_ball_state* state);
+/* BoostPad::GetState / SetState (BoostPad.h:44-45); pad order of Arena.cpp:514-531 */
+int rsg_get_pad_state(rsg_batch* batch, uint32_t arena, uint32_t pad, rsg_pad_state* out);
+int rsg_set_pad_state(rsg_batch* batch, uint32_t arena, uint32_t pad, const rsg_pad_state* state);
+/* BoostPadConfig of pad `pad` (BoostPad.h:14-18) */
+int rsg_get_pad_config(const rsg_batch* batch, uint32_t pad, rsg_vec3* pos, int* is_big);
+/* Arena::tickCount (Arena.h:64) */
+int rsg_get_tick_count(rsg_batch* batch, uint32_t arena, uint64_t* out);
+int rsg_set_tick_count(rsg_batch* batch, uint32_t arena, uint64_t tick_count);
+/* Arena::IsBallScored (Arena.cpp:893-927) */
+int rsg_is_ball_scored(rsg_batch* batch, uint32_t arena, int* out);
+
+/* Bulk state transfer of the whole batch to / from host memory.  Car arrays are
+ * [arena][slot] with max_cars_per_arena slots; empty slots are left untouched
+ * on get and ignored on set.  Pads are [arena][34]. */
+int rsg_get_all_states(rsg_batch* batch, rsg_car_state* cars, rsg_ball_state* balls, rsg_pad_state* pads);
+int rsg_set_all_states(rsg_batch* batch, const rsg_car_state* cars, const rsg_ball_state* balls,
+                       const rsg_pad_state* pads);
+
+/* ---- stepping ------------------------------------------------------------- */
+
+/* Arena::Step(ticks) (Arena.h:132, Arena.cpp:689-756) for every arena of the
+ * batch.  Synchronous: returns after the device work is done and the event
+ * callbacks have run. */
+int rsg_step(rsg_batch* batch, int ticks);
+
+/* Asynchronous variant on the batch's own stream for callers that keep
+ * inputs resident in device memory: d_controls (device pointer, may be NULL
+ * to keep the current controls) holds [ticks][arena][slot] controls.  Events
+ * are queued on the device and delivered by the next rsg_sync(). */
+int rsg_step_async(rsg_batch* batch, const rsg_car_controls* d_controls, int ticks);
+int rsg_sync(rsg_batch* batch);
+/* CUDA stream (cudaStream_t) the batch launches on, as void*. */
+void* rsg_batch_stream(rsg_batch* batch);
+
+/* Arena::SetGoalScoreCallback / SetCarBumpCallback (Arena.h:98-108), and a
+ * ball-hit callback the reference does not have (it only records the hit in
+ * CarState::ballHitInfo, Ball.cpp:251-259). */
+int rsg_set_goal_callback(rsg_batch* batch, rsg_goal_fn fn, void* user);
+int rsg_set_bump_callback(rsg_batch* batch, rsg_bump_fn fn, void* user);
+int rsg_set_ball_hit_callback(rsg_batch* batch, rsg_ball_hit_fn fn, void* user);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ROCKETSIM_GB300_H */

@@ -1,0 +1,362 @@
+// ref_driver.cpp -- test-only C shim over the reference RocketSim library.
+//
+// This file is ORACLE infrastructure: it is compiled (by oracle/Makefile) only
+// where the reference source tree is present, linked against the reference's
+// own sources built unmodified, and loaded only by tests/ to pin the CPU
+// restatement (oracle/rs_oracle.cpp) and to write the golden fixtures under
+// tests/golden/.  Nothing in the product links or loads it.
+//
+// It converts between the POD mirrors of include/rocketsim_gb300.h and the
+// reference's CarState / BallState / BoostPadState (src/Sim/Car/Car.h:17-120,
+// src/Sim/Ball/Ball.h:18-57, src/Sim/BoostPad/BoostPad.h:23-35).
+
+#include "RocketSim.h"
+#include "../include/rocketsim_gb300.h"
+
+#include <cstring>
+#include <vector>
+
+using namespace RocketSim;
+
+namespace {
+
+struct RefEvent {
+    uint32_t kind;
+    uint64_t tick;
+    uint32_t a, b, flag;
+};
+
+struct RefArena {
+    Arena* arena = nullptr;
+    std::vector<RefEvent> events;
+};
+
+Vec V(const rsg_vec3& v) { return Vec(v.x, v.y, v.z); }
+rsg_vec3 P(const Vec& v) { return rsg_vec3{v.x, v.y, v.z}; }
+
+RotMat RM(const rsg_rotmat& m) { return RotMat(V(m.forward), V(m.right), V(m.up)); }
+rsg_rotmat PM(const RotMat& m) { return rsg_rotmat{P(m.forward), P(m.right), P(m.up)}; }
+
+CarControls CC(const rsg_car_controls& c) {
+    CarControls r;
+    r.throttle = c.throttle; r.steer = c.steer; r.pitch = c.pitch; r.yaw = c.yaw; r.roll = c.roll;
+    r.jump = c.jump != 0; r.boost = c.boost != 0; r.handbrake = c.handbrake != 0;
+    return r;
+}
+rsg_car_controls PC(const CarControls& c) {
+    rsg_car_controls r{};
+    r.throttle = c.throttle; r.steer = c.steer; r.pitch = c.pitch; r.yaw = c.yaw; r.roll = c.roll;
+    r.jump = c.jump; r.boost = c.boost; r.handbrake = c.handbrake;
+    return r;
+}
+
+void CarToPod(const CarState& s, rsg_car_state* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->pos = P(s.pos); o->rot_mat = PM(s.rotMat); o->vel = P(s.vel); o->ang_vel = P(s.angVel);
+    o->tick_count_since_update = s.tickCountSinceUpdate;
+    o->is_on_ground = s.isOnGround;
+    for (int i = 0; i < 4; i++) o->wheels_with_contact[i] = s.wheelsWithContact[i];
+    o->has_jumped = s.hasJumped; o->has_double_jumped = s.hasDoubleJumped; o->has_flipped = s.hasFlipped;
+    o->flip_rel_torque = P(s.flipRelTorque);
+    o->jump_time = s.jumpTime; o->flip_time = s.flipTime;
+    o->is_flipping = s.isFlipping; o->is_jumping = s.isJumping;
+    o->air_time = s.airTime; o->air_time_since_jump = s.airTimeSinceJump;
+    o->boost = s.boost; o->time_since_boosted = s.timeSinceBoosted;
+    o->is_boosting = s.isBoosting; o->boosting_time = s.boostingTime;
+    o->is_supersonic = s.isSupersonic; o->supersonic_time = s.supersonicTime;
+    o->handbrake_val = s.handbrakeVal;
+    o->is_auto_flipping = s.isAutoFlipping; o->auto_flip_timer = s.autoFlipTimer;
+    o->auto_flip_torque_scale = s.autoFlipTorqueScale;
+    o->world_contact_has_contact = s.worldContact.hasContact;
+    o->world_contact_normal = P(s.worldContact.contactNormal);
+    o->car_contact_other_car_id = s.carContact.otherCarID;
+    o->car_contact_cooldown_timer = s.carContact.cooldownTimer;
+    o->is_demoed = s.isDemoed; o->demo_respawn_timer = s.demoRespawnTimer;
+    o->ball_hit_info.is_valid = s.ballHitInfo.isValid;
+    o->ball_hit_info.relative_pos_on_ball = P(s.ballHitInfo.relativePosOnBall);
+    o->ball_hit_info.ball_pos = P(s.ballHitInfo.ballPos);
+    o->ball_hit_info.extra_hit_vel = P(s.ballHitInfo.extraHitVel);
+    o->ball_hit_info.tick_count_when_hit = s.ballHitInfo.tickCountWhenHit;
+    o->ball_hit_info.tick_count_when_extra_impulse_applied = s.ballHitInfo.tickCountWhenExtraImpulseApplied;
+    o->last_controls = PC(s.lastControls);
+}
+
+CarState PodToCar(const rsg_car_state* o) {
+    CarState s;
+    s.pos = V(o->pos); s.rotMat = RM(o->rot_mat); s.vel = V(o->vel); s.angVel = V(o->ang_vel);
+    s.tickCountSinceUpdate = o->tick_count_since_update;
+    s.isOnGround = o->is_on_ground;
+    for (int i = 0; i < 4; i++) s.wheelsWithContact[i] = o->wheels_with_contact[i];
+    s.hasJumped = o->has_jumped; s.hasDoubleJumped = o->has_double_jumped; s.hasFlipped = o->has_flipped;
+    s.flipRelTorque = V(o->flip_rel_torque);
+    s.jumpTime = o->jump_time; s.flipTime = o->flip_time;
+    s.isFlipping = o->is_flipping; s.isJumping = o->is_jumping;
+    s.airTime = o->air_time; s.airTimeSinceJump = o->air_time_since_jump;
+    s.boost = o->boost; s.timeSinceBoosted = o->time_since_boosted;
+    s.isBoosting = o->is_boosting; s.boostingTime = o->boosting_time;
+    s.isSupersonic = o->is_supersonic; s.supersonicTime = o->supersonic_time;
+    s.handbrakeVal = o->handbrake_val;
+    s.isAutoFlipping = o->is_auto_flipping; s.autoFlipTimer = o->auto_flip_timer;
+    s.autoFlipTorqueScale = o->auto_flip_torque_scale;
+    s.worldContact.hasContact = o->world_contact_has_contact;
+    s.worldContact.contactNormal = V(o->world_contact_normal);
+    s.carContact.otherCarID = o->car_contact_other_car_id;
+    s.carContact.cooldownTimer = o->car_contact_cooldown_timer;
+    s.isDemoed = o->is_demoed; s.demoRespawnTimer = o->demo_respawn_timer;
+    s.ballHitInfo.isValid = o->ball_hit_info.is_valid;
+    s.ballHitInfo.relativePosOnBall = V(o->ball_hit_info.relative_pos_on_ball);
+    s.ballHitInfo.ballPos = V(o->ball_hit_info.ball_pos);
+    s.ballHitInfo.extraHitVel = V(o->ball_hit_info.extra_hit_vel);
+    s.ballHitInfo.tickCountWhenHit = o->ball_hit_info.tick_count_when_hit;
+    s.ballHitInfo.tickCountWhenExtraImpulseApplied = o->ball_hit_info.tick_count_when_extra_impulse_applied;
+    s.lastControls = CC(o->last_controls);
+    return s;
+}
+
+const CarConfig* PRESETS[6] = {&CAR_CONFIG_OCTANE, &CAR_CONFIG_DOMINUS, &CAR_CONFIG_PLANK,
+                               &CAR_CONFIG_BREAKOUT, &CAR_CONFIG_HYBRID, &CAR_CONFIG_MERC};
+
+void OnGoal(Arena* arena, Team team, void* user) {
+    RefArena* ra = (RefArena*)user;
+    ra->events.push_back({RSG_EVENT_GOAL, arena->tickCount, (uint32_t)team, 0, 0});
+}
+
+void OnBump(Arena* arena, Car* bumper, Car* victim, bool isDemo, void* user) {
+    RefArena* ra = (RefArena*)user;
+    ra->events.push_back({RSG_EVENT_BUMP, arena->tickCount, bumper->id, victim->id, (uint32_t)isDemo});
+}
+
+Car* FindCar(RefArena* ra, uint32_t id) {
+    for (Car* c : ra->arena->GetCars())
+        if (c->id == id) return c;
+    return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsref_init(const uint8_t* cmf, uint64_t len) {
+    std::map<GameMode, std::vector<FileData>> m;
+    FileData fd(cmf, cmf + len);
+    m[GameMode::SOCCAR].push_back(fd);
+    try {
+        RocketSim::InitFromMem(m, true);
+    } catch (...) {
+        return -1;
+    }
+    return 0;
+}
+
+void* rsref_arena_create(int game_mode, float tick_rate) {
+    RefArena* ra = new RefArena();
+    try {
+        ra->arena = Arena::Create((GameMode)game_mode, ArenaConfig(), tick_rate);
+    } catch (...) {
+        delete ra;
+        return nullptr;
+    }
+    ra->arena->SetCarBumpCallback(OnBump, ra);
+    if ((GameMode)game_mode != GameMode::THE_VOID) ra->arena->SetGoalScoreCallback(OnGoal, ra);
+    return ra;
+}
+
+void rsref_arena_destroy(void* h) {
+    RefArena* ra = (RefArena*)h;
+    delete ra->arena;
+    delete ra;
+}
+
+int rsref_preset(int preset, rsg_car_config* out) {
+    if (preset < 0 || preset > 5) return -1;
+    const CarConfig& c = *PRESETS[preset];
+    std::memset(out, 0, sizeof(*out));
+    out->hitbox_size = P(c.hitboxSize);
+    out->hitbox_pos_offset = P(c.hitboxPosOffset);
+    out->front_wheels.wheel_radius = c.frontWheels.wheelRadius;
+    out->front_wheels.suspension_rest_length = c.frontWheels.suspensionRestLength;
+    out->front_wheels.connection_point_offset = P(c.frontWheels.connectionPointOffset);
+    out->back_wheels.wheel_radius = c.backWheels.wheelRadius;
+    out->back_wheels.suspension_rest_length = c.backWheels.suspensionRestLength;
+    out->back_wheels.connection_point_offset = P(c.backWheels.connectionPointOffset);
+    out->three_wheels = c.threeWheels;
+    out->dodge_deadzone = c.dodgeDeadzone;
+    return 0;
+}
+
+uint32_t rsref_add_car(void* h, int team, int preset) {
+    RefArena* ra = (RefArena*)h;
+    Car* c = ra->arena->AddCar((Team)team, *PRESETS[preset]);
+    return c->id;
+}
+
+int rsref_car_order(void* h, uint32_t* out, uint32_t cap) {
+    RefArena* ra = (RefArena*)h;
+    uint32_t n = 0;
+    for (Car* c : ra->arena->GetCars()) {
+        if (n < cap) out[n] = c->id;
+        n++;
+    }
+    return (int)n;
+}
+
+int rsref_set_controls(void* h, uint32_t id, const rsg_car_controls* c) {
+    Car* car = FindCar((RefArena*)h, id);
+    if (!car) return -1;
+    car->controls = CC(*c);
+    return 0;
+}
+
+int rsref_get_car(void* h, uint32_t id, rsg_car_state* out) {
+    Car* car = FindCar((RefArena*)h, id);
+    if (!car) return -1;
+    CarToPod(car->GetState(), out);
+    return 0;
+}
+
+int rsref_set_car(void* h, uint32_t id, const rsg_car_state* s) {
+    Car* car = FindCar((RefArena*)h, id);
+    if (!car) return -1;
+    car->SetState(PodToCar(s));
+    return 0;
+}
+
+int rsref_get_ball(void* h, rsg_ball_state* out) {
+    RefArena* ra = (RefArena*)h;
+    BallState s = ra->arena->ball->GetState();
+    std::memset(out, 0, sizeof(*out));
+    out->pos = P(s.pos); out->rot_mat = PM(s.rotMat); out->vel = P(s.vel); out->ang_vel = P(s.angVel);
+    out->tick_count_since_update = s.tickCountSinceUpdate;
+    return 0;
+}
+
+int rsref_set_ball(void* h, const rsg_ball_state* in) {
+    RefArena* ra = (RefArena*)h;
+    BallState s;
+    s.pos = V(in->pos); s.rotMat = RM(in->rot_mat); s.vel = V(in->vel); s.angVel = V(in->ang_vel);
+    ra->arena->ball->SetState(s);
+    return 0;
+}
+
+int rsref_num_pads(void* h) { return (int)((RefArena*)h)->arena->GetBoostPads().size(); }
+
+int rsref_get_pad(void* h, int i, rsg_pad_state* out) {
+    RefArena* ra = (RefArena*)h;
+    auto& pads = ra->arena->GetBoostPads();
+    if (i < 0 || i >= (int)pads.size()) return -1;
+    BoostPadState s = pads[i]->GetState();
+    std::memset(out, 0, sizeof(*out));
+    out->is_active = s.isActive;
+    out->cooldown = s.cooldown;
+    out->cur_locked_car_id = s.curLockedCar ? s.curLockedCar->id : 0;
+    out->prev_locked_car_id = s.prevLockedCarID;
+    return 0;
+}
+
+int rsref_set_pad(void* h, int i, const rsg_pad_state* in) {
+    RefArena* ra = (RefArena*)h;
+    auto& pads = ra->arena->GetBoostPads();
+    if (i < 0 || i >= (int)pads.size()) return -1;
+    BoostPadState s;
+    s.isActive = in->is_active;
+    s.cooldown = in->cooldown;
+    s.curLockedCar = nullptr;
+    s.prevLockedCarID = in->prev_locked_car_id;
+    pads[i]->SetState(s);
+    return 0;
+}
+
+int rsref_pad_config(void* h, int i, rsg_vec3* pos, int* is_big) {
+    RefArena* ra = (RefArena*)h;
+    auto& pads = ra->arena->GetBoostPads();
+    if (i < 0 || i >= (int)pads.size()) return -1;
+    *pos = P(pads[i]->config.pos);
+    *is_big = pads[i]->config.isBig;
+    return 0;
+}
+
+uint64_t rsref_get_tick(void* h) { return ((RefArena*)h)->arena->tickCount; }
+void rsref_set_tick(void* h, uint64_t t) { ((RefArena*)h)->arena->tickCount = t; }
+
+int rsref_step(void* h, int ticks) {
+    RefArena* ra = (RefArena*)h;
+    try {
+        ra->arena->Step(ticks);
+    } catch (...) {
+        return -1;
+    }
+    return 0;
+}
+
+int rsref_is_scored(void* h) { return ((RefArena*)h)->arena->IsBallScored() ? 1 : 0; }
+
+// Events recorded since the last call: each event is 5 uint64 words
+// (kind, tick, a, b, flag).  Returns the number of events copied.
+int rsref_pop_events(void* h, uint64_t* out, int cap) {
+    RefArena* ra = (RefArena*)h;
+    int n = 0;
+    for (auto& e : ra->events) {
+        if (n >= cap) break;
+        out[n * 5 + 0] = e.kind;
+        out[n * 5 + 1] = e.tick;
+        out[n * 5 + 2] = e.a;
+        out[n * 5 + 3] = e.b;
+        out[n * 5 + 4] = e.flag;
+        n++;
+    }
+    ra->events.clear();
+    return n;
+}
+
+// Wheel internals of btVehicleRL (src/Sim/btVehicleRL/btVehicleRL.h:9-27) that
+// persist across ticks but are not part of CarState: steer angle and extra
+// pushback per wheel.  Used by tests to check the restatement's hidden state.
+int rsref_get_wheel_internals(void* h, uint32_t id, float* out8) {
+    Car* car = FindCar((RefArena*)h, id);
+    if (!car) return -1;
+    for (int i = 0; i < 4; i++) {
+        out8[i] = car->_bulletVehicle.m_wheelInfo[i].m_steerAngle;
+        out8[4 + i] = car->_bulletVehicle.m_wheelInfo[i].m_extraPushback;
+    }
+    return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+// Per-wheel raycast/friction internals for debugging the restatement:
+// 16 floats per wheel: contact point(3) normal(3) susp_len rel_vel clipped_inv
+// impulse(3) lat long hard_point.z ground(0 none,1 static,2 dynamic)
+int rsref_wheel_debug(void* h, uint32_t id, float* out) {
+    Car* car = FindCar((RefArena*)h, id);
+    if (!car) return -1;
+    for (int i = 0; i < 4; i++) {
+        auto& w = car->_bulletVehicle.m_wheelInfo[i];
+        float* o = out + i * 16;
+        o[0] = w.m_raycastInfo.m_contactPointWS.x(); o[1] = w.m_raycastInfo.m_contactPointWS.y(); o[2] = w.m_raycastInfo.m_contactPointWS.z();
+        o[3] = w.m_raycastInfo.m_contactNormalWS.x(); o[4] = w.m_raycastInfo.m_contactNormalWS.y(); o[5] = w.m_raycastInfo.m_contactNormalWS.z();
+        o[6] = w.m_raycastInfo.m_suspensionLength; o[7] = w.m_suspensionRelativeVelocity; o[8] = w.m_clippedInvContactDotSuspension;
+        o[9] = w.m_impulse.x(); o[10] = w.m_impulse.y(); o[11] = w.m_impulse.z();
+        o[12] = w.m_latFriction; o[13] = w.m_longFriction; o[14] = w.m_raycastInfo.m_hardPointWS.z();
+        const btCollisionObject* g = (const btCollisionObject*)w.m_raycastInfo.m_groundObject;
+        o[15] = g ? (g->isStaticObject() ? 1.f : 2.f) : 0.f;
+    }
+    return 0;
+}
+}
+
+extern "C" {
+// Rigid-body internals of a car: inv inertia local(3), inv mass, inv inertia world(9)
+int rsref_body_debug(void* h, uint32_t id, float* out) {
+    Car* car = FindCar((RefArena*)h, id);
+    if (!car) return -1;
+    btVector3 il = car->_rigidBody.getInvInertiaDiagLocal();
+    out[0] = il.x(); out[1] = il.y(); out[2] = il.z();
+    out[3] = car->_rigidBody.getInvMass();
+    const btMatrix3x3& m = car->_rigidBody.getInvInertiaTensorWorld();
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) out[4 + i * 3 + j] = m[i][j];
+    btVector3 he = car->_childHitboxShape.getHalfExtentsWithoutMargin();
+    out[13] = he.x(); out[14] = he.y(); out[15] = he.z(); out[16] = car->_childHitboxShape.getMargin();
+    return 0;
+}
+}
