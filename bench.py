@@ -1,0 +1,427 @@
+"""Benchmark of the batched arena tick: 2v2 arena-ticks/s on one GB300.
+
+Workload (the batched, uniform 2v2 configuration): 4096 independent arenas on
+the seeded procedural soccar mesh, each with 4 Octane cars (2v2) and a ball.
+Per-arena seeded starting states: car positions uniform in the field,
+velocities of uniform direction with |v| <= 2300 uu/s, a quarter of the cars
+airborne with uniformly random orientation; ball |v| <= 6000 uu/s.  Controls
+follow the 2v2 input process (analog inputs uniform in [-1, 1], jump / boost /
+handbrake Bernoulli(0.3), each car re-drawing after a hold of 2..60 ticks).
+
+A step is 8 ticks of every arena.  ``value`` runs each step as one
+rsg_step_async launch whose per-tick controls are already in device memory;
+``e2e`` runs it through the synchronous host API: controls from pinned host
+memory (rsg_set_controls_all), rsg_step(8), and every car, ball and pad state
+read back to host memory (rsg_get_all_states).  The L2 cache is flushed
+(a 256 MiB device write) between timed steps.
+
+``--impl reference`` times the CPU implementation of the same tick on the
+host cores instead: the reference library built from its sources when it is
+loadable on this machine, else the CPU restatement of it (oracle/).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+TICKS_PER_STEP = 8
+CARS = 4
+WORKLOAD = "batched uniform 2v2: 4096 arenas x (4 Octane + ball), procedural soccar mesh seed 0, 8 ticks/step"
+
+
+# ---------------------------------------------------------------- workload
+def initial_states(n_arenas: int, seed: int, car_dt, ball_dt):
+    rng = np.random.default_rng(seed)
+    A = n_arenas
+    cars = np.zeros(A * CARS, car_dt)
+    n = A * CARS
+    air = rng.random(n) < 0.25
+    x, y = rng.uniform(-3500, 3500, n), rng.uniform(-4500, 4500, n)
+    z = np.where(air, rng.uniform(200, 1800, n), 17.0)
+    # orientation: yaw only on the ground, a uniformly random quaternion in the air
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    yaw = rng.uniform(0, 2 * np.pi, n)
+    q[~air] = np.stack([np.cos(yaw / 2), np.zeros(n), np.zeros(n), np.sin(yaw / 2)], 1)[~air]
+    w, qx, qy, qz = q.T
+    R = np.stack([
+        np.stack([1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - w * qz), 2 * (qx * qz + w * qy)], 1),
+        np.stack([2 * (qx * qy + w * qz), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - w * qx)], 1),
+        np.stack([2 * (qx * qz - w * qy), 2 * (qy * qz + w * qx), 1 - 2 * (qx * qx + qy * qy)], 1),
+    ], 1)  # [n, row, col]
+    d = rng.normal(size=(n, 3))
+    d[~air, 2] = 0
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    v = d * rng.uniform(0, 2300, (n, 1))
+    for k, c in enumerate("xyz"):
+        cars["pos"][c] = (x, y, z)[k]
+        cars["vel"][c] = v[:, k]
+        cars["ang_vel"][c] = np.where(air, rng.uniform(-3, 3, n), 0.0)
+        for j, col in enumerate(("forward", "right", "up")):
+            cars["rot_mat"][col][c] = R[:, k, j]
+    cars["is_on_ground"] = (~air).astype(np.uint8)
+    cars["boost"] = rng.uniform(0, 100, n)
+    cars["ball_hit_info"]["tick_count_when_hit"] = np.uint64(2 ** 64 - 1)
+    cars["ball_hit_info"]["tick_count_when_extra_impulse_applied"] = np.uint64(2 ** 64 - 1)
+    balls = np.zeros(A, ball_dt)
+    d = rng.normal(size=(A, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    bv = d * rng.uniform(0, 6000, (A, 1))
+    for k, c in enumerate("xyz"):
+        balls["pos"][c] = (rng.uniform(-3000, 3000, A), rng.uniform(-4000, 4000, A), rng.uniform(93.15, 1800, A))[k]
+        balls["vel"][c] = bv[:, k]
+        balls["ang_vel"][c] = rng.uniform(-2, 2, A)
+    for j, col in enumerate(("forward", "right", "up")):
+        for k, c in enumerate("xyz"):
+            balls["rot_mat"][col][c] = 1.0 if j == k else 0.0
+    return cars, balls
+
+
+class ControlProcess:
+    """Per-car hold-and-redraw input process, vectorised over all cars."""
+
+    def __init__(self, n_cars: int, seed: int, ctl_dt):
+        self.rng = np.random.default_rng(seed)
+        self.n = n_cars
+        self.dt = ctl_dt
+        self.cur = np.zeros(n_cars, ctl_dt)
+        self.hold = np.zeros(n_cars, np.int64)
+
+    def tick(self) -> np.ndarray:
+        redraw = self.hold <= 0
+        m = int(redraw.sum())
+        if m:
+            for name in ("throttle", "steer", "pitch", "yaw", "roll"):
+                self.cur[name][redraw] = self.rng.uniform(-1, 1, m)
+            for name in ("jump", "boost", "handbrake"):
+                self.cur[name][redraw] = (self.rng.random(m) < 0.3).astype(np.uint8)
+            self.hold[redraw] = self.rng.integers(2, 61, m)
+        self.hold -= 1
+        return self.cur.copy()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU timing
+def cpu_kind() -> str:
+    """'ref' when the reference library built from its sources loads here, else 'oracle'."""
+    from oracle.pyoracle import REF_SO, load
+    if os.path.exists(REF_SO):
+        try:
+            load("ref")
+            return "ref"
+        except OSError:
+            pass
+    return "oracle"
+
+
+def cpu_ticks_per_second(threads: int, seconds: float, seed: int = 7, kind: str | None = None):
+    """Arena-ticks/s of the CPU implementation: `threads` threads, each stepping its
+    own 2v2 arena with the same input process for about `seconds`.  Controls are
+    generated before the timed region and fed 240 ticks per native call, which
+    releases the GIL, so the threads run in parallel."""
+    from oracle.pyoracle import SimArena, CarState as OCarState, BallState as OBallState, CarControls as OCtl
+    from rocketsim_gb300.arena_mesh import arena_cmf
+    kind = kind or cpu_kind()
+    cmf = arena_cmf(0)
+    cars, balls = initial_states(max(threads, 1), seed, np.dtype(OCarState), np.dtype(OBallState))
+    ctl_dt = np.dtype(OCtl)
+    chunk, nchunks = 240, 8
+    counts = [0] * threads
+    stop = threading.Event()
+    arenas, buffers = [], []
+    for t in range(threads):
+        a = SimArena(kind, cmf)
+        ids = [a.add_car(i % 2, 0) for i in range(CARS)]
+        for i, cid in enumerate(ids):
+            a.set_car(cid, OCarState.from_buffer_copy(cars[t * CARS + i].tobytes()))
+        a.set_ball(OBallState.from_buffer_copy(balls[t].tobytes()))
+        proc = ControlProcess(CARS, seed + 100 + t, ctl_dt)
+        buffers.append(np.ascontiguousarray(np.stack([proc.tick() for _ in range(chunk * nchunks)])))
+        arenas.append(a)
+    a.run(buffers[0].ctypes.data, CARS, 1)  # load / first-tick work outside the timed region
+    for a, buf in zip(arenas[1:], buffers[1:]):
+        a.run(buf.ctypes.data, CARS, 1)
+
+    def worker(t):
+        a, buf = arenas[t], buffers[t]
+        n, k = 0, 0
+        while not stop.is_set():
+            a.run(buf[k * chunk:(k + 1) * chunk].ctypes.data, CARS, chunk)
+            n += chunk
+            k = (k + 1) % nchunks
+        counts[t] = n
+
+    ths = [threading.Thread(target=worker, args=(t,)) for t in range(threads)]
+    t0 = time.perf_counter()
+    for th in ths:
+        th.start()
+    time.sleep(seconds)
+    stop.set()
+    for th in ths:
+        th.join()
+    el = time.perf_counter() - t0
+    for a in arenas:
+        a.close()
+    return sum(counts) / el, sum(counts), el, kind
+
+
+def reference_kind_note(kind: str) -> str:
+    if kind == "ref":
+        return "the reference RocketSim built from its own sources (oracle/_ref)"
+    return ("CPU restatement of the reference tick (oracle/; its SSE build reproduces the reference bit for bit "
+            "on x86, the reference library itself is not built on this host)")
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args, rank: int, world: int):
+    import torch
+    import rocketsim_gb300 as rsg
+    from rocketsim_gb300 import abi
+    from rocketsim_gb300.arena_mesh import arena_cmf
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    rsg.init_from_mem([arena_cmf(0)])
+    A = args.arenas
+    batch = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, A, CARS, 120.0)
+    for a in range(A):
+        for i in range(CARS):
+            batch.add_car(a, i % 2, abi.CAR_OCTANE, 0)
+    cars, balls = initial_states(A, 1234 + rank, rsg.CAR_STATE_DTYPE, rsg.BALL_STATE_DTYPE)
+    batch.set_all_states(cars, balls, None)
+
+    nsteps = args.warmup + args.steps
+    proc = ControlProcess(A * CARS, 99 + rank, rsg.CONTROLS_DTYPE)
+    seq = np.stack([np.stack([proc.tick() for _ in range(TICKS_PER_STEP)]) for _ in range(nsteps)])
+    d_seq = torch.from_numpy(seq.view(np.uint8).reshape(nsteps, -1).copy()).to(f"cuda:{dev}")
+    step_bytes = d_seq.shape[1]
+    stream = torch.cuda.ExternalStream(batch.stream(), device=f"cuda:{dev}")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- value: device-resident inputs, one launch per step
+    for s in range(args.warmup):
+        batch.step_async(d_seq[s].data_ptr(), TICKS_PER_STEP)
+    batch.sync()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(dev)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            ev[k][0].record(stream)
+            batch.step_async(d_seq[args.warmup + k].data_ptr(), TICKS_PER_STEP)
+            ev[k][1].record(stream)
+    batch.sync()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    times_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(times_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    arena_ticks = A * TICKS_PER_STEP * args.steps * world
+    value = arena_ticks / (total_ms / 1e3)
+    flags = batch.device_flags()
+
+    # ---- e2e: host buffers through the synchronous API
+    h_ctl = torch.empty(A * CARS * rsg.CONTROLS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    ctl_np = h_ctl.numpy().view(rsg.CONTROLS_DTYPE)
+    out_cars = np.zeros(A * CARS, rsg.CAR_STATE_DTYPE)
+    out_balls = np.zeros(A, rsg.BALL_STATE_DTYPE)
+    out_pads = np.zeros(A * abi.NUM_BOOST_PADS, rsg.PAD_STATE_DTYPE)
+    e2e_steps = max(3, min(args.steps, 20))
+    for s in range(2):
+        ctl_np[:] = seq[s, 0]
+        batch.set_controls_all(ctl_np)
+        batch.step(TICKS_PER_STEP)
+        batch.get_all_states(out_cars, out_balls, out_pads)
+    barrier()
+    e2e_time = 0.0
+    for s in range(e2e_steps):
+        ctl_np[:] = seq[(s + 2) % nsteps, 0]
+        flush.fill_(s & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        batch.set_controls_all(ctl_np)
+        batch.step(TICKS_PER_STEP)
+        batch.get_all_states(out_cars, out_balls, out_pads)
+        e2e_time += time.perf_counter() - t0
+    e2e_value = A * TICKS_PER_STEP * e2e_steps * world / e2e_time
+    h2d = ctl_np.nbytes
+    d2h = out_cars.nbytes + out_balls.nbytes + out_pads.nbytes
+    batch.close()
+
+    # roofline of the tick kernel: algorithmic bytes per launch
+    state_rt = 1548  # minimal 2v2 arena state read + written once per launch (bytes)
+    ctl_per_tick = CARS * 24
+    alg_bytes = A * (state_rt + ctl_per_tick * TICKS_PER_STEP)
+    avg_launch_s = (sum(times_ms) / len(times_ms)) / 1e3
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / avg_launch_s / 1e9
+    traffic = None
+    tp = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        per_arena = tj.get("rsg_tick_kernel_bytes_per_arena_launch")
+        if per_arena:
+            traffic = per_arena * A
+    return {
+        "value": value, "ms_per_step": total_ms / args.steps, "e2e": {
+            "value": e2e_value, "unit": "arena-ticks/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+        "clocks": clk, "gpu_launches": args.steps, "step_bytes_controls": step_bytes,
+        "warn_flags_any": int(np.bitwise_or.reduce(flags)) if flags.size else 0,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--arenas", type=int, default=4096)
+    ap.add_argument("--cpu-seconds", type=float, default=1.5)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    threads = os.cpu_count() or 1
+    config = {"workload": WORKLOAD, "arenas": args.arenas, "cars_per_arena": CARS, "ticks_per_step": TICKS_PER_STEP,
+              "tick_rate": 120, "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # each step: every host thread steps its own 2v2 arena for a bounded time
+        vals = []
+        kind = cpu_kind()
+        for s in range(args.warmup + args.steps):
+            v, n, el, kind = cpu_ticks_per_second(threads, 0.25 if s < args.warmup else 0.5, kind=kind)
+            if s >= args.warmup:
+                vals.append(v)
+        value = statistics.mean(vals)
+        line = {"impl": "reference", "metric": "2v2 arena-ticks/s", "value": value, "unit": "arena-ticks/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 500.0,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": value, "unit": "arena-ticks/s", "cores": threads,
+                                 "kind": "reference" if kind == "ref" else "port",
+                                 "sample": f"{threads} threads x one 2v2 arena each, 0.5 s per step; "
+                                           + reference_kind_note(kind)},
+                "e2e": {"value": value, "unit": "arena-ticks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}"))
+    r = run_gpu(args, rank, world)
+    if rank != 0:
+        return
+    single, _, _, kind = cpu_ticks_per_second(1, args.cpu_seconds)
+    allc, n, el, _ = cpu_ticks_per_second(threads, args.cpu_seconds)
+    line = {
+        "metric": "2v2 arena-ticks/s", "value": r["value"], "unit": "arena-ticks/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+        "e2e": r["e2e"], "roofline": r["roofline"],
+        "cpu_baseline": {"value": allc, "unit": "arena-ticks/s", "cores": threads,
+                         "kind": "reference" if kind == "ref" else "port", "single_thread": single,
+                         "sample": f"{threads} threads x one 2v2 arena each for {args.cpu_seconds:.1f} s "
+                                   f"({n} arena-ticks) plus 1 thread for {args.cpu_seconds:.1f} s; "
+                                   + reference_kind_note(kind)},
+        "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "device_warn_flags": r["warn_flags_any"],
+        "host": platform.machine(),
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -284,6 +284,13 @@ int rsg_set_goal_callback(rsg_batch* batch, rsg_goal_fn fn, void* user);
 int rsg_set_bump_callback(rsg_batch* batch, rsg_bump_fn fn, void* user);
 int rsg_set_ball_hit_callback(rsg_batch* batch, rsg_ball_hit_fn fn, void* user);
 
+/* Device flags of every arena after the last step ([n_arenas] words).  Bits 0-7
+ * are capacity overflows (the step also returns RSG_ERR_DEVICE); bit 8 marks a
+ * box contact deeper than GJK resolves and bit 9 overlapping car boxes, two
+ * contact kinds the restated narrow phase does not produce yet.  No counterpart
+ * in the reference. */
+int rsg_get_device_flags(rsg_batch* batch, uint32_t* out);
+
 #ifdef __cplusplus
 }
 #endif

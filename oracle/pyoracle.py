@@ -122,6 +122,7 @@ def _setup(lib, prefix: str):
     lib[p + "get_tick"].argtypes = [C.c_void_p]
     lib[p + "set_tick"].argtypes = [C.c_void_p, C.c_uint64]
     lib[p + "step"].argtypes = [C.c_void_p, C.c_int]
+    lib[p + "run"].argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
     lib[p + "is_scored"].argtypes = [C.c_void_p]
     lib[p + "pop_events"].argtypes = [C.c_void_p, C.POINTER(C.c_uint64), C.c_int]
     lib[p + "get_wheel_internals"].argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_float)]
@@ -243,6 +244,10 @@ class SimArena:
 
     def step(self, ticks: int = 1):
         assert self.lib[self.p + "step"](self.h, ticks) == 0
+
+    def run(self, controls_ptr: int, ncars: int, ticks: int):
+        """Steps `ticks` ticks with controls [ticks][ncars] (AddCar order) from native memory."""
+        assert self.lib[self.p + "run"](self.h, controls_ptr, ncars, ticks) == 0
 
     def is_scored(self) -> bool:
         return bool(self.lib[self.p + "is_scored"](self.h))

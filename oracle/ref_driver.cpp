@@ -288,6 +288,28 @@ int rsref_step(void* h, int ticks) {
     return 0;
 }
 
+// Steps `ticks` ticks, setting the controls of car k (in AddCar order, ids 1..n) from
+// controls[t * ncars + k] before tick t.  Used to time the reference without a
+// per-tick round trip through the caller's language.
+int rsref_run(void* h, const rsg_car_controls* controls, int ncars, int ticks) {
+    RefArena* ra = (RefArena*)h;
+    std::vector<Car*> cars;
+    for (int k = 0; k < ncars; k++) {
+        Car* c = FindCar(ra, (uint32_t)(k + 1));
+        if (!c) return -1;
+        cars.push_back(c);
+    }
+    try {
+        for (int t = 0; t < ticks; t++) {
+            for (int k = 0; k < ncars; k++) cars[k]->controls = CC(controls[(size_t)t * ncars + k]);
+            ra->arena->Step(1);
+        }
+    } catch (...) {
+        return -1;
+    }
+    return 0;
+}
+
 int rsref_is_scored(void* h) { return ((RefArena*)h)->arena->IsBallScored() ? 1 : 0; }
 
 // Events recorded since the last call: each event is 5 uint64 words

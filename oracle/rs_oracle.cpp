@@ -728,6 +728,7 @@ struct Arena {
     float ball_radius = RL::BALL_COLLISION_RADIUS_SOCCAR * UU_TO_BT;
     float ball_threshold;
     V3 ball_cache;
+    uint64_t ball_ticks = 0;    // BallState::tickCountSinceUpdate
     std::vector<Car> cars;      // AddCar order
     std::vector<int> order;     // per-car update order (indices into cars)
     Pad pads[34];
@@ -775,10 +776,12 @@ void set_ball_state(Arena& a, const rsg_ball_state& s) {  // Ball::SetState (Bal
         if (b.act != DISABLE_DEACTIVATION && b.act != DISABLE_SIMULATION) b.act = ACTIVE_TAG;
     }
     a.ball_cache = V3(0, 0, 0);
+    a.ball_ticks = 0;
 }
 
 void get_ball_state(Arena& a, rsg_ball_state& s) {
     std::memset(&s, 0, sizeof(s));
+    s.tick_count_since_update = a.ball_ticks;
     s.pos = P(a.ball.xf.o * BT_TO_UU);
     s.rot_mat = m3_to_rot(a.ball.xf.b);
     s.vel = P(a.ball.lin_vel * BT_TO_UU);
@@ -1562,7 +1565,9 @@ void update_double_jump_or_flip(Car& c, float dt, bool pressed, float fwd_speed)
 // Angle::FromRotMat (MathTypes.cpp:62-71) -> btMatrix3x3::getEulerYPR roll only
 float roll_from_rot(const rsg_rotmat& r) {
     M3 m = rot_to_m3(r);
-    float pitch = std::asin(-m.r[2].x);
+    float sp = -m.r[2].x;  // btAsin clamps to [-1, 1] (LinearMath/btScalar.h:510-516)
+    sp = sp < -1.f ? -1.f : (sp > 1.f ? 1.f : sp);
+    float pitch = std::asin(sp);
     float roll = std::atan2(m.r[2].y, m.r[2].z);
     if (std::fabs(pitch) == HALF_PI_F) {
         if (roll > 0) roll -= PI_F;
@@ -3290,6 +3295,7 @@ void arena_step(Arena& a) {  // Arena::Step (Arena.cpp:689-756)
         if (len2(w) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) w = normalized(w) * RL::BALL_MAX_ANG_SPEED;
         ball.lin_vel = v;
         ball.ang_vel = w;
+        a.ball_ticks++;
     }
     if (a.has_arena && ball_scored(a)) {
         uint32_t team = (-(a.ball.xf.o.y) < 0) ? 0 : 1;  // RS_TEAM_FROM_Y(-y)
@@ -3458,6 +3464,18 @@ void rsora_set_tick(void* h, uint64_t t) { ((Arena*)h)->tick_count = t; }
 int rsora_step(void* h, int ticks) {
     Arena& a = *(Arena*)h;
     for (int i = 0; i < ticks; i++) arena_step(a);
+    return 0;
+}
+
+// Steps `ticks` ticks, setting the controls of car k (AddCar order) from
+// controls[t * ncars + k] before tick t (timing helper, no per-tick caller round trip).
+int rsora_run(void* h, const rsg_car_controls* controls, int ncars, int ticks) {
+    Arena& a = *(Arena*)h;
+    if (ncars != (int)a.cars.size()) return -1;
+    for (int t = 0; t < ticks; t++) {
+        for (int k = 0; k < ncars; k++) a.cars[k].controls = controls[(size_t)t * ncars + k];
+        arena_step(a);
+    }
     return 0;
 }
 

@@ -31,6 +31,7 @@ int rsora_pad_config(void* h, int i, rsg_vec3* pos, int* is_big);
 uint64_t rsora_get_tick(void* h);
 void rsora_set_tick(void* h, uint64_t t);
 int rsora_step(void* h, int ticks);
+int rsora_run(void* h, const rsg_car_controls* controls, int ncars, int ticks);
 int rsora_is_scored(void* h);
 int rsora_pop_events(void* h, uint64_t* out, int cap);
 int rsora_get_wheel_internals(void* h, uint32_t id, float* out8);

@@ -1,0 +1,900 @@
+// rsg_capi.cpp -- host side of the C ABI declared in include/rocketsim_gb300.h.
+//
+// A batch owns the structure-of-arrays state of many arenas in device memory
+// (layout in rsg_layout.h) and one CUDA stream.  Host-side bookkeeping that the
+// reference keeps in its Arena object (car ids, update order, the last id
+// handed out) is mirrored here so that id lookups need no device round trip.
+// Everything that changes during a tick lives only on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/rocketsim_gb300.h"
+#include "rsg_consts.cuh"
+#include "rsg_kernels.h"
+#include "rsg_layout.h"
+#include "rsg_mesh.h"
+
+using namespace rsg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(RSG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define RSG_CUDA(call)                                      \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// ---------------------------------------------------------------- shared arena mesh
+struct MeshStore {
+    bool ready = false;
+    int device = -1;
+    HostMesh host;
+    float* tv = nullptr;
+    QNode* nodes = nullptr;
+    Subtree* sub = nullptr;
+    TriInfo* info = nullptr;
+    uint8_t* cells = nullptr;
+};
+std::mutex g_mesh_mutex;
+MeshStore g_soccar;
+
+DevMeshPtrs mesh_ptrs(const MeshStore& m) {
+    DevMeshPtrs p{};
+    if (!m.ready) return p;
+    p.tv = m.tv;
+    p.nodes = m.nodes;
+    p.sub = m.sub;
+    p.info = m.info;
+    p.cells = m.cells;
+    p.ntri = m.host.ntri;
+    p.nnodes = m.host.cur_node;
+    p.nsub = (int)m.host.subtrees.size();
+    p.bvh_min = m.host.bvh_min;
+    p.bvh_max = m.host.bvh_max;
+    p.quant = m.host.quant;
+    p.aabb_min = m.host.aabb_min;
+    p.aabb_max = m.host.aabb_max;
+    return p;
+}
+
+template <class T>
+int upload(T*& dst, const std::vector<T>& src, const char* what) {
+    size_t bytes = src.size() * sizeof(T);
+    if (bytes == 0) bytes = sizeof(T);
+    cudaError_t e = cudaMalloc((void**)&dst, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (!src.empty()) {
+        e = cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, what);
+    }
+    return RSG_OK;
+}
+
+// Car::_BulletSetup derived constants (src/Sim/Car/Car.cpp:195-292)
+CarCfgDev derive_config(const rsg_car_config& c) {
+    const float U = RL::UU_TO_BT;
+    CarCfgDev d;
+    std::memset(&d, 0, sizeof(d));
+    V3 size(c.hitbox_size.x, c.hitbox_size.y, c.hitbox_size.z);
+    V3 he = (size * U) / 2.f;
+    // btBoxShape: implicit dimensions keep the default 0.04 margin while setSafeMargin shrinks the
+    // margin itself (B/BulletCollision/CollisionShapes/btBoxShape.cpp:17-25, btConvexInternalShape.h:63-90)
+    float margin = 0.04f;
+    V3 implicit = he - V3(margin, margin, margin);
+    int minax = he.x < he.y ? (he.x < he.z ? 0 : 2) : (he.y < he.z ? 1 : 2);
+    float safe = 0.1f * he[minax];
+    if (safe < margin) margin = safe;
+    V3 off = V3(c.hitbox_pos_offset.x, c.hitbox_pos_offset.y, c.hitbox_pos_offset.z) * U;
+    V3 hm = implicit + V3(margin, margin, margin);
+    V3 cmin = off - hm, cmax = off + hm;
+    float lx = 2.f * hm.x, ly = 2.f * hm.y, lz = 2.f * hm.z;
+    float m = RL::CAR_MASS_BT;
+    V3 inertia(m / 12.f * (ly * ly + lz * lz), m / 12.f * (lx * lx + lz * lz), m / 12.f * (lx * lx + ly * ly));
+    V3 lhe = 0.5f * (cmax - cmin), lc = 0.5f * (cmax + cmin);
+    V3 amin = lc - lhe, amax = lc + lhe;
+    float rad = len(amax - amin) * 0.5f;
+    V3 cen = (amin + amax) * 0.5f;
+    for (int k = 0; k < 3; k++) {
+        d.he[k] = implicit[k];
+        d.off[k] = off[k];
+        d.comp_min[k] = cmin[k];
+        d.comp_max[k] = cmax[k];
+        d.inv_inertia[k] = inertia[k] != 0 ? 1.f / inertia[k] : 0.f;
+    }
+    d.margin = margin;
+    d.breaking = (rad + len(cen)) * 0.02f;
+    for (int i = 0; i < 4; i++) {
+        bool front = i < 2, left = (i % 2) != 0;
+        const rsg_wheel_pair_config& wp = front ? c.front_wheels : c.back_wheels;
+        V3 o(wp.connection_point_offset.x, wp.connection_point_offset.y, wp.connection_point_offset.z);
+        if (left) o.y *= -1;
+        o = o * U;
+        d.conn[i][0] = o.x;
+        d.conn[i][1] = o.y;
+        d.conn[i][2] = o.z;
+    }
+    d.rest[0] = (c.front_wheels.suspension_rest_length - RL::MAX_SUSPENSION_TRAVEL) * U;
+    d.rest[1] = (c.back_wheels.suspension_rest_length - RL::MAX_SUSPENSION_TRAVEL) * U;
+    d.radius[0] = c.front_wheels.wheel_radius * U;
+    d.radius[1] = c.back_wheels.wheel_radius * U;
+    d.dodge_deadzone = c.dodge_deadzone;
+    d.three_wheels = c.three_wheels ? 1 : 0;
+    return d;
+}
+
+// Car::Respawn's state (src/Sim/Car/Car.cpp:43-56) with CarState's defaults (Car.h:17-120)
+rsg_car_state respawn_state(int team, int idx, float boost) {
+    rsg_car_state s;
+    std::memset(&s, 0, sizeof(s));
+    const float xs[4] = {-2304, -2688, 2304, 2688};
+    const float ys[4] = {-4608, -4608, -4608, -4608};
+    float yaw0 = (float)(3.14159265358979323846 / 2);
+    s.pos.x = xs[idx];
+    s.pos.y = ys[idx] * (team == RSG_TEAM_BLUE ? 1 : -1);
+    s.pos.z = RL::CAR_RESPAWN_Z;
+    float yaw = (float)((double)yaw0 + (team == RSG_TEAM_BLUE ? 0 : 3.14159265358979323846));
+    M3 m = m_euler_ypr(yaw, -0.f, -0.f);
+    V3 f = m.col(0), r = m.col(1), u = m.col(2);
+    s.rot_mat.forward = {f.x, f.y, f.z};
+    s.rot_mat.right = {r.x, r.y, r.z};
+    s.rot_mat.up = {u.x, u.y, u.z};
+    s.boost = boost;
+    s.is_on_ground = 1;
+    s.ball_hit_info.tick_count_when_hit = ~0ULL;
+    s.ball_hit_info.tick_count_when_extra_impulse_applied = ~0ULL;
+    return s;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- batch
+struct DevEventHost {  // mirror of the device event record
+    uint32_t kind, tick_lo, tick_hi, a, b, flag;
+};
+static_assert(sizeof(DevEventHost) == DEV_EVENT_BYTES, "event record");
+
+struct rsg_batch {
+    int game_mode = 0;
+    int device = 0;
+    BatchBuffers buf{};
+    cudaStream_t stream = nullptr;
+    std::vector<CarCfgDev> cfgs;
+    CarCfgDev* d_cfgs = nullptr;
+    int cfg_cap = 0;
+    // host mirror of per-arena bookkeeping
+    std::vector<uint32_t> ncars, last_id;
+    std::vector<uint32_t> ids;     // [A][MC] car id by slot
+    std::vector<uint8_t> order;    // [A][MC] slot by update position
+    // staging
+    void* d_stage = nullptr;
+    size_t stage_bytes = 0;
+    std::vector<uint32_t> h_counts;
+    std::vector<DevEventHost> h_events;
+    rsg_goal_fn goal_fn = nullptr;
+    void* goal_user = nullptr;
+    rsg_bump_fn bump_fn = nullptr;
+    void* bump_user = nullptr;
+    rsg_ball_hit_fn hit_fn = nullptr;
+    void* hit_user = nullptr;
+};
+
+namespace {
+
+int ensure_stage(rsg_batch* b, size_t bytes) {
+    if (b->stage_bytes >= bytes) return RSG_OK;
+    if (b->d_stage) cudaFree(b->d_stage);
+    b->d_stage = nullptr;
+    b->stage_bytes = 0;
+    RSG_CUDA(cudaMalloc(&b->d_stage, bytes));
+    b->stage_bytes = bytes;
+    return RSG_OK;
+}
+
+int set_device(rsg_batch* b) {
+    RSG_CUDA(cudaSetDevice(b->device));
+    return RSG_OK;
+}
+
+int check_arena(const rsg_batch* b, uint32_t arena) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    if (arena >= (uint32_t)b->buf.A) return fail(RSG_ERR_ARG, "arena index out of range");
+    return RSG_OK;
+}
+
+int find_slot(const rsg_batch* b, uint32_t arena, uint32_t car_id) {
+    int MC = b->buf.MC;
+    for (uint32_t s = 0; s < b->ncars[arena]; s++)
+        if (b->ids[(size_t)arena * MC + s] == car_id) return (int)s;
+    return -1;
+}
+
+uint32_t pack_order(const rsg_batch* b, uint32_t arena) {
+    uint32_t v = 0;
+    for (uint32_t k = 0; k < b->ncars[arena]; k++) v |= (uint32_t)b->order[(size_t)arena * b->buf.MC + k] << (4 * k);
+    return v;
+}
+
+// index of an arena-scalar word in the au array
+size_t au_index(const rsg_batch* b, int field, uint32_t arena) { return (size_t)field * b->buf.A + arena; }
+
+int write_au(rsg_batch* b, int field, uint32_t arena, uint32_t v) {
+    RSG_CUDA(cudaMemcpyAsync(b->buf.au + au_index(b, field, arena), &v, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+int read_au(rsg_batch* b, int field, uint32_t arena, uint32_t* v) {
+    RSG_CUDA(cudaMemcpyAsync(v, b->buf.au + au_index(b, field, arena), 4, cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int cfg_index(rsg_batch* b, const CarCfgDev& d) {
+    for (size_t i = 0; i < b->cfgs.size(); i++)
+        if (std::memcmp(&b->cfgs[i], &d, sizeof(d)) == 0) return (int)i;
+    b->cfgs.push_back(d);
+    if ((int)b->cfgs.size() > b->cfg_cap) {
+        int cap = b->cfg_cap ? b->cfg_cap * 2 : 16;
+        CarCfgDev* nd = nullptr;
+        cudaError_t e = cudaMalloc((void**)&nd, sizeof(CarCfgDev) * cap);
+        if (e != cudaSuccess) { b->cfgs.pop_back(); return cuda_fail(e, "cudaMalloc(car configs)"); }
+        cudaStreamSynchronize(b->stream);
+        if (b->d_cfgs) cudaFree(b->d_cfgs);
+        b->d_cfgs = nd;
+        b->cfg_cap = cap;
+        b->buf.cfgs = nd;
+    }
+    cudaError_t e = cudaMemcpyAsync(b->d_cfgs, b->cfgs.data(), sizeof(CarCfgDev) * b->cfgs.size(), cudaMemcpyHostToDevice,
+                                    b->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(car configs)");
+    return (int)b->cfgs.size() - 1;
+}
+
+// Delivers queued events to the callbacks and clears the device queues.
+int drain_events(rsg_batch* b) {
+    if (!b->buf.event_mask) return RSG_OK;
+    int A = b->buf.A;
+    b->h_counts.resize(A);
+    RSG_CUDA(cudaMemcpyAsync(b->h_counts.data(), b->buf.au + au_index(b, AU_EVENTS, 0), 4 * (size_t)A,
+                             cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    bool any = false;
+    for (int a = 0; a < A; a++) any |= b->h_counts[a] != 0;
+    if (!any) return RSG_OK;
+    b->h_events.resize((size_t)A * MAX_EVENTS_PER_ARENA);
+    RSG_CUDA(cudaMemcpyAsync(b->h_events.data(), b->buf.events, sizeof(DevEventHost) * b->h_events.size(),
+                             cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_EVENTS, 0), 0, 4 * (size_t)A, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    for (int a = 0; a < A; a++) {
+        uint32_t n = b->h_counts[a];
+        if (n > (uint32_t)MAX_EVENTS_PER_ARENA) n = MAX_EVENTS_PER_ARENA;
+        for (uint32_t k = 0; k < n; k++) {
+            const DevEventHost& e = b->h_events[(size_t)a * MAX_EVENTS_PER_ARENA + k];
+            uint64_t tick = (uint64_t)e.tick_lo | ((uint64_t)e.tick_hi << 32);
+            if (e.kind == RSG_EVENT_GOAL && b->goal_fn) b->goal_fn(b, (uint32_t)a, (int)e.a, b->goal_user);
+            else if (e.kind == RSG_EVENT_BUMP && b->bump_fn) b->bump_fn(b, (uint32_t)a, e.a, e.b, (int)e.flag, b->bump_user);
+            else if (e.kind == RSG_EVENT_BALL_HIT && b->hit_fn) b->hit_fn(b, (uint32_t)a, e.a, tick, b->hit_user);
+        }
+    }
+    return RSG_OK;
+}
+
+void update_event_mask(rsg_batch* b) {
+    uint32_t m = 0;
+    if (b->goal_fn) m |= 1u << RSG_EVENT_GOAL;
+    if (b->bump_fn) m |= 1u << RSG_EVENT_BUMP;
+    if (b->hit_fn) m |= 1u << RSG_EVENT_BALL_HIT;
+    b->buf.event_mask = m;
+}
+
+// Reads the device error words; warnings (bits >= 8) are not failures.
+int check_device_errors(rsg_batch* b) {
+    int A = b->buf.A;
+    b->h_counts.resize(A);
+    RSG_CUDA(cudaMemcpyAsync(b->h_counts.data(), b->buf.au + au_index(b, AU_ERR, 0), 4 * (size_t)A, cudaMemcpyDeviceToHost,
+                             b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    for (int a = 0; a < A; a++) {
+        uint32_t e = b->h_counts[a] & 0xffu;
+        if (e) {
+            char msg[160];
+            std::snprintf(msg, sizeof(msg), "arena %d reported device error flags 0x%x (capacity overflow)", a, e);
+            return fail(RSG_ERR_DEVICE, msg);
+        }
+    }
+    return RSG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- kernels used only here
+namespace rsg {
+cudaError_t launch_add_car(const BatchBuffers& b, uint32_t arena, uint32_t slot, uint32_t id, uint32_t cfg, uint32_t flags,
+                           uint32_t cell, uint32_t ncars, uint32_t order, cudaStream_t st);
+cudaError_t launch_remove_car(const BatchBuffers& b, uint32_t arena, uint32_t slot, uint32_t ncars, uint32_t order,
+                              cudaStream_t st);
+cudaError_t launch_init_arenas(const BatchBuffers& b, uint32_t ball_cell, cudaStream_t st);
+cudaError_t launch_demolish(const BatchBuffers& b, uint32_t arena, uint32_t slot, float delay, cudaStream_t st);
+}  // namespace rsg
+
+extern "C" {
+
+int rsg_get_last_error(char* buf, uint64_t buf_len) {
+    if (!buf || buf_len == 0) return RSG_ERR_ARG;
+    std::snprintf(buf, (size_t)buf_len, "%s", g_last_error.c_str());
+    return RSG_OK;
+}
+
+int rsg_init_from_mem(int game_mode, const uint8_t* const* mesh_files, const uint64_t* mesh_sizes, int n_files) {
+    if (game_mode != RSG_GAMEMODE_SOCCAR) return fail(RSG_ERR_ARG, "only soccar meshes are loaded");
+    if (!mesh_files || !mesh_sizes || n_files <= 0) return fail(RSG_ERR_ARG, "no mesh files");
+    std::lock_guard<std::mutex> lock(g_mesh_mutex);
+    if (g_soccar.ready) return RSG_OK;  // idempotent like RocketSim::InitFromMem (RocketSim.cpp:100-105)
+    if (n_files != 1) return fail(RSG_ERR_MESH, "exactly one soccar collision mesh is supported");
+    MeshStore m;
+    std::string err;
+    if (!build_mesh(mesh_files[0], mesh_sizes[0], m.host, err)) return fail(RSG_ERR_MESH, "mesh rejected: " + err);
+    RSG_CUDA(cudaGetDevice(&m.device));
+    std::vector<float> tv(m.host.tri_verts.size() * 3);
+    for (size_t i = 0; i < m.host.tri_verts.size(); i++) {
+        tv[i * 3 + 0] = m.host.tri_verts[i].x;
+        tv[i * 3 + 1] = m.host.tri_verts[i].y;
+        tv[i * 3 + 2] = m.host.tri_verts[i].z;
+    }
+    int rc;
+    if ((rc = upload(m.tv, tv, "mesh vertices")) != RSG_OK) return rc;
+    if ((rc = upload(m.nodes, m.host.nodes, "mesh nodes")) != RSG_OK) return rc;
+    if ((rc = upload(m.sub, m.host.subtrees, "mesh subtrees")) != RSG_OK) return rc;
+    if ((rc = upload(m.info, m.host.info, "mesh edge info")) != RSG_OK) return rc;
+    if ((rc = upload(m.cells, m.host.mesh_cells, "mesh cells")) != RSG_OK) return rc;
+    m.ready = true;
+    g_soccar = std::move(m);
+    return RSG_OK;
+}
+
+int rsg_get_car_config_preset(int preset, rsg_car_config* out) {
+    if (!out || preset < 0 || preset > 5) return fail(RSG_ERR_ARG, "preset out of range");
+    const PresetData& p = PRESETS[preset];
+    std::memset(out, 0, sizeof(*out));
+    out->hitbox_size = {p.size[0], p.size[1], p.size[2]};
+    out->hitbox_pos_offset = {p.off[0], p.off[1], p.off[2]};
+    out->front_wheels.wheel_radius = p.frad;
+    out->front_wheels.suspension_rest_length = p.fsus;
+    out->front_wheels.connection_point_offset = {p.fwo[0], p.fwo[1], p.fwo[2]};
+    out->back_wheels.wheel_radius = p.brad;
+    out->back_wheels.suspension_rest_length = p.bsus;
+    out->back_wheels.connection_point_offset = {p.bwo[0], p.bwo[1], p.bwo[2]};
+    out->three_wheels = 0;
+    out->dodge_deadzone = 0.5f;
+    return RSG_OK;
+}
+
+rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate) {
+    if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_THE_VOID) {
+        fail(RSG_ERR_ARG, "game mode not supported (soccar and the void only)");
+        return nullptr;
+    }
+    if (n_arenas == 0 || n_arenas > (1u << 24)) { fail(RSG_ERR_ARG, "n_arenas out of range"); return nullptr; }
+    if (max_cars_per_arena == 0 || max_cars_per_arena > (uint32_t)MAX_CARS) {
+        fail(RSG_ERR_ARG, "max_cars_per_arena must be 1..8");
+        return nullptr;
+    }
+    if (!(tick_rate >= 15.f && tick_rate <= 120.f)) {  // Arena.cpp:419
+        fail(RSG_ERR_ARG, "tick rate must be 15..120");
+        return nullptr;
+    }
+    bool arena = game_mode == RSG_GAMEMODE_SOCCAR;
+    if (arena && !g_soccar.ready) {
+        fail(RSG_ERR_STATE, "no soccar mesh loaded (rsg_init_from_mem)");
+        return nullptr;
+    }
+    rsg_batch* b = new rsg_batch();
+    b->game_mode = game_mode;
+    cudaError_t de = cudaGetDevice(&b->device);
+    if (de != cudaSuccess) {
+        delete b;
+        cuda_fail(de, "cudaGetDevice");
+        return nullptr;
+    }
+    if (arena && g_soccar.device != b->device) {
+        delete b;
+        fail(RSG_ERR_STATE, "the mesh was loaded on another device");
+        return nullptr;
+    }
+    BatchBuffers& B = b->buf;
+    B.A = (int)n_arenas;
+    B.MC = (int)max_cars_per_arena;
+    B.has_arena = arena ? 1 : 0;
+    B.dt = 1.f / tick_rate;
+    B.mesh = mesh_ptrs(g_soccar);
+    B.grid = default_grid();
+    size_t A = n_arenas, MC = max_cars_per_arena;
+    auto alloc = [&](void** p, size_t bytes) -> bool {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) { cuda_fail(e, "cudaMalloc(batch)"); return false; }
+        cudaMemset(*p, 0, bytes);
+        return true;
+    };
+    cudaError_t se = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (se != cudaSuccess) {
+        cuda_fail(se, "cudaStreamCreateWithFlags");
+        b->stream = nullptr;
+        rsg_batch_destroy(b);
+        return nullptr;
+    }
+    bool ok = alloc((void**)&B.cf, sizeof(float) * CF_COUNT * MC * A);
+    ok = ok && alloc((void**)&B.cu, sizeof(uint32_t) * CU_COUNT * MC * A);
+    ok = ok && alloc((void**)&B.bf, sizeof(float) * BF_COUNT * A);
+    ok = ok && alloc((void**)&B.bu, sizeof(uint32_t) * BU_COUNT * A);
+    ok = ok && alloc((void**)&B.pf, sizeof(float) * PF_COUNT * NUM_PADS * A);
+    ok = ok && alloc((void**)&B.pu, sizeof(uint32_t) * PU_COUNT * NUM_PADS * A);
+    ok = ok && alloc((void**)&B.au, sizeof(uint32_t) * AU_COUNT * A);
+    ok = ok && alloc(&B.events, (size_t)DEV_EVENT_BYTES * MAX_EVENTS_PER_ARENA * A);
+    if (!ok) {
+        rsg_batch_destroy(b);
+        return nullptr;
+    }
+    b->ncars.assign(A, 0);
+    b->last_id.assign(A, 0);
+    b->ids.assign(A * MC, 0);
+    b->order.assign(A * MC, 0);
+    // ball at rest (Arena.cpp:491-496) and its broadphase proxy created before any car
+    {
+        V3 p(0, 0, RL::BALL_REST_Z * RL::UU_TO_BT);
+        float m = RL::BALL_COLLISION_RADIUS_SOCCAR * RL::UU_TO_BT + 0.08f;
+        V3 mn = p - V3(m, m, m) - V3(0.02f, 0.02f, 0.02f);
+        V3 f = (mn - B.grid.mn) / B.grid.cell;
+        int i = std::min(std::max((int)f.x, 0), B.grid.nx - 1);
+        int j = std::min(std::max((int)f.y, 0), B.grid.ny - 1);
+        int k = std::min(std::max((int)f.z, 0), B.grid.nz - 1);
+        uint32_t cell = (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16);
+        cudaError_t e = launch_init_arenas(B, cell, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) {
+            cuda_fail(e, "init arenas");
+            rsg_batch_destroy(b);
+            return nullptr;
+        }
+    }
+    return b;
+}
+
+void rsg_batch_destroy(rsg_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    BatchBuffers& B = b->buf;
+    void* ptrs[] = {B.cf, B.cu, B.bf, B.bu, B.pf, B.pu, B.au, B.events, b->d_cfgs, b->d_stage};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int rsg_batch_num_arenas(const rsg_batch* b, uint32_t* out) {
+    if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
+    *out = (uint32_t)b->buf.A;
+    return RSG_OK;
+}
+
+int rsg_add_car(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* config, int respawn_index,
+                uint32_t* out_car_id) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!config) return fail(RSG_ERR_ARG, "null car config");
+    if (team != RSG_TEAM_BLUE && team != RSG_TEAM_ORANGE) return fail(RSG_ERR_ARG, "team must be 0 or 1");
+    if (respawn_index < -1 || respawn_index > 3) return fail(RSG_ERR_ARG, "respawn index must be -1..3");
+    if (b->ncars[arena] >= (uint32_t)b->buf.MC) return fail(RSG_ERR_STATE, "arena is full (max_cars_per_arena)");
+    if ((rc = set_device(b))) return rc;
+    CarCfgDev d = derive_config(*config);
+    int ci = cfg_index(b, d);
+    if (ci < 0) return ci;
+    uint32_t slot = b->ncars[arena];
+    uint32_t id = ++b->last_id[arena];
+    size_t MC = b->buf.MC;
+    b->ids[arena * MC + slot] = id;
+    b->order[arena * MC + slot] = (uint8_t)slot;
+    b->ncars[arena] = slot + 1;
+    // broadphase proxy at the AddCar-time transform (identity): cell of the compound AABB minimum
+    V3 cmin(d.comp_min[0], d.comp_min[1], d.comp_min[2]), cmax(d.comp_max[0], d.comp_max[1], d.comp_max[2]);
+    V3 lhe = 0.5f * (cmax - cmin), lc = 0.5f * (cmax + cmin);
+    V3 mn = lc - lhe;
+    const GridSpec& g = b->buf.grid;
+    V3 f = (mn - g.mn) / g.cell;
+    int i = std::min(std::max((int)f.x, 0), g.nx - 1);
+    int j = std::min(std::max((int)f.y, 0), g.ny - 1);
+    int k = std::min(std::max((int)f.z, 0), g.nz - 1);
+    uint32_t cell = (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16);
+    uint32_t flags = F_PRESENT | (team == RSG_TEAM_ORANGE ? F_TEAM_ORANGE : 0u);
+    RSG_CUDA(launch_add_car(b->buf, arena, slot, id, (uint32_t)ci, flags, cell, slot + 1, pack_order(b, arena), b->stream));
+    rsg_car_state s = respawn_state(team, respawn_index < 0 ? 0 : respawn_index, RL::BOOST_SPAWN_AMOUNT);
+    if ((rc = ensure_stage(b, sizeof(rsg_car_state) + 8))) return rc;
+    uint32_t idx[2] = {arena, slot};
+    char* st = (char*)b->d_stage;
+    RSG_CUDA(cudaMemcpyAsync(st, &s, sizeof(s), cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(st + sizeof(s), idx, 8, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_set_cars(b->buf, (const uint32_t*)(st + sizeof(s)), 1, (const rsg_car_state*)st, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    if (out_car_id) *out_car_id = id;
+    return RSG_OK;
+}
+
+int rsg_remove_car(rsg_batch* b, uint32_t arena, uint32_t car_id) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    int slot = find_slot(b, arena, car_id);
+    if (slot < 0) return fail(RSG_ERR_ARG, "no car with that id");
+    if ((rc = set_device(b))) return rc;
+    size_t MC = b->buf.MC;
+    uint32_t n = b->ncars[arena];
+    for (uint32_t s = (uint32_t)slot; s + 1 < n; s++) b->ids[arena * MC + s] = b->ids[arena * MC + s + 1];
+    // drop the slot from the update order and renumber the slots behind it
+    std::vector<uint8_t> ord;
+    for (uint32_t k = 0; k < n; k++) {
+        uint8_t v = b->order[arena * MC + k];
+        if (v == (uint8_t)slot) continue;
+        ord.push_back(v > slot ? (uint8_t)(v - 1) : v);
+    }
+    for (size_t k = 0; k < ord.size(); k++) b->order[arena * MC + k] = ord[k];
+    b->ncars[arena] = n - 1;
+    RSG_CUDA(launch_remove_car(b->buf, arena, (uint32_t)slot, n - 1, pack_order(b, arena), b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_get_car_ids(const rsg_batch* b, uint32_t arena, uint32_t* out_ids, uint32_t cap, uint32_t* out_n) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    uint32_t n = b->ncars[arena];
+    for (uint32_t k = 0; k < n && k < cap; k++)
+        if (out_ids) out_ids[k] = b->ids[(size_t)arena * b->buf.MC + b->order[(size_t)arena * b->buf.MC + k]];
+    if (out_n) *out_n = n;
+    return RSG_OK;
+}
+
+int rsg_set_car_update_order(rsg_batch* b, uint32_t arena, const uint32_t* ids, uint32_t n) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!ids || n != b->ncars[arena]) return fail(RSG_ERR_ARG, "order must list every car of the arena once");
+    std::vector<uint8_t> ord;
+    uint32_t seen = 0;
+    for (uint32_t k = 0; k < n; k++) {
+        int s = find_slot(b, arena, ids[k]);
+        if (s < 0 || (seen >> s) & 1u) return fail(RSG_ERR_ARG, "order must list every car of the arena once");
+        seen |= 1u << s;
+        ord.push_back((uint8_t)s);
+    }
+    for (uint32_t k = 0; k < n; k++) b->order[(size_t)arena * b->buf.MC + k] = ord[k];
+    if ((rc = set_device(b))) return rc;
+    return write_au(b, AU_ORDER, arena, pack_order(b, arena));
+}
+
+int rsg_set_car_controls(rsg_batch* b, uint32_t arena, uint32_t car_id, const rsg_car_controls* c) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!c) return fail(RSG_ERR_ARG, "null controls");
+    int slot = find_slot(b, arena, car_id);
+    if (slot < 0) return fail(RSG_ERR_ARG, "no car with that id");
+    if ((rc = set_device(b))) return rc;
+    // controls of one car: five floats and three flag bits in the car's SoA columns
+    float v[5] = {c->throttle, c->steer, c->pitch, c->yaw, c->roll};
+    size_t A = b->buf.A, MC = b->buf.MC;
+    for (int k = 0; k < 5; k++)
+        RSG_CUDA(cudaMemcpyAsync(b->buf.cf + ((size_t)(CF_CTRL + k) * MC + slot) * A + arena, &v[k], 4,
+                                 cudaMemcpyHostToDevice, b->stream));
+    uint32_t* fl = b->buf.cu + ((size_t)CU_FLAGS * MC + slot) * A + arena;
+    uint32_t flags = 0;
+    RSG_CUDA(cudaMemcpyAsync(&flags, fl, 4, cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    flags &= ~(uint32_t)(F_CTRL_JUMP | F_CTRL_BOOST | F_CTRL_HB);
+    if (c->jump) flags |= F_CTRL_JUMP;
+    if (c->boost) flags |= F_CTRL_BOOST;
+    if (c->handbrake) flags |= F_CTRL_HB;
+    RSG_CUDA(cudaMemcpyAsync(fl, &flags, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_set_controls_all(rsg_batch* b, const rsg_car_controls* controls, uint64_t count) {
+    if (!b || !controls) return fail(RSG_ERR_ARG, "null argument");
+    size_t n = (size_t)b->buf.A * b->buf.MC;
+    if (count != n) return fail(RSG_ERR_ARG, "controls count must be n_arenas * max_cars_per_arena");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    if ((rc = ensure_stage(b, n * sizeof(rsg_car_controls)))) return rc;
+    RSG_CUDA(cudaMemcpyAsync(b->d_stage, controls, n * sizeof(rsg_car_controls), cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_set_controls(b->buf, (const rsg_car_controls*)b->d_stage, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_get_car_state(rsg_batch* b, uint32_t arena, uint32_t car_id, rsg_car_state* out) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    int slot = find_slot(b, arena, car_id);
+    if (slot < 0) return fail(RSG_ERR_ARG, "no car with that id");
+    if ((rc = set_device(b))) return rc;
+    if ((rc = ensure_stage(b, sizeof(rsg_car_state) + 8))) return rc;
+    uint32_t idx[2] = {arena, (uint32_t)slot};
+    char* st = (char*)b->d_stage;
+    RSG_CUDA(cudaMemcpyAsync(st + sizeof(rsg_car_state), idx, 8, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_get_cars(b->buf, (const uint32_t*)(st + sizeof(rsg_car_state)), 1, (rsg_car_state*)st, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(out, st, sizeof(rsg_car_state), cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_set_car_state(rsg_batch* b, uint32_t arena, uint32_t car_id, const rsg_car_state* in) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!in) return fail(RSG_ERR_ARG, "null state");
+    int slot = find_slot(b, arena, car_id);
+    if (slot < 0) return fail(RSG_ERR_ARG, "no car with that id");
+    if ((rc = set_device(b))) return rc;
+    if ((rc = ensure_stage(b, sizeof(rsg_car_state) + 8))) return rc;
+    uint32_t idx[2] = {arena, (uint32_t)slot};
+    char* st = (char*)b->d_stage;
+    RSG_CUDA(cudaMemcpyAsync(st, in, sizeof(rsg_car_state), cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(st + sizeof(rsg_car_state), idx, 8, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_set_cars(b->buf, (const uint32_t*)(st + sizeof(rsg_car_state)), 1, (const rsg_car_state*)st, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_demolish_car(rsg_batch* b, uint32_t arena, uint32_t car_id, float respawn_delay) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    int slot = find_slot(b, arena, car_id);
+    if (slot < 0) return fail(RSG_ERR_ARG, "no car with that id");
+    if ((rc = set_device(b))) return rc;
+    RSG_CUDA(launch_demolish(b->buf, arena, (uint32_t)slot, respawn_delay, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_get_ball_state(rsg_batch* b, uint32_t arena, rsg_ball_state* out) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    if ((rc = set_device(b))) return rc;
+    if ((rc = ensure_stage(b, sizeof(rsg_ball_state) + 8))) return rc;
+    char* st = (char*)b->d_stage;
+    RSG_CUDA(cudaMemcpyAsync(st + sizeof(rsg_ball_state), &arena, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_get_balls(b->buf, (const uint32_t*)(st + sizeof(rsg_ball_state)), 1, (rsg_ball_state*)st, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(out, st, sizeof(rsg_ball_state), cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_set_ball_state(rsg_batch* b, uint32_t arena, const rsg_ball_state* in) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!in) return fail(RSG_ERR_ARG, "null state");
+    if ((rc = set_device(b))) return rc;
+    if ((rc = ensure_stage(b, sizeof(rsg_ball_state) + 8))) return rc;
+    char* st = (char*)b->d_stage;
+    RSG_CUDA(cudaMemcpyAsync(st, in, sizeof(rsg_ball_state), cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(st + sizeof(rsg_ball_state), &arena, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_set_balls(b->buf, (const uint32_t*)(st + sizeof(rsg_ball_state)), 1, (const rsg_ball_state*)st,
+                              b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_get_pad_state(rsg_batch* b, uint32_t arena, uint32_t pad, rsg_pad_state* out) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!out || pad >= (uint32_t)NUM_PADS) return fail(RSG_ERR_ARG, "pad index out of range");
+    if (!b->buf.has_arena) return fail(RSG_ERR_STATE, "this game mode has no boost pads");
+    if ((rc = set_device(b))) return rc;
+    size_t bytes = sizeof(rsg_pad_state) * NUM_PADS;
+    if ((rc = ensure_stage(b, bytes + 8))) return rc;
+    char* st = (char*)b->d_stage;
+    RSG_CUDA(cudaMemcpyAsync(st + bytes, &arena, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_get_pads(b->buf, (const uint32_t*)(st + bytes), 1, (rsg_pad_state*)st, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(out, st + sizeof(rsg_pad_state) * pad, sizeof(rsg_pad_state), cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_set_pad_state(rsg_batch* b, uint32_t arena, uint32_t pad, const rsg_pad_state* in) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!in || pad >= (uint32_t)NUM_PADS) return fail(RSG_ERR_ARG, "pad index out of range");
+    if (!b->buf.has_arena) return fail(RSG_ERR_STATE, "this game mode has no boost pads");
+    if ((rc = set_device(b))) return rc;
+    size_t A = b->buf.A;
+    uint32_t active = in->is_active ? 1u : 0u, zero = 0;
+    RSG_CUDA(cudaMemcpyAsync(b->buf.pu + ((size_t)PU_ACTIVE * NUM_PADS + pad) * A + arena, &active, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(b->buf.pf + ((size_t)PF_COOLDOWN * NUM_PADS + pad) * A + arena, &in->cooldown, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(b->buf.pu + ((size_t)PU_CUR_LOCKED * NUM_PADS + pad) * A + arena, &zero, 4, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(b->buf.pu + ((size_t)PU_PREV_LOCKED * NUM_PADS + pad) * A + arena, &in->prev_locked_car_id, 4,
+                             cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_get_pad_config(const rsg_batch* b, uint32_t pad, rsg_vec3* pos, int* is_big) {
+    if (!b || pad >= (uint32_t)NUM_PADS || !pos || !is_big) return fail(RSG_ERR_ARG, "bad argument");
+    if (!b->buf.has_arena) return fail(RSG_ERR_STATE, "this game mode has no boost pads");
+    pos->x = PAD_LOCS[pad][0];
+    pos->y = PAD_LOCS[pad][1];
+    pos->z = PAD_LOCS[pad][2];
+    *is_big = pad < 6 ? 1 : 0;
+    return RSG_OK;
+}
+
+int rsg_get_tick_count(rsg_batch* b, uint32_t arena, uint64_t* out) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    if ((rc = set_device(b))) return rc;
+    uint32_t lo = 0, hi = 0;
+    if ((rc = read_au(b, AU_TICK_LO, arena, &lo))) return rc;
+    if ((rc = read_au(b, AU_TICK_HI, arena, &hi))) return rc;
+    *out = (uint64_t)lo | ((uint64_t)hi << 32);
+    return RSG_OK;
+}
+
+int rsg_set_tick_count(rsg_batch* b, uint32_t arena, uint64_t tick) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if ((rc = set_device(b))) return rc;
+    if ((rc = write_au(b, AU_TICK_LO, arena, (uint32_t)tick))) return rc;
+    return write_au(b, AU_TICK_HI, arena, (uint32_t)(tick >> 32));
+}
+
+int rsg_is_ball_scored(rsg_batch* b, uint32_t arena, int* out) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    if (!b->buf.has_arena) { *out = 0; return RSG_OK; }
+    rsg_ball_state s;
+    if ((rc = rsg_get_ball_state(b, arena, &s))) return rc;
+    // Arena::IsBallScored, soccar (Arena.cpp:893-901), on the state in uu
+    *out = std::fabs(s.pos.y) > (RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y + RL::BALL_COLLISION_RADIUS_SOCCAR) ? 1 : 0;
+    return RSG_OK;
+}
+
+int rsg_get_all_states(rsg_batch* b, rsg_car_state* cars, rsg_ball_state* balls, rsg_pad_state* pads) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    size_t A = b->buf.A, MC = b->buf.MC;
+    size_t cb = cars ? sizeof(rsg_car_state) * A * MC : 0, bb = balls ? sizeof(rsg_ball_state) * A : 0;
+    size_t pb = (pads && b->buf.has_arena) ? sizeof(rsg_pad_state) * A * NUM_PADS : 0;
+    if ((rc = ensure_stage(b, cb + bb + pb + 16))) return rc;
+    char* st = (char*)b->d_stage;
+    if (cars) {
+        // slots without a car keep the caller's contents: stage them first
+        RSG_CUDA(cudaMemcpyAsync(st, cars, cb, cudaMemcpyHostToDevice, b->stream));
+        RSG_CUDA(launch_get_cars(b->buf, nullptr, (int)(A * MC), (rsg_car_state*)st, b->stream));
+        RSG_CUDA(cudaMemcpyAsync(cars, st, cb, cudaMemcpyDeviceToHost, b->stream));
+    }
+    if (balls) {
+        RSG_CUDA(launch_get_balls(b->buf, nullptr, (int)A, (rsg_ball_state*)(st + cb), b->stream));
+        RSG_CUDA(cudaMemcpyAsync(balls, st + cb, bb, cudaMemcpyDeviceToHost, b->stream));
+    }
+    if (pb) {
+        RSG_CUDA(launch_get_pads(b->buf, nullptr, (int)A, (rsg_pad_state*)(st + cb + bb), b->stream));
+        RSG_CUDA(cudaMemcpyAsync(pads, st + cb + bb, pb, cudaMemcpyDeviceToHost, b->stream));
+    }
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_set_all_states(rsg_batch* b, const rsg_car_state* cars, const rsg_ball_state* balls, const rsg_pad_state* pads) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    size_t A = b->buf.A, MC = b->buf.MC;
+    size_t cb = cars ? sizeof(rsg_car_state) * A * MC : 0, bb = balls ? sizeof(rsg_ball_state) * A : 0;
+    size_t pb = (pads && b->buf.has_arena) ? sizeof(rsg_pad_state) * A * NUM_PADS : 0;
+    if ((rc = ensure_stage(b, cb + bb + pb + 16))) return rc;
+    char* st = (char*)b->d_stage;
+    if (cars) {
+        RSG_CUDA(cudaMemcpyAsync(st, cars, cb, cudaMemcpyHostToDevice, b->stream));
+        RSG_CUDA(launch_set_cars(b->buf, nullptr, (int)(A * MC), (const rsg_car_state*)st, b->stream));
+    }
+    if (balls) {
+        RSG_CUDA(cudaMemcpyAsync(st + cb, balls, bb, cudaMemcpyHostToDevice, b->stream));
+        RSG_CUDA(launch_set_balls(b->buf, nullptr, (int)A, (const rsg_ball_state*)(st + cb), b->stream));
+    }
+    if (pb) {
+        RSG_CUDA(cudaMemcpyAsync(st + cb + bb, pads, pb, cudaMemcpyHostToDevice, b->stream));
+        RSG_CUDA(launch_set_pads(b->buf, nullptr, (int)A, (const rsg_pad_state*)(st + cb + bb), b->stream));
+    }
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_step(rsg_batch* b, int ticks) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    if (ticks < 0) return fail(RSG_ERR_ARG, "negative tick count");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    // with callbacks registered, events are drained at least every 32 ticks so the
+    // per-arena queues (64 entries) cannot overflow from goal events alone
+    int chunk = b->buf.event_mask ? 32 : ticks;
+    RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
+    for (int done = 0; done < ticks;) {
+        int n = std::min(chunk, ticks - done);
+        RSG_CUDA(launch_tick(b->buf, nullptr, n, 64, b->stream));
+        done += n;
+        if (b->buf.event_mask && (rc = drain_events(b))) return rc;
+    }
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return check_device_errors(b);
+}
+
+int rsg_step_async(rsg_batch* b, const rsg_car_controls* d_controls, int ticks) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    if (ticks < 0) return fail(RSG_ERR_ARG, "negative tick count");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
+    RSG_CUDA(launch_tick(b->buf, d_controls, ticks, 64, b->stream));
+    return RSG_OK;
+}
+
+int rsg_sync(rsg_batch* b) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    if ((rc = drain_events(b))) return rc;
+    return check_device_errors(b);
+}
+
+void* rsg_batch_stream(rsg_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+int rsg_set_goal_callback(rsg_batch* b, rsg_goal_fn fn, void* user) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    if (fn && !b->buf.has_arena) return fail(RSG_ERR_STATE, "no goal callback in THE_VOID (Arena.cpp:101-102)");
+    b->goal_fn = fn;
+    b->goal_user = user;
+    update_event_mask(b);
+    return RSG_OK;
+}
+int rsg_set_bump_callback(rsg_batch* b, rsg_bump_fn fn, void* user) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    b->bump_fn = fn;
+    b->bump_user = user;
+    update_event_mask(b);
+    return RSG_OK;
+}
+int rsg_set_ball_hit_callback(rsg_batch* b, rsg_ball_hit_fn fn, void* user) {
+    if (!b) return fail(RSG_ERR_ARG, "null batch");
+    b->hit_fn = fn;
+    b->hit_user = user;
+    update_event_mask(b);
+    return RSG_OK;
+}
+
+int rsg_get_device_flags(rsg_batch* b, uint32_t* out) {
+    if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    RSG_CUDA(cudaMemcpyAsync(out, b->buf.au + au_index(b, AU_ERR, 0), 4 * (size_t)b->buf.A, cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+}  // extern "C"

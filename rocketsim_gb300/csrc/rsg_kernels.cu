@@ -1,0 +1,481 @@
+// rsg_kernels.cu -- kernels of the batched arena tick and the state gather /
+// scatter kernels behind the C ABI.
+//
+// rsg_tick_kernel: one thread advances one arena by `ticks` ticks (load the
+// arena's SoA state, run the ticks in registers / local memory, store it back).
+// Arenas are independent, so the grid is simply ceil(A / block) blocks.
+#include "rsg_kernels.h"
+#include "rsg_tick.cuh"
+
+namespace rsg {
+
+static_assert(sizeof(DevEvent) == DEV_EVENT_BYTES, "event record size");
+
+static BatchView make_view(const BatchBuffers& b) {
+    BatchView v;
+    v.A = b.A;
+    v.MC = b.MC;
+    v.has_arena = b.has_arena;
+    v.dt = b.dt;
+    v.cf = b.cf;
+    v.cu = b.cu;
+    v.bf = b.bf;
+    v.bu = b.bu;
+    v.pf = b.pf;
+    v.pu = b.pu;
+    v.au = b.au;
+    v.cfgs = b.cfgs;
+    v.events = (DevEvent*)b.events;
+    v.event_mask = b.event_mask;
+    v.mesh.tv = b.mesh.tv;
+    v.mesh.nodes = b.mesh.nodes;
+    v.mesh.sub = b.mesh.sub;
+    v.mesh.info = b.mesh.info;
+    v.mesh.cells = b.mesh.cells;
+    v.mesh.ntri = b.mesh.ntri;
+    v.mesh.nnodes = b.mesh.nnodes;
+    v.mesh.nsub = b.mesh.nsub;
+    v.mesh.bvh_min = b.mesh.bvh_min;
+    v.mesh.bvh_max = b.mesh.bvh_max;
+    v.mesh.quant = b.mesh.quant;
+    v.mesh.aabb_min = b.mesh.aabb_min;
+    v.mesh.aabb_max = b.mesh.aabb_max;
+    v.grid.mn = b.grid.mn;
+    v.grid.cell = b.grid.cell;
+    v.grid.nx = b.grid.nx;
+    v.grid.ny = b.grid.ny;
+    v.grid.nz = b.grid.nz;
+    return v;
+}
+
+RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
+    c.ctrl[0] = k.throttle;
+    c.ctrl[1] = k.steer;
+    c.ctrl[2] = k.pitch;
+    c.ctrl[3] = k.yaw;
+    c.ctrl[4] = k.roll;
+    c.setf(F_CTRL_JUMP, k.jump != 0);
+    c.setf(F_CTRL_BOOST, k.boost != 0);
+    c.setf(F_CTRL_HB, k.handbrake != 0);
+}
+
+__global__ void __launch_bounds__(128) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls, int ticks) {
+    int ar = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ar >= bv.A) return;
+    Ctx a;
+    load_ctx(bv, ar, a);
+    for (int t = 0; t < ticks; t++) {
+        if (controls) {
+            const rsg_car_controls* k = controls + ((size_t)t * bv.A + ar) * bv.MC;
+            for (int i = 0; i < a.ncars; i++) apply_controls(a.cars[i], k[i]);
+        }
+        arena_tick(bv, a);
+        a.stepped = true;
+    }
+    store_ctx(bv, ar, a);
+}
+
+cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int block, cudaStream_t st) {
+    if (b.A <= 0 || ticks <= 0) return cudaSuccess;
+    if (block <= 0 || block > 128) block = 64;
+    int grid = (b.A + block - 1) / block;
+    rsg_tick_kernel<<<grid, block, 0, st>>>(make_view(b), controls, ticks);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- state gather / scatter
+RSG_D rsg_vec3 to_rv(V3 v) { rsg_vec3 r; r.x = v.x; r.y = v.y; r.z = v.z; return r; }
+RSG_D V3 from_rv(const rsg_vec3& v) { return V3(v.x, v.y, v.z); }
+RSG_D M3 rot_to_basis(const rsg_rotmat& r) {  // columns forward / right / up
+    return M3(r.forward.x, r.right.x, r.up.x, r.forward.y, r.right.y, r.up.y, r.forward.z, r.right.z, r.up.z);
+}
+RSG_D rsg_rotmat basis_to_rot(const M3& m) {
+    rsg_rotmat r;
+    r.forward = to_rv(m.col(0));
+    r.right = to_rv(m.col(1));
+    r.up = to_rv(m.col(2));
+    return r;
+}
+RSG_D uint64_t u64(uint32_t lo, uint32_t hi) { return (uint64_t)lo | ((uint64_t)hi << 32); }
+
+// Car::GetState (src/Sim/Car/Car.cpp:10-20)
+RSG_D void car_get(const SoA& s, int i, rsg_car_state& o) {
+    uint32_t fl = s.cu(CU_FLAGS, i);
+    auto F = [&](uint32_t m) -> uint8_t { return (fl & m) ? 1 : 0; };
+    o.pos = to_rv(s.v3(CF_POS, i) * RL::BT_TO_UU);
+    o.rot_mat = basis_to_rot(s.m3(CF_ROT, i));
+    o.vel = to_rv(s.v3(CF_VEL, i) * RL::BT_TO_UU);
+    o.ang_vel = to_rv(s.v3(CF_ANG, i));
+    o.tick_count_since_update = u64(s.cu(CU_TICKS_LO, i), s.cu(CU_TICKS_HI, i));
+    o.is_on_ground = F(F_ON_GROUND);
+    for (int w = 0; w < 4; w++) o.wheels_with_contact[w] = F(F_WHEEL0 << w);
+    o.has_jumped = F(F_HAS_JUMPED);
+    o.has_double_jumped = F(F_HAS_DJ);
+    o.has_flipped = F(F_HAS_FLIPPED);
+    o.flip_rel_torque = to_rv(s.v3(CF_FLIP_REL, i));
+    o.jump_time = s.cf(CF_JUMP_TIME, i);
+    o.flip_time = s.cf(CF_FLIP_TIME, i);
+    o.is_flipping = F(F_FLIPPING);
+    o.is_jumping = F(F_JUMPING);
+    o._pad0[0] = o._pad0[1] = 0;
+    o.air_time = s.cf(CF_AIR_TIME, i);
+    o.air_time_since_jump = s.cf(CF_AIR_TIME_SJ, i);
+    o.boost = s.cf(CF_BOOST, i);
+    o.time_since_boosted = s.cf(CF_TIME_SINCE_BOOST, i);
+    o.is_boosting = F(F_BOOSTING);
+    o._pad1[0] = o._pad1[1] = o._pad1[2] = 0;
+    o.boosting_time = s.cf(CF_BOOSTING_TIME, i);
+    o.is_supersonic = F(F_SUPERSONIC);
+    o._pad2[0] = o._pad2[1] = o._pad2[2] = 0;
+    o.supersonic_time = s.cf(CF_SUPERSONIC_TIME, i);
+    o.handbrake_val = s.cf(CF_HANDBRAKE, i);
+    o.is_auto_flipping = F(F_AUTOFLIPPING);
+    o._pad3[0] = o._pad3[1] = o._pad3[2] = 0;
+    o.auto_flip_timer = s.cf(CF_AUTOFLIP_TIMER, i);
+    o.auto_flip_torque_scale = s.cf(CF_AUTOFLIP_SCALE, i);
+    o.world_contact_has_contact = F(F_WC_CONTACT);
+    o._pad4[0] = o._pad4[1] = o._pad4[2] = 0;
+    o.world_contact_normal = to_rv(s.v3(CF_WC_NORMAL, i));
+    o.car_contact_other_car_id = s.cu(CU_CC_OTHER, i);
+    o.car_contact_cooldown_timer = s.cf(CF_CC_COOLDOWN, i);
+    o.is_demoed = F(F_DEMOED);
+    o._pad5[0] = o._pad5[1] = o._pad5[2] = 0;
+    o.demo_respawn_timer = s.cf(CF_DEMO_TIMER, i);
+    o.ball_hit_info.is_valid = F(F_BHI_VALID);
+    o.ball_hit_info._pad0[0] = o.ball_hit_info._pad0[1] = o.ball_hit_info._pad0[2] = 0;
+    o.ball_hit_info.relative_pos_on_ball = to_rv(s.v3(CF_BHI_REL, i));
+    o.ball_hit_info.ball_pos = to_rv(s.v3(CF_BHI_BALLPOS, i));
+    o.ball_hit_info.extra_hit_vel = to_rv(s.v3(CF_BHI_EXTRA, i));
+    o.ball_hit_info.tick_count_when_hit = u64(s.cu(CU_BHI_HIT_LO, i), s.cu(CU_BHI_HIT_HI, i));
+    o.ball_hit_info.tick_count_when_extra_impulse_applied = u64(s.cu(CU_BHI_EXTRA_LO, i), s.cu(CU_BHI_EXTRA_HI, i));
+    o.last_controls.throttle = s.cf(CF_LAST_CTRL + 0, i);
+    o.last_controls.steer = s.cf(CF_LAST_CTRL + 1, i);
+    o.last_controls.pitch = s.cf(CF_LAST_CTRL + 2, i);
+    o.last_controls.yaw = s.cf(CF_LAST_CTRL + 3, i);
+    o.last_controls.roll = s.cf(CF_LAST_CTRL + 4, i);
+    o.last_controls.jump = F(F_LAST_JUMP);
+    o.last_controls.boost = F(F_LAST_BOOST);
+    o.last_controls.handbrake = F(F_LAST_HB);
+    o.last_controls._pad0 = 0;
+}
+
+// Car::SetState (src/Sim/Car/Car.cpp:23-36)
+RSG_D void car_set(const SoA& s, int i, const rsg_car_state& st) {
+    uint32_t fl = s.cu(CU_FLAGS, i) & (F_PRESENT | F_TEAM_ORANGE | F_CTRL_JUMP | F_CTRL_BOOST | F_CTRL_HB | F_NO_RESPONSE);
+    auto S = [&](uint32_t m, uint8_t v) { if (v) fl |= m; };
+    M3 basis = rot_to_basis(st.rot_mat);
+    s.set_v3(CF_POS, i, from_rv(st.pos) * RL::UU_TO_BT);
+    s.set_m3(CF_BASIS, i, basis);
+    s.set_m3(CF_ROT, i, basis);
+    s.set_v3(CF_VEL, i, from_rv(st.vel) * RL::UU_TO_BT);
+    s.set_v3(CF_ANG, i, from_rv(st.ang_vel));
+    s.set_v3(CF_VEL_CACHE, i, V3(0, 0, 0));
+    s.cu(CU_TICKS_LO, i) = 0;
+    s.cu(CU_TICKS_HI, i) = 0;
+    S(F_ON_GROUND, st.is_on_ground);
+    for (int w = 0; w < 4; w++) S(F_WHEEL0 << w, st.wheels_with_contact[w]);
+    S(F_HAS_JUMPED, st.has_jumped);
+    S(F_HAS_DJ, st.has_double_jumped);
+    S(F_HAS_FLIPPED, st.has_flipped);
+    s.set_v3(CF_FLIP_REL, i, from_rv(st.flip_rel_torque));
+    s.cf(CF_JUMP_TIME, i) = st.jump_time;
+    s.cf(CF_FLIP_TIME, i) = st.flip_time;
+    S(F_FLIPPING, st.is_flipping);
+    S(F_JUMPING, st.is_jumping);
+    s.cf(CF_AIR_TIME, i) = st.air_time;
+    s.cf(CF_AIR_TIME_SJ, i) = st.air_time_since_jump;
+    s.cf(CF_BOOST, i) = st.boost;
+    s.cf(CF_TIME_SINCE_BOOST, i) = st.time_since_boosted;
+    S(F_BOOSTING, st.is_boosting);
+    s.cf(CF_BOOSTING_TIME, i) = st.boosting_time;
+    S(F_SUPERSONIC, st.is_supersonic);
+    s.cf(CF_SUPERSONIC_TIME, i) = st.supersonic_time;
+    s.cf(CF_HANDBRAKE, i) = st.handbrake_val;
+    S(F_AUTOFLIPPING, st.is_auto_flipping);
+    s.cf(CF_AUTOFLIP_TIMER, i) = st.auto_flip_timer;
+    s.cf(CF_AUTOFLIP_SCALE, i) = st.auto_flip_torque_scale;
+    S(F_WC_CONTACT, st.world_contact_has_contact);
+    s.set_v3(CF_WC_NORMAL, i, from_rv(st.world_contact_normal));
+    s.cu(CU_CC_OTHER, i) = st.car_contact_other_car_id;
+    s.cf(CF_CC_COOLDOWN, i) = st.car_contact_cooldown_timer;
+    S(F_DEMOED, st.is_demoed);
+    s.cf(CF_DEMO_TIMER, i) = st.demo_respawn_timer;
+    S(F_BHI_VALID, st.ball_hit_info.is_valid);
+    s.set_v3(CF_BHI_REL, i, from_rv(st.ball_hit_info.relative_pos_on_ball));
+    s.set_v3(CF_BHI_BALLPOS, i, from_rv(st.ball_hit_info.ball_pos));
+    s.set_v3(CF_BHI_EXTRA, i, from_rv(st.ball_hit_info.extra_hit_vel));
+    uint64_t th = st.ball_hit_info.tick_count_when_hit, te = st.ball_hit_info.tick_count_when_extra_impulse_applied;
+    s.cu(CU_BHI_HIT_LO, i) = (uint32_t)th;
+    s.cu(CU_BHI_HIT_HI, i) = (uint32_t)(th >> 32);
+    s.cu(CU_BHI_EXTRA_LO, i) = (uint32_t)te;
+    s.cu(CU_BHI_EXTRA_HI, i) = (uint32_t)(te >> 32);
+    s.cf(CF_LAST_CTRL + 0, i) = st.last_controls.throttle;
+    s.cf(CF_LAST_CTRL + 1, i) = st.last_controls.steer;
+    s.cf(CF_LAST_CTRL + 2, i) = st.last_controls.pitch;
+    s.cf(CF_LAST_CTRL + 3, i) = st.last_controls.yaw;
+    s.cf(CF_LAST_CTRL + 4, i) = st.last_controls.roll;
+    S(F_LAST_JUMP, st.last_controls.jump);
+    S(F_LAST_BOOST, st.last_controls.boost);
+    S(F_LAST_HB, st.last_controls.handbrake);
+    s.cu(CU_FLAGS, i) = fl;
+}
+
+__global__ void rsg_get_cars_kernel(BatchView bv, const uint32_t* __restrict__ idx, int n, rsg_car_state* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int ar, slot;
+    if (idx) { ar = (int)idx[2 * k]; slot = (int)idx[2 * k + 1]; }
+    else { ar = k / bv.MC; slot = k % bv.MC; }
+    if (ar < 0 || ar >= bv.A || slot < 0 || slot >= bv.MC) return;
+    SoA s{bv, ar};
+    if (slot >= (int)s.au(AU_NCARS)) return;
+    rsg_car_state o;
+    car_get(s, slot, o);
+    out[k] = o;
+}
+__global__ void rsg_set_cars_kernel(BatchView bv, const uint32_t* __restrict__ idx, int n, const rsg_car_state* __restrict__ in) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int ar, slot;
+    if (idx) { ar = (int)idx[2 * k]; slot = (int)idx[2 * k + 1]; }
+    else { ar = k / bv.MC; slot = k % bv.MC; }
+    if (ar < 0 || ar >= bv.A || slot < 0 || slot >= bv.MC) return;
+    SoA s{bv, ar};
+    if (slot >= (int)s.au(AU_NCARS)) return;
+    rsg_car_state st = in[k];
+    car_set(s, slot, st);
+}
+
+// Ball::GetState / SetState (src/Sim/Ball/Ball.cpp:27-51)
+__global__ void rsg_get_balls_kernel(BatchView bv, const uint32_t* __restrict__ arenas, int n, rsg_ball_state* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int ar = arenas ? (int)arenas[k] : k;
+    if (ar < 0 || ar >= bv.A) return;
+    SoA s{bv, ar};
+    rsg_ball_state o;
+    o.pos = to_rv(V3(s.bf(BF_POS), s.bf(BF_POS + 1), s.bf(BF_POS + 2)) * RL::BT_TO_UU);
+    M3 m;
+    for (int r = 0; r < 3; r++) m.r[r] = V3(s.bf(BF_BASIS + 3 * r), s.bf(BF_BASIS + 3 * r + 1), s.bf(BF_BASIS + 3 * r + 2));
+    o.rot_mat = basis_to_rot(m);
+    o.vel = to_rv(V3(s.bf(BF_VEL), s.bf(BF_VEL + 1), s.bf(BF_VEL + 2)) * RL::BT_TO_UU);
+    o.ang_vel = to_rv(V3(s.bf(BF_ANG), s.bf(BF_ANG + 1), s.bf(BF_ANG + 2)));
+    o.tick_count_since_update = u64(s.bu(BU_TICKS_LO), s.bu(BU_TICKS_HI));
+    out[k] = o;
+}
+__global__ void rsg_set_balls_kernel(BatchView bv, const uint32_t* __restrict__ arenas, int n, const rsg_ball_state* __restrict__ in) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int ar = arenas ? (int)arenas[k] : k;
+    if (ar < 0 || ar >= bv.A) return;
+    SoA s{bv, ar};
+    rsg_ball_state st = in[k];
+    V3 p = from_rv(st.pos) * RL::UU_TO_BT, v = from_rv(st.vel) * RL::UU_TO_BT;
+    M3 m = rot_to_basis(st.rot_mat);
+    s.bf(BF_POS) = p.x; s.bf(BF_POS + 1) = p.y; s.bf(BF_POS + 2) = p.z;
+    for (int r = 0; r < 3; r++) {
+        s.bf(BF_BASIS + 3 * r) = m.r[r].x;
+        s.bf(BF_BASIS + 3 * r + 1) = m.r[r].y;
+        s.bf(BF_BASIS + 3 * r + 2) = m.r[r].z;
+    }
+    s.bf(BF_VEL) = v.x; s.bf(BF_VEL + 1) = v.y; s.bf(BF_VEL + 2) = v.z;
+    s.bf(BF_ANG) = st.ang_vel.x; s.bf(BF_ANG + 1) = st.ang_vel.y; s.bf(BF_ANG + 2) = st.ang_vel.z;
+    s.bu(BU_TICKS_LO) = 0;
+    s.bu(BU_TICKS_HI) = 0;
+}
+
+// BoostPad::GetState / SetState (src/Sim/BoostPad/BoostPad.h:44-45)
+__global__ void rsg_get_pads_kernel(BatchView bv, const uint32_t* __restrict__ arenas, int n, rsg_pad_state* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n * NUM_PADS) return;
+    int q = k / NUM_PADS, p = k % NUM_PADS;
+    int ar = arenas ? (int)arenas[q] : q;
+    if (ar < 0 || ar >= bv.A) return;
+    SoA s{bv, ar};
+    rsg_pad_state o;
+    o.is_active = s.pu(PU_ACTIVE, p) ? 1 : 0;
+    o._pad0[0] = o._pad0[1] = o._pad0[2] = 0;
+    o.cooldown = s.pf(PF_COOLDOWN, p);
+    uint32_t cur = s.pu(PU_CUR_LOCKED, p);
+    o.cur_locked_car_id = (cur > 0 && (int)cur <= bv.MC) ? s.cu(CU_ID, (int)cur - 1) : 0u;
+    o.prev_locked_car_id = s.pu(PU_PREV_LOCKED, p);
+    out[k] = o;
+}
+__global__ void rsg_set_pads_kernel(BatchView bv, const uint32_t* __restrict__ arenas, int n, const rsg_pad_state* __restrict__ in) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n * NUM_PADS) return;
+    int q = k / NUM_PADS, p = k % NUM_PADS;
+    int ar = arenas ? (int)arenas[q] : q;
+    if (ar < 0 || ar >= bv.A) return;
+    SoA s{bv, ar};
+    rsg_pad_state st = in[k];
+    s.pu(PU_ACTIVE, p) = st.is_active ? 1u : 0u;
+    s.pf(PF_COOLDOWN, p) = st.cooldown;
+    s.pu(PU_CUR_LOCKED, p) = 0;
+    s.pu(PU_PREV_LOCKED, p) = st.prev_locked_car_id;
+}
+
+__global__ void rsg_set_controls_kernel(BatchView bv, const rsg_car_controls* __restrict__ in) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= bv.A * bv.MC) return;
+    int ar = k / bv.MC, slot = k % bv.MC;
+    SoA s{bv, ar};
+    rsg_car_controls c = in[k];
+    s.cf(CF_CTRL + 0, slot) = c.throttle;
+    s.cf(CF_CTRL + 1, slot) = c.steer;
+    s.cf(CF_CTRL + 2, slot) = c.pitch;
+    s.cf(CF_CTRL + 3, slot) = c.yaw;
+    s.cf(CF_CTRL + 4, slot) = c.roll;
+    uint32_t fl = s.cu(CU_FLAGS, slot) & ~(F_CTRL_JUMP | F_CTRL_BOOST | F_CTRL_HB);
+    if (c.jump) fl |= F_CTRL_JUMP;
+    if (c.boost) fl |= F_CTRL_BOOST;
+    if (c.handbrake) fl |= F_CTRL_HB;
+    s.cu(CU_FLAGS, slot) = fl;
+}
+
+__global__ void rsg_is_scored_kernel(BatchView bv, int* __restrict__ out) {
+    int ar = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ar >= bv.A) return;
+    SoA s{bv, ar};
+    float y = s.bf(BF_POS + 1) * RL::BT_TO_UU;
+    out[ar] = fabsf(y) > (RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y + RL::BALL_COLLISION_RADIUS_SOCCAR) ? 1 : 0;
+}
+
+static int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }
+
+cudaError_t launch_get_cars(const BatchBuffers& b, const uint32_t* idx, int n, rsg_car_state* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    rsg_get_cars_kernel<<<blocks_for(n, 128), 128, 0, st>>>(make_view(b), idx, n, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_set_cars(const BatchBuffers& b, const uint32_t* idx, int n, const rsg_car_state* in, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    rsg_set_cars_kernel<<<blocks_for(n, 128), 128, 0, st>>>(make_view(b), idx, n, in);
+    return cudaGetLastError();
+}
+cudaError_t launch_get_balls(const BatchBuffers& b, const uint32_t* arenas, int n, rsg_ball_state* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    rsg_get_balls_kernel<<<blocks_for(n, 128), 128, 0, st>>>(make_view(b), arenas, n, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_set_balls(const BatchBuffers& b, const uint32_t* arenas, int n, const rsg_ball_state* in, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    rsg_set_balls_kernel<<<blocks_for(n, 128), 128, 0, st>>>(make_view(b), arenas, n, in);
+    return cudaGetLastError();
+}
+cudaError_t launch_get_pads(const BatchBuffers& b, const uint32_t* arenas, int n, rsg_pad_state* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    rsg_get_pads_kernel<<<blocks_for(n * NUM_PADS, 128), 128, 0, st>>>(make_view(b), arenas, n, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_set_pads(const BatchBuffers& b, const uint32_t* arenas, int n, const rsg_pad_state* in, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    rsg_set_pads_kernel<<<blocks_for(n * NUM_PADS, 128), 128, 0, st>>>(make_view(b), arenas, n, in);
+    return cudaGetLastError();
+}
+cudaError_t launch_set_controls(const BatchBuffers& b, const rsg_car_controls* in, cudaStream_t st) {
+    int n = b.A * b.MC;
+    if (n <= 0) return cudaSuccess;
+    rsg_set_controls_kernel<<<blocks_for(n, 128), 128, 0, st>>>(make_view(b), in);
+    return cudaGetLastError();
+}
+cudaError_t launch_is_scored(const BatchBuffers& b, int* out, cudaStream_t st) {
+    if (b.A <= 0) return cudaSuccess;
+    rsg_is_scored_kernel<<<blocks_for(b.A, 128), 128, 0, st>>>(make_view(b), out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- batch bookkeeping kernels
+// Arena::Arena's initial ball, pads and counters (src/Sim/Arena/Arena.cpp:416-540)
+__global__ void rsg_init_arenas_kernel(BatchView bv, uint32_t ball_cell) {
+    int ar = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ar >= bv.A) return;
+    SoA s{bv, ar};
+    V3 p = V3(0, 0, RL::BALL_REST_Z) * RL::UU_TO_BT;
+    for (int f = 0; f < BF_COUNT; f++) s.bf(f) = 0.f;
+    s.bf(BF_POS) = p.x; s.bf(BF_POS + 1) = p.y; s.bf(BF_POS + 2) = p.z;
+    s.bf(BF_BASIS + 0) = 1.f; s.bf(BF_BASIS + 4) = 1.f; s.bf(BF_BASIS + 8) = 1.f;
+    s.bu(BU_CELL) = ball_cell;
+    s.bu(BU_CELL_SEQ) = 2;  // the ball proxy is the first dynamic proxy created
+    s.bu(BU_TICKS_LO) = 0;
+    s.bu(BU_TICKS_HI) = 0;
+    for (int k = 0; k < NUM_PADS; k++) {
+        s.pu(PU_ACTIVE, k) = 1;
+        s.pf(PF_COOLDOWN, k) = 0.f;
+        s.pu(PU_PREV_LOCKED, k) = 0;
+        s.pu(PU_CUR_LOCKED, k) = 0;
+    }
+    for (int f = 0; f < AU_COUNT; f++) s.au(f) = 0;
+    s.au(AU_SEQ) = 3;
+}
+
+// Arena::AddCar bookkeeping (src/Sim/Arena/Arena.cpp:50-62): clears the slot and registers the
+// broadphase proxy; the respawn state is written afterwards by the state scatter kernel.
+__global__ void rsg_add_car_kernel(BatchView bv, uint32_t ar, uint32_t slot, uint32_t id, uint32_t cfg, uint32_t flags,
+                                   uint32_t cell, uint32_t ncars, uint32_t order) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (ar >= (uint32_t)bv.A || slot >= (uint32_t)bv.MC) return;
+    SoA s{bv, (int)ar};
+    for (int f = 0; f < CF_COUNT; f++) s.cf(f, slot) = 0.f;
+    for (int f = 0; f < CU_COUNT; f++) s.cu(f, slot) = 0u;
+    s.cu(CU_FLAGS, slot) = flags;
+    s.cu(CU_ID, slot) = id;
+    s.cu(CU_CFG, slot) = cfg;
+    s.cu(CU_CELL, slot) = cell;
+    uint32_t seq = s.au(AU_SEQ);
+    s.cu(CU_CELL_SEQ, slot) = seq;
+    s.au(AU_SEQ) = seq + 1;
+    s.au(AU_NCARS) = ncars;
+    s.au(AU_ORDER) = order;
+}
+
+// Arena::RemoveCar (src/Sim/Arena/Arena.cpp:80-94): the slots behind the removed one move down,
+// keeping the relative order of the remaining cars' collision objects.
+__global__ void rsg_remove_car_kernel(BatchView bv, uint32_t ar, uint32_t slot, uint32_t ncars, uint32_t order) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (ar >= (uint32_t)bv.A || slot >= (uint32_t)bv.MC || ncars >= (uint32_t)bv.MC) return;
+    SoA s{bv, (int)ar};
+    for (uint32_t t = slot; t < ncars; t++) {
+        for (int f = 0; f < CF_COUNT; f++) s.cf(f, t) = s.cf(f, t + 1);
+        for (int f = 0; f < CU_COUNT; f++) s.cu(f, t) = s.cu(f, t + 1);
+    }
+    for (int f = 0; f < CF_COUNT; f++) s.cf(f, ncars) = 0.f;
+    for (int f = 0; f < CU_COUNT; f++) s.cu(f, ncars) = 0u;
+    for (int k = 0; k < NUM_PADS; k++) {
+        uint32_t cur = s.pu(PU_CUR_LOCKED, k);
+        if (cur == slot + 1) s.pu(PU_CUR_LOCKED, k) = 0;
+        else if (cur > slot + 1) s.pu(PU_CUR_LOCKED, k) = cur - 1;
+    }
+    s.au(AU_NCARS) = ncars;
+    s.au(AU_ORDER) = order;
+}
+
+// Car::Demolish (src/Sim/Car/Car.cpp:38-41)
+__global__ void rsg_demolish_kernel(BatchView bv, uint32_t ar, uint32_t slot, float delay) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (ar >= (uint32_t)bv.A || slot >= (uint32_t)bv.MC) return;
+    SoA s{bv, (int)ar};
+    s.cu(CU_FLAGS, slot) |= F_DEMOED;
+    s.cf(CF_DEMO_TIMER, slot) = delay;
+}
+
+cudaError_t launch_init_arenas(const BatchBuffers& b, uint32_t ball_cell, cudaStream_t st) {
+    rsg_init_arenas_kernel<<<blocks_for(b.A, 128), 128, 0, st>>>(make_view(b), ball_cell);
+    return cudaGetLastError();
+}
+cudaError_t launch_add_car(const BatchBuffers& b, uint32_t arena, uint32_t slot, uint32_t id, uint32_t cfg, uint32_t flags,
+                           uint32_t cell, uint32_t ncars, uint32_t order, cudaStream_t st) {
+    rsg_add_car_kernel<<<1, 1, 0, st>>>(make_view(b), arena, slot, id, cfg, flags, cell, ncars, order);
+    return cudaGetLastError();
+}
+cudaError_t launch_remove_car(const BatchBuffers& b, uint32_t arena, uint32_t slot, uint32_t ncars, uint32_t order,
+                              cudaStream_t st) {
+    rsg_remove_car_kernel<<<1, 1, 0, st>>>(make_view(b), arena, slot, ncars, order);
+    return cudaGetLastError();
+}
+cudaError_t launch_demolish(const BatchBuffers& b, uint32_t arena, uint32_t slot, float delay, cudaStream_t st) {
+    rsg_demolish_kernel<<<1, 1, 0, st>>>(make_view(b), arena, slot, delay);
+    return cudaGetLastError();
+}
+
+}  // namespace rsg

@@ -1,0 +1,60 @@
+// rsg_kernels.h -- host-side launchers of the device tick and of the state
+// gather / scatter kernels (implemented in rsg_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/rocketsim_gb300.h"
+#include "rsg_layout.h"
+#include "rsg_mesh.h"
+
+namespace rsg {
+
+struct DevMeshPtrs {
+    const float* tv;
+    const QNode* nodes;
+    const Subtree* sub;
+    const TriInfo* info;
+    const uint8_t* cells;
+    int ntri, nnodes, nsub;
+    V3 bvh_min, bvh_max, quant, aabb_min, aabb_max;
+};
+
+// Device buffers of one batch (all SoA arrays as described in rsg_layout.h)
+struct BatchBuffers {
+    int A, MC, has_arena;
+    float dt;
+    float* cf;
+    uint32_t* cu;
+    float* bf;
+    uint32_t* bu;
+    float* pf;
+    uint32_t* pu;
+    uint32_t* au;
+    const CarCfgDev* cfgs;
+    void* events;  // DevEvent[A * MAX_EVENTS_PER_ARENA]
+    uint32_t event_mask;
+    DevMeshPtrs mesh;
+    GridSpec grid;
+};
+
+constexpr int DEV_EVENT_BYTES = 24;
+
+// Advances every arena by `ticks` ticks.  `controls` (device, may be null) holds
+// [ticks][A][MC] rsg_car_controls applied before each tick.
+cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int block, cudaStream_t st);
+
+// Gathers states of `n` (arena, slot) pairs (idx[2k], idx[2k+1]); idx == null means
+// all arenas x all slots in [arena][slot] order.  Slots beyond the arena's car count
+// are not written.  Cars/balls/pads outputs are device arrays; any may be null.
+cudaError_t launch_get_cars(const BatchBuffers& b, const uint32_t* idx, int n, rsg_car_state* out, cudaStream_t st);
+cudaError_t launch_set_cars(const BatchBuffers& b, const uint32_t* idx, int n, const rsg_car_state* in, cudaStream_t st);
+cudaError_t launch_get_balls(const BatchBuffers& b, const uint32_t* arenas, int n, rsg_ball_state* out, cudaStream_t st);
+cudaError_t launch_set_balls(const BatchBuffers& b, const uint32_t* arenas, int n, const rsg_ball_state* in, cudaStream_t st);
+cudaError_t launch_get_pads(const BatchBuffers& b, const uint32_t* arenas, int n, rsg_pad_state* out, cudaStream_t st);
+cudaError_t launch_set_pads(const BatchBuffers& b, const uint32_t* arenas, int n, const rsg_pad_state* in, cudaStream_t st);
+// Writes controls [A][MC] into the per-car control fields.
+cudaError_t launch_set_controls(const BatchBuffers& b, const rsg_car_controls* in, cudaStream_t st);
+// Ball-scored test of every arena into out[A] (0/1).
+cudaError_t launch_is_scored(const BatchBuffers& b, int* out, cudaStream_t st);
+
+}  // namespace rsg

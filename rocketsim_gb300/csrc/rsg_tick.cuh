@@ -1,0 +1,2937 @@
+// rsg_tick.cuh -- device implementation of one RocketSim Arena::Step tick.
+//
+// One arena is advanced by one CUDA thread (arena-per-thread); all arenas of a
+// batch advance in parallel.  The per-arena algorithm restates RocketSim v2.2's
+// tick (src/Sim/Arena/Arena.cpp:689-756) including the parts of Bullet 3.24
+// that decide its results: the voxel broadphase pair order, manifold creation
+// order, the island quicksort that orders solver rows, 4-point manifolds, the
+// sequential-impulse solver with split impulse and RocketSim's averaged
+// ball-world contact.  Citations are <file>:<line> in the RocketSim tree; B/ is
+// libsrc/bullet3-3.24/.
+#pragma once
+#include <cstdint>
+
+#include "rsg_consts.cuh"
+#include "rsg_layout.h"
+#include "rsg_math.cuh"
+#include "rsg_mesh.h"
+
+namespace rsg {
+
+#if !defined(__CUDACC__)
+#error "rsg_tick.cuh is device code"
+#endif
+#define RSG_D __device__ __forceinline__
+#define RSG_DN __device__ __noinline__
+
+__constant__ Curve c_curves[CV_COUNT] = RSG_CURVES_INIT;
+__constant__ float c_pad_locs[NUM_PADS][3] = RSG_PAD_LOCS_INIT;
+__constant__ float c_respawn_locs[4][2] = {{-2304, -4608}, {-2688, -4608}, {2304, -4608}, {2688, -4608}};
+
+struct DevMesh {
+    const float* tv;  // 9 floats per triangle
+    const QNode* nodes;
+    const Subtree* sub;
+    const TriInfo* info;
+    const uint8_t* cells;
+    int ntri, nnodes, nsub;
+    V3 bvh_min, bvh_max, quant, aabb_min, aabb_max;
+};
+struct DevGrid {
+    V3 mn;
+    float cell;
+    int nx, ny, nz;
+};
+
+struct DevEvent {
+    uint32_t kind;
+    uint32_t tick_lo, tick_hi;
+    uint32_t a, b, flag;
+};
+
+// Everything a kernel needs to reach one batch (passed by value)
+struct BatchView {
+    int A, MC;  // arenas, car slots per arena
+    int has_arena;
+    float dt;
+    float* cf;
+    uint32_t* cu;
+    float* bf;
+    uint32_t* bu;
+    float* pf;
+    uint32_t* pu;
+    uint32_t* au;
+    const CarCfgDev* cfgs;
+    DevEvent* events;
+    uint32_t event_mask;
+    DevMesh mesh;
+    DevGrid grid;
+};
+
+constexpr int OBJ_MESH = 0, OBJ_PLANE0 = 1, OBJ_BALL = 5, OBJ_CAR0 = 6;
+enum ActState { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
+
+constexpr int MAX_PAIRS = 96;
+constexpr int MAX_MANIFOLDS = 96;
+constexpr int MAX_POINTS = 64;
+constexpr int MAX_ROWS = MAX_POINTS + MAX_CARS + 1;
+
+struct Body {
+    Xf xf, interp;
+    V3 lin_vel, ang_vel, total_force, total_torque;
+    float inv_mass;
+    V3 inv_inertia_local;
+    M3 inv_inertia_world;
+    float lin_damping;
+    int act;
+    bool no_rot, no_contact_response;
+    float friction, restitution;
+    V3 bp_min, bp_max;
+    int ci, cj, ck;
+    uint32_t cell, cell_seq;
+    int n_special;
+    float sp_friction, sp_restitution, sp_total_dist;
+    V3 sp_total_normal;
+
+    RSG_D void update_inertia() { inv_inertia_world = scaled(xf.b, inv_inertia_local) * transpose(xf.b); }
+    RSG_D bool is_active() const { return act != ISLAND_SLEEPING && act != DISABLE_SIMULATION; }
+    RSG_D V3 vel_at(V3 rel) const { return lin_vel + cross(ang_vel, rel); }
+    RSG_D void apply_central_impulse(V3 imp) { lin_vel += imp * inv_mass; }
+    RSG_D void apply_impulse(V3 imp, V3 rel) {
+        if (inv_mass != 0.f) {
+            apply_central_impulse(imp);
+            ang_vel += inv_inertia_world * cross(rel, imp);
+        }
+    }
+    RSG_D float impulse_denom(V3 pos, V3 n) const {
+        V3 r0 = pos - xf.o;
+        V3 c0 = cross(r0, n);
+        V3 vec = cross(c0 * inv_inertia_world, r0);
+        return inv_mass + dot(n, vec);
+    }
+};
+
+struct WheelRT {
+    V3 contact_normal, contact_point, hard_point, dir_ws, axle_ws, vel_at_contact, impulse;
+    M3 wbasis;
+    float susp_len, susp_rel_vel, clipped_inv_dot, susp_force;
+    int ground;
+    bool in_contact, contact_world;
+};
+
+struct Car {
+    Body rb;
+    const CarCfgDev* cfg;
+    uint32_t flags, id, cc_other;
+    int obj;
+    float steer, pushback[4], latf[4], longf[4], engine, brake;
+    V3 flip_rel;
+    float jump_time, flip_time, air_time, air_time_sj, boost, time_since_boost, boosting_time, supersonic_time;
+    float handbrake, autoflip_timer, autoflip_scale, cc_cooldown, demo_timer;
+    V3 wc_normal, bhi_rel, bhi_ballpos, bhi_extra;
+    uint64_t bhi_hit, bhi_extra_tick, ticks_since;
+    float ctrl[5], last_ctrl[5];
+    M3 rot;  // CarState::rotMat as basis rows
+    V3 vel_cache;
+    WheelRT w[4];
+
+    RSG_D bool f(uint32_t m) const { return (flags & m) != 0; }
+    RSG_D void setf(uint32_t m, bool v) { flags = v ? (flags | m) : (flags & ~m); }
+    RSG_D V3 fwd() const { return rot.col(0); }
+    RSG_D V3 right() const { return rot.col(1); }
+    RSG_D V3 up() const { return rot.col(2); }
+};
+
+struct Pad {
+    bool active;
+    float cooldown;
+    int cur_locked;
+    uint32_t prev_locked;
+};
+
+struct MPoint {
+    V3 local_a, local_b, pos_a, pos_b, normal;
+    float dist, friction, restitution;
+    bool special;
+};
+struct Manifold {
+    int8_t body0, body1, n, island;
+    float breaking;
+    int8_t pt[4];
+};
+
+struct Ctx {
+    DevEvent* ev;  // this arena's event slots
+    uint32_t event_mask;  // bit k set: record events of kind k
+    uint64_t ball_ticks;
+    int ncars;
+    int order[MAX_CARS];
+    Car cars[MAX_CARS];
+    Body ball;
+    V3 ball_cache;
+    Pad pads[NUM_PADS];
+    uint64_t tick;
+    uint32_t seq;
+    bool stepped;
+    uint32_t err;
+    int nevents;
+    float solver_dt;
+    // scratch of one world step
+    int npairs;
+    int8_t pair0[MAX_PAIRS], pair1[MAX_PAIRS];
+    int nman, npts;
+    Manifold man[MAX_MANIFOLDS];
+    MPoint pts[MAX_POINTS];
+
+    RSG_D Body& body(int o) { return o == OBJ_BALL ? ball : cars[o - OBJ_CAR0].rb; }
+};
+
+RSG_D bool is_static_obj(int o) { return o < OBJ_BALL; }
+
+// ---------------------------------------------------------------- geometry consts
+struct PlaneC {
+    V3 n, origin, raw_min, raw_max, bp_min, bp_max;
+};
+RSG_D void plane_const(int p, PlaneC& out) {
+    const float H = RL::ARENA_HEIGHT, EX = RL::ARENA_EXTENT_X;
+    V3 pos, nrm;
+    if (p == 0) { pos = V3(0, 0, 0); nrm = V3(0, 0, 1); }
+    else if (p == 1) { pos = V3(0, 0, H); nrm = V3(0, 0, -1); }
+    else if (p == 2) { pos = V3(-EX, 0, H / 2); nrm = V3(1, 0, 0); }
+    else { pos = V3(EX, 0, H / 2); nrm = V3(-1, 0, 0); }
+    out.n = normalized(nrm);
+    out.origin = pos * RL::UU_TO_BT;
+    V3 mn(-BT_LARGE, -BT_LARGE, -BT_LARGE), mx(BT_LARGE, BT_LARGE, BT_LARGE);
+    int ax = fabsf(out.n.x) > 0.5f ? 0 : (fabsf(out.n.y) > 0.5f ? 1 : 2);
+    bool back = out.n[ax] < 0;
+    mn[ax] = out.origin[ax] + (0.f - 0.2f);
+    mx[ax] = out.origin[ax] + (0.f + 0.2f);
+    if (back) mx[ax] = BT_LARGE; else mn[ax] = -BT_LARGE;
+    out.raw_min = mn;
+    out.raw_max = mx;
+    out.bp_min = mn - V3(0.02f, 0.02f, 0.02f);
+    out.bp_max = mx + V3(0.02f, 0.02f, 0.02f);
+}
+
+// ---------------------------------------------------------------- mesh queries
+RSG_D void tri_load(const DevMesh& m, int t, V3 v[3]) {
+    const float* p = m.tv + (size_t)t * 9;
+#if defined(__CUDA_ARCH__)
+    v[0] = V3(__ldg(p + 0), __ldg(p + 1), __ldg(p + 2));
+    v[1] = V3(__ldg(p + 3), __ldg(p + 4), __ldg(p + 5));
+    v[2] = V3(__ldg(p + 6), __ldg(p + 7), __ldg(p + 8));
+#else
+    v[0] = V3(p[0], p[1], p[2]);
+    v[1] = V3(p[3], p[4], p[5]);
+    v[2] = V3(p[6], p[7], p[8]);
+#endif
+}
+RSG_D void node_load(const DevMesh& m, int i, uint16_t qmin[3], uint16_t qmax[3], int& esc) {
+#if defined(__CUDA_ARCH__)
+    const uint4 raw = __ldg(reinterpret_cast<const uint4*>(m.nodes) + i);
+    qmin[0] = raw.x & 0xffff; qmin[1] = raw.x >> 16; qmin[2] = raw.y & 0xffff;
+    qmax[0] = raw.y >> 16; qmax[1] = raw.z & 0xffff; qmax[2] = raw.z >> 16;
+    esc = (int)raw.w;
+#else
+    const QNode& n = m.nodes[i];
+    for (int k = 0; k < 3; k++) { qmin[k] = n.qmin[k]; qmax[k] = n.qmax[k]; }
+    esc = n.esc_or_tri;
+#endif
+}
+RSG_D void quantize(const DevMesh& m, uint16_t* out, V3 p, bool is_max) {
+    V3 v = (p - m.bvh_min) * m.quant;
+    if (is_max) {
+        out[0] = (uint16_t)(((uint16_t)(v.x + 1.f)) | 1);
+        out[1] = (uint16_t)(((uint16_t)(v.y + 1.f)) | 1);
+        out[2] = (uint16_t)(((uint16_t)(v.z + 1.f)) | 1);
+    } else {
+        out[0] = (uint16_t)(((uint16_t)(v.x)) & 0xfffe);
+        out[1] = (uint16_t)(((uint16_t)(v.y)) & 0xfffe);
+        out[2] = (uint16_t)(((uint16_t)(v.z)) & 0xfffe);
+    }
+}
+RSG_D void quantize_clamp(const DevMesh& m, uint16_t* out, V3 p, bool is_max) {
+    quantize(m, out, vmin(vmax(p, m.bvh_min), m.bvh_max), is_max);
+}
+RSG_D V3 unquantize(const DevMesh& m, const uint16_t* q) {
+    V3 o((float)q[0] / m.quant.x, (float)q[1] / m.quant.y, (float)q[2] / m.quant.z);
+    return o + m.bvh_min;
+}
+RSG_D bool qov(const uint16_t* a0, const uint16_t* a1, const uint16_t* b0, const uint16_t* b1) {
+    bool o = true;
+    o = (a0[0] > b1[0] || a1[0] < b0[0]) ? false : o;
+    o = (a0[2] > b1[2] || a1[2] < b0[2]) ? false : o;
+    o = (a0[1] > b1[1] || a1[1] < b0[1]) ? false : o;
+    return o;
+}
+
+// walkStacklessQuantizedTreeCacheFriendly (btQuantizedBvh.cpp:551-575)
+template <class F>
+RSG_D void mesh_query_aabb(const DevMesh& m, V3 mn, V3 mx, F&& f) {
+    uint16_t qa[3], qb[3];
+    quantize_clamp(m, qa, mn, false);
+    quantize_clamp(m, qb, mx, true);
+    for (int s = 0; s < m.nsub; s++) {
+        Subtree st = m.sub[s];
+        if (!qov(qa, qb, st.qmin, st.qmax)) continue;
+        int cur = st.root, end = st.root + st.size;
+        while (cur < end) {
+            uint16_t nmin[3], nmax[3];
+            int esc;
+            node_load(m, cur, nmin, nmax, esc);
+            bool ov = qov(qa, qb, nmin, nmax);
+            bool leaf = esc >= 0;
+            if (leaf && ov) f(esc);
+            if (ov || leaf) cur++;
+            else cur += -esc;
+        }
+    }
+}
+
+// walkStacklessQuantizedTreeAgainstRay (btQuantizedBvh.cpp:436-548)
+template <class F>
+RSG_D void mesh_query_ray(const DevMesh& m, V3 src, V3 dst, F&& f) {
+    V3 dir = safe_normalized(dst - src);
+    float lambda_max = dot(dir, dst - src);
+    V3 inv(dir.x == 0.f ? BT_LARGE : 1.f / dir.x, dir.y == 0.f ? BT_LARGE : 1.f / dir.y,
+           dir.z == 0.f ? BT_LARGE : 1.f / dir.z);
+    unsigned sg0 = inv.x < 0.f, sg1 = inv.y < 0.f, sg2 = inv.z < 0.f;
+    uint16_t qa[3], qb[3];
+    quantize_clamp(m, qa, vmin(src, dst), false);
+    quantize_clamp(m, qb, vmax(src, dst), true);
+    int cur = 0;
+    while (cur < m.nnodes) {
+        uint16_t nmin[3], nmax[3];
+        int esc;
+        node_load(m, cur, nmin, nmax, esc);
+        bool rayov = false;
+        bool leaf = esc >= 0;
+        if (qov(qa, qb, nmin, nmax)) {
+            V3 b0 = unquantize(m, nmin), b1 = unquantize(m, nmax);
+            float tmin = ((sg0 ? b1 : b0).x - src.x) * inv.x;
+            float tmax = ((sg0 ? b0 : b1).x - src.x) * inv.x;
+            float tymin = ((sg1 ? b1 : b0).y - src.y) * inv.y;
+            float tymax = ((sg1 ? b0 : b1).y - src.y) * inv.y;
+            if (!((tmin > tymax) || (tymin > tmax))) {
+                if (tymin > tmin) tmin = tymin;
+                if (tymax < tmax) tmax = tymax;
+                float tzmin = ((sg2 ? b1 : b0).z - src.z) * inv.z;
+                float tzmax = ((sg2 ? b0 : b1).z - src.z) * inv.z;
+                if (!((tmin > tzmax) || (tzmin > tmax))) {
+                    if (tzmin > tmin) tmin = tzmin;
+                    if (tzmax < tmax) tmax = tzmax;
+                    rayov = (tmin < lambda_max) && (tmax > 0.f);
+                }
+            }
+        }
+        if (leaf && rayov) f(esc);
+        if (rayov || leaf) cur++;
+        else cur += -esc;
+    }
+}
+
+// ---------------------------------------------------------------- ray tests
+// btTriangleRaycastCallback::processTriangle (B/.../NarrowPhaseCollision/btRaycastCallback.cpp:35-118)
+RSG_D bool ray_triangle(V3 from, V3 to, const V3 tv[3], float& hit_frac, V3& out_n) {
+    V3 v10 = tv[1] - tv[0], v20 = tv[2] - tv[0];
+    V3 n = cross(v10, v20);
+    float dist = dot(tv[0], n);
+    float da = dot(n, from) - dist;
+    float db = dot(n, to) - dist;
+    if (da * db >= 0.f) return false;
+    float distance = da / (da - db);
+    if (!(distance < hit_frac)) return false;
+    float tol = len2(n) * -0.0001f;
+    V3 point = lerp(from, to, distance);
+    V3 v0p = tv[0] - point, v1p = tv[1] - point;
+    if (!(dot(cross(v0p, v1p), n) >= tol)) return false;
+    V3 v2p = tv[2] - point;
+    if (!(dot(cross(v1p, v2p), n) >= tol)) return false;
+    if (!(dot(cross(v2p, v0p), n) >= tol)) return false;
+    n = normalized(n);
+    out_n = (da <= 0.f) ? -n : n;
+    hit_frac = distance;
+    return true;
+}
+// btStaticPlaneShape::processAllTriangles (btStaticPlaneShape.cpp:56-87) fed to the ray callback
+RSG_D bool ray_plane(const PlaneC& p, V3 from_w, V3 to_w, float& hit_frac, V3& out_n) {
+    // the plane body has an identity basis, so world-to-object is a translation
+    V3 from = from_w - p.origin, to = to_w - p.origin;
+    V3 amin = vmin(from, to), amax = vmax(from, to);
+    V3 he = (amax - amin) * 0.5f;
+    float radius = len(he);
+    V3 center = (amax + amin) * 0.5f;
+    V3 t0, t1;
+    plane_space(p.n, t0, t1);
+    V3 pc = center - (dot(p.n, center) - 0.f) * p.n;
+    bool any = false;
+    V3 tri[3], n;
+    tri[0] = pc + t0 * radius + t1 * radius;
+    tri[1] = pc + t0 * radius - t1 * radius;
+    tri[2] = pc - t0 * radius - t1 * radius;
+    if (ray_triangle(from, to, tri, hit_frac, n)) { any = true; out_n = n; }
+    tri[0] = pc - t0 * radius - t1 * radius;
+    tri[1] = pc - t0 * radius + t1 * radius;
+    tri[2] = pc + t0 * radius + t1 * radius;
+    if (ray_triangle(from, to, tri, hit_frac, n)) { any = true; out_n = n; }
+    return any;
+}
+// Rays against the ball / another car's box (the reference runs btSubsimplexConvexCast;
+// both solve the same intersection, this one directly)
+RSG_D bool ray_sphere(V3 from, V3 to, V3 c, float r, float& hit_frac, V3& out_n) {
+    V3 d = to - from, mm = from - c;
+    float a = dot(d, d), b = dot(mm, d), cc = dot(mm, mm) - r * r;
+    if (cc > 0.f && b > 0.f) return false;
+    float disc = b * b - a * cc;
+    if (disc < 0.f) return false;
+    float t = (-b - sqrtf(disc)) / a;
+    if (t < 0.f) t = 0.f;
+    if (!(t < hit_frac)) return false;
+    V3 n = (from + d * t) - c;
+    if (len2(n) <= 0.0001f) return false;
+    hit_frac = t;
+    out_n = normalized(n);
+    return true;
+}
+RSG_D bool ray_box(V3 from_w, V3 to_w, const Xf& bx, V3 he, float& hit_frac, V3& out_n) {
+    V3 from = xf_inv_apply(bx, from_w), to = xf_inv_apply(bx, to_w);
+    V3 d = to - from;
+    float tmin = 0.f, tmax = 1.f, sgn = 1;
+    int axis = -1;
+    for (int k = 0; k < 3; k++) {
+        if (fabsf(d[k]) < 1e-12f) {
+            if (from[k] < -he[k] || from[k] > he[k]) return false;
+            continue;
+        }
+        float inv = 1.f / d[k];
+        float t1 = (-he[k] - from[k]) * inv, t2 = (he[k] - from[k]) * inv;
+        float s = -1;
+        if (t1 > t2) { float tt = t1; t1 = t2; t2 = tt; s = 1; }
+        if (t1 > tmin) { tmin = t1; axis = k; sgn = s; }
+        if (t2 < tmax) tmax = t2;
+        if (tmin > tmax) return false;
+    }
+    if (axis < 0 || !(tmin < hit_frac)) return false;
+    V3 nl(0, 0, 0);
+    nl[axis] = sgn;
+    hit_frac = tmin;
+    out_n = bx.b * nl;
+    return true;
+}
+
+
+// ---------------------------------------------------------------- broadphase helpers
+RSG_D void grid_idx(const DevGrid& g, V3 p, int& i, int& j, int& k) {
+    V3 f = (p - g.mn) / g.cell;
+    i = (int)f.x; j = (int)f.y; k = (int)f.z;
+    i = i < 0 ? 0 : (i > g.nx - 1 ? g.nx - 1 : i);
+    j = j < 0 ? 0 : (j > g.ny - 1 ? g.ny - 1 : j);
+    k = k < 0 ? 0 : (k > g.nz - 1 ? g.nz - 1 : k);
+}
+RSG_D bool dyn_registered(const Body& b, int ci, int cj, int ck) {
+    if (b.cell == 0xffffffffu) return false;
+    int di = b.ci - ci, dj = b.cj - cj, dk = b.ck - ck;
+    return di >= -1 && di <= 1 && dj >= -1 && dj <= 1 && dk >= -1 && dk <= 1;
+}
+// dynamic proxies registered in cell (ci,cj,ck) ordered like the cell's handle list
+RSG_D int cell_dyn_list(Ctx& a, int ci, int cj, int ck, int* out) {
+    int n = 0;
+    if (dyn_registered(a.ball, ci, cj, ck)) out[n++] = OBJ_BALL;
+    for (int i = 0; i < a.ncars; i++)
+        if (dyn_registered(a.cars[i].rb, ci, cj, ck)) out[n++] = OBJ_CAR0 + i;
+    for (int i = 1; i < n; i++) {  // insertion sort by cell-change sequence (stable)
+        int v = out[i];
+        uint32_t sv = a.body(v).cell_seq;
+        int j = i - 1;
+        while (j >= 0 && a.body(out[j]).cell_seq > sv) { out[j + 1] = out[j]; j--; }
+        out[j + 1] = v;
+    }
+    return n;
+}
+
+// ---------------------------------------------------------------- vehicle
+struct RayHit {
+    bool hit;
+    int obj;
+    float frac;
+    V3 normal, point;
+};
+
+RSG_D void car_child_xf(const Car& c, Xf& out) {
+    Xf off = xf_identity();
+    off.o = V3(c.cfg->off[0], c.cfg->off[1], c.cfg->off[2]);
+    out = xf_mul(c.rb.xf, off);
+}
+RSG_D V3 car_he(const Car& c) { return V3(c.cfg->he[0], c.cfg->he[1], c.cfg->he[2]); }
+
+RSG_DN RayHit cast_ray(const BatchView& bv, Ctx& a, V3 from, V3 to, int self_obj) {
+    RayHit r;
+    r.hit = false;
+    float frac = 1.f;
+    int obj = -1;
+    V3 nrm;
+    if (bv.has_arena) {
+        mesh_query_ray(bv.mesh, from, to, [&](int t) {
+            V3 tv[3];
+            tri_load(bv.mesh, t, tv);
+            V3 n;
+            if (ray_triangle(from, to, tv, frac, n)) { obj = OBJ_MESH; nrm = n; }
+        });
+        for (int p = 0; p < 4; p++) {
+            PlaneC pl;
+            plane_const(p, pl);
+            V3 n;
+            if (ray_plane(pl, from, to, frac, n)) { obj = OBJ_PLANE0 + p; nrm = n; }
+        }
+    }
+    int ci, cj, ck;
+    grid_idx(bv.grid, from, ci, cj, ck);
+    int dyn[MAX_CARS + 1];
+    int nd = cell_dyn_list(a, ci, cj, ck, dyn);
+    for (int k = 0; k < nd; k++) {
+        int o = dyn[k];
+        if (o == self_obj) continue;
+        if (frac == 0.f) break;
+        V3 n;
+        if (o == OBJ_BALL) {
+            if (ray_sphere(from, to, a.ball.xf.o, RL::BALL_COLLISION_RADIUS_SOCCAR * RL::UU_TO_BT, frac, n)) { obj = o; nrm = n; }
+        } else {
+            Car& c = a.cars[o - OBJ_CAR0];
+            Xf bx = c.rb.xf;
+            bx.o = xf_apply(c.rb.xf, V3(c.cfg->off[0], c.cfg->off[1], c.cfg->off[2]));
+            V3 he = car_he(c) + V3(c.cfg->margin, c.cfg->margin, c.cfg->margin);
+            if (ray_box(from, to, bx, he, frac, n)) { obj = o; nrm = n; }
+        }
+    }
+    if (obj < 0) return r;
+    if (!is_static_obj(obj) && a.body(obj).no_contact_response) return r;
+    r.hit = true;
+    r.obj = obj;
+    r.frac = frac;
+    r.normal = normalized(nrm);
+    r.point = lerp(from, to, frac);
+    return r;
+}
+
+RSG_D V3 static_origin(int o) {
+    if (o == OBJ_MESH) return V3(0, 0, 0);
+    PlaneC p;
+    plane_const(o - OBJ_PLANE0, p);
+    return p.origin;
+}
+
+RSG_D void wheel_ws(Car& c, int i) {  // btVehicleRL::updateWheelTransformsWS (btVehicleRL.cpp:110-118)
+    WheelRT& w = c.w[i];
+    w.in_contact = false;
+    w.contact_world = false;
+    w.hard_point = xf_apply(c.rb.xf, V3(c.cfg->conn[i][0], c.cfg->conn[i][1], c.cfg->conn[i][2]));
+    w.dir_ws = c.rb.xf.b * V3(0, 0, -1);
+    w.axle_ws = c.rb.xf.b * V3(0, -1, 0);
+}
+RSG_D void update_wheel_transform(Car& c, int i) {  // btVehicleRL::updateWheelTransform (btVehicleRL.cpp:66-94)
+    wheel_ws(c, i);
+    WheelRT& w = c.w[i];
+    V3 up = -w.dir_ws;
+    V3 right = w.axle_ws;
+    V3 fwd = normalized(cross(up, right));
+    float steer = i < 2 ? c.steer : 0.f;
+    M3 sm = m_from_q(q_axis_angle(up, steer));
+    M3 b2;
+    for (int r = 0; r < 3; r++) {
+        b2.r[r][1] = -right[r];
+        b2.r[r][2] = up[r];
+        b2.r[r][0] = fwd[r];
+    }
+    w.wbasis = sm * b2;
+}
+
+RSG_D float resolve_single_collision(Ctx& a, Body& b1, int obj2, V3 pos, V3 n, float distance) {
+    V3 rel1 = pos - b1.xf.o;
+    bool dyn2 = !is_static_obj(obj2);
+    V3 o2 = dyn2 ? a.body(obj2).xf.o : static_origin(obj2);
+    V3 rel2 = pos - o2;
+    V3 v1 = b1.vel_at(rel1);
+    V3 v2 = dyn2 ? a.body(obj2).vel_at(rel2) : V3(0, 0, 0);
+    float rel_vel = dot(n, v1 - v2);
+    float restitution = 0.f * -rel_vel;
+    float pos_err = 0.2f * -distance / a.solver_dt;
+    float vel_err = -(1.0f + restitution) * rel_vel;
+    float d0 = b1.impulse_denom(pos, n);
+    float d1 = dyn2 ? a.body(obj2).impulse_denom(pos, n) : 0.f;
+    float jac = 1.f / (d0 + d1);
+    float imp = pos_err * jac + vel_err * jac;
+    return 0.f > imp ? 0.f : imp;
+}
+
+RSG_D void ray_cast_wheel(const BatchView& bv, Ctx& a, Car& c, int i) {  // btVehicleRL::rayCast (btVehicleRL.cpp:120-209)
+    wheel_ws(c, i);
+    WheelRT& w = c.w[i];
+    int fb = i < 2 ? 0 : 1;
+    float rest = c.cfg->rest[fb], radius = c.cfg->radius[fb];
+    float travel_cm = (RL::MAX_SUSPENSION_TRAVEL * RL::UU_TO_BT) * 100;
+    float travel = travel_cm / 100;
+    float ray_len = rest + travel + radius - RL::SUSPENSION_SUBTRACTION;
+    V3 src = w.hard_point;
+    V3 dst = src + (w.dir_ws * ray_len);
+    w.contact_point = dst;
+    w.ground = -1;
+    RayHit h = cast_ray(bv, a, src, dst, c.obj);
+    if (h.hit) {
+        w.contact_point = h.point;
+        w.contact_normal = h.normal;
+        w.in_contact = true;
+        bool stat = is_static_obj(h.obj);
+        w.contact_world = stat;
+        w.ground = h.obj;
+        V3 up = c.rb.xf.b.col(2);
+        float trace = dot(w.hard_point - w.contact_point, up);
+        w.susp_len = trace - radius;
+        float lo = rest - travel, hi = rest + travel;
+        w.susp_len = w.susp_len < lo ? lo : (hi < w.susp_len ? hi : w.susp_len);
+        float denom = dot(w.contact_normal, up);
+        V3 relpos = w.contact_point - c.rb.xf.o;
+        w.vel_at_contact = c.rb.vel_at(relpos);
+        float projv = dot(w.contact_normal, w.vel_at_contact);
+        if (denom > 0.1f) {
+            float inv = 1 / denom;
+            w.susp_rel_vel = projv * inv;
+            w.clipped_inv_dot = inv;
+        } else {
+            w.susp_rel_vel = 0;
+            w.clipped_inv_dot = 10;
+        }
+        if (stat) {
+            float thresh = (rest + radius) - RL::SUSPENSION_SUBTRACTION;
+            if (trace < thresh) {
+                float res = resolve_single_collision(a, c.rb, h.obj, h.point, h.normal, trace - thresh);
+                c.pushback[i] = res / 4;
+            }
+        }
+    } else {
+        w.susp_len = rest + travel;
+        w.susp_rel_vel = 0;
+        w.contact_normal = -w.dir_ws;
+        w.clipped_inv_dot = 1;
+        c.pushback[i] = 0;
+    }
+}
+
+RSG_D float resolve_single_bilateral(Ctx& a, Body& b1, V3 pos, int obj2, V3 normal) {  // btContactConstraint.cpp:103-150
+    if (len2(normal) > 1.1f) return 0.f;
+    bool dyn2 = !is_static_obj(obj2);
+    V3 o2 = dyn2 ? a.body(obj2).xf.o : static_origin(obj2);
+    V3 rel1 = pos - b1.xf.o;
+    V3 rel2 = pos - o2;
+    V3 v1 = b1.vel_at(rel1);
+    V3 v2 = dyn2 ? a.body(obj2).vel_at(rel2) : V3(0, 0, 0);
+    M3 w2a = transpose(b1.xf.b);
+    M3 w2b = dyn2 ? transpose(a.body(obj2).xf.b) : M3();
+    V3 aJ = w2a * cross(rel1, normal);
+    V3 bJ = w2b * cross(rel2, -normal);
+    V3 invIB = dyn2 ? a.body(obj2).inv_inertia_local : V3(0, 0, 0);
+    float invMB = dyn2 ? a.body(obj2).inv_mass : 0.f;
+    V3 m0 = b1.inv_inertia_local * aJ, m1 = invIB * bJ;
+    float diag = b1.inv_mass + dot(m0, aJ) + invMB + dot(m1, bJ);
+    float jinv = 1.f / diag;
+    return -0.2f * dot(normal, v1 - v2) * jinv;
+}
+
+RSG_D void calc_friction_impulses(Ctx& a, Car& c, float dt) {  // btVehicleRL::calcFrictionImpulses (btVehicleRL.cpp:306-380)
+    float fscale = (1.f / c.rb.inv_mass) / 3;
+    for (int i = 0; i < 4; i++) {
+        WheelRT& w = c.w[i];
+        if (w.ground >= 0) {
+            V3 axle = w.wbasis.col(1);
+            V3 n = w.contact_normal;
+            float proj = dot(axle, n);
+            axle -= n * proj;
+            axle = safe_normalized(axle);
+            V3 fwd = safe_normalized(cross(n, axle));
+            float side = resolve_single_bilateral(a, c.rb, w.contact_point, w.ground, axle);
+            float roll;
+            if (c.engine == 0) {
+                if (c.brake) {
+                    V3 crel = w.contact_point - c.rb.xf.o;
+                    bool dyn2 = !is_static_obj(w.ground);
+                    V3 v1 = c.rb.vel_at(crel);
+                    V3 v2 = dyn2 ? a.body(w.ground).vel_at(crel) : V3(0, 0, 0);
+                    float rv = dot(v1 - v2, fwd);
+                    if (dt > (1 / 80.f)) {
+                        float th = -(1 / (dt * 150.f)) + 0.8f;
+                        if (fabsf(rv) < th) rv = 0;
+                    }
+                    const float MAGIC = 113.73963f;
+                    float x = -rv * MAGIC;
+                    float lo = -c.brake, hi = c.brake;
+                    roll = x > lo ? x : lo;
+                    roll = roll < hi ? roll : hi;
+                } else {
+                    roll = 0;
+                }
+            } else {
+                roll = -c.engine / fscale;
+            }
+            V3 total = (fwd * roll * c.longf[i]) + (axle * side * c.latf[i]);
+            w.impulse = total * fscale;
+        } else {
+            w.impulse = V3(0, 0, 0);
+        }
+    }
+}
+
+RSG_D V3 upwards_from_wheels(const Car& c) {  // btVehicleRL.cpp:397-410
+    V3 sum(0, 0, 0);
+    for (int i = 0; i < 4; i++)
+        if (c.w[i].in_contact) sum += c.w[i].contact_normal;
+    if (sum == V3(0, 0, 0)) return c.rb.xf.b.col(2);
+    return safe_normalized(sum);
+}
+
+RSG_D void update_suspension(Car& c, float dt) {  // btVehicleRL.cpp:270-303
+    for (int i = 0; i < 4; i++) {
+        WheelRT& w = c.w[i];
+        if (w.in_contact) {
+            int fb = i < 2 ? 0 : 1;
+            float force = (c.cfg->rest[fb] - w.susp_len) * RL::SUSPENSION_STIFFNESS * w.clipped_inv_dot;
+            float damp = (w.susp_rel_vel < 0) ? RL::WHEELS_DAMPING_COMPRESSION : RL::WHEELS_DAMPING_RELAXATION;
+            w.susp_force = force - (damp * w.susp_rel_vel);
+            w.susp_force *= (i < 2) ? RL::SUSPENSION_FORCE_SCALE_FRONT : RL::SUSPENSION_FORCE_SCALE_BACK;
+            if (w.susp_force < 0) w.susp_force = 0;
+        } else {
+            w.susp_force = 0;
+        }
+    }
+    for (int i = 0; i < 4; i++) {
+        WheelRT& w = c.w[i];
+        if (w.susp_force != 0) {
+            V3 off = w.contact_point - c.rb.xf.o;
+            float base = (w.susp_force * dt) + c.pushback[i];
+            c.rb.apply_impulse(w.contact_normal * base, off);
+        }
+    }
+}
+
+RSG_D void apply_friction_impulses(Car& c, float dt) {  // btVehicleRL.cpp:383-395
+    V3 up = c.rb.xf.b.col(2);
+    for (int i = 0; i < 4; i++) {
+        WheelRT& w = c.w[i];
+        if (!is_zero(w.impulse)) {
+            V3 off = w.contact_point - c.rb.xf.o;
+            float d = dot(up, off);
+            c.rb.apply_impulse(w.impulse * dt, off - up * d);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- car logic (Car.cpp)
+RSG_D float rs_maxf(float a, float b) { return (a > b) ? a : b; }
+RSG_D float rs_minf(float a, float b) { return (a < b) ? a : b; }
+RSG_D float rs_clampf(float v, float lo, float hi) { return rs_minf(rs_maxf(v, lo), hi); }
+RSG_D int rs_sgn(float v) { return (v > 0) - (v < 0); }
+
+RSG_D void update_wheels(Car& c, float dt, int nwc, float fwd_speed) {  // Car::_UpdateWheels (Car.cpp:339-484)
+    float absfs = fabsf(fwd_speed);
+    bool world_contact = false;
+    for (int i = 0; i < 4; i++) world_contact |= c.w[i].contact_world;
+    if (c.f(F_CTRL_HB)) c.handbrake += RL::POWERSLIDE_RISE_RATE * dt;
+    else c.handbrake -= RL::POWERSLIDE_FALL_RATE * dt;
+    c.handbrake = rs_clampf(c.handbrake, 0, 1);
+    float real_throttle = c.ctrl[0];
+    float real_brake = 0;
+    if (c.f(F_CTRL_BOOST) && c.boost > 0) real_throttle = 1;
+    {
+        float dss = curve_eval(c_curves[CV_DRIVE_TORQUE], absfs);
+        float eng = real_throttle;
+        if (!c.f(F_CTRL_HB)) {
+            float at = fabsf(real_throttle);
+            if (at >= RL::THROTTLE_DEADZONE) {
+                if (absfs > RL::STOPPING_FORWARD_VEL && rs_sgn(real_throttle) != rs_sgn(fwd_speed)) {
+                    real_brake = 1;
+                    if (absfs > RL::BRAKING_NO_THROTTLE_SPEED_THRESH) eng = 0;
+                }
+            } else {
+                eng = 0;
+                real_brake = (absfs < RL::STOPPING_FORWARD_VEL) ? 1 : RL::COASTING_BRAKE_FACTOR;
+            }
+        }
+        if (nwc < 3) dss /= 4;
+        c.engine = eng * (RL::THROTTLE_TORQUE_AMOUNT * RL::UU_TO_BT) * dss;
+        c.brake = real_brake * (RL::BRAKE_TORQUE_AMOUNT * RL::UU_TO_BT);
+    }
+    {
+        bool tw = c.cfg->three_wheels != 0;
+        float steer = curve_eval(c_curves[tw ? CV_STEER_3W : CV_STEER], absfs);
+        if (c.handbrake) steer += (curve_eval(c_curves[CV_POWERSLIDE_STEER], absfs) - steer) * c.handbrake;
+        steer *= c.ctrl[1];
+        c.steer = steer;
+    }
+    for (int i = 0; i < 4; i++) {
+        WheelRT& w = c.w[i];
+        if (w.ground >= 0) {
+            V3 vel = c.rb.lin_vel, av = c.rb.ang_vel;
+            V3 lat = w.wbasis.col(1);
+            V3 lng = cross(lat, w.contact_normal);
+            float in = 0;
+            V3 wd = w.hard_point - c.rb.xf.o;
+            V3 cv = (cross(av, wd) + vel) * RL::BT_TO_UU;
+            float base = fabsf(dot(cv, lat));
+            if (base > 5) in = base / (fabsf(dot(cv, lng)) + base);
+            bool tw = c.cfg->three_wheels != 0;
+            float latf = curve_eval(c_curves[tw ? CV_LAT_FRIC_3W : CV_LAT_FRIC], in);
+            float longf = curve_eval(c_curves[CV_LONG_FRIC], in);
+            if (c.handbrake) {
+                float hb = c.handbrake;
+                latf *= (curve_eval(c_curves[CV_HB_LAT], in) - 1) * hb + 1;
+                longf *= (curve_eval(c_curves[CV_HB_LONG], in) - 1) * hb + 1;
+            } else {
+                longf = 1;
+            }
+            if (!(real_throttle != 0)) {
+                float ns = curve_eval(c_curves[CV_NON_STICKY], w.contact_normal.z);
+                latf *= ns;
+                longf *= ns;
+            }
+            c.latf[i] = latf;
+            c.longf[i] = longf;
+        }
+    }
+    if (world_contact) {
+        V3 updir = upwards_from_wheels(c);
+        bool full = (real_throttle != 0) || (absfs > RL::STOPPING_FORWARD_VEL);
+        float sfs = c.cfg->three_wheels ? 0 : 0.5f;
+        if (full) sfs += 1 - fabsf(updir.z);
+        c.rb.total_force += updir * sfs * (RL::GRAVITY_Z * RL::UU_TO_BT) * RL::CAR_MASS_BT;
+    }
+}
+
+RSG_D void update_boost(Car& c, float dt) {  // Car::_UpdateBoost (Car.cpp:486-533)
+    bool has = c.boost > 0;
+    bool boosting = c.f(F_BOOSTING);
+    if (has) {
+        if (boosting) boosting = (c.f(F_CTRL_BOOST) || c.boosting_time < RL::BOOST_MIN_TIME);
+        else if (c.f(F_CTRL_BOOST)) boosting = true;
+    } else {
+        boosting = false;
+    }
+    c.setf(F_BOOSTING, boosting);
+    if (boosting) c.boosting_time += dt;
+    else c.boosting_time = 0;
+    if (boosting) {
+        c.boost = rs_maxf(c.boost - RL::BOOST_USED_PER_SECOND * dt, 0);
+        c.rb.total_force += (c.f(F_ON_GROUND) ? RL::BOOST_ACCEL_GROUND : RL::BOOST_ACCEL_AIR) * RL::UU_TO_BT * c.fwd() *
+                            RL::CAR_MASS_BT;
+        c.time_since_boost = 0;
+    } else {
+        c.time_since_boost += dt;
+    }
+    c.boost = rs_minf(c.boost, RL::BOOST_MAX);
+}
+
+RSG_D void update_jump(Car& c, float dt, bool pressed) {  // Car::_UpdateJump (Car.cpp:535-582)
+    if (c.f(F_ON_GROUND) && !c.f(F_JUMPING)) {
+        if (c.f(F_HAS_JUMPED) && c.jump_time < RL::JUMP_MIN_TIME + RL::JUMP_RESET_TIME_PAD) {
+        } else {
+            c.setf(F_HAS_JUMPED, false);
+            c.jump_time = 0;
+        }
+    }
+    if (c.f(F_JUMPING)) {
+        c.setf(F_JUMPING, c.jump_time < RL::JUMP_MIN_TIME || (c.f(F_CTRL_JUMP) && c.jump_time < RL::JUMP_MAX_TIME));
+    } else if (c.f(F_ON_GROUND) && pressed) {
+        c.setf(F_JUMPING, true);
+        c.jump_time = 0;
+        c.rb.apply_central_impulse(c.up() * RL::JUMP_IMMEDIATE_FORCE * RL::UU_TO_BT * RL::CAR_MASS_BT);
+    }
+    if (c.f(F_JUMPING)) {
+        c.setf(F_HAS_JUMPED, true);
+        V3 tf = c.up() * RL::JUMP_ACCEL;
+        if (c.jump_time < RL::JUMP_MIN_TIME) tf *= 0.62f;
+        c.rb.total_force += tf * RL::UU_TO_BT * RL::CAR_MASS_BT;
+    }
+    if (c.f(F_JUMPING) || c.f(F_HAS_JUMPED)) c.jump_time += dt;
+}
+
+RSG_D void update_air_torque(Car& c, bool update_air_control) {  // Car::_UpdateAirTorque (Car.cpp:584-669)
+    V3 pitch_right = -c.right(), yaw_up = c.up(), roll_fwd = -c.fwd();
+    bool do_air = false;
+    if (c.f(F_FLIPPING)) c.setf(F_FLIPPING, c.f(F_HAS_FLIPPED) && c.flip_time < RL::FLIP_TORQUE_TIME);
+    float pitch = c.ctrl[2], yaw = c.ctrl[3], roll = c.ctrl[4];
+    if (c.f(F_FLIPPING)) {
+        V3 rel = c.flip_rel;
+        if (!is_zero(rel)) {
+            float ps = 1;
+            if (rel.y != 0 && pitch != 0) {
+                if (rs_sgn(rel.y) == rs_sgn(pitch)) {
+                    ps = 1 - rs_minf(fabsf(pitch), 1);
+                    do_air = true;
+                }
+            }
+            rel.y *= ps;
+            V3 dodge = rel * V3(RL::FLIP_TORQUE_X, RL::FLIP_TORQUE_Y, 0);
+            c.rb.total_torque += inverse(c.rb.inv_inertia_world) * c.rb.xf.b * dodge;
+        } else {
+            do_air = true;
+        }
+    } else {
+        do_air = true;
+    }
+    do_air &= !c.f(F_AUTOFLIPPING);
+    do_air &= update_air_control;
+    if (do_air) {
+        float pts = 1;
+        V3 torque;
+        if (pitch || yaw || roll) {
+            if (c.f(F_FLIPPING)) pts = 0;
+            else if (c.f(F_HAS_FLIPPED)) {
+                if (c.flip_time < RL::FLIP_TORQUE_TIME + RL::FLIP_PITCHLOCK_EXTRA_TIME) pts = 0;
+            }
+            torque = (pitch * pitch_right * pts * RL::AIR_TORQUE_X) + (yaw * yaw_up * RL::AIR_TORQUE_Y) +
+                     (roll * roll_fwd * RL::AIR_TORQUE_Z);
+        } else {
+            torque = V3(0, 0, 0);
+        }
+        V3 av = c.rb.ang_vel;
+        float dp = dot(pitch_right, av) * RL::AIR_DAMP_X * (1 - fabsf(do_air ? (pitch * pts) : 0));
+        float dy = dot(yaw_up, av) * RL::AIR_DAMP_Y * (1 - fabsf(do_air ? yaw : 0));
+        float dr = dot(roll_fwd, av) * RL::AIR_DAMP_Z;
+        V3 damping = (yaw_up * dy) + (pitch_right * dp) + (roll_fwd * dr);
+        c.rb.total_torque += inverse(c.rb.inv_inertia_world) * (torque - damping) * RL::CAR_TORQUE_SCALE;
+    }
+    if (c.ctrl[0] != 0) c.rb.total_force += c.fwd() * c.ctrl[0] * RL::THROTTLE_AIR_ACCEL * RL::UU_TO_BT * RL::CAR_MASS_BT;
+}
+
+RSG_D void update_double_jump_or_flip(Car& c, float dt, bool pressed, float fwd_speed) {  // Car.cpp:671-781
+    if (c.f(F_ON_GROUND)) {
+        c.setf(F_HAS_DJ, false);
+        c.setf(F_HAS_FLIPPED, false);
+        c.air_time = 0;
+        c.air_time_sj = 0;
+        c.flip_time = 0;
+    } else {
+        c.air_time += dt;
+        if (c.f(F_HAS_JUMPED) && !c.f(F_JUMPING)) c.air_time_sj += dt;
+        else c.air_time_sj = 0;
+        if (pressed && c.air_time_sj < RL::DOUBLEJUMP_MAX_DELAY) {
+            float pitch = c.ctrl[2], yaw = c.ctrl[3], roll = c.ctrl[4];
+            float mag = fabsf(yaw) + fabsf(pitch) + fabsf(roll);
+            bool flip_input = mag >= c.cfg->dodge_deadzone;
+            bool can = (!c.f(F_HAS_DJ) && !c.f(F_HAS_FLIPPED));
+            if (c.f(F_AUTOFLIPPING)) can = false;
+            if (can) {
+                if (flip_input) {
+                    c.flip_time = 0;
+                    c.setf(F_HAS_FLIPPED, true);
+                    c.setf(F_FLIPPING, true);
+                    float ratio = fabsf(fwd_speed) / RL::CAR_MAX_SPEED;
+                    V3 dd(-pitch, yaw + roll, 0);
+                    if (fabsf(yaw + roll) < 0.1f && fabsf(pitch) < 0.1f) dd = V3(0, 0, 0);
+                    else dd = safe_normalized(dd);
+                    c.flip_rel = V3(-dd.y, dd.x, 0);
+                    if (fabsf(dd.x) < 0.1f) dd.x = 0;
+                    if (fabsf(dd.y) < 0.1f) dd.y = 0;
+                    if (!fuzzy_zero(dd)) {
+                        bool back;
+                        if (fabsf(fwd_speed) < 100.0f) back = dd.x < 0.0f;
+                        else back = (dd.x >= 0.0f) != (fwd_speed >= 0.0f);
+                        V3 iv = dd * RL::FLIP_INITIAL_VEL_SCALE;
+                        float msx = back ? RL::FLIP_BACKWARD_IMPULSE_MAX_SPEED_SCALE : RL::FLIP_FORWARD_IMPULSE_MAX_SPEED_SCALE;
+                        iv.x *= ((msx - 1) * ratio) + 1.f;
+                        iv.y *= ((RL::FLIP_SIDE_IMPULSE_MAX_SPEED_SCALE - 1) * ratio) + 1.f;
+                        if (back) iv.x *= RL::FLIP_BACKWARD_IMPULSE_SCALE_X;
+                        V3 f2 = c.fwd();
+                        f2.z = 0;
+                        f2 = rs_normalized(f2);
+                        V3 r2(-f2.y, f2.x, 0.f);
+                        V3 fdv = iv.x * f2 + iv.y * r2;
+                        c.rb.apply_central_impulse(fdv * RL::UU_TO_BT * RL::CAR_MASS_BT);
+                    }
+                } else {
+                    c.rb.apply_central_impulse(c.up() * RL::JUMP_IMMEDIATE_FORCE * RL::UU_TO_BT * RL::CAR_MASS_BT);
+                    c.setf(F_HAS_DJ, true);
+                }
+            }
+        }
+    }
+    if (c.f(F_FLIPPING)) {
+        c.flip_time += dt;
+        if (c.flip_time <= RL::FLIP_TORQUE_TIME) {
+            if (c.flip_time >= RL::FLIP_Z_DAMP_START && (c.rb.lin_vel.z < 0 || c.flip_time < RL::FLIP_Z_DAMP_END))
+                c.rb.lin_vel.z *= powf(1 - RL::FLIP_Z_DAMP_120, dt / (1 / 120.f));
+        }
+    } else if (c.f(F_HAS_FLIPPED)) {
+        c.flip_time += dt;
+    }
+}
+
+RSG_D float roll_from_rot(const M3& m) {  // Angle::FromRotMat roll (MathTypes.cpp:62-71)
+    float sp = -m.r[2].x;
+    sp = sp < -1.f ? -1.f : (sp > 1.f ? 1.f : sp);
+    float pitch = asinf(sp);
+    float roll = atan2f(m.r[2].y, m.r[2].z);
+    if (fabsf(pitch) == HALF_PI_F) {  // getEulerYPR pole case (B/LinearMath/btMatrix3x3.h:527-547)
+        if (roll > 0) roll -= PI_F;
+        else roll += PI_F;
+    }
+    return -roll;
+}
+
+RSG_D void update_auto_flip(Car& c, float dt, bool pressed) {  // Car::_UpdateAutoFlip (Car.cpp:783-817)
+    if (pressed && c.f(F_WC_CONTACT) && c.wc_normal.z > RL::CAR_AUTOFLIP_NORMZ_THRESH) {
+        float roll = roll_from_rot(c.rot);
+        float ar = fabsf(roll);
+        if (ar > RL::CAR_AUTOFLIP_ROLL_THRESH) {
+            c.autoflip_timer = (float)((double)RL::CAR_AUTOFLIP_TIME * ((double)ar / 3.14159265358979323846));
+            c.autoflip_scale = (roll > 0) ? 1 : -1;
+            c.setf(F_AUTOFLIPPING, true);
+            c.rb.apply_central_impulse(-c.up() * RL::CAR_AUTOFLIP_IMPULSE * RL::UU_TO_BT * RL::CAR_MASS_BT);
+        }
+    }
+    if (c.f(F_AUTOFLIPPING)) {
+        if (c.autoflip_timer <= 0) {
+            c.setf(F_AUTOFLIPPING, false);
+            c.autoflip_timer = 0;
+        } else {
+            c.rb.ang_vel += c.fwd() * RL::CAR_AUTOFLIP_TORQUE * c.autoflip_scale * dt;
+            c.autoflip_timer -= dt;
+        }
+    }
+}
+
+RSG_D void update_auto_roll(Car& c, int nwc) {  // Car::_UpdateAutoRoll (Car.cpp:819-853)
+    V3 gup = nwc > 0 ? upwards_from_wheels(c) : c.wc_normal;
+    V3 gdown = -gup;
+    V3 f = c.fwd(), r = c.right();
+    V3 crossR = cross(gup, f), crossF = cross(gdown, crossR);
+    float rtf = 1 - rs_clampf(dot(r, crossR), 0, 1);
+    float ftf = 1 - rs_clampf(dot(f, crossF), 0, 1);
+    V3 tdr = f * (dot(r, gup) >= 0 ? -1.f : 1.f);
+    V3 tdf = r * (dot(f, gup) >= 0 ? 1.f : -1.f);
+    c.rb.total_force += gdown * RL::CAR_AUTOROLL_FORCE * RL::UU_TO_BT * RL::CAR_MASS_BT;
+    c.rb.total_torque += inverse(c.rb.inv_inertia_world) * ((tdf * ftf) + (tdr * rtf)) * RL::CAR_AUTOROLL_TORQUE;
+}
+
+RSG_D void car_set_respawn(Car& c, int idx, float boost);
+
+RSG_DN void car_pre_tick(const BatchView& bv, Ctx& a, Car& c) {  // Car::_PreTickUpdate (Car.cpp:58-131)
+    float dt = bv.dt;
+    for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
+    if (c.f(F_DEMOED)) {
+        c.demo_timer = rs_maxf(c.demo_timer - dt, 0);
+        if (c.demo_timer == 0) car_set_respawn(c, 0, RL::BOOST_SPAWN_AMOUNT);
+        c.rb.act = DISABLE_SIMULATION;
+        c.rb.no_contact_response = true;
+    } else {
+        c.rb.act = ACTIVE_TAG;
+        c.rb.no_contact_response = false;
+    }
+    if (c.f(F_DEMOED)) return;
+    for (int i = 0; i < 4; i++) update_wheel_transform(c, i);
+    for (int i = 0; i < 4; i++) ray_cast_wheel(bv, a, c, i);
+    calc_friction_impulses(a, c, dt);
+    bool pressed = c.f(F_CTRL_JUMP) && !c.f(F_LAST_JUMP);
+    int nwc = 0;
+    for (int i = 0; i < 4; i++) {
+        bool ic = c.w[i].in_contact;
+        c.setf(F_WHEEL0 << i, ic);
+        nwc += ic;
+    }
+    c.setf(F_ON_GROUND, nwc >= 3);
+    float fwd_speed = dot(c.rb.lin_vel, c.rb.xf.b.col(0)) * RL::BT_TO_UU;
+    update_wheels(c, dt, nwc, fwd_speed);
+    if (nwc < 3) update_air_torque(c, nwc == 0);
+    else c.setf(F_FLIPPING, false);
+    update_jump(c, dt, pressed);
+    update_auto_flip(c, dt, pressed);
+    update_double_jump_or_flip(c, dt, pressed, fwd_speed);
+    if (c.ctrl[0] && ((nwc > 0 && nwc < 4) || c.f(F_WC_CONTACT))) update_auto_roll(c, nwc);
+    c.setf(F_WC_CONTACT, false);
+    update_suspension(c, dt);
+    apply_friction_impulses(c, dt);
+    update_boost(c, dt);
+}
+
+RSG_D void car_post_tick(Car& c, float dt) {  // Car::_PostTickUpdate (Car.cpp:133-163)
+    if (c.f(F_DEMOED)) return;
+    c.rot = c.rb.xf.b;
+    float sp2 = len2(c.rb.lin_vel * RL::BT_TO_UU);
+    bool ss;
+    if (c.f(F_SUPERSONIC) && c.supersonic_time < RL::SUPERSONIC_MAINTAIN_MAX_TIME)
+        ss = (sp2 >= RL::SUPERSONIC_MAINTAIN_MIN_SPEED * RL::SUPERSONIC_MAINTAIN_MIN_SPEED);
+    else
+        ss = (sp2 >= RL::SUPERSONIC_START_SPEED * RL::SUPERSONIC_START_SPEED);
+    c.setf(F_SUPERSONIC, ss);
+    if (ss) c.supersonic_time += dt;
+    else c.supersonic_time = 0;
+    if (c.cc_cooldown > 0) c.cc_cooldown = rs_maxf(c.cc_cooldown - dt, 0);
+    for (int k = 0; k < 5; k++) c.last_ctrl[k] = c.ctrl[k];
+    c.setf(F_LAST_JUMP, c.f(F_CTRL_JUMP));
+    c.setf(F_LAST_BOOST, c.f(F_CTRL_BOOST));
+    c.setf(F_LAST_HB, c.f(F_CTRL_HB));
+}
+
+RSG_D void car_finish_physics(Car& c) {  // Car::_FinishPhysicsTick (Car.cpp:165-193)
+    if (c.f(F_DEMOED)) return;
+    if (!is_zero(c.vel_cache)) {
+        c.rb.lin_vel += c.vel_cache;
+        c.vel_cache = V3(0, 0, 0);
+    }
+    V3 v = c.rb.lin_vel, w = c.rb.ang_vel;
+    const float ms = RL::CAR_MAX_SPEED * RL::UU_TO_BT;
+    if (len2(v) > ms * ms) v = normalized(v) * ms;
+    if (len2(w) > (RL::CAR_MAX_ANG_SPEED * RL::CAR_MAX_ANG_SPEED)) w = normalized(w) * RL::CAR_MAX_ANG_SPEED;
+    c.rb.lin_vel = v;
+    c.rb.ang_vel = w;
+    c.ticks_since++;
+}
+
+RSG_D void car_set_respawn(Car& c, int idx, float boost) {  // Car::Respawn (Car.cpp:43-56) + SetState
+    float team_sign = c.f(F_TEAM_ORANGE) ? -1.f : 1.f;
+    V3 pos(c_respawn_locs[idx][0], c_respawn_locs[idx][1] * team_sign, RL::CAR_RESPAWN_Z);
+    float yaw = (float)((double)(float)(3.14159265358979323846 / 2) + (c.f(F_TEAM_ORANGE) ? 3.14159265358979323846 : 0));
+    M3 m = m_euler_ypr(yaw, -0.f, -0.f);
+    c.rb.xf.o = pos * RL::UU_TO_BT;
+    c.rb.xf.b = m;
+    c.rb.lin_vel = V3(0, 0, 0);
+    c.rb.ang_vel = V3(0, 0, 0);
+    c.rb.update_inertia();
+    c.vel_cache = V3(0, 0, 0);
+    c.rot = m;
+    uint32_t keep = c.flags & (F_PRESENT | F_TEAM_ORANGE | F_CTRL_JUMP | F_CTRL_BOOST | F_CTRL_HB);
+    c.flags = keep | F_ON_GROUND;
+    c.flip_rel = V3(0, 0, 0);
+    c.jump_time = c.flip_time = c.air_time = c.air_time_sj = 0;
+    c.boost = boost;
+    c.time_since_boost = c.boosting_time = c.supersonic_time = c.handbrake = 0;
+    c.autoflip_timer = c.autoflip_scale = 0;
+    c.wc_normal = V3(0, 0, 0);
+    c.cc_other = 0;
+    c.cc_cooldown = 0;
+    c.demo_timer = 0;
+    c.bhi_rel = c.bhi_ballpos = c.bhi_extra = V3(0, 0, 0);
+    c.bhi_hit = ~0ull;
+    c.bhi_extra_tick = ~0ull;
+    c.ticks_since = 0;
+    for (int k = 0; k < 5; k++) c.last_ctrl[k] = 0;
+}
+
+
+// ---------------------------------------------------------------- shapes / AABBs
+RSG_D void car_box_aabb(const Car& c, const Xf& child, V3& mn, V3& mx) { transform_aabb(car_he(c), c.cfg->margin, child, mn, mx); }
+RSG_D void car_compound_aabb(const Car& c, const Xf& t, V3& mn, V3& mx) {  // btCompoundShape::getAabb
+    V3 cmin(c.cfg->comp_min[0], c.cfg->comp_min[1], c.cfg->comp_min[2]);
+    V3 cmax(c.cfg->comp_max[0], c.cfg->comp_max[1], c.cfg->comp_max[2]);
+    V3 lhe = 0.5f * (cmax - cmin);
+    V3 lc = 0.5f * (cmax + cmin);
+    M3 ab = absolute(t.b);
+    V3 center = xf_apply(t, lc);
+    V3 ext(dot(ab.r[0], lhe), dot(ab.r[1], lhe), dot(ab.r[2], lhe));
+    mn = center - ext;
+    mx = center + ext;
+}
+constexpr float BALL_RADIUS_BT = RL::BALL_COLLISION_RADIUS_SOCCAR * RL::UU_TO_BT;
+RSG_D void ball_aabb(const Xf& t, V3& mn, V3& mx) {
+    float m = BALL_RADIUS_BT + 0.08f;
+    mn = t.o - V3(m, m, m);
+    mx = t.o + V3(m, m, m);
+}
+RSG_D void mesh_aabb(const DevMesh& m, V3& mn, V3& mx) {  // btTriangleMeshShape::getAabb, identity transform
+    V3 lhe = 0.5f * (m.aabb_max - m.aabb_min);
+    V3 lc = 0.5f * (m.aabb_max + m.aabb_min);
+    mn = lc - lhe;
+    mx = lc + lhe;
+}
+
+// btTransformUtil::integrateTransform (B/LinearMath/btTransformUtil.h:37-80)
+RSG_D void integrate_transform(const Xf& cur, V3 lv, V3 av, float dt, bool no_rot, Xf& out) {
+    out.o = cur.o + lv * dt;
+    if (no_rot) { out.b = cur.b; return; }
+    const float ANGULAR_MOTION_THRESHOLD = 0.5f * HALF_PI_F;
+    float a2 = len2(av);
+    float ang = 0;
+    if (a2 > SIMD_EPS) ang = sqrtf(a2);
+    if (ang * dt > ANGULAR_MOTION_THRESHOLD) ang = ANGULAR_MOTION_THRESHOLD / dt;
+    V3 axis;
+    if (ang < 0.001f) axis = av * (0.5f * dt - (dt * dt * dt) * (0.020833333333f) * ang * ang);
+    else axis = av * (sinf(0.5f * ang * dt) / ang);
+    Q dorn(axis.x, axis.y, axis.z, cosf(ang * dt * 0.5f));
+    Q orn0 = q_from_m(cur.b);
+    Q pred = q_safe_normalize(q_mul(dorn, orn0));
+    if (q_len2(pred) > SIMD_EPS) out.b = m_from_q(pred);
+    else out.b = cur.b;
+}
+
+// ---------------------------------------------------------------- contact manifolds
+// btManifoldResult::addContactPoint (B/.../CollisionDispatch/btManifoldResult.cpp:109-194)
+RSG_D int add_point(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1, V3 n, V3 pb, float depth, float friction,
+                    float restitution) {
+    if (depth > m.breaking) return -1;
+    V3 pa = pb + n * depth;
+    MPoint p;
+    p.local_a = xf_inv_apply(x0, pa);
+    p.local_b = xf_inv_apply(x1, pb);
+    p.normal = n;
+    p.dist = depth;
+    p.pos_a = pa;
+    p.pos_b = pb;
+    p.friction = friction;
+    p.restitution = restitution;
+    p.special = false;
+    int idx;
+    if (m.n == 4) {
+        // btPersistentManifold::sortCachedPoints (btPersistentManifold.cpp:113-190)
+        int maxPen = -1;
+        float maxv = p.dist;
+        for (int i = 0; i < 4; i++)
+            if (a.pts[m.pt[i]].dist < maxv) { maxPen = i; maxv = a.pts[m.pt[i]].dist; }
+        V3 l0 = a.pts[m.pt[0]].local_a, l1 = a.pts[m.pt[1]].local_a, l2 = a.pts[m.pt[2]].local_a, l3 = a.pts[m.pt[3]].local_a;
+        float r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+        if (maxPen != 0) r0 = len2(cross(p.local_a - l1, l3 - l2));
+        if (maxPen != 1) r1 = len2(cross(p.local_a - l0, l3 - l2));
+        if (maxPen != 2) r2 = len2(cross(p.local_a - l0, l3 - l1));
+        if (maxPen != 3) r3 = len2(cross(p.local_a - l0, l2 - l1));
+        idx = closest_axis4(r0, r1, r2, r3);
+        if (idx < 0) idx = 0;
+    } else {
+        if (a.npts >= MAX_POINTS) {
+            a.err |= ERR_POINT_OVERFLOW;
+            return -1;
+        }
+        idx = m.n++;
+        m.pt[idx] = (int8_t)a.npts++;
+    }
+    a.pts[m.pt[idx]] = p;
+    return idx;
+}
+
+// btPersistentManifold::refreshContactPoints (btPersistentManifold.cpp:263-318)
+RSG_D void refresh(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1) {
+    for (int i = m.n - 1; i >= 0; i--) {
+        MPoint& p = a.pts[m.pt[i]];
+        p.pos_a = xf_apply(x0, p.local_a);
+        p.pos_b = xf_apply(x1, p.local_b);
+        p.dist = dot(p.pos_a - p.pos_b, p.normal);
+    }
+    for (int i = m.n - 1; i >= 0; i--) {
+        MPoint& p = a.pts[m.pt[i]];
+        bool remove = false;
+        if (!(p.dist <= m.breaking)) remove = true;
+        else {
+            V3 proj = p.pos_a - p.normal * p.dist;
+            V3 diff = p.pos_b - proj;
+            if (dot(diff, diff) > m.breaking * m.breaking) remove = true;
+        }
+        if (remove) {
+            int last = m.n - 1;
+            if (i != last) m.pt[i] = m.pt[last];
+            m.n--;
+        }
+    }
+}
+
+// btAdjustInternalEdgeContacts (B/.../CollisionDispatch/btInternalEdgeUtility.cpp:414-840) for a
+// mesh triangle contact; the mesh transform is the identity and the flags argument is 0.
+RSG_D void nearest_on_segment(V3 p, V3 l0, V3 l1, V3& out) {
+    V3 d = l1 - l0;
+    if (fuzzy_zero(d)) { out = l0; return; }
+    float t = dot(p - l0, d) / dot(d, d);
+    if (t < 0) t = 0;
+    else if (t > 1) t = 1;
+    out = l0 + d * t;
+}
+RSG_D bool clamp_normal(V3 edge, V3 tri_n, V3 local_n, float corrected, V3& out) {
+    V3 ec = normalized(cross(edge, tri_n));
+    float cur = atan2f(dot(local_n, ec), dot(local_n, tri_n));
+    if (corrected < 0) {
+        if (cur < corrected) {
+            out = m_from_q(q_axis_angle(edge, corrected - cur)) * local_n;
+            return true;
+        }
+    }
+    if (corrected >= 0) {
+        if (cur > corrected) {
+            out = m_from_q(q_axis_angle(edge, corrected - cur)) * local_n;
+            return true;
+        }
+    }
+    return false;
+}
+RSG_D void edge_case(MPoint& cp, const TriInfo& inf, V3 tri_n, V3 lcn, V3 edge, float angle, int convflag,
+                     int swapflag, bool recompute_local, bool& near_edge, int& concave) {
+    near_edge = true;
+    if (angle == 0.f) { concave++; return; }
+    bool conv = (inf.flags & convflag) != 0;
+    float sf = conv ? 1.f : -1.f;
+    V3 nA = sf * tri_n;
+    V3 cnB = q_rotate(q_axis_angle(edge, angle), tri_n);
+    if (inf.flags & swapflag) cnB *= -1;
+    V3 nB = sf * cnB;
+    float ndA = dot(lcn, nA), ndB = dot(lcn, nB);
+    if ((ndA < 0.f) && (ndB < 0.f)) { concave++; return; }
+    V3 ln = recompute_local ? cp.normal : lcn;
+    V3 clamped;
+    if (clamp_normal(edge, sf * tri_n, ln, angle, clamped)) {
+        if (dot(clamped, tri_n) > 0) {
+            cp.normal = clamped;
+            cp.pos_b = cp.pos_a - cp.normal * cp.dist;
+            cp.local_b = cp.pos_b;
+        }
+    }
+}
+RSG_DN void adjust_internal_edge(const DevMesh& mesh, MPoint& cp, int tri) {
+    TriInfo inf = mesh.info[tri];
+    if (!inf.present) return;
+    V3 v[3];
+    tri_load(mesh, tri, v);
+    V3 tri_n = normalized(cross(v[1] - v[0], v[2] - v[0]));
+    V3 nearest;
+    nearest_on_segment(cp.local_b, v[0], v[1], nearest);
+    V3 contact = cp.local_b;
+    bool near_edge = false;
+    int concave = 0;
+    V3 lcn = normalized(cp.normal);
+    int best = -1;
+    float bestd = BT_LARGE;
+    const float MAXA = TWO_PI_F, EDGE_D = 0.1f;
+    if (fabsf(inf.a01) < MAXA) {
+        V3 nn; nearest_on_segment(cp.local_b, v[0], v[1], nn);
+        float l = len(contact - nn);
+        if (l < bestd) { best = 0; bestd = l; }
+    }
+    if (fabsf(inf.a12) < MAXA) {
+        V3 nn; nearest_on_segment(cp.local_b, v[1], v[2], nn);
+        float l = len(contact - nn);
+        if (l < bestd) { best = 1; bestd = l; }
+    }
+    if (fabsf(inf.a20) < MAXA) {
+        V3 nn; nearest_on_segment(cp.local_b, v[2], v[0], nn);
+        float l = len(contact - nn);
+        if (l < bestd) { best = 2; bestd = l; }
+    }
+    if (fabsf(inf.a01) < MAXA) {
+        float l = len(contact - nearest);
+        if (l < EDGE_D && best == 0)
+            edge_case(cp, inf, tri_n, lcn, v[0] - v[1], inf.a01, TRI_V0V1_CONVEX, TRI_V0V1_SWAP, false, near_edge, concave);
+    }
+    nearest_on_segment(contact, v[1], v[2], nearest);
+    if (fabsf(inf.a12) < MAXA) {
+        float l = len(contact - nearest);
+        if (l < EDGE_D && best == 1)
+            edge_case(cp, inf, tri_n, lcn, v[1] - v[2], inf.a12, TRI_V1V2_CONVEX, TRI_V1V2_SWAP, true, near_edge, concave);
+    }
+    nearest_on_segment(contact, v[2], v[0], nearest);
+    if (fabsf(inf.a20) < MAXA) {
+        float l = len(contact - nearest);
+        if (l < EDGE_D && best == 2)
+            edge_case(cp, inf, tri_n, lcn, v[2] - v[0], inf.a20, TRI_V2V0_CONVEX, TRI_V2V0_SWAP, true, near_edge, concave);
+    }
+    if (near_edge && concave > 0) {
+        if (dot(tri_n, lcn) < 0) return;
+        cp.normal = tri_n;
+        cp.pos_b = cp.pos_a - cp.normal * cp.dist;
+        cp.local_b = cp.pos_b;
+    }
+}
+
+// ---------------------------------------------------------------- GJK
+// btGjkPairDetector::getClosestPointsNonVirtual (B/.../NarrowPhaseCollision/btGjkPairDetector.cpp:693-959)
+// with btVoronoiSimplexSolver (btVoronoiSimplexSolver.cpp)
+struct Convex {
+    int type;  // 0 box (implicit half extents he), 1 sphere (point core), 2 triangle
+    V3 he;
+    V3 tv[3];
+    float margin;
+    RSG_D V3 support_nomargin(V3 d) const {
+        if (type == 0) return V3(d.x >= 0 ? he.x : -he.x, d.y >= 0 ? he.y : -he.y, d.z >= 0 ? he.z : -he.z);
+        if (type == 1) return V3(0, 0, 0);
+        V3 dots(dot(d, tv[0]), dot(d, tv[1]), dot(d, tv[2]));
+        return tv[max_axis(dots)];
+    }
+    RSG_D void aabb(const Xf& t, V3& mn, V3& mx) const {
+        if (type == 0) { transform_aabb(he, margin, t, mn, mx); return; }
+        if (type == 1) {
+            float m = margin + 0.08f;
+            mn = t.o - V3(m, m, m);
+            mx = t.o + V3(m, m, m);
+            return;
+        }
+        V3 a(BT_LARGE, BT_LARGE, BT_LARGE), b(-BT_LARGE, -BT_LARGE, -BT_LARGE);
+        for (int i = 0; i < 3; i++) {
+            V3 w = xf_apply(t, tv[i]);
+            a = vmin(a, w);
+            b = vmax(b, w);
+        }
+        mn = a - V3(margin, margin, margin);
+        mx = b + V3(margin, margin, margin);
+    }
+};
+
+struct SubResult {
+    V3 closest;
+    bool used[4];
+    float bary[4];
+    bool degenerate;
+    RSG_D void reset() {
+        degenerate = false;
+        for (int i = 0; i < 4; i++) { used[i] = false; bary[i] = 0; }
+    }
+    RSG_D bool valid() const { return bary[0] >= 0 && bary[1] >= 0 && bary[2] >= 0 && bary[3] >= 0; }
+    RSG_D void set_bary(float a, float b, float c, float d) { bary[0] = a; bary[1] = b; bary[2] = c; bary[3] = d; }
+};
+
+RSG_D void closest_tri(V3 p, V3 a, V3 b, V3 c, SubResult& r) {  // closestPtPointTriangle
+    r.used[0] = r.used[1] = r.used[2] = r.used[3] = false;
+    V3 ab = b - a, ac = c - a, ap = p - a;
+    float d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.f && d2 <= 0.f) { r.closest = a; r.used[0] = true; r.set_bary(1, 0, 0, 0); return; }
+    V3 bp = p - b;
+    float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) { r.closest = b; r.used[1] = true; r.set_bary(0, 1, 0, 0); return; }
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+        float v = d1 / (d1 - d3);
+        r.closest = a + v * ab; r.used[0] = r.used[1] = true; r.set_bary(1 - v, v, 0, 0);
+        return;
+    }
+    V3 cp = p - c;
+    float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) { r.closest = c; r.used[2] = true; r.set_bary(0, 0, 1, 0); return; }
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+        float w = d2 / (d2 - d6);
+        r.closest = a + w * ac; r.used[0] = r.used[2] = true; r.set_bary(1 - w, 0, w, 0);
+        return;
+    }
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+        float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        r.closest = b + w * (c - b); r.used[1] = r.used[2] = true; r.set_bary(0, 1 - w, w, 0);
+        return;
+    }
+    float denom = 1.f / (va + vb + vc);
+    float v = vb * denom, w = vc * denom;
+    r.closest = a + ab * v + ac * w;
+    r.used[0] = r.used[1] = r.used[2] = true;
+    r.set_bary(1 - v - w, v, w, 0);
+}
+RSG_D int point_outside(V3 p, V3 a, V3 b, V3 c, V3 d) {  // pointOutsideOfPlane
+    V3 nrm = cross(b - a, c - a);
+    float sp = dot(p - a, nrm), sd = dot(d - a, nrm);
+    if (sd * sd < (1e-4f * 1e-4f)) return -1;
+    return sp * sd < 0.f;
+}
+RSG_DN bool closest_tet(V3 p, V3 a, V3 b, V3 c, V3 d, SubResult& fr) {  // closestPtPointTetrahedron
+    SubResult t;
+    t.reset();
+    fr.closest = p;
+    fr.used[0] = fr.used[1] = fr.used[2] = fr.used[3] = true;
+    int oABC = point_outside(p, a, b, c, d), oACD = point_outside(p, a, c, d, b), oADB = point_outside(p, a, d, b, c),
+        oBDC = point_outside(p, b, d, c, a);
+    if (oABC < 0 || oACD < 0 || oADB < 0 || oBDC < 0) { fr.degenerate = true; return false; }
+    if (!oABC && !oACD && !oADB && !oBDC) return false;
+    float best = FLT_MAX;
+    if (oABC) {
+        closest_tri(p, a, b, c, t);
+        V3 q = t.closest;
+        float sq = dot(q - p, q - p);
+        if (sq < best) {
+            best = sq; fr.closest = q;
+            fr.used[0] = t.used[0]; fr.used[1] = t.used[1]; fr.used[2] = t.used[2]; fr.used[3] = false;
+            fr.set_bary(t.bary[0], t.bary[1], t.bary[2], 0);
+        }
+    }
+    if (oACD) {
+        closest_tri(p, a, c, d, t);
+        V3 q = t.closest;
+        float sq = dot(q - p, q - p);
+        if (sq < best) {
+            best = sq; fr.closest = q;
+            fr.used[0] = t.used[0]; fr.used[1] = false; fr.used[2] = t.used[1]; fr.used[3] = t.used[2];
+            fr.set_bary(t.bary[0], 0, t.bary[1], t.bary[2]);
+        }
+    }
+    if (oADB) {
+        closest_tri(p, a, d, b, t);
+        V3 q = t.closest;
+        float sq = dot(q - p, q - p);
+        if (sq < best) {
+            best = sq; fr.closest = q;
+            fr.used[0] = t.used[0]; fr.used[1] = t.used[2]; fr.used[2] = false; fr.used[3] = t.used[1];
+            fr.set_bary(t.bary[0], t.bary[2], 0, t.bary[1]);
+        }
+    }
+    if (oBDC) {
+        closest_tri(p, b, d, c, t);
+        V3 q = t.closest;
+        float sq = dot(q - p, q - p);
+        if (sq < best) {
+            best = sq; fr.closest = q;
+            fr.used[0] = false; fr.used[1] = t.used[0]; fr.used[2] = t.used[2]; fr.used[3] = t.used[1];
+            fr.set_bary(0, t.bary[0], t.bary[2], t.bary[1]);
+        }
+    }
+    return true;
+}
+
+struct Simplex {
+    int n;
+    V3 W[5], Pp[5], Qq[5];
+    V3 lastW;
+    bool needs_update, cached_valid;
+    V3 cP1, cP2, cV;
+    SubResult bc;
+    RSG_D void reset() {
+        cached_valid = false;
+        n = 0;
+        needs_update = true;
+        lastW = V3(BT_LARGE, BT_LARGE, BT_LARGE);
+        bc.reset();
+    }
+    RSG_D void remove(int i) {
+        n--;
+        W[i] = W[n]; Pp[i] = Pp[n]; Qq[i] = Qq[n];
+    }
+    RSG_D void reduce(const SubResult& r) {
+        if (n >= 4 && !r.used[3]) remove(3);
+        if (n >= 3 && !r.used[2]) remove(2);
+        if (n >= 2 && !r.used[1]) remove(1);
+        if (n >= 1 && !r.used[0]) remove(0);
+    }
+    RSG_D void add(V3 w, V3 p, V3 q) {
+        lastW = w;
+        needs_update = true;
+        W[n] = w; Pp[n] = p; Qq[n] = q;
+        n++;
+    }
+    RSG_D bool update() {
+        if (!needs_update) return cached_valid;
+        bc.reset();
+        needs_update = false;
+        V3 p(0, 0, 0);
+        switch (n) {
+            case 0: cached_valid = false; break;
+            case 1:
+                cP1 = Pp[0]; cP2 = Qq[0]; cV = cP1 - cP2;
+                bc.reset(); bc.set_bary(1, 0, 0, 0);
+                cached_valid = bc.valid();
+                break;
+            case 2: {
+                V3 from = W[0], to = W[1];
+                V3 diff = p - from, v = to - from;
+                float t = dot(v, diff);
+                if (t > 0) {
+                    float vv = dot(v, v);
+                    if (t < vv) { t /= vv; bc.used[0] = bc.used[1] = true; }
+                    else { t = 1; bc.used[1] = true; }
+                } else {
+                    t = 0;
+                    bc.used[0] = true;
+                }
+                bc.set_bary(1 - t, t, 0, 0);
+                cP1 = Pp[0] + t * (Pp[1] - Pp[0]);
+                cP2 = Qq[0] + t * (Qq[1] - Qq[0]);
+                cV = cP1 - cP2;
+                reduce(bc);
+                cached_valid = bc.valid();
+                break;
+            }
+            case 3: {
+                closest_tri(p, W[0], W[1], W[2], bc);
+                cP1 = Pp[0] * bc.bary[0] + Pp[1] * bc.bary[1] + Pp[2] * bc.bary[2];
+                cP2 = Qq[0] * bc.bary[0] + Qq[1] * bc.bary[1] + Qq[2] * bc.bary[2];
+                cV = cP1 - cP2;
+                reduce(bc);
+                cached_valid = bc.valid();
+                break;
+            }
+            case 4: {
+                bool sep = closest_tet(p, W[0], W[1], W[2], W[3], bc);
+                if (sep) {
+                    cP1 = Pp[0] * bc.bary[0] + Pp[1] * bc.bary[1] + Pp[2] * bc.bary[2] + Pp[3] * bc.bary[3];
+                    cP2 = Qq[0] * bc.bary[0] + Qq[1] * bc.bary[1] + Qq[2] * bc.bary[2] + Qq[3] * bc.bary[3];
+                    cV = cP1 - cP2;
+                    reduce(bc);
+                } else {
+                    if (bc.degenerate) cached_valid = false;
+                    else { cached_valid = true; cV = V3(0, 0, 0); }
+                    break;
+                }
+                cached_valid = bc.valid();
+                break;
+            }
+            default: cached_valid = false;
+        }
+        return cached_valid;
+    }
+    RSG_D bool closest(V3& v) { bool ok = update(); v = cV; return ok; }
+    RSG_D bool in_simplex(V3 w) const {
+        bool found = false;
+        for (int i = 0; i < n; i++)
+            if (len2(W[i] - w) <= 0.0001f) { found = true; break; }
+        if (w == lastW) return true;
+        return found;
+    }
+    RSG_D void points(V3& p1, V3& p2) { update(); p1 = cP1; p2 = cP2; }
+};
+
+struct GjkOut {
+    bool valid;
+    V3 normal, point_on_b;
+    float dist;
+    bool epa_needed;
+};
+
+RSG_DN GjkOut gjk(const Convex& A, const Xf& ta_in, const Convex& B, const Xf& tb_in, float max_dist2) {
+    GjkOut out;
+    out.valid = false;
+    out.epa_needed = false;
+    out.dist = 0;
+    float distance = 0;
+    V3 normalInB(0, 0, 0), pA, pB;
+    Xf ta = ta_in, tb = tb_in;
+    V3 off = (ta.o + tb.o) * 0.5f;
+    ta.o -= off;
+    tb.o -= off;
+    float mA = A.margin, mB = B.margin;
+    V3 sep(0, 1, 0);
+    bool is_valid = false, check_simplex = false;
+    int degenerate = 0;
+    Simplex sx;
+    sx.reset();
+    float sqd = BT_LARGE, delta = 0, margin = mA + mB;
+    int iter = 0;
+    while (true) {
+        V3 sa = (-sep) * ta_in.b;
+        V3 sb = sep * tb_in.b;
+        V3 pin = A.support_nomargin(sa), qin = B.support_nomargin(sb);
+        V3 pw = xf_apply(ta, pin), qw = xf_apply(tb, qin);
+        V3 w = pw - qw;
+        delta = dot(sep, w);
+        if ((delta > 0.f) && (delta * delta > sqd * max_dist2)) { degenerate = 10; check_simplex = true; break; }
+        if (sx.in_simplex(w)) { degenerate = 1; check_simplex = true; break; }
+        float f0 = sqd - delta, f1 = sqd * 1.0e-6f;
+        if (f0 <= f1) { degenerate = f0 <= 0.f ? 2 : 11; check_simplex = true; break; }
+        sx.add(w, pw, qw);
+        V3 nsep;
+        if (!sx.closest(nsep)) { degenerate = 3; check_simplex = true; break; }
+        if (len2(nsep) < 1.0e-6f) { sep = nsep; degenerate = 6; check_simplex = true; break; }
+        float prev = sqd;
+        sqd = len2(nsep);
+        if (prev - sqd <= SIMD_EPS * prev) { check_simplex = true; degenerate = 12; break; }
+        sep = nsep;
+        if (iter++ > 1000) break;
+        if (sx.n == 4) { degenerate = 13; break; }
+    }
+    if (check_simplex) {
+        sx.points(pA, pB);
+        normalInB = sep;
+        float l2 = len2(sep);
+        if (l2 < 0.0001f) degenerate = 5;
+        if (l2 > SIMD_EPS * SIMD_EPS) {
+            float rlen = 1.f / sqrtf(l2);
+            normalInB *= rlen;
+            float s = sqrtf(sqd);
+            pA -= sep * (mA / s);
+            pB += sep * (mB / s);
+            distance = ((1.f / rlen) - margin);
+            is_valid = true;
+        }
+    }
+    bool catch_deg = degenerate && ((distance + margin) < 0.01f);
+    if (!is_valid || catch_deg) {
+        out.epa_needed = true;
+        if (!is_valid) return out;
+    }
+    if (is_valid && ((distance < 0) || (distance * distance < max_dist2))) {
+        V3 amn, amx, bmn, bmx;  // m_fixContactNormalDirection
+        A.aabb(ta, amn, amx);
+        B.aabb(tb, bmn, bmx);
+        V3 posA = (amx + amn) * 0.5f, posB = (bmn + bmx) * 0.5f;
+        if (dot(posA - posB, normalInB) < 0.f) normalInB *= -1.f;
+        out.valid = true;
+        out.normal = normalInB;
+        out.point_on_b = pB + off;
+        out.dist = distance;
+    }
+    return out;
+}
+
+// closestPointTriangle (B/.../CollisionDispatch/SphereTriangleDetector.cpp:87-128): vertex
+// regions are tested before edge regions, unlike the simplex solver's variant above
+RSG_D V3 closest_point_triangle(V3 p, V3 a, V3 b, V3 c) {
+    V3 ab = b - a, ac = c - a, ap = p - a;
+    float d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.f && d2 <= 0.f) return a;
+    V3 bp = p - b;
+    float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) return b;
+    V3 cp = p - c;
+    float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) return c;
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) return a + (d1 / (d1 - d3)) * ab;
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) return a + (d2 / (d2 - d6)) * ac;
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) return b + ((d4 - d3) / ((d4 - d3) + (d5 - d6))) * (c - b);
+    float denom = 1.f / (va + vb + vc);
+    float v = vb * denom, w = vc * denom;
+    return a + v * ab + w * ac;
+}
+
+// SphereTriangleDetector::collide (B/.../CollisionDispatch/SphereTriangleDetector.cpp:139-281)
+RSG_DN bool sphere_triangle(V3 center, float radius, const V3 v[3], float threshold, V3& point, V3& normal_out,
+                            float& depth) {
+    float rwt = radius + threshold;
+    V3 n = cross(v[1] - v[0], v[2] - v[0]);
+    float l2 = len2(n);
+    bool has = false;
+    V3 cpnt;
+    if (l2 >= SIMD_EPS * SIMD_EPS) {
+        n = n / sqrtf(l2);
+        V3 p1c = center - v[0];
+        float dfp = dot(p1c, n);
+        if (dfp < 0.f) { dfp *= -1.f; n *= -1.f; }
+        if (dfp < rwt) {
+            V3 u = v[1] - v[0], vv = v[2] - v[0];
+            V3 nn = cross(u, vv);
+            float nl = dot(nn, nn);
+            V3 w = center - v[0];
+            float gamma = dot(cross(u, w), nn) / nl;
+            float beta = dot(cross(w, vv), nn) / nl;
+            float alpha = 1 - gamma - beta;
+            bool inside = (0 <= alpha) && (alpha <= 1) && (0 <= beta) && (beta <= 1) && (0 <= gamma) && (gamma <= 1);
+            if (inside) {
+                has = true;
+                cpnt = center - n * dfp;
+            } else {
+                V3 res = closest_point_triangle(center, v[0], v[1], v[2]);
+                float dsq = len2(res - center);
+                if (dsq < rwt * rwt) { has = true; cpnt = res; }
+            }
+        }
+    }
+    if (has) {
+        V3 c2 = center - cpnt;
+        float dsq = len2(c2);
+        if (dsq < rwt * rwt) {
+            if (dsq > SIMD_EPS) {
+                float d = sqrtf(dsq);
+                normal_out = normalized(c2);
+                point = cpnt;
+                depth = -(radius - d);
+            } else {
+                normal_out = n;
+                point = cpnt;
+                depth = -radius;
+            }
+            return true;
+        }
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------- contact-added callback
+RSG_D void push_event(Ctx& a, uint32_t kind, uint32_t x, uint32_t y, uint32_t flag) {
+    if (!((a.event_mask >> kind) & 1u) || a.ev == nullptr) return;
+    if (a.nevents >= MAX_EVENTS_PER_ARENA) {
+        a.err |= ERR_EVENT_OVERFLOW;
+        return;
+    }
+    DevEvent& e = a.ev[a.nevents++];
+    e.kind = kind;
+    e.tick_lo = (uint32_t)a.tick;
+    e.tick_hi = (uint32_t)(a.tick >> 32);
+    e.a = x;
+    e.b = y;
+    e.flag = flag;
+}
+
+// Arena::_BulletContactAddedCallback (src/Sim/Arena/Arena.cpp:244-414) for the point stored in
+// manifold m at index idx; `tri` is the mesh triangle or -1.
+RSG_DN void contact_added(const BatchView& bv, Ctx& a, Manifold& m, int idx, int tri) {
+    MPoint& cp = a.pts[m.pt[idx]];
+    int A = m.body0, B = m.body1;
+    auto user_index = [](int o) { return o == OBJ_BALL ? 2 : (o >= OBJ_CAR0 ? 1 : -1); };
+    auto responds = [&](int o) { return is_static_obj(o) ? true : !a.body(o).no_contact_response; };
+    if (!responds(A) || !responds(B)) return;
+    int ua = user_index(A), ub = user_index(B);
+    bool swap;
+    if (ua != -1 && ub != -1) swap = ua > ub;
+    else swap = ub != -1;
+    if (swap) {
+        int t = A; A = B; B = t;
+        t = ua; ua = ub; ub = t;
+    }
+    if (ua == 1) {
+        Car& car = a.cars[A - OBJ_CAR0];
+        if (ub == 2) {
+            // car-ball: Ball::_OnHit (src/Sim/Ball/Ball.cpp:237-289)
+            V3 rel_ball = (swap ? cp.local_a : cp.local_b) * RL::BT_TO_UU;
+            V3 car_pos = car.rb.xf.o * RL::BT_TO_UU, car_vel = car.rb.lin_vel * RL::BT_TO_UU;
+            V3 ball_pos = a.ball.xf.o * RL::BT_TO_UU, ball_vel = a.ball.lin_vel * RL::BT_TO_UU;
+            cp.friction = RL::CARBALL_COLLISION_FRICTION;
+            cp.restitution = RL::CARBALL_COLLISION_RESTITUTION;
+            car.setf(F_BHI_VALID, true);
+            car.bhi_rel = rel_ball;
+            car.bhi_hit = a.tick;
+            car.bhi_ballpos = ball_pos;
+            car.bhi_extra = V3(0, 0, 0);
+            push_event(a, RSG_EVENT_BALL_HIT, car.id, 0, 0);
+            if ((a.tick > car.bhi_extra_tick + 1) || (car.bhi_extra_tick > a.tick)) {
+                car.bhi_extra_tick = a.tick;
+                V3 cf = car.fwd();
+                V3 rel_pos = ball_pos - car_pos;
+                V3 rel_vel = ball_vel - car_vel;
+                float rs = rs_minf(rs_len(rel_vel), RL::BALL_CAR_EXTRA_IMPULSE_MAXDELTAVEL_UU);
+                if (rs > 0) {
+                    V3 hit = rs_normalized(rel_pos * V3(1, 1, RL::BALL_CAR_EXTRA_IMPULSE_Z_SCALE));
+                    V3 adj = cf * dot(hit, cf) * (1 - RL::BALL_CAR_EXTRA_IMPULSE_FORWARD_SCALE);
+                    hit = rs_normalized(hit - adj);
+                    V3 added = (hit * rs) * curve_eval(c_curves[CV_BALL_EXTRA], rs) * 1.f;
+                    car.bhi_extra = added;
+                    a.ball_cache += added * RL::UU_TO_BT;
+                }
+            }
+        } else if (ub == 1) {
+            // car-car: Arena::_BtCallback_OnCarCarCollision (src/Sim/Arena/Arena.cpp:323-405)
+            Car* c1 = &car;
+            Car* c2 = &a.cars[B - OBJ_CAR0];
+            cp.friction = RL::CARCAR_COLLISION_FRICTION;
+            cp.restitution = RL::CARCAR_COLLISION_RESTITUTION;
+            for (int i = 0; i < 2; i++) {
+                bool sw = i == 1;
+                if (sw) { Car* t = c1; c1 = c2; c2 = t; }
+                Car& s = *c1;
+                Car& o = *c2;
+                if (s.f(F_DEMOED) || o.f(F_DEMOED)) return;
+                if (s.cc_other == o.id && s.cc_cooldown > 0) continue;
+                V3 spos = s.rb.xf.o * RL::BT_TO_UU, svel = s.rb.lin_vel * RL::BT_TO_UU;
+                V3 opos = o.rb.xf.o * RL::BT_TO_UU, ovel = o.rb.lin_vel * RL::BT_TO_UU;
+                V3 dp = opos - spos;
+                if (dot(svel, dp) > 0) {
+                    V3 vd = rs_normalized(svel);
+                    V3 dir = rs_normalized(dp);
+                    float sto = dot(svel, dir);
+                    float oas = dot(ovel, vd);
+                    if (sto > oas) {
+                        V3 lp = sw ? cp.local_b : cp.local_a;
+                        bool bumper = (lp.x * RL::BT_TO_UU) > RL::BUMP_MIN_FORWARD_DIST;
+                        if (bumper) {
+                            bool demo = s.f(F_SUPERSONIC);
+                            if (demo) demo = s.f(F_TEAM_ORANGE) != o.f(F_TEAM_ORANGE);
+                            if (demo) {
+                                o.setf(F_DEMOED, true);
+                                o.demo_timer = RL::DEMO_RESPAWN_TIME;
+                            } else {
+                                bool gh = o.f(F_ON_GROUND);
+                                float bs = curve_eval(c_curves[gh ? CV_BUMP_GROUND : CV_BUMP_AIR], sto);
+                                V3 hu = gh ? o.up() : V3(0, 0, 1);
+                                V3 bi = vd * bs + hu * curve_eval(c_curves[CV_BUMP_UP], sto) * 1.f;
+                                o.vel_cache += bi * RL::UU_TO_BT;
+                            }
+                            s.cc_other = o.id;
+                            s.cc_cooldown = RL::BUMP_COOLDOWN_TIME;
+                            push_event(a, RSG_EVENT_BUMP, s.id, o.id, demo ? 1u : 0u);
+                        }
+                    }
+                }
+            }
+        } else {
+            // car-world (src/Sim/Arena/Arena.cpp:407-414)
+            car.setf(F_WC_CONTACT, true);
+            car.wc_normal = cp.normal;
+            cp.friction = RL::CARWORLD_COLLISION_FRICTION;
+            cp.restitution = RL::CARWORLD_COLLISION_RESTITUTION;
+        }
+    } else if (ua == 2 && ub == -1) {
+        cp.special = true;  // ball-world (src/Sim/Arena/Arena.cpp:298-306)
+    }
+    if (tri >= 0) adjust_internal_edge(bv.mesh, cp, tri);
+}
+
+// btManifoldResult::calculateCombined{Friction,Restitution} as RocketSim patches them
+RSG_D float obj_friction(Ctx& a, int o) { return is_static_obj(o) ? RL::ARENA_COLLISION_BASE_FRICTION : a.body(o).friction; }
+RSG_D float obj_restitution(Ctx& a, int o) { return is_static_obj(o) ? RL::ARENA_COLLISION_BASE_RESTITUTION : a.body(o).restitution; }
+RSG_D float combined_friction(Ctx& a, int o0, int o1) {
+    float x = obj_friction(a, o0), y = obj_friction(a, o1);
+    if (is_static_obj(o0) || is_static_obj(o1)) return x < y ? x : y;
+    return x * y;
+}
+RSG_D float combined_restitution(Ctx& a, int o0, int o1) {
+    float x = obj_restitution(a, o0), y = obj_restitution(a, o1);
+    if (is_static_obj(o0) || is_static_obj(o1)) return x > y ? x : y;
+    return x * y;
+}
+RSG_D Xf obj_xf(Ctx& a, int o) {
+    if (o < OBJ_BALL) {
+        Xf t = xf_identity();
+        t.o = static_origin(o);
+        return t;
+    }
+    return a.body(o).xf;
+}
+
+// Convex object (ball sphere or car box) against the arena mesh: btConvexConcaveCollisionAlgorithm
+// (B/.../CollisionDispatch/btConvexConcaveCollisionAlgorithm.cpp:71-250)
+RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, const Xf& conv_xf, const Convex& cshape) {
+    V3 mn, mx;
+    cshape.aabb(conv_xf, mn, mx);
+    Xf x0 = a.body(m.body0).xf, x1 = obj_xf(a, m.body1);
+    float fr = combined_friction(a, OBJ_MESH, conv), re = combined_restitution(a, OBJ_MESH, conv);
+    M3 inv_basis = inverse(conv_xf.b);
+    mesh_query_aabb(bv.mesh, mn, mx, [&](int t) {
+        V3 tv[3];
+        tri_load(bv.mesh, t, tv);
+        // TestTriangleAgainstAabb2 (z, x, y)
+        const int ord[3] = {2, 0, 1};
+        for (int q = 0; q < 3; q++) {
+            int k = ord[q];
+            float lo = fminf(fminf(tv[0][k], tv[1][k]), tv[2][k]);
+            float hi = fmaxf(fmaxf(tv[0][k], tv[1][k]), tv[2][k]);
+            if (lo > mx[k]) return;
+            if (hi < mn[k]) return;
+        }
+        {  // early out on the triangle plane
+            V3 tn = normalized(cross(tv[1] - tv[0], tv[2] - tv[0]));
+            float thr = m.breaking;
+            for (int side = 0; side < 2; side++) {
+                V3 dir = side ? -tn : tn;
+                V3 ld = inv_basis * dir;
+                V3 lp;
+                if (cshape.type == 1) {
+                    V3 vn = ld;
+                    if (len2(vn) < SIMD_EPS * SIMD_EPS) vn = normalized(V3(-1, -1, -1));
+                    else vn = normalized(vn);
+                    lp = cshape.margin * vn;
+                } else {
+                    V3 hm = cshape.he + V3(cshape.margin, cshape.margin, cshape.margin);
+                    lp = V3(ld.x >= 0 ? hm.x : -hm.x, ld.y >= 0 ? hm.y : -hm.y, ld.z >= 0 ? hm.z : -hm.z);
+                }
+                V3 wp = xf_apply(conv_xf, lp);
+                float pp = dot(dir, wp), pt = dot(dir, tv[0]);
+                if (pt - pp > thr) return;
+            }
+        }
+        if (cshape.type == 1) {
+            V3 point, nrm;
+            float depth;
+            if (sphere_triangle(conv_xf.o, cshape.margin, tv, m.breaking, point, nrm, depth)) {
+                int idx = add_point(a, m, x0, x1, nrm, point, depth, fr, re);
+                if (idx >= 0) contact_added(bv, a, m, idx, t);
+            }
+        } else {
+            Convex tri;
+            tri.type = 2;
+            tri.margin = 0.f;
+            tri.he = V3(0, 0, 0);
+            for (int k = 0; k < 3; k++) tri.tv[k] = tv[k];
+            float md = cshape.margin + tri.margin + m.breaking;
+            GjkOut g = gjk(cshape, conv_xf, tri, xf_identity(), md * md);
+            if (g.epa_needed) a.err |= WARN_EPA_SKIPPED;
+            if (g.valid) {
+                int idx = add_point(a, m, x0, x1, g.normal, g.point_on_b, g.dist, fr, re);
+                if (idx >= 0) contact_added(bv, a, m, idx, t);
+            }
+        }
+    });
+    refresh(a, m, x0, x1);
+}
+
+// btConvexPlaneCollisionAlgorithm::processCollision (B/.../btConvexPlaneCollisionAlgorithm.cpp:94-161)
+RSG_DN void convex_vs_plane(const BatchView& bv, Ctx& a, Manifold& m, const Xf& conv_xf, const Convex& cshape, int plane_obj) {
+    PlaneC pl;
+    plane_const(plane_obj - OBJ_PLANE0, pl);
+    Xf pxf = xf_identity();
+    pxf.o = pl.origin;
+    Xf plane_in_convex = xf_mul(xf_inverse(conv_xf), pxf);
+    Xf convex_in_plane = xf_mul(xf_inverse(pxf), conv_xf);
+    V3 dir = plane_in_convex.b * (-pl.n);
+    V3 vtx;
+    if (cshape.type == 1) {
+        V3 vn = dir;
+        if (len2(vn) < SIMD_EPS * SIMD_EPS) vn = normalized(V3(-1, -1, -1));
+        else vn = normalized(vn);
+        vtx = cshape.margin * vn;
+    } else {
+        V3 hm = cshape.he + V3(cshape.margin, cshape.margin, cshape.margin);
+        vtx = V3(dir.x >= 0 ? hm.x : -hm.x, dir.y >= 0 ? hm.y : -hm.y, dir.z >= 0 ? hm.z : -hm.z);
+    }
+    V3 vip = xf_apply(convex_in_plane, vtx);
+    float distance = dot(pl.n, vip) - 0.f;
+    Xf x0 = a.body(m.body0).xf, x1 = pxf;
+    if (distance < m.breaking) {
+        V3 proj = vip - distance * pl.n;
+        V3 pw = xf_apply(pxf, proj);
+        V3 nw = pxf.b * pl.n;
+        int conv = m.body0;
+        float fr = combined_friction(a, plane_obj, conv), re = combined_restitution(a, plane_obj, conv);
+        int idx = add_point(a, m, x0, x1, nw, pw, distance, fr, re);
+        if (idx >= 0) contact_added(bv, a, m, idx, -1);
+    }
+    if (m.n) refresh(a, m, x0, x1);
+}
+
+// btAlignedObjectArray::quickSortInternal (B/LinearMath/btAlignedObjectArray.h:370-400) over manifold
+// indices keyed by island id; sub-ranges are disjoint, so an explicit stack gives the same result.
+RSG_D void island_quicksort(const Ctx& a, int* v, int n) {
+    int stk_lo[MAX_MANIFOLDS], stk_hi[MAX_MANIFOLDS];
+    int sp = 0;
+    stk_lo[sp] = 0;
+    stk_hi[sp] = n - 1;
+    sp++;
+    while (sp > 0) {
+        sp--;
+        int lo = stk_lo[sp], hi = stk_hi[sp];
+        int i = lo, j = hi;
+        int x = a.man[v[(lo + hi) / 2]].island;
+        do {
+            while (a.man[v[i]].island < x) i++;
+            while (x < a.man[v[j]].island) j--;
+            if (i <= j) {
+                int t = v[i]; v[i] = v[j]; v[j] = t;
+                i++;
+                j--;
+            }
+        } while (i <= j);
+        if (lo < j) { stk_lo[sp] = lo; stk_hi[sp] = j; sp++; }
+        if (i < hi) { stk_lo[sp] = i; stk_hi[sp] = hi; sp++; }
+    }
+}
+
+// ---------------------------------------------------------------- solver
+// btSequentialImpulseConstraintSolver (B/BulletDynamics/ConstraintSolver/btSequentialImpulseConstraintSolver.cpp)
+// in RocketSim's configuration: 10 iterations, split impulse, no warm starting (manifolds are rebuilt
+// every tick), one friction direction, erp2 0.8.
+constexpr int SB_FIXED = MAX_CARS + 1;
+struct SBody {
+    int obj;  // -1 fixed body
+    V3 dlv, dav, push, turn;
+    float inv_mass;
+    V3 lv, av, ext_f, ext_t;
+    Xf xf;
+};
+struct Row {
+    int8_t ba, bb, special;
+    int16_t friction_index;
+    V3 n1, n2, rp1xn, rp2xn, angA, angB;
+    float jac_inv, rhs, rhs_pen, cfm, lo, hi, applied, applied_push, friction;
+};
+struct Solver {
+    SBody b[MAX_CARS + 2];
+    int nc, nf;
+    Row c[MAX_ROWS], f[MAX_ROWS];
+};
+
+RSG_D void init_solver_body(Ctx& a, SBody& sb, int obj, float dt) {
+    Body& b = a.body(obj);
+    sb.obj = obj;
+    sb.xf = b.xf;
+    sb.inv_mass = b.inv_mass;
+    sb.lv = b.lin_vel;
+    sb.av = b.ang_vel;
+    sb.ext_f = b.total_force * b.inv_mass * dt;
+    sb.ext_t = b.total_torque * b.inv_inertia_world * dt;
+    sb.dlv = sb.dav = sb.push = sb.turn = V3(0, 0, 0);
+}
+
+RSG_D void setup_contact_row(Ctx& a, Solver& s, Row& r, int ia, int ib, const MPoint& cp, V3 rel1, V3 rel2, float dt) {
+    SBody& A = s.b[ia];
+    SBody& B = s.b[ib];
+    Body* rb0 = A.obj >= 0 ? &a.body(A.obj) : nullptr;
+    Body* rb1 = B.obj >= 0 ? &a.body(B.obj) : nullptr;
+    float inv_dt = 1.f / dt;
+    float cfm = 0.f * inv_dt;
+    const float erp = 0.8f;  // m_erp2 (src/Sim/Arena/Arena.cpp:473-475)
+    V3 ta0 = cross(rel1, cp.normal);
+    r.angA = rb0 ? rb0->inv_inertia_world * ta0 : V3(0, 0, 0);
+    V3 ta1 = cross(rel2, cp.normal);
+    r.angB = rb1 ? rb1->inv_inertia_world * (-ta1) : V3(0, 0, 0);
+    float d0 = 0, d1 = 0;
+    if (rb0) { V3 v = cross(r.angA, rel1); d0 = rb0->inv_mass + dot(cp.normal, v); }
+    if (rb1) { V3 v = cross(-r.angB, rel2); d1 = rb1->inv_mass + dot(cp.normal, v); }
+    r.jac_inv = 1.f / (d0 + d1 + cfm);
+    if (rb0) { r.n1 = cp.normal; r.rp1xn = ta0; } else { r.n1 = V3(0, 0, 0); r.rp1xn = V3(0, 0, 0); }
+    if (rb1) { r.n2 = -cp.normal; r.rp2xn = -ta1; } else { r.n2 = V3(0, 0, 0); r.rp2xn = V3(0, 0, 0); }
+    float restitution = 0.f;
+    float penetration = cp.dist + 0.f;
+    {
+        V3 v1 = rb0 ? rb0->vel_at(rel1) : V3(0, 0, 0);
+        V3 v2 = rb1 ? rb1->vel_at(rel2) : V3(0, 0, 0);
+        float rel_vel = dot(cp.normal, v1 - v2);
+        r.friction = cp.friction;
+        if (fabsf(rel_vel) < 0.2f) restitution = 0.f;  // restitutionCurve, threshold 0.2
+        else restitution = cp.restitution * -rel_vel;
+        if (restitution <= 0.f) restitution = 0.f;
+    }
+    r.applied = 0.f * 0.85f;
+    r.applied_push = 0.f;
+    {
+        V3 efA = A.obj >= 0 ? A.ext_f : V3(0, 0, 0), etA = A.obj >= 0 ? A.ext_t : V3(0, 0, 0);
+        V3 efB = B.obj >= 0 ? B.ext_f : V3(0, 0, 0), etB = B.obj >= 0 ? B.ext_t : V3(0, 0, 0);
+        float v1 = dot(r.n1, A.lv + efA) + dot(r.rp1xn, A.av + etA);
+        float v2 = dot(r.n2, B.lv + efB) + dot(r.rp2xn, B.av + etB);
+        float rel_vel = v1 + v2;
+        float pos_err = 0.f;
+        float vel_err = restitution - rel_vel;
+        if (penetration > 0) pos_err = 0;
+        else pos_err = -penetration * erp * inv_dt;
+        float pen_imp = pos_err * r.jac_inv;
+        float vel_imp = vel_err * r.jac_inv;
+        if (penetration > 1.0e30f) {  // split impulse threshold 1e30 (src/Sim/Arena/Arena.cpp:474)
+            r.rhs = pen_imp + vel_imp;
+            r.rhs_pen = 0.f;
+        } else {
+            r.rhs = vel_imp;
+            r.rhs_pen = pen_imp;
+        }
+        r.cfm = cfm * r.jac_inv;
+        r.lo = 0;
+        r.hi = 1e10f;
+    }
+    r.special = cp.special;
+}
+
+RSG_D void setup_friction_row(Ctx& a, Solver& s, Row& r, V3 n, int ia, int ib, float friction, V3 rel1, V3 rel2) {
+    SBody& A = s.b[ia];
+    SBody& B = s.b[ib];
+    Body* b0 = A.obj >= 0 ? &a.body(A.obj) : nullptr;
+    Body* b1 = B.obj >= 0 ? &a.body(B.obj) : nullptr;
+    r.ba = (int8_t)ia;
+    r.bb = (int8_t)ib;
+    r.special = 0;
+    r.friction = friction;
+    r.applied = 0;
+    r.applied_push = 0;
+    if (b0) {
+        r.n1 = n;
+        V3 t = cross(rel1, r.n1);
+        r.rp1xn = t;
+        r.angA = b0->inv_inertia_world * t;
+    } else {
+        r.n1 = r.rp1xn = r.angA = V3(0, 0, 0);
+    }
+    if (b1) {
+        r.n2 = -n;
+        V3 t = cross(rel2, r.n2);
+        r.rp2xn = t;
+        r.angB = b1->inv_inertia_world * t;
+    } else {
+        r.n2 = r.rp2xn = r.angB = V3(0, 0, 0);
+    }
+    float d0 = 0, d1 = 0;
+    if (b0) { V3 v = cross(r.angA, rel1); d0 = b0->inv_mass + dot(n, v); }
+    if (b1) { V3 v = cross(-r.angB, rel2); d1 = b1->inv_mass + dot(n, v); }
+    r.jac_inv = 1.f / (d0 + d1);
+    float v1 = dot(r.n1, b0 ? A.lv + A.ext_f : V3(0, 0, 0)) + dot(r.rp1xn, b0 ? A.av : V3(0, 0, 0));
+    float v2 = dot(r.n2, b1 ? B.lv + B.ext_f : V3(0, 0, 0)) + dot(r.rp2xn, b1 ? B.av : V3(0, 0, 0));
+    float rel_vel = v1 + v2;
+    float vel_imp = (0.f - rel_vel) * r.jac_inv;
+    r.rhs = 0.f + vel_imp;
+    r.rhs_pen = 0.f;
+    r.cfm = 0.f;
+    r.lo = -r.friction;
+    r.hi = r.friction;
+}
+
+// convertContactInner friction part (btSequentialImpulseConstraintSolver.cpp:1071-1162)
+RSG_D void add_friction(Ctx& a, Solver& s, int ia, int ib, V3 normal, float friction, V3 rel1, V3 rel2, int fidx) {
+    SBody& A = s.b[ia];
+    SBody& B = s.b[ib];
+    V3 v1 = A.obj >= 0 ? A.lv + A.ext_f + cross(A.av + A.ext_t, rel1) : V3(0, 0, 0);
+    V3 v2 = B.obj >= 0 ? B.lv + B.ext_f + cross(B.av + B.ext_t, rel2) : V3(0, 0, 0);
+    V3 vel = v1 - v2;
+    float rel_vel = dot(normal, vel);
+    V3 lat = vel - normal * rel_vel;
+    float lat2 = len2(lat);
+    V3 dir;
+    if (lat2 > SIMD_EPS) {
+        dir = lat * (1.f / sqrtf(lat2));
+    } else {
+        V3 d2;
+        plane_space(normal, dir, d2);
+    }
+    Row& fr = s.f[s.nf++];
+    fr.friction_index = (int16_t)fidx;
+    setup_friction_row(a, s, fr, dir, ia, ib, friction, rel1, rel2);
+}
+
+RSG_D void solve_row(Solver& s, Row& c, bool lower_only) {  // gResolveSingleConstraintRow{Generic,LowerLimit}
+    SBody& A = s.b[c.ba];
+    SBody& B = s.b[c.bb];
+    float d = c.rhs - c.applied * c.cfm;
+    float d1 = simd_dot(c.n1, A.dlv) + simd_dot(c.rp1xn, A.dav);
+    float d2 = simd_dot(c.n2, B.dlv) + simd_dot(c.rp2xn, B.dav);
+    d -= d1 * c.jac_inv;
+    d -= d2 * c.jac_inv;
+    float sum = c.applied + d;
+    if (sum < c.lo) { d = c.lo - c.applied; c.applied = c.lo; }
+    else if (!lower_only && sum > c.hi) { d = c.hi - c.applied; c.applied = c.hi; }
+    else c.applied = sum;
+    if (A.obj >= 0) { A.dlv += c.n1 * A.inv_mass * d; A.dav += c.angA * d; }
+    if (B.obj >= 0) { B.dlv += c.n2 * B.inv_mass * d; B.dav += c.angB * d; }
+}
+
+RSG_D float solve_split(Solver& s, Row& c) {  // gResolveSplitPenetrationImpulse_sse2
+    if (!c.rhs_pen) return 0.f;
+    SBody& A = s.b[c.ba];
+    SBody& B = s.b[c.bb];
+    float d = c.rhs_pen - c.applied_push * c.cfm;
+    float d1 = simd_dot(c.n1, A.push) + simd_dot(c.rp1xn, A.turn);
+    float d2 = simd_dot(c.n2, B.push) + simd_dot(c.rp2xn, B.turn);
+    d -= d1 * c.jac_inv;
+    d -= d2 * c.jac_inv;
+    float sum = c.applied_push + d;
+    if (sum < c.lo) { d = c.lo - c.applied_push; c.applied_push = c.lo; }
+    else c.applied_push = sum;
+    if (A.obj >= 0) { A.push += c.n1 * A.inv_mass * d; A.turn += c.angA * d; }
+    if (B.obj >= 0) { B.push += c.n2 * B.inv_mass * d; B.turn += c.angB * d; }
+    return (float)((double)d * (1. / (double)c.jac_inv));
+}
+
+// Solves one batch: `bodies` are dynamic object ids in island order, `mans` manifold indices in
+// sorted island order (btSequentialImpulseConstraintSolver::solveGroup)
+RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, float dt) {
+    Solver s;
+    s.nc = s.nf = 0;
+    int sb_of[MAX_CARS + 1];
+    for (int i = 0; i <= MAX_CARS; i++) sb_of[i] = -1;
+    for (int i = 0; i < nb; i++) {
+        init_solver_body(a, s.b[i], bodies[i], dt);
+        sb_of[bodies[i] - OBJ_BALL] = i;
+    }
+    SBody& fixed = s.b[SB_FIXED];
+    fixed.obj = -1;
+    fixed.xf = xf_identity();
+    fixed.inv_mass = 0;
+    fixed.dlv = fixed.dav = fixed.push = fixed.turn = fixed.lv = fixed.av = fixed.ext_f = fixed.ext_t = V3(0, 0, 0);
+    auto sbi = [&](int o) { return is_static_obj(o) ? SB_FIXED : sb_of[o - OBJ_BALL]; };
+    for (int mi = 0; mi < nm; mi++) {
+        Manifold& m = a.man[mans[mi]];
+        int ia = sbi(m.body0), ib = sbi(m.body1);
+        if (ia < 0 || ib < 0) continue;
+        for (int j = 0; j < m.n; j++) {
+            const MPoint& cp = a.pts[m.pt[j]];
+            if (!(cp.dist <= BT_LARGE)) continue;
+            if (s.nc >= MAX_ROWS) { a.err |= ERR_ROW_OVERFLOW; continue; }
+            Row& r = s.c[s.nc];
+            r.ba = (int8_t)ia;
+            r.bb = (int8_t)ib;
+            V3 rel1 = cp.pos_a - obj_xf(a, m.body0).o;
+            V3 rel2 = cp.pos_b - obj_xf(a, m.body1).o;
+            setup_contact_row(a, s, r, ia, ib, cp, rel1, rel2, dt);
+            r.friction_index = (int16_t)s.nf;
+            if (cp.special) {
+                for (int k = 0; k < 2; k++) {
+                    int o = k ? m.body1 : m.body0;
+                    if (!is_static_obj(o)) {
+                        Body& b = a.body(o);
+                        b.n_special++;
+                        b.sp_friction = cp.friction;
+                        b.sp_restitution = cp.restitution;
+                        b.sp_total_normal += cp.normal;
+                        b.sp_total_dist += len(k ? rel2 : rel1);
+                    }
+                }
+            }
+            int fidx = s.nc++;
+            add_friction(a, s, ia, ib, cp.normal, cp.friction, rel1, rel2, fidx);
+        }
+    }
+    // RocketSim's averaged ball-world contact (convertContactSpecial,
+    // btSequentialImpulseConstraintSolver.cpp:1164-1211)
+    for (int i = 0; i < nb; i++) {
+        Body& b = a.body(bodies[i]);
+        if (b.n_special > 0) {
+            float dist = b.sp_total_dist / b.n_special;
+            V3 nrm = b.sp_total_normal / (float)b.n_special;
+            MPoint tmp;
+            tmp.dist = dist;
+            tmp.normal = nrm;
+            tmp.friction = b.sp_friction;
+            tmp.restitution = b.sp_restitution;
+            tmp.special = false;
+            if (s.nc < MAX_ROWS) {
+                Row& r = s.c[s.nc];
+                r.ba = (int8_t)i;
+                r.bb = (int8_t)SB_FIXED;
+                V3 rel1 = nrm * -dist, rel2(0, 0, 0);
+                setup_contact_row(a, s, r, i, SB_FIXED, tmp, rel1, rel2, dt);
+                int fidx = s.nc;
+                r.friction_index = (int16_t)s.nf;
+                s.nc++;
+                add_friction(a, s, i, SB_FIXED, tmp.normal, tmp.friction, rel1, rel2, fidx);
+            } else {
+                a.err |= ERR_ROW_OVERFLOW;
+            }
+            b.n_special = 0;
+            b.sp_friction = b.sp_restitution = b.sp_total_dist = 0;
+            b.sp_total_normal = V3(0, 0, 0);
+        }
+    }
+    const int ITER = 10;
+    for (int it = 0; it < ITER; it++) {
+        float lsr = 0;
+        for (int k = 0; k < s.nc; k++) {
+            float res = solve_split(s, s.c[k]);
+            float r2 = res * res;
+            lsr = lsr < r2 ? r2 : lsr;
+        }
+        if (lsr <= 0.f || it >= ITER - 1) break;
+    }
+    for (int it = 0; it < ITER; it++) {
+        for (int k = 0; k < s.nc; k++) {
+            if (s.c[k].special) continue;
+            solve_row(s, s.c[k], true);
+        }
+        for (int k = 0; k < s.nf; k++) {
+            Row& f = s.f[k];
+            float total = s.c[f.friction_index].applied;
+            if (total > 0.f) {
+                f.lo = -(f.friction * total);
+                f.hi = f.friction * total;
+                solve_row(s, f, false);
+            }
+        }
+    }
+    // writeBackBodies (btSequentialImpulseConstraintSolver.cpp:1878-1904)
+    for (int i = 0; i < nb; i++) {
+        SBody& sb = s.b[i];
+        Body& b = a.body(sb.obj);
+        sb.lv += sb.dlv;
+        sb.av += sb.dav;
+        if (sb.push.x != 0.f || sb.push.y != 0 || sb.push.z != 0 || sb.turn.x != 0.f || sb.turn.y != 0 || sb.turn.z != 0) {
+            Xf nt;
+            integrate_transform(sb.xf, sb.push, sb.turn * 0.1f, dt, b.no_rot, nt);
+            sb.xf = nt;
+        }
+        b.lin_vel = sb.lv + sb.ext_f;
+        b.ang_vel = sb.av + sb.ext_t;
+        b.xf = sb.xf;
+    }
+}
+
+// ---------------------------------------------------------------- world step
+// btDiscreteDynamicsWorld::stepSimulation with one fixed substep as RocketSim drives it
+// (src/Sim/Arena/Arena.cpp:731, B/BulletDynamics/Dynamics/btDiscreteDynamicsWorld.cpp:360-450)
+RSG_D uint32_t grid_cell_index(const DevGrid& g, int i, int j, int k) { return (uint32_t)(i * g.ny * g.nz + j * g.nz + k); }
+
+RSG_D void update_bp_aabb(const BatchView& bv, Ctx& a, int obj) {  // updateSingleAabb + btRSBroadphase::setAabb
+    V3 mn, mx, mn2, mx2;
+    Body& b = a.body(obj);
+    if (obj == OBJ_BALL) {
+        ball_aabb(b.xf, mn, mx);
+        ball_aabb(b.interp, mn2, mx2);
+    } else {
+        Car& c = a.cars[obj - OBJ_CAR0];
+        car_compound_aabb(c, b.xf, mn, mx);
+        car_compound_aabb(c, b.interp, mn2, mx2);
+    }
+    V3 th(0.02f, 0.02f, 0.02f);
+    mn -= th; mx += th;
+    mn2 -= th; mx2 += th;
+    mn = vmin(mn, mn2);
+    mx = vmax(mx, mx2);
+    b.bp_min = mn;
+    b.bp_max = mx;
+    int i, j, k;
+    grid_idx(bv.grid, mn, i, j, k);
+    uint32_t nidx = grid_cell_index(bv.grid, i, j, k);
+    if (b.cell != nidx) {
+        b.cell = nidx;
+        b.ci = i; b.cj = j; b.ck = k;
+        b.cell_seq = a.seq++;
+    }
+}
+
+RSG_D bool has_pair(const Ctx& a, int x, int y) {
+    for (int p = 0; p < a.npairs; p++)
+        if ((a.pair0[p] == x && a.pair1[p] == y) || (a.pair0[p] == y && a.pair1[p] == x)) return true;
+    return false;
+}
+RSG_D void add_pair(Ctx& a, int x, int y) {
+    if (a.npairs >= MAX_PAIRS) { a.err |= ERR_PAIR_OVERFLOW; return; }
+    a.pair0[a.npairs] = (int8_t)x;
+    a.pair1[a.npairs] = (int8_t)y;
+    a.npairs++;
+}
+RSG_D Manifold& new_manifold(Ctx& a, int b0, int b1, float breaking) {
+    Manifold& m = a.man[a.nman++];
+    m.body0 = (int8_t)b0;
+    m.body1 = (int8_t)b1;
+    m.n = 0;
+    m.island = -1;
+    m.breaking = breaking;
+    return m;
+}
+
+RSG_DN void step_world(const BatchView& bv, Ctx& a) {
+    const float dt = bv.dt;
+    const int nd = 1 + a.ncars;  // dynamic objects: ball, then cars in AddCar order
+    // applyGravity (btDiscreteDynamicsWorld.cpp:265-277)
+    for (int d = 0; d < nd; d++) {
+        Body& b = a.body(OBJ_BALL + d);
+        if (b.is_active()) b.total_force += V3(0, 0, RL::GRAVITY_Z * RL::UU_TO_BT) * (1.f / b.inv_mass);
+    }
+    // predictUnconstraintMotion (btDiscreteDynamicsWorld.cpp:1029-1044)
+    for (int d = 0; d < nd; d++) {
+        Body& b = a.body(OBJ_BALL + d);
+        b.lin_vel *= powf(1.f - b.lin_damping, dt);
+        b.ang_vel *= powf(1.f - 0.f, dt);
+        integrate_transform(b.xf, b.lin_vel, b.ang_vel, dt, b.no_rot, b.interp);
+    }
+    for (int d = 0; d < nd; d++) update_bp_aabb(bv, a, OBJ_BALL + d);
+    // calculateOverlappingPairs (btRSBroadphase.cpp:392-468)
+    a.npairs = 0;
+    V3 mesh_mn, mesh_mx;
+    if (bv.has_arena) {
+        mesh_aabb(bv.mesh, mesh_mn, mesh_mx);
+        mesh_mn -= V3(0.02f, 0.02f, 0.02f);
+        mesh_mx += V3(0.02f, 0.02f, 0.02f);
+    }
+    for (int d = 0; d < nd; d++) {
+        int o = OBJ_BALL + d;
+        Body& b = a.body(o);
+        if (bv.has_arena) {
+            if (bv.mesh.cells[b.cell] && aabb_overlap(b.bp_min, b.bp_max, mesh_mn, mesh_mx))
+                if (!has_pair(a, OBJ_MESH, o)) add_pair(a, OBJ_MESH, o);
+            for (int p = 0; p < 4; p++) {
+                PlaneC pl;
+                plane_const(p, pl);
+                if (aabb_overlap(b.bp_min, b.bp_max, pl.bp_min, pl.bp_max))
+                    if (!has_pair(a, OBJ_PLANE0 + p, o)) add_pair(a, OBJ_PLANE0 + p, o);
+            }
+        }
+        int cd[MAX_CARS + 1];
+        int ncd = cell_dyn_list(a, b.ci, b.cj, b.ck, cd);
+        if (ncd > 1) {
+            for (int qi = 0; qi < ncd; qi++) {
+                int q = cd[qi];
+                if (q == o) continue;
+                Body& bq = a.body(q);
+                if (aabb_overlap(b.bp_min, b.bp_max, bq.bp_min, bq.bp_max) && !has_pair(a, o, q))
+                    add_pair(a, o < q ? o : q, o < q ? q : o);
+            }
+        }
+    }
+    // dispatchAllCollisionPairs: one manifold per pair with a collision algorithm, in pair order
+    a.nman = 0;
+    a.npts = 0;
+    for (int pi = 0; pi < a.npairs; pi++) {
+        int o0 = a.pair0[pi], o1 = a.pair1[pi];
+        bool act0 = is_static_obj(o0) ? false : a.body(o0).is_active();
+        bool act1 = a.body(o1).is_active();
+        if (!act0 && !act1) continue;  // btCollisionDispatcher::needsCollision
+        if (is_static_obj(o0)) {
+            if (o1 == OBJ_BALL) {
+                Convex sph;
+                sph.type = 1;
+                sph.margin = BALL_RADIUS_BT;
+                sph.he = V3(0, 0, 0);
+                Manifold& m = new_manifold(a, OBJ_BALL, o0, (BALL_RADIUS_BT + 0.08f) * 0.02f);
+                if (o0 == OBJ_MESH) convex_vs_mesh(bv, a, m, OBJ_BALL, a.ball.xf, sph);
+                else convex_vs_plane(bv, a, m, a.ball.xf, sph, o0);
+            } else {
+                Car& c = a.cars[o1 - OBJ_CAR0];
+                Xf cx;
+                car_child_xf(c, cx);
+                Convex box;
+                box.type = 0;
+                box.he = car_he(c);
+                box.margin = c.cfg->margin;
+                V3 bmn, bmx, omn, omx;
+                car_box_aabb(c, cx, bmn, bmx);
+                if (o0 == OBJ_MESH) mesh_aabb(bv.mesh, omn, omx);
+                else {
+                    PlaneC pl;
+                    plane_const(o0 - OBJ_PLANE0, pl);
+                    omn = pl.raw_min;
+                    omx = pl.raw_max;
+                }
+                if (aabb_overlap(bmn, bmx, omn, omx)) {
+                    Manifold& m = new_manifold(a, o1, o0, c.cfg->breaking);
+                    if (o0 == OBJ_MESH) convex_vs_mesh(bv, a, m, o1, cx, box);
+                    else convex_vs_plane(bv, a, m, cx, box, o0);
+                }
+            }
+        } else if (o0 == OBJ_BALL) {
+            // ball sphere vs the car compound's box child: GJK, manifold (car, ball)
+            Car& c = a.cars[o1 - OBJ_CAR0];
+            Xf cx;
+            car_child_xf(c, cx);
+            V3 bmn, bmx, smn, smx;
+            car_box_aabb(c, cx, bmn, bmx);
+            ball_aabb(a.ball.xf, smn, smx);
+            if (aabb_overlap(bmn, bmx, smn, smx)) {
+                float bt = (BALL_RADIUS_BT + 0.08f) * 0.02f;
+                Manifold& m = new_manifold(a, o1, OBJ_BALL, c.cfg->breaking < bt ? c.cfg->breaking : bt);
+                Convex box;
+                box.type = 0;
+                box.he = car_he(c);
+                box.margin = c.cfg->margin;
+                Convex sph;
+                sph.type = 1;
+                sph.margin = BALL_RADIUS_BT;
+                sph.he = V3(0, 0, 0);
+                float md = box.margin + sph.margin + m.breaking;
+                GjkOut g = gjk(box, cx, sph, a.ball.xf, md * md);
+                if (g.epa_needed) a.err |= WARN_EPA_SKIPPED;
+                Xf x0 = c.rb.xf, x1 = a.ball.xf;
+                if (g.valid) {
+                    float fr = combined_friction(a, OBJ_BALL, o1), re = combined_restitution(a, OBJ_BALL, o1);
+                    int idx = add_point(a, m, x0, x1, g.normal, g.point_on_b, g.dist, fr, re);
+                    if (idx >= 0) contact_added(bv, a, m, idx, -1);
+                }
+                refresh(a, m, x0, x1);
+            }
+        } else {
+            a.err |= WARN_CARCAR_SKIPPED;  // car box vs car box (btBoxBoxDetector)
+        }
+    }
+    // islands (btSimulationIslandManager, STATIC_SIMULATION_ISLAND_OPTIMIZATION)
+    int uf_id[MAX_CARS + 1], uf_sz[MAX_CARS + 1], tag[MAX_CARS + 1];
+    for (int i = 0; i < nd; i++) { uf_id[i] = i; uf_sz[i] = 1; }
+    auto find = [&](int x) { while (x != uf_id[x]) x = uf_id[x]; return x; };
+    auto merges = [&](int o) { return !is_static_obj(o) && !a.body(o).no_contact_response; };
+    for (int pi = 0; pi < a.npairs; pi++) {
+        int p0 = a.pair0[pi], p1 = a.pair1[pi];
+        if (merges(p0) && merges(p1)) {
+            int i = find(p0 - OBJ_BALL), j = find(p1 - OBJ_BALL);
+            if (i == j) continue;
+            if (uf_sz[i] < uf_sz[j]) { uf_id[i] = j; uf_sz[j] += uf_sz[i]; }
+            else { uf_id[j] = i; uf_sz[i] += uf_sz[j]; }
+        }
+    }
+    for (int i = 0; i < nd; i++) tag[i] = find(i);
+    // buildIslands: activation per island, island ids ascending
+    for (int id = 0; id < nd; id++) {
+        bool present = false, all_sleeping = true;
+        for (int i = 0; i < nd; i++) {
+            if (tag[i] != id) continue;
+            present = true;
+            int st = a.body(OBJ_BALL + i).act;
+            if (st == ACTIVE_TAG || st == DISABLE_DEACTIVATION) { all_sleeping = false; break; }
+        }
+        if (!present) continue;
+        for (int i = 0; i < nd; i++) {
+            if (tag[i] != id) continue;
+            Body& b = a.body(OBJ_BALL + i);
+            if (all_sleeping) {
+                if (b.act != DISABLE_DEACTIVATION && b.act != DISABLE_SIMULATION) b.act = ISLAND_SLEEPING;
+            } else if (b.act == ISLAND_SLEEPING) {
+                b.act = WANTS_DEACTIVATION;
+            }
+        }
+    }
+    int island_mans[MAX_MANIFOLDS];
+    int nim = 0;
+    for (int mi = 0; mi < a.nman; mi++) {
+        Manifold& m = a.man[mi];
+        int s0 = is_static_obj(m.body0) ? ISLAND_SLEEPING : a.body(m.body0).act;
+        int s1 = is_static_obj(m.body1) ? ISLAND_SLEEPING : a.body(m.body1).act;
+        if (s0 != ISLAND_SLEEPING || s1 != ISLAND_SLEEPING) {
+            bool r0 = is_static_obj(m.body0) ? true : !a.body(m.body0).no_contact_response;
+            bool r1 = is_static_obj(m.body1) ? true : !a.body(m.body1).no_contact_response;
+            bool resp = r0 && r1 && (!is_static_obj(m.body0) || !is_static_obj(m.body1));
+            if (resp) {
+                int i0 = is_static_obj(m.body0) ? -1 : tag[m.body0 - OBJ_BALL];
+                int i1 = is_static_obj(m.body1) ? -1 : tag[m.body1 - OBJ_BALL];
+                m.island = (int8_t)(i0 >= 0 ? i0 : i1);
+                island_mans[nim++] = mi;
+            }
+        }
+    }
+    if (nim > 1) island_quicksort(a, island_mans, nim);
+    // processIslands: bodies and manifolds of awake islands, solved as one batch
+    int bodies[MAX_CARS + 1], nb = 0;
+    int solve_mans[MAX_MANIFOLDS], nsm = 0;
+    for (int id = 0; id < nd; id++) {
+        bool present = false, sleeping = true;
+        for (int i = 0; i < nd; i++)
+            if (tag[i] == id) {
+                present = true;
+                if (a.body(OBJ_BALL + i).is_active()) sleeping = false;
+            }
+        if (!present || sleeping) continue;
+        for (int i = 0; i < nd; i++)
+            if (tag[i] == id) bodies[nb++] = OBJ_BALL + i;
+        for (int k = 0; k < nim; k++)
+            if (a.man[island_mans[k]].island == id) solve_mans[nsm++] = island_mans[k];
+    }
+    a.solver_dt = dt;
+    if (nb > 0) solve(a, bodies, nb, solve_mans, nsm, dt);
+    // integrateTransforms (btDiscreteDynamicsWorld.cpp:889-991)
+    for (int d = 0; d < nd; d++) {
+        Body& b = a.body(OBJ_BALL + d);
+        if (b.is_active()) {
+            Xf nt;
+            integrate_transform(b.xf, b.lin_vel, b.ang_vel, dt, b.no_rot, nt);
+            b.interp = nt;
+            b.xf = nt;
+            b.update_inertia();
+        }
+    }
+    // updateActivationState (btDiscreteDynamicsWorld.cpp:516-551).  The deactivation timer can only
+    // move a body to WANTS_DEACTIVATION, which the next tick overwrites before anything reads it,
+    // so it is not carried between ticks.
+    for (int d = 0; d < nd; d++) {
+        Body& b = a.body(OBJ_BALL + d);
+        if (b.act == ISLAND_SLEEPING || b.act == DISABLE_DEACTIVATION) {
+        } else if (len2(b.lin_vel) < 0.8f * 0.8f && len2(b.ang_vel) < 1.f * 1.f) {
+        } else {
+            if (b.act != DISABLE_DEACTIVATION && b.act != DISABLE_SIMULATION) b.act = 0;
+        }
+        bool wants = b.act != DISABLE_DEACTIVATION && (b.act == ISLAND_SLEEPING || b.act == WANTS_DEACTIVATION);
+        if (wants) {
+            if (b.act == ISLAND_SLEEPING) { b.ang_vel = V3(0, 0, 0); b.lin_vel = V3(0, 0, 0); }
+        } else {
+            if (b.act != DISABLE_DEACTIVATION && b.act != DISABLE_SIMULATION) b.act = ACTIVE_TAG;
+        }
+        b.total_force = V3(0, 0, 0);  // clearForces
+        b.total_torque = V3(0, 0, 0);
+    }
+}
+
+// ---------------------------------------------------------------- boost pads and goal
+RSG_D bool ball_scored(const Ctx& a) {  // Arena::IsBallScored, soccar (src/Sim/Arena/Arena.cpp:893-901)
+    float y = a.ball.xf.o.y * RL::BT_TO_UU;
+    return fabsf(y) > (RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y + RL::BALL_COLLISION_RADIUS_SOCCAR);
+}
+
+RSG_D void pad_check(Ctx& a, Pad& p, int pi, int ci) {  // BoostPad::_CheckCollide (src/Sim/BoostPad/BoostPad.cpp:62-86)
+    Car& c = a.cars[ci];
+    V3 cp = c.rb.xf.o;
+    bool big = pi < 6;
+    V3 pos_bt = V3(c_pad_locs[pi][0], c_pad_locs[pi][1], c_pad_locs[pi][2]) * RL::UU_TO_BT;
+    bool col = false;
+    if (p.prev_locked == c.id) {
+        V3 mn, mx;
+        car_compound_aabb(c, c.rb.xf, mn, mx);
+        float br = (big ? RL::PAD_BOX_RAD_BIG : RL::PAD_BOX_RAD_SMALL) * RL::UU_TO_BT;
+        V3 bmin = pos_bt - V3(br, br, 0);
+        V3 bmax = pos_bt + V3(br, br, RL::PAD_BOX_HEIGHT * RL::UU_TO_BT);
+        bool gt = (bmax.x > mn.x) && (bmax.y > mn.y) && (bmax.z > mn.z);
+        bool lt = (bmin.x < mx.x) && (bmin.y < mx.y) && (bmin.z < mx.z);
+        col = gt && lt;
+    } else {
+        float rad = (big ? RL::PAD_CYL_RAD_BIG : RL::PAD_CYL_RAD_SMALL) * RL::UU_TO_BT;
+        float dx = cp.x - pos_bt.x, dy = cp.y - pos_bt.y;
+        if (dx * dx + dy * dy < rad * rad) col = fabsf(cp.z - pos_bt.z) < (RL::PAD_CYL_HEIGHT * RL::UU_TO_BT);
+    }
+    if (col) p.cur_locked = ci;
+}
+
+RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25)
+    Car& c = a.cars[ci];
+    if (c.f(F_DEMOED) || c.boost >= RL::BOOST_MAX) return;
+    V3 cp = c.rb.xf.o * RL::BT_TO_UU;
+    const float EXT_Z = RL::PAD_CYL_HEIGHT + 250.f;
+    if (cp.z > EXT_Z) return;
+    const int CX = 8, CY = 10, SX = (int)(4096.f / (CX / 2)), SY = (int)(5120.f / (CY / 2));
+    int ix = (int)(cp.x / SX + (CX / 2));
+    int iy = (int)(cp.y / SY + (CY / 2));
+    int i0 = ix - 1 > 0 ? ix - 1 : 0, i1 = ix + 1 < CX - 1 ? ix + 1 : CX - 1;
+    int j0 = iy - 1 > 0 ? iy - 1 : 0, j1 = iy + 1 < CY - 1 ? iy + 1 : CY - 1;
+    for (int i = i0; i <= i1; i++)
+        for (int j = j0; j <= j1; j++)
+            for (int k = 0; k < NUM_PADS; k++) {
+                int px = (int)(c_pad_locs[k][0] / SX + (CX / 2));
+                int py = (int)(c_pad_locs[k][1] / SY + (CY / 2));
+                if (px == i && py == j) pad_check(a, a.pads[k], k, ci);
+            }
+}
+
+// Arena::Step, one tick (src/Sim/Arena/Arena.cpp:689-756)
+RSG_DN void arena_tick(const BatchView& bv, Ctx& a) {
+    Body& ball = a.ball;
+    bool ball_off = ball.act == DISABLE_DEACTIVATION || ball.act == DISABLE_SIMULATION;
+    if (len2(ball.lin_vel) == 0 && len2(ball.ang_vel) == 0) {
+        if (!ball_off) ball.act = ISLAND_SLEEPING;
+    } else {
+        if (!ball_off) ball.act = ACTIVE_TAG;
+    }
+    bool ball_only = a.ncars == 0;
+    for (int k = 0; k < a.ncars; k++) car_pre_tick(bv, a, a.cars[a.order[k]]);
+    if (bv.has_arena && !ball_only)
+        for (int i = 0; i < NUM_PADS; i++) {  // BoostPad::_PreTickUpdate (src/Sim/BoostPad/BoostPad.cpp:51-60)
+            Pad& p = a.pads[i];
+            if (p.cooldown > 0) p.cooldown = rs_maxf(p.cooldown - bv.dt, 0);
+            p.active = (p.cooldown == 0);
+            p.cur_locked = -1;
+        }
+    step_world(bv, a);
+    for (int k = 0; k < a.ncars; k++) {
+        int ci = a.order[k];
+        car_post_tick(a.cars[ci], bv.dt);
+        car_finish_physics(a.cars[ci]);
+        if (bv.has_arena) grid_check(a, ci);
+    }
+    if (bv.has_arena && !ball_only)
+        for (int i = 0; i < NUM_PADS; i++) {  // BoostPad::_PostTickUpdate (src/Sim/BoostPad/BoostPad.cpp:88-105)
+            Pad& p = a.pads[i];
+            uint32_t locked = 0;
+            if (p.cur_locked >= 0) {
+                Car& c = a.cars[p.cur_locked];
+                locked = c.id;
+                if (p.active) {
+                    bool big = i < 6;
+                    c.boost = rs_minf(c.boost + (big ? RL::PAD_BOOST_BIG : RL::PAD_BOOST_SMALL), RL::BOOST_MAX);
+                    p.active = false;
+                    p.cooldown = big ? RL::PAD_COOLDOWN_BIG : RL::PAD_COOLDOWN_SMALL;
+                }
+            }
+            p.prev_locked = locked;
+        }
+    {  // Ball::_FinishPhysicsTick (src/Sim/Ball/Ball.cpp:117-143)
+        if (!is_zero(a.ball_cache)) {
+            ball.lin_vel += a.ball_cache;
+            a.ball_cache = V3(0, 0, 0);
+        }
+        V3 v = ball.lin_vel, w = ball.ang_vel;
+        const float ms = RL::BALL_MAX_SPEED * RL::UU_TO_BT;
+        if (len2(v) > ms * ms) v = normalized(v) * ms;
+        if (len2(w) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) w = normalized(w) * RL::BALL_MAX_ANG_SPEED;
+        ball.lin_vel = v;
+        ball.ang_vel = w;
+        a.ball_ticks++;
+    }
+    if (bv.has_arena && ball_scored(a)) {
+        uint32_t team = (-(a.ball.xf.o.y) < 0) ? 0u : 1u;  // RS_TEAM_FROM_Y(-y)
+        push_event(a, RSG_EVENT_GOAL, team, 0, 0);
+    }
+    a.tick++;
+}
+
+// ---------------------------------------------------------------- SoA load / store
+RSG_D uint32_t pack_cell(int i, int j, int k) { return (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16); }
+
+struct SoA {  // address helpers for one arena
+    const BatchView& bv;
+    int ar;
+    RSG_D float& cf(int f, int s) const { return bv.cf[((size_t)f * bv.MC + s) * bv.A + ar]; }
+    RSG_D uint32_t& cu(int f, int s) const { return bv.cu[((size_t)f * bv.MC + s) * bv.A + ar]; }
+    RSG_D float& bf(int f) const { return bv.bf[(size_t)f * bv.A + ar]; }
+    RSG_D uint32_t& bu(int f) const { return bv.bu[(size_t)f * bv.A + ar]; }
+    RSG_D float& pf(int f, int p) const { return bv.pf[((size_t)f * NUM_PADS + p) * bv.A + ar]; }
+    RSG_D uint32_t& pu(int f, int p) const { return bv.pu[((size_t)f * NUM_PADS + p) * bv.A + ar]; }
+    RSG_D uint32_t& au(int f) const { return bv.au[(size_t)f * bv.A + ar]; }
+    RSG_D V3 v3(int f, int s) const { return V3(cf(f, s), cf(f + 1, s), cf(f + 2, s)); }
+    RSG_D void set_v3(int f, int s, V3 v) const { cf(f, s) = v.x; cf(f + 1, s) = v.y; cf(f + 2, s) = v.z; }
+    RSG_D M3 m3(int f, int s) const {
+        M3 m;
+        for (int r = 0; r < 3; r++) m.r[r] = v3(f + 3 * r, s);
+        return m;
+    }
+    RSG_D void set_m3(int f, int s, const M3& m) const {
+        for (int r = 0; r < 3; r++) set_v3(f + 3 * r, s, m.r[r]);
+    }
+};
+
+RSG_D void body_cell_load(const DevGrid& g, Body& b, uint32_t packed) {
+    if (packed == 0xffffffffu) {
+        b.cell = 0xffffffffu;
+        b.ci = b.cj = b.ck = 0;
+        return;
+    }
+    b.ci = (int)(packed & 0xff);
+    b.cj = (int)((packed >> 8) & 0xff);
+    b.ck = (int)((packed >> 16) & 0xff);
+    b.cell = grid_cell_index(g, b.ci, b.cj, b.ck);
+}
+RSG_D uint32_t body_cell_store(const Body& b) { return b.cell == 0xffffffffu ? 0xffffffffu : pack_cell(b.ci, b.cj, b.ck); }
+
+RSG_D void body_common(Body& b) {
+    b.interp = b.xf;
+    b.total_force = b.total_torque = V3(0, 0, 0);
+    b.n_special = 0;
+    b.sp_friction = b.sp_restitution = b.sp_total_dist = 0;
+    b.sp_total_normal = V3(0, 0, 0);
+    b.bp_min = b.bp_max = V3(0, 0, 0);
+    b.update_inertia();
+}
+
+RSG_DN void load_ctx(const BatchView& bv, int ar, Ctx& a) {
+    SoA s{bv, ar};
+    a.ev = bv.events ? bv.events + (size_t)ar * MAX_EVENTS_PER_ARENA : nullptr;
+    a.event_mask = bv.event_mask;
+    a.tick = (uint64_t)s.au(AU_TICK_LO) | ((uint64_t)s.au(AU_TICK_HI) << 32);
+    a.ncars = (int)s.au(AU_NCARS);
+    uint32_t ord = s.au(AU_ORDER);
+    for (int k = 0; k < MAX_CARS; k++) a.order[k] = (int)((ord >> (4 * k)) & 0xf);
+    a.seq = s.au(AU_SEQ);
+    a.stepped = s.au(AU_STEPPED) != 0;
+    a.err = 0;
+    a.nevents = (int)s.au(AU_EVENTS);
+    a.solver_dt = a.stepped ? bv.dt : 1.f / 60.f;
+    // ball (Ball::_BulletSetup, src/Sim/Ball/Ball.cpp:85-115)
+    Body& b = a.ball;
+    b.xf.o = V3(s.bf(BF_POS), s.bf(BF_POS + 1), s.bf(BF_POS + 2));
+    for (int r = 0; r < 3; r++) b.xf.b.r[r] = V3(s.bf(BF_BASIS + 3 * r), s.bf(BF_BASIS + 3 * r + 1), s.bf(BF_BASIS + 3 * r + 2));
+    b.lin_vel = V3(s.bf(BF_VEL), s.bf(BF_VEL + 1), s.bf(BF_VEL + 2));
+    b.ang_vel = V3(s.bf(BF_ANG), s.bf(BF_ANG + 1), s.bf(BF_ANG + 2));
+    {
+        const float r = BALL_RADIUS_BT, mass = RL::BALL_MASS_BT;
+        float elem = 0.4f * mass * r * r;
+        b.inv_mass = 1.f / mass;
+        b.inv_inertia_local = V3(1.f / elem, 1.f / elem, 1.f / elem);
+    }
+    b.lin_damping = RL::BALL_DRAG;
+    b.act = ACTIVE_TAG;
+    b.no_rot = true;
+    b.no_contact_response = false;
+    b.friction = RL::BALL_FRICTION;
+    b.restitution = RL::BALL_RESTITUTION;
+    body_cell_load(bv.grid, b, s.bu(BU_CELL));
+    b.cell_seq = s.bu(BU_CELL_SEQ);
+    body_common(b);
+    a.ball_ticks = (uint64_t)s.bu(BU_TICKS_LO) | ((uint64_t)s.bu(BU_TICKS_HI) << 32);
+    a.ball_cache = V3(0, 0, 0);
+    // cars (Car::_BulletSetup, src/Sim/Car/Car.cpp:195-292, derived per config on the host)
+    for (int i = 0; i < a.ncars; i++) {
+        Car& c = a.cars[i];
+        c.cfg = bv.cfgs + s.cu(CU_CFG, i);
+        c.obj = OBJ_CAR0 + i;
+        c.flags = s.cu(CU_FLAGS, i);
+        c.id = s.cu(CU_ID, i);
+        c.cc_other = s.cu(CU_CC_OTHER, i);
+        Body& rb = c.rb;
+        rb.xf.o = s.v3(CF_POS, i);
+        rb.xf.b = s.m3(CF_BASIS, i);
+        rb.lin_vel = s.v3(CF_VEL, i);
+        rb.ang_vel = s.v3(CF_ANG, i);
+        rb.inv_mass = 1.f / RL::CAR_MASS_BT;
+        rb.inv_inertia_local = V3(c.cfg->inv_inertia[0], c.cfg->inv_inertia[1], c.cfg->inv_inertia[2]);
+        rb.lin_damping = 0;
+        rb.no_rot = false;
+        rb.no_contact_response = c.f(F_NO_RESPONSE);
+        rb.act = rb.no_contact_response ? DISABLE_SIMULATION : ACTIVE_TAG;
+        rb.friction = RL::CAR_COLLISION_FRICTION;
+        rb.restitution = RL::CAR_COLLISION_RESTITUTION;
+        body_cell_load(bv.grid, rb, s.cu(CU_CELL, i));
+        rb.cell_seq = s.cu(CU_CELL_SEQ, i);
+        body_common(rb);
+        c.rot = s.m3(CF_ROT, i);
+        c.steer = s.cf(CF_STEER, i);
+        for (int w = 0; w < 4; w++) {
+            c.pushback[w] = s.cf(CF_PUSHBACK + w, i);
+            c.latf[w] = s.cf(CF_LATF + w, i);
+            c.longf[w] = s.cf(CF_LONGF + w, i);
+        }
+        c.engine = s.cf(CF_ENGINE, i);
+        c.brake = s.cf(CF_BRAKE, i);
+        c.flip_rel = s.v3(CF_FLIP_REL, i);
+        c.jump_time = s.cf(CF_JUMP_TIME, i);
+        c.flip_time = s.cf(CF_FLIP_TIME, i);
+        c.air_time = s.cf(CF_AIR_TIME, i);
+        c.air_time_sj = s.cf(CF_AIR_TIME_SJ, i);
+        c.boost = s.cf(CF_BOOST, i);
+        c.time_since_boost = s.cf(CF_TIME_SINCE_BOOST, i);
+        c.boosting_time = s.cf(CF_BOOSTING_TIME, i);
+        c.supersonic_time = s.cf(CF_SUPERSONIC_TIME, i);
+        c.handbrake = s.cf(CF_HANDBRAKE, i);
+        c.autoflip_timer = s.cf(CF_AUTOFLIP_TIMER, i);
+        c.autoflip_scale = s.cf(CF_AUTOFLIP_SCALE, i);
+        c.wc_normal = s.v3(CF_WC_NORMAL, i);
+        c.cc_cooldown = s.cf(CF_CC_COOLDOWN, i);
+        c.demo_timer = s.cf(CF_DEMO_TIMER, i);
+        c.bhi_rel = s.v3(CF_BHI_REL, i);
+        c.bhi_ballpos = s.v3(CF_BHI_BALLPOS, i);
+        c.bhi_extra = s.v3(CF_BHI_EXTRA, i);
+        c.bhi_hit = (uint64_t)s.cu(CU_BHI_HIT_LO, i) | ((uint64_t)s.cu(CU_BHI_HIT_HI, i) << 32);
+        c.bhi_extra_tick = (uint64_t)s.cu(CU_BHI_EXTRA_LO, i) | ((uint64_t)s.cu(CU_BHI_EXTRA_HI, i) << 32);
+        c.ticks_since = (uint64_t)s.cu(CU_TICKS_LO, i) | ((uint64_t)s.cu(CU_TICKS_HI, i) << 32);
+        for (int k = 0; k < 5; k++) {
+            c.ctrl[k] = s.cf(CF_CTRL + k, i);
+            c.last_ctrl[k] = s.cf(CF_LAST_CTRL + k, i);
+        }
+        c.vel_cache = s.v3(CF_VEL_CACHE, i);
+    }
+    for (int p = 0; p < NUM_PADS; p++) {
+        Pad& pd = a.pads[p];
+        pd.active = s.pu(PU_ACTIVE, p) != 0;
+        pd.cooldown = s.pf(PF_COOLDOWN, p);
+        pd.prev_locked = s.pu(PU_PREV_LOCKED, p);
+        pd.cur_locked = (int)s.pu(PU_CUR_LOCKED, p) - 1;
+    }
+}
+
+RSG_DN void store_ctx(const BatchView& bv, int ar, Ctx& a) {
+    SoA s{bv, ar};
+    s.au(AU_TICK_LO) = (uint32_t)a.tick;
+    s.au(AU_TICK_HI) = (uint32_t)(a.tick >> 32);
+    s.au(AU_SEQ) = a.seq;
+    s.au(AU_STEPPED) = a.stepped ? 1u : 0u;
+    s.au(AU_ERR) |= a.err;
+    s.au(AU_EVENTS) = (uint32_t)a.nevents;
+    Body& b = a.ball;
+    s.bf(BF_POS) = b.xf.o.x; s.bf(BF_POS + 1) = b.xf.o.y; s.bf(BF_POS + 2) = b.xf.o.z;
+    for (int r = 0; r < 3; r++) {
+        s.bf(BF_BASIS + 3 * r) = b.xf.b.r[r].x;
+        s.bf(BF_BASIS + 3 * r + 1) = b.xf.b.r[r].y;
+        s.bf(BF_BASIS + 3 * r + 2) = b.xf.b.r[r].z;
+    }
+    s.bf(BF_VEL) = b.lin_vel.x; s.bf(BF_VEL + 1) = b.lin_vel.y; s.bf(BF_VEL + 2) = b.lin_vel.z;
+    s.bf(BF_ANG) = b.ang_vel.x; s.bf(BF_ANG + 1) = b.ang_vel.y; s.bf(BF_ANG + 2) = b.ang_vel.z;
+    s.bu(BU_CELL) = body_cell_store(b);
+    s.bu(BU_CELL_SEQ) = b.cell_seq;
+    s.bu(BU_TICKS_LO) = (uint32_t)a.ball_ticks;
+    s.bu(BU_TICKS_HI) = (uint32_t)(a.ball_ticks >> 32);
+    for (int i = 0; i < a.ncars; i++) {
+        Car& c = a.cars[i];
+        c.setf(F_NO_RESPONSE, c.rb.no_contact_response);
+        s.cu(CU_FLAGS, i) = c.flags;
+        s.cu(CU_CC_OTHER, i) = c.cc_other;
+        s.set_v3(CF_POS, i, c.rb.xf.o);
+        s.set_m3(CF_BASIS, i, c.rb.xf.b);
+        s.set_v3(CF_VEL, i, c.rb.lin_vel);
+        s.set_v3(CF_ANG, i, c.rb.ang_vel);
+        s.cu(CU_CELL, i) = body_cell_store(c.rb);
+        s.cu(CU_CELL_SEQ, i) = c.rb.cell_seq;
+        s.set_m3(CF_ROT, i, c.rot);
+        s.cf(CF_STEER, i) = c.steer;
+        for (int w = 0; w < 4; w++) {
+            s.cf(CF_PUSHBACK + w, i) = c.pushback[w];
+            s.cf(CF_LATF + w, i) = c.latf[w];
+            s.cf(CF_LONGF + w, i) = c.longf[w];
+        }
+        s.cf(CF_ENGINE, i) = c.engine;
+        s.cf(CF_BRAKE, i) = c.brake;
+        s.set_v3(CF_FLIP_REL, i, c.flip_rel);
+        s.cf(CF_JUMP_TIME, i) = c.jump_time;
+        s.cf(CF_FLIP_TIME, i) = c.flip_time;
+        s.cf(CF_AIR_TIME, i) = c.air_time;
+        s.cf(CF_AIR_TIME_SJ, i) = c.air_time_sj;
+        s.cf(CF_BOOST, i) = c.boost;
+        s.cf(CF_TIME_SINCE_BOOST, i) = c.time_since_boost;
+        s.cf(CF_BOOSTING_TIME, i) = c.boosting_time;
+        s.cf(CF_SUPERSONIC_TIME, i) = c.supersonic_time;
+        s.cf(CF_HANDBRAKE, i) = c.handbrake;
+        s.cf(CF_AUTOFLIP_TIMER, i) = c.autoflip_timer;
+        s.cf(CF_AUTOFLIP_SCALE, i) = c.autoflip_scale;
+        s.set_v3(CF_WC_NORMAL, i, c.wc_normal);
+        s.cf(CF_CC_COOLDOWN, i) = c.cc_cooldown;
+        s.cf(CF_DEMO_TIMER, i) = c.demo_timer;
+        s.set_v3(CF_BHI_REL, i, c.bhi_rel);
+        s.set_v3(CF_BHI_BALLPOS, i, c.bhi_ballpos);
+        s.set_v3(CF_BHI_EXTRA, i, c.bhi_extra);
+        s.cu(CU_BHI_HIT_LO, i) = (uint32_t)c.bhi_hit;
+        s.cu(CU_BHI_HIT_HI, i) = (uint32_t)(c.bhi_hit >> 32);
+        s.cu(CU_BHI_EXTRA_LO, i) = (uint32_t)c.bhi_extra_tick;
+        s.cu(CU_BHI_EXTRA_HI, i) = (uint32_t)(c.bhi_extra_tick >> 32);
+        s.cu(CU_TICKS_LO, i) = (uint32_t)c.ticks_since;
+        s.cu(CU_TICKS_HI, i) = (uint32_t)(c.ticks_since >> 32);
+        for (int k = 0; k < 5; k++) {
+            s.cf(CF_CTRL + k, i) = c.ctrl[k];
+            s.cf(CF_LAST_CTRL + k, i) = c.last_ctrl[k];
+        }
+        s.set_v3(CF_VEL_CACHE, i, c.vel_cache);
+    }
+    for (int p = 0; p < NUM_PADS; p++) {
+        Pad& pd = a.pads[p];
+        s.pu(PU_ACTIVE, p) = pd.active ? 1u : 0u;
+        s.pf(PF_COOLDOWN, p) = pd.cooldown;
+        s.pu(PU_PREV_LOCKED, p) = pd.prev_locked;
+        s.pu(PU_CUR_LOCKED, p) = (uint32_t)(pd.cur_locked + 1);
+    }
+}
+
+}  // namespace rsg

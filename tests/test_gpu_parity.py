@@ -1,0 +1,218 @@
+"""CUDA tick through the C ABI against the reference's golden rollouts and the
+CPU restatement.
+
+Continuous state (positions, velocities, angular velocities, rotation) is
+compared after 1 and 8 ticks within golden_data.TOL; discrete state (flags,
+jump/flip/air/boost/supersonic timers, boost amounts, pad activity and
+cooldowns, demo timers) must be identical over 120-tick rollouts.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from golden_data import TOL, check_continuous
+from scenarios import (CONTROLS_DTYPE, cpu_snapshot, discrete_car, discrete_pads, gpu_controls, gpu_snapshot,
+                       make_scenario, mesh_bytes, run_cpu, setup_gpu)
+
+pytestmark = pytest.mark.gpu
+
+
+def play_gpu(scs, ticks, every_tick=True):
+    batch, ids = setup_gpu(scs)
+    snaps = []
+    for t in range(ticks):
+        batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
+        batch.step(1)
+        if every_tick or t in (0, 7, ticks - 1):
+            snaps.append(gpu_snapshot(batch, scs))
+        else:
+            snaps.append(None)
+    return batch, snaps
+
+
+def test_gpu_matches_reference_golden(golden):
+    scs = golden.scenarios
+    batch, snaps = play_gpu(scs, 120)
+    for si in range(golden.S):
+        for t in (1, 8):
+            cars, ball, _ = snaps[t - 1][si]
+            check_continuous(cars, ball, golden.cars_at(si, t), golden.ball_at(si, t), t, f"golden scenario {si}")
+        epa = golden.epa_tick(si)
+        for t in range(120 if epa < 0 else epa):
+            cars, ball, pads = snaps[t][si]
+            np.testing.assert_array_equal(discrete_car(cars).astype(np.float32), golden.disc_cars(si)[t],
+                                          err_msg=f"golden scenario {si} tick {t + 1}: car discrete state")
+            np.testing.assert_array_equal(discrete_pads(pads).astype(np.float32), golden.disc_pads(si)[t],
+                                          err_msg=f"golden scenario {si} tick {t + 1}: pads")
+    batch.close()
+
+
+def random_scenarios(n, base_seed=1000):
+    rng = np.random.default_rng(base_seed)
+    out = []
+    for k in range(n):
+        nc = int(rng.choice([2, 4, 6]))
+        presets = [int(p) for p in rng.integers(0, 6, nc)]
+        out.append(make_scenario(base_seed + k, ncars=nc, presets=presets, air_frac=float(rng.uniform(0, 0.6)),
+                                 max_ball_speed=6000.0))
+    return out
+
+
+def test_gpu_matches_restatement_random():
+    scs = random_scenarios(40)
+    batch, snaps = play_gpu(scs, 120)
+    for si, sc in enumerate(scs):
+        ref = []
+        first_epa = [-1]
+
+        def rec(t, a, ids):
+            ref.append(cpu_snapshot(a, ids))
+            if first_epa[0] < 0 and a.counters()[3] > 0:
+                first_epa[0] = t
+        a, _ = run_cpu("oracle", sc, 120, rec)
+        a.close()
+        for t in (1, 8):
+            cars, ball, _ = snaps[t - 1][si]
+            check_continuous(cars, ball, ref[t - 1][0], ref[t - 1][1], t, f"random scenario {si}")
+        until = 120 if first_epa[0] < 0 else first_epa[0]
+        for t in range(until):
+            np.testing.assert_array_equal(discrete_car(snaps[t][si][0]), discrete_car(ref[t][0]),
+                                          err_msg=f"random scenario {si} tick {t + 1}")
+            np.testing.assert_array_equal(discrete_pads(snaps[t][si][2]), discrete_pads(ref[t][2]),
+                                          err_msg=f"random scenario {si} tick {t + 1}: pads")
+    batch.close()
+
+
+def test_full_size_batch_is_deterministic_and_independent():
+    """4096 arenas holding 8 scenarios 512 times each: every copy of a scenario
+    must end bit-identical after 8 ticks, and all states stay finite."""
+    base = random_scenarios(8, base_seed=2000)
+    scs = [base[k % 8] for k in range(4096)]
+    batch, ids = setup_gpu(scs, max_cars=6)
+    for t in range(8):
+        batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
+        batch.step(1)
+    cars, balls, pads = batch.get_all_states()
+    mc = batch.max_cars
+    for k in range(8):
+        n = len(base[k].cars)
+        rows = [cars[a * mc:a * mc + n].tobytes() for a in range(k, 4096, 8)]
+        assert len(set(rows)) == 1, f"scenario {k}: copies differ"
+        brows = [balls[a].tobytes() for a in range(k, 4096, 8)]
+        assert len(set(brows)) == 1
+    for f in ("pos", "vel", "ang_vel"):
+        for c in "xyz":
+            assert np.isfinite(cars[f][c]).all() and np.isfinite(balls[f][c]).all()
+    batch.close()
+
+
+def test_state_round_trip_and_ids():
+    sc = make_scenario(7)
+    batch, ids = setup_gpu([sc])
+    assert batch.get_cars(0) == [ids[0][i] for i in sc.order]
+    for cid, s in zip(ids[0], sc.cars):
+        g = batch.get_car_state(0, cid)
+        for f in ("pos", "vel", "ang_vel", "rot_mat", "boost", "is_on_ground", "has_jumped"):
+            assert bytes(getattr(g, f)) == bytes(getattr(s, f)) if hasattr(getattr(g, f), "_fields_") \
+                else getattr(g, f) == getattr(s, f), f
+    b = batch.get_ball_state(0)
+    assert bytes(b.pos) == bytes(sc.ball.pos) and bytes(b.vel) == bytes(sc.ball.vel)
+    batch.close()
+
+
+def test_async_device_controls_match_host_controls():
+    import torch
+    scs = random_scenarios(6, base_seed=3000)
+    b1, _ = setup_gpu(scs)
+    for t in range(8):
+        b1.set_controls_all(gpu_controls(scs, t, b1.max_cars))
+        b1.step(1)
+    s1 = b1.get_all_states()
+    b2, _ = setup_gpu(scs)
+    seq = np.concatenate([gpu_controls(scs, t, b2.max_cars) for t in range(8)])
+    dev = torch.from_numpy(seq.view(np.uint8).copy()).cuda()
+    torch.cuda.synchronize()
+    b2.step_async(dev.data_ptr(), 8)
+    b2.sync()
+    s2 = b2.get_all_states()
+    assert s1[0].tobytes() == s2[0].tobytes() and s1[1].tobytes() == s2[1].tobytes()
+    b1.close()
+    b2.close()
+
+
+def test_goal_event_matches_restatement():
+    from rocketsim_gb300 import abi
+    sc = make_scenario(11, ncars=2, air_frac=0.0)
+    sc.ball.pos = abi.Vec3(0.0, 4700.0, 200.0)
+    sc.ball.vel = abi.Vec3(0.0, 3000.0, 0.0)
+    batch, ids = setup_gpu([sc])
+    goals = []
+    batch.set_goal_score_callback(lambda arena, team: goals.append((arena, team, batch.get_tick_count(arena))))
+    for t in range(60):
+        batch.set_controls_all(gpu_controls([sc], t, batch.max_cars))
+        batch.step(1)
+    a, _ = run_cpu("oracle", sc, 60)
+    ev = [e for e in a.pop_events() if e[0] == 1]
+    a.close()
+    assert goals, "no goal event on the GPU"
+    assert [(0, int(e[2])) for e in ev] == [(g[0], g[1]) for g in goals]
+    batch.close()
+
+
+def test_errors_are_reported():
+    import rocketsim_gb300 as rsg
+    from rocketsim_gb300 import abi
+    rsg.init_from_mem([mesh_bytes()])
+    b = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, 2, 2)
+    with pytest.raises(abi.RSGError) as e:
+        b.add_car(5, 0)
+    assert e.value.code == abi.ERR_ARG
+    b.add_car(0, 0)
+    b.add_car(0, 1)
+    with pytest.raises(abi.RSGError) as e:
+        b.add_car(0, 0)
+    assert e.value.code == abi.ERR_STATE
+    with pytest.raises(abi.RSGError):
+        b.set_car_update_order(0, [1, 1])
+    with pytest.raises(abi.RSGError):
+        b.get_car_state(1, 1)
+    b.close()
+    with pytest.raises(abi.RSGError):
+        rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, 1, 2, tick_rate=200.0)
+
+
+def test_remove_car_keeps_the_others():
+    sc = make_scenario(21, ncars=4)
+    batch, ids = setup_gpu([sc])
+    keep = [c for c in ids[0] if c != ids[0][1]]
+    before = {c: bytes(batch.get_car_state(0, c)) for c in keep}
+    batch.remove_car(0, ids[0][1])
+    assert sorted(batch.get_cars(0)) == sorted(keep)
+    for c in keep:
+        assert bytes(batch.get_car_state(0, c)) == before[c]
+    batch.step(4)
+    batch.close()
+
+
+def test_the_void_free_flight_matches_restatement():
+    import rocketsim_gb300 as rsg
+    from oracle.pyoracle import SimArena, CarState as OCarState
+    from rocketsim_gb300 import abi
+    sc = make_scenario(31, ncars=2, air_frac=1.0)
+    b = rsg.ArenaBatch(abi.GAMEMODE_THE_VOID, 1, 2)
+    ids = [b.add_car(0, t, 0, 0) for t in sc.teams]
+    o = SimArena("oracle", None, game_mode=5)
+    oids = [o.add_car(t, 0) for t in sc.teams]
+    for cid, ocid, s in zip(ids, oids, sc.cars):
+        b.set_car_state(0, cid, s)
+        o.set_car(ocid, OCarState.from_buffer_copy(bytes(s)))
+    o.set_car_order(oids)
+    b.step(8)
+    o.step(8)
+    for cid, ocid in zip(ids, oids):
+        g, r = b.get_car_state(0, cid), o.get_car(ocid)
+        d = max(abs(getattr(g.pos, c) - getattr(r.pos, c)) for c in "xyz")
+        assert d <= TOL[8]["pos"], d
+    b.close()
+    o.close()
