@@ -2333,6 +2333,327 @@ bool sphere_triangle(V3 center, float radius, const V3 v[3], float threshold, V3
     return false;
 }
 
+// ---------------------------------------------------------------- box-box
+
+// btTransformAabb(min, max, margin 0, t) (B/LinearMath/btAabbUtil2.h:166-181)
+void transform_aabb_mm(V3 mn, V3 mx, const Xf& t, V3& omn, V3& omx) {
+    V3 lhe = 0.5f * (mx - mn), lc = 0.5f * (mx + mn);
+    M3 ab = absolute(t.b);
+    V3 c = xf_apply(t, lc);
+    V3 e(dot(ab.r[0], lhe), dot(ab.r[1], lhe), dot(ab.r[2], lhe));
+    omn = c - e;
+    omx = c + e;
+}
+// btBoxBoxDetector (B/.../CollisionDispatch/btBoxBoxDetector.cpp:30-767), the ODE
+// separating-axis box test, restated.  Boxes are (center, basis, half extents
+// with margin); each contact is reported the way the detector feeds
+// btManifoldResult::addContactPoint: normal on B = -n, point on B, depth.
+struct BoxHit { V3 point; float depth; };
+
+// column j of a basis dotted with v, in the detector's summation order
+inline float col_dot(const M3& m, int j, V3 v) { return m.r[0][j] * v.x + m.r[1][j] * v.y + m.r[2][j] * v.z; }
+inline float cols_dot(const M3& a, int i, const M3& b, int j) {
+    return a.r[0][i] * b.r[0][j] + a.r[1][i] * b.r[1][j] + a.r[2][i] * b.r[2][j];
+}
+
+// dLineClosestApproach (btBoxBoxDetector.cpp:82-108)
+void line_closest(V3 pa, V3 ua, V3 pb, V3 ub, float& alpha, float& beta) {
+    V3 p(pb.x - pa.x, pb.y - pa.y, pb.z - pa.z);
+    float uaub = dot(ua, ub), q1 = dot(ua, p), q2 = -dot(ub, p);
+    float d = 1 - uaub * uaub;
+    if (d <= 0.0001f) {
+        alpha = 0;
+        beta = 0;
+    } else {
+        d = 1.f / d;
+        alpha = (q1 + uaub * q2) * d;
+        beta = (uaub * q1 + q2) * d;
+    }
+}
+
+// intersectRectQuad2 (btBoxBoxDetector.cpp:118-175): clips the quad q[8] against the
+// rectangle |x| < h[0], |y| < h[1]; returns the polygon (at most 8 points) in ret.
+int clip_quad(const float h[2], const float quad[8], float ret[16]) {
+    float bufA[16], bufB[16];
+    for (int i = 0; i < 8; i++) bufA[i] = quad[i];
+    float* q = bufA;
+    float* r = ret;
+    float* other = bufB;
+    int nq = 4, nr = 0;
+    bool full = false;
+    for (int dir = 0; dir <= 1 && !full; dir++) {
+        for (int sign = -1; sign <= 1 && !full; sign += 2) {
+            float* pq = q;
+            float* pr = r;
+            nr = 0;
+            for (int i = nq; i > 0; i--) {
+                bool in = sign * pq[dir] < h[dir];
+                if (in) {
+                    pr[0] = pq[0];
+                    pr[1] = pq[1];
+                    pr += 2;
+                    nr++;
+                    if (nr & 8) { full = true; break; }
+                }
+                float* nq_ = (i > 1) ? pq + 2 : q;
+                bool nin = sign * nq_[dir] < h[dir];
+                if (in != nin) {
+                    pr[1 - dir] = pq[1 - dir] + (nq_[1 - dir] - pq[1 - dir]) / (nq_[dir] - pq[dir]) * (sign * h[dir] - pq[dir]);
+                    pr[dir] = sign * h[dir];
+                    pr += 2;
+                    nr++;
+                    if (nr & 8) { full = true; break; }
+                }
+                pq += 2;
+            }
+            if (full) { q = r; break; }
+            // the chopped polygon becomes the input of the next pass
+            q = r;
+            if (r == ret) { r = other; }
+            else { r = ret; }
+            nq = nr;
+        }
+    }
+    if (q != ret)
+        for (int i = 0; i < nr * 2; i++) ret[i] = q[i];
+    return nr;
+}
+
+// cullPoints2 (btBoxBoxDetector.cpp:187-245): picks m of n polygon points spread by angle
+void cull_points(int n, const float p[], int m, int i0, int iret[]) {
+    const float PI_ODE = 3.14159265f;
+    float a, cx, cy, q;
+    if (n == 1) {
+        cx = p[0];
+        cy = p[1];
+    } else if (n == 2) {
+        cx = 0.5f * (p[0] + p[2]);
+        cy = 0.5f * (p[1] + p[3]);
+    } else {
+        a = 0;
+        cx = 0;
+        cy = 0;
+        for (int i = 0; i < n - 1; i++) {
+            q = p[i * 2] * p[i * 2 + 3] - p[i * 2 + 2] * p[i * 2 + 1];
+            a += q;
+            cx += q * (p[i * 2] + p[i * 2 + 2]);
+            cy += q * (p[i * 2 + 1] + p[i * 2 + 3]);
+        }
+        q = p[n * 2 - 2] * p[1] - p[0] * p[n * 2 - 1];
+        if (std::fabs(a + q) > SIMD_EPS) a = 1.f / (3.0f * (a + q));
+        else a = BT_LARGE;
+        cx = a * (cx + q * (p[n * 2 - 2] + p[0]));
+        cy = a * (cy + q * (p[n * 2 - 1] + p[1]));
+    }
+    float ang[8];
+    for (int i = 0; i < n; i++) ang[i] = std::atan2(p[i * 2 + 1] - cy, p[i * 2] - cx);
+    int avail[8];
+    for (int i = 0; i < n; i++) avail[i] = 1;
+    avail[i0] = 0;
+    iret[0] = i0;
+    for (int j = 1; j < m; j++) {
+        a = (float)j * (2 * PI_ODE / m) + ang[i0];
+        if (a > PI_ODE) a -= 2 * PI_ODE;
+        float maxdiff = 1e9f;
+        iret[j] = i0;
+        for (int i = 0; i < n; i++) {
+            if (avail[i]) {
+                float diff = std::fabs(ang[i] - a);
+                if (diff > PI_ODE) diff = 2 * PI_ODE - diff;
+                if (diff < maxdiff) {
+                    maxdiff = diff;
+                    iret[j] = i;
+                }
+            }
+        }
+        avail[iret[j]] = 0;
+    }
+}
+
+// dBoxBox2 (btBoxBoxDetector.cpp:247-712) with maxc = 4.  Returns the contact count;
+// `normal` is the detector's normal (contacts go in with -normal).
+int box_box(V3 p1, const M3& R1, V3 A, V3 p2, const M3& R2, V3 B, V3& normal, BoxHit out[4]) {
+    const float fudge_factor = 1.05f;
+    V3 p(p2.x - p1.x, p2.y - p1.y, p2.z - p1.z);
+    float pp[3] = {col_dot(R1, 0, p), col_dot(R1, 1, p), col_dot(R1, 2, p)};
+    float Rm[3][3], Q[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            Rm[i][j] = cols_dot(R1, i, R2, j);
+            Q[i][j] = std::fabs(Rm[i][j]);
+        }
+    float s = -FLT_MAX, s2, l;
+    int normal_axis = -1;  // >= 0: column of R1 (0..2) or R2 (3..5)
+    V3 normalC(0.f, 0.f, 0.f);
+    bool invert = false;
+    int code = 0;
+    auto face = [&](float e1, float e2, int axis, int cc) -> bool {
+        s2 = std::fabs(e1) - e2;
+        if (s2 > 0) return false;
+        if (s2 > s) {
+            s = s2;
+            normal_axis = axis;
+            invert = e1 < 0;
+            code = cc;
+        }
+        return true;
+    };
+    const float* Av = &A.x;
+    const float* Bv = &B.x;
+    if (!face(pp[0], A.x + B.x * Q[0][0] + B.y * Q[0][1] + B.z * Q[0][2], 0, 1)) return 0;
+    if (!face(pp[1], A.y + B.x * Q[1][0] + B.y * Q[1][1] + B.z * Q[1][2], 1, 2)) return 0;
+    if (!face(pp[2], A.z + B.x * Q[2][0] + B.y * Q[2][1] + B.z * Q[2][2], 2, 3)) return 0;
+    if (!face(col_dot(R2, 0, p), A.x * Q[0][0] + A.y * Q[1][0] + A.z * Q[2][0] + B.x, 3, 4)) return 0;
+    if (!face(col_dot(R2, 1, p), A.x * Q[0][1] + A.y * Q[1][1] + A.z * Q[2][1] + B.y, 4, 5)) return 0;
+    if (!face(col_dot(R2, 2, p), A.x * Q[0][2] + A.y * Q[1][2] + A.z * Q[2][2] + B.z, 5, 6)) return 0;
+    auto edge = [&](float e1, float e2, float n1, float n2, float n3, int cc) -> bool {
+        s2 = std::fabs(e1) - e2;
+        if (s2 > SIMD_EPS) return false;
+        l = std::sqrt(n1 * n1 + n2 * n2 + n3 * n3);
+        if (l > SIMD_EPS) {
+            s2 /= l;
+            if (s2 * fudge_factor > s) {
+                s = s2;
+                normal_axis = -1;
+                normalC = V3(n1 / l, n2 / l, n3 / l);
+                invert = e1 < 0;
+                code = cc;
+            }
+        }
+        return true;
+    };
+    const float f2 = 1.0e-5f;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) Q[i][j] += f2;
+    const float (&R)[3][3] = Rm;
+    // u1 x (v1, v2, v3)
+    if (!edge(pp[2] * R[1][0] - pp[1] * R[2][0], A.y * Q[2][0] + A.z * Q[1][0] + B.y * Q[0][2] + B.z * Q[0][1], 0, -R[2][0], R[1][0], 7)) return 0;
+    if (!edge(pp[2] * R[1][1] - pp[1] * R[2][1], A.y * Q[2][1] + A.z * Q[1][1] + B.x * Q[0][2] + B.z * Q[0][0], 0, -R[2][1], R[1][1], 8)) return 0;
+    if (!edge(pp[2] * R[1][2] - pp[1] * R[2][2], A.y * Q[2][2] + A.z * Q[1][2] + B.x * Q[0][1] + B.y * Q[0][0], 0, -R[2][2], R[1][2], 9)) return 0;
+    // u2 x (v1, v2, v3)
+    if (!edge(pp[0] * R[2][0] - pp[2] * R[0][0], A.x * Q[2][0] + A.z * Q[0][0] + B.y * Q[1][2] + B.z * Q[1][1], R[2][0], 0, -R[0][0], 10)) return 0;
+    if (!edge(pp[0] * R[2][1] - pp[2] * R[0][1], A.x * Q[2][1] + A.z * Q[0][1] + B.x * Q[1][2] + B.z * Q[1][0], R[2][1], 0, -R[0][1], 11)) return 0;
+    if (!edge(pp[0] * R[2][2] - pp[2] * R[0][2], A.x * Q[2][2] + A.z * Q[0][2] + B.x * Q[1][1] + B.y * Q[1][0], R[2][2], 0, -R[0][2], 12)) return 0;
+    // u3 x (v1, v2, v3)
+    if (!edge(pp[1] * R[0][0] - pp[0] * R[1][0], A.x * Q[1][0] + A.y * Q[0][0] + B.y * Q[2][2] + B.z * Q[2][1], -R[1][0], R[0][0], 0, 13)) return 0;
+    if (!edge(pp[1] * R[0][1] - pp[0] * R[1][1], A.x * Q[1][1] + A.y * Q[0][1] + B.x * Q[2][2] + B.z * Q[2][0], -R[1][1], R[0][1], 0, 14)) return 0;
+    if (!edge(pp[1] * R[0][2] - pp[0] * R[1][2], A.x * Q[1][2] + A.y * Q[0][2] + B.x * Q[2][1] + B.y * Q[2][0], -R[1][2], R[0][2], 0, 15)) return 0;
+    if (!code) return 0;
+    if (normal_axis >= 0) {
+        const M3& Rn = normal_axis < 3 ? R1 : R2;
+        int c = normal_axis % 3;
+        normal = V3(Rn.r[0][c], Rn.r[1][c], Rn.r[2][c]);
+    } else {
+        normal = V3(dot(R1.r[0], normalC), dot(R1.r[1], normalC), dot(R1.r[2], normalC));
+    }
+    if (invert) normal = V3(-normal.x, -normal.y, -normal.z);
+    float depth = -s;
+    if (code > 6) {
+        // edge-edge: closest points of the two touching edges
+        V3 pa = p1;
+        for (int j = 0; j < 3; j++) {
+            float sign = (col_dot(R1, j, normal) > 0) ? 1.0f : -1.0f;
+            for (int i = 0; i < 3; i++) pa[i] += sign * Av[j] * R1.r[i][j];
+        }
+        V3 pb = p2;
+        for (int j = 0; j < 3; j++) {
+            float sign = (col_dot(R2, j, normal) > 0) ? -1.0f : 1.0f;
+            for (int i = 0; i < 3; i++) pb[i] += sign * Bv[j] * R2.r[i][j];
+        }
+        int ca = (code - 7) / 3, cb = (code - 7) % 3;
+        V3 ua(R1.r[0][ca], R1.r[1][ca], R1.r[2][ca]), ub(R2.r[0][cb], R2.r[1][cb], R2.r[2][cb]);
+        float alpha, beta;
+        line_closest(pa, ua, pb, ub, alpha, beta);
+        for (int i = 0; i < 3; i++) pb[i] += ub[i] * beta;
+        out[0].point = pb;
+        out[0].depth = depth;
+        return 1;
+    }
+    // face contact: reference face a, incident face b
+    const M3& Ra = code <= 3 ? R1 : R2;
+    const M3& Rb = code <= 3 ? R2 : R1;
+    V3 pa = code <= 3 ? p1 : p2, pb = code <= 3 ? p2 : p1;
+    const float* Sa = code <= 3 ? Av : Bv;
+    const float* Sb = code <= 3 ? Bv : Av;
+    V3 normal2 = code <= 3 ? normal : V3(-normal.x, -normal.y, -normal.z);
+    float nr[3] = {col_dot(Rb, 0, normal2), col_dot(Rb, 1, normal2), col_dot(Rb, 2, normal2)};
+    float anr[3] = {std::fabs(nr[0]), std::fabs(nr[1]), std::fabs(nr[2])};
+    int lanr, a1, a2;
+    if (anr[1] > anr[0]) {
+        if (anr[1] > anr[2]) { a1 = 0; lanr = 1; a2 = 2; }
+        else { a1 = 0; a2 = 1; lanr = 2; }
+    } else {
+        if (anr[0] > anr[2]) { lanr = 0; a1 = 1; a2 = 2; }
+        else { a1 = 0; a2 = 1; lanr = 2; }
+    }
+    V3 center;
+    for (int i = 0; i < 3; i++) {
+        if (nr[lanr] < 0) center[i] = pb[i] - pa[i] + Sb[lanr] * Rb.r[i][lanr];
+        else center[i] = pb[i] - pa[i] - Sb[lanr] * Rb.r[i][lanr];
+    }
+    int codeN = code <= 3 ? code - 1 : code - 4;
+    int code1 = codeN == 0 ? 1 : 0;
+    int code2 = codeN == 2 ? 1 : 2;
+    float c1 = col_dot(Ra, code1, center), c2 = col_dot(Ra, code2, center);
+    float m11 = cols_dot(Ra, code1, Rb, a1), m12 = cols_dot(Ra, code1, Rb, a2);
+    float m21 = cols_dot(Ra, code2, Rb, a1), m22 = cols_dot(Ra, code2, Rb, a2);
+    float quad[8];
+    {
+        float k1 = m11 * Sb[a1], k2 = m21 * Sb[a1], k3 = m12 * Sb[a2], k4 = m22 * Sb[a2];
+        quad[0] = c1 - k1 - k3;
+        quad[1] = c2 - k2 - k4;
+        quad[2] = c1 - k1 + k3;
+        quad[3] = c2 - k2 + k4;
+        quad[4] = c1 + k1 + k3;
+        quad[5] = c2 + k2 + k4;
+        quad[6] = c1 + k1 - k3;
+        quad[7] = c2 + k2 - k4;
+    }
+    float rect[2] = {Sa[code1], Sa[code2]};
+    float ret[16];
+    int n = clip_quad(rect, quad, ret);
+    if (n < 1) return 0;
+    float point[3 * 8], dep[8];
+    float det1 = 1.f / (m11 * m22 - m12 * m21);
+    m11 *= det1;
+    m12 *= det1;
+    m21 *= det1;
+    m22 *= det1;
+    int cnum = 0;
+    for (int j = 0; j < n; j++) {
+        float k1 = m22 * (ret[j * 2] - c1) - m12 * (ret[j * 2 + 1] - c2);
+        float k2 = -m21 * (ret[j * 2] - c1) + m11 * (ret[j * 2 + 1] - c2);
+        for (int i = 0; i < 3; i++) point[cnum * 3 + i] = center[i] + k1 * Rb.r[i][a1] + k2 * Rb.r[i][a2];
+        dep[cnum] = Sa[codeN] - (normal2.x * point[cnum * 3] + normal2.y * point[cnum * 3 + 1] + normal2.z * point[cnum * 3 + 2]);
+        if (dep[cnum] >= 0) {
+            ret[cnum * 2] = ret[j * 2];
+            ret[cnum * 2 + 1] = ret[j * 2 + 1];
+            cnum++;
+        }
+    }
+    if (cnum < 1) return 0;
+    int maxc = 4;
+    if (maxc > cnum) maxc = cnum;
+    auto emit = [&](int k, int j) {
+        V3 w(point[j * 3] + pa.x, point[j * 3 + 1] + pa.y, point[j * 3 + 2] + pa.z);
+        if (code >= 4) w = w - normal * dep[j];
+        out[k].point = w;
+        out[k].depth = dep[j];
+    };
+    if (cnum <= maxc) {
+        for (int j = 0; j < cnum; j++) emit(j, j);
+        return cnum;
+    }
+    int i1 = 0;
+    float maxdepth = dep[0];
+    for (int i = 1; i < cnum; i++)
+        if (dep[i] > maxdepth) { maxdepth = dep[i]; i1 = i; }
+    int iret[8];
+    cull_points(cnum, ret, maxc, i1, iret);
+    for (int j = 0; j < maxc; j++) emit(j, iret[j]);
+    return maxc;
+}
+
 // ================================================================ collision dispatch
 struct PairRec { int o0, o1; };  // o0 has the lower broadphase uid
 
@@ -3076,8 +3397,53 @@ void step_world(Arena& a) {
                 mans.push_back(m);
             }
         } else {
-            // car vs car: box-box (btBoxBoxDetector) not restated yet
+            // car vs car: btCompoundCompoundCollisionAlgorithm (btCompoundCompoundCollisionAlgorithm.cpp:
+            // 213-330) over the single box child of each car, then btBoxBoxCollisionAlgorithm
+            // (btBoxBoxCollisionAlgorithm.cpp:47-72) with its own manifold
             a.counters[6]++;
+            // the pair's algorithm runs with the later-added car as body 0: the manifold is
+            // (higher car, lower car), which is what reproduces the reference's contacts
+            int ca = o1, cb = o0;
+            Car& c0 = a.cars[ca - OBJ_CAR0];
+            Car& c1 = a.cars[cb - OBJ_CAR0];
+            // root volumes of the compounds' child trees: child AABBs in compound space
+            V3 h0 = c0.hitbox_he + V3(c0.hitbox_margin, c0.hitbox_margin, c0.hitbox_margin);
+            V3 h1 = c1.hitbox_he + V3(c1.hitbox_margin, c1.hitbox_margin, c1.hitbox_margin);
+            Xf l0 = xf_identity(), l1 = xf_identity();
+            l0.o = c0.hitbox_off;
+            l1.o = c1.hitbox_off;
+            V3 amn, amx, bmn, bmx;
+            transform_aabb(c0.hitbox_he, c0.hitbox_margin, l0, amn, amx);
+            transform_aabb(c1.hitbox_he, c1.hitbox_margin, l1, bmn, bmx);
+            Xf rel = xf_mul(xf_inverse(c0.rb.xf), c1.rb.xf);
+            V3 rmn, rmx;
+            transform_aabb_mm(bmn, bmx, rel, rmn, rmx);
+            bool root = (amn.x <= rmx.x) && (amx.x >= rmn.x) && (amn.y <= rmx.y) && (amx.y >= rmn.y) && (amn.z <= rmx.z) &&
+                        (amx.z >= rmn.z);
+            if (root) {
+                Xf w0, w1;
+                car_child_xf(c0, w0);
+                car_child_xf(c1, w1);
+                V3 m0, x0v, m1, x1v;
+                car_box_aabb(c0, w0, m0, x0v);
+                car_box_aabb(c1, w1, m1, x1v);
+                if (aabb_overlap(m0, x0v, m1, x1v)) {
+                    Manifold m;
+                    m.body0 = ca;
+                    m.body1 = cb;
+                    m.breaking = std::min(c0.breaking_threshold, c1.breaking_threshold);
+                    V3 nrm;
+                    BoxHit hits[4];
+                    int nh = box_box(w0.o, w0.b, h0, w1.o, w1.b, h1, nrm, hits);
+                    float fr = combined_friction(a, ca, cb), re = combined_restitution(a, ca, cb);
+                    for (int k = 0; k < nh; k++) {
+                        int idx = add_point(a, m, c0.rb.xf, c1.rb.xf, -nrm, hits[k].point, -hits[k].depth, false, fr, re);
+                        if (idx >= 0) contact_added(a, m, idx, -1);
+                    }
+                    refresh(m, c0.rb.xf, c1.rb.xf);
+                    mans.push_back(m);
+                }
+            }
         }
     }
     // islands (btSimulationIslandManager with STATIC_SIMULATION_ISLAND_OPTIMIZATION)

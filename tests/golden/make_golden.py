@@ -21,8 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from scenarios import (CONTROLS_DTYPE, cpu_snapshot, discrete_car, discrete_pads, make_scenario,  # noqa: E402
-                       run_cpu)
+from scenarios import (CONTROLS_DTYPE, cpu_snapshot, discrete_car, discrete_pads, make_carcar_scenario,  # noqa: E402
+                       make_scenario, run_cpu)
 from rocketsim_gb300 import abi  # noqa: E402
 
 TICKS = 120
@@ -35,6 +35,7 @@ def scenario_list():
     out.append(make_scenario(101, ncars=6, presets=[0, 1, 2, 3, 4, 5]))  # 3v3, every hitbox
     out.append(make_scenario(102, ncars=4, presets=[3, 4, 5, 0], air_frac=0.0))  # all on the ground
     out.append(make_scenario(103, ncars=4, air_frac=1.0))  # all airborne
+    out += [make_carcar_scenario(s) for s in (0, 3, 6, 8)]  # bumps and demolitions
     return out
 
 

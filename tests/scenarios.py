@@ -131,6 +131,28 @@ def make_scenario(seed: int, ncars: int = 4, ticks: int = 120, presets: list[int
     return Scenario(seed, presets, teams, cars, b, [int(o) for o in order], ctl)
 
 
+def make_carcar_scenario(seed: int, ticks: int = 120) -> Scenario:
+    """Two cars on the ground driving into each other at 800..2300 uu/s (full throttle and
+    boost), so that bumps and demolitions happen within the first 30 ticks."""
+    rng = np.random.default_rng(seed)
+    sc = make_scenario(seed, ncars=2, ticks=ticks, air_frac=0.0, random_order=False)
+    x0, y0 = rng.uniform(-2000, 2000), rng.uniform(-2000, 2000)
+    ang = rng.uniform(0, 2 * math.pi)
+    for i, s in enumerate(sc.cars):
+        yaw = ang + (math.pi if i else 0) + rng.uniform(-0.6, 0.6)
+        off = (-1 if i == 0 else 1) * 260
+        M = rot_cols((math.cos(yaw / 2), 0, 0, math.sin(yaw / 2)))
+        set_rot(s.rot_mat, M)
+        sp = rng.uniform(800, 2300)
+        s.pos = abi.Vec3(x0 + off * math.cos(ang), y0 + off * math.sin(ang), 17.0)
+        s.vel = abi.Vec3(float(M[0, 0] * sp), float(M[1, 0] * sp), 0.0)
+        s.is_supersonic = int(sp > 2200)
+    sc.controls["throttle"] = 1.0
+    sc.controls["boost"] = 1
+    sc.controls["jump"] = 0
+    return sc
+
+
 def _controls_struct(row) -> abi.CarControls:
     c = abi.CarControls()
     c.throttle, c.steer, c.pitch, c.yaw, c.roll = (float(row[k]) for k in ("throttle", "steer", "pitch", "yaw", "roll"))
