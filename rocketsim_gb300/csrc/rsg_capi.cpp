@@ -836,7 +836,7 @@ int rsg_step(rsg_batch* b, int ticks) {
     RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
     for (int done = 0; done < ticks;) {
         int n = std::min(chunk, ticks - done);
-        RSG_CUDA(launch_tick(b->buf, nullptr, n, 64, b->stream));
+        RSG_CUDA(launch_tick(b->buf, nullptr, n, 32, b->stream));
         done += n;
         if (b->buf.event_mask && (rc = drain_events(b))) return rc;
     }
@@ -850,7 +850,7 @@ int rsg_step_async(rsg_batch* b, const rsg_car_controls* d_controls, int ticks) 
     int rc;
     if ((rc = set_device(b))) return rc;
     RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
-    RSG_CUDA(launch_tick(b->buf, d_controls, ticks, 64, b->stream));
+    RSG_CUDA(launch_tick(b->buf, d_controls, ticks, 32, b->stream));
     return RSG_OK;
 }
 
