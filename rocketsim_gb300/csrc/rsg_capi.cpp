@@ -172,6 +172,7 @@ static_assert(sizeof(DevEventHost) == DEV_EVENT_BYTES, "event record");
 struct rsg_batch {
     int game_mode = 0;
     int device = 0;
+    int warps_per_block = 2;  // arenas per block of the tick kernel
     BatchBuffers buf{};
     cudaStream_t stream = nullptr;
     std::vector<CarCfgDev> cfgs;
@@ -438,12 +439,7 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
         rsg_batch_destroy(b);
         return nullptr;
     }
-    bool ok = alloc((void**)&B.cf, sizeof(float) * CF_COUNT * MC * A);
-    ok = ok && alloc((void**)&B.cu, sizeof(uint32_t) * CU_COUNT * MC * A);
-    ok = ok && alloc((void**)&B.bf, sizeof(float) * BF_COUNT * A);
-    ok = ok && alloc((void**)&B.bu, sizeof(uint32_t) * BU_COUNT * A);
-    ok = ok && alloc((void**)&B.pf, sizeof(float) * PF_COUNT * NUM_PADS * A);
-    ok = ok && alloc((void**)&B.pu, sizeof(uint32_t) * PU_COUNT * NUM_PADS * A);
+    bool ok = alloc((void**)&B.rec, sizeof(uint32_t) * (size_t)rec_words((int)MC) * A);
     ok = ok && alloc((void**)&B.au, sizeof(uint32_t) * AU_COUNT * A);
     ok = ok && alloc(&B.events, (size_t)DEV_EVENT_BYTES * MAX_EVENTS_PER_ARENA * A);
     if (!ok) {
@@ -480,7 +476,7 @@ void rsg_batch_destroy(rsg_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     BatchBuffers& B = b->buf;
-    void* ptrs[] = {B.cf, B.cu, B.bf, B.bu, B.pf, B.pu, B.au, B.events, b->d_cfgs, b->d_stage};
+    void* ptrs[] = {B.rec, B.au, B.events, b->d_cfgs, b->d_stage};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -594,11 +590,9 @@ int rsg_set_car_controls(rsg_batch* b, uint32_t arena, uint32_t car_id, const rs
     if ((rc = set_device(b))) return rc;
     // controls of one car: five floats and three flag bits in the car's SoA columns
     float v[5] = {c->throttle, c->steer, c->pitch, c->yaw, c->roll};
-    size_t A = b->buf.A, MC = b->buf.MC;
-    for (int k = 0; k < 5; k++)
-        RSG_CUDA(cudaMemcpyAsync(b->buf.cf + ((size_t)(CF_CTRL + k) * MC + slot) * A + arena, &v[k], 4,
-                                 cudaMemcpyHostToDevice, b->stream));
-    uint32_t* fl = b->buf.cu + ((size_t)CU_FLAGS * MC + slot) * A + arena;
+    uint32_t* rec = b->buf.rec + (size_t)arena * rec_words(b->buf.MC);
+    RSG_CUDA(cudaMemcpyAsync(rec + rec_car_f(CF_CTRL, slot), v, sizeof(v), cudaMemcpyHostToDevice, b->stream));
+    uint32_t* fl = rec + rec_car_u(CU_FLAGS, slot);
     uint32_t flags = 0;
     RSG_CUDA(cudaMemcpyAsync(&flags, fl, 4, cudaMemcpyDeviceToHost, b->stream));
     RSG_CUDA(cudaStreamSynchronize(b->stream));
@@ -720,13 +714,14 @@ int rsg_set_pad_state(rsg_batch* b, uint32_t arena, uint32_t pad, const rsg_pad_
     if (!in || pad >= (uint32_t)NUM_PADS) return fail(RSG_ERR_ARG, "pad index out of range");
     if (!b->buf.has_arena) return fail(RSG_ERR_STATE, "this game mode has no boost pads");
     if ((rc = set_device(b))) return rc;
-    size_t A = b->buf.A;
-    uint32_t active = in->is_active ? 1u : 0u, zero = 0;
-    RSG_CUDA(cudaMemcpyAsync(b->buf.pu + ((size_t)PU_ACTIVE * NUM_PADS + pad) * A + arena, &active, 4, cudaMemcpyHostToDevice, b->stream));
-    RSG_CUDA(cudaMemcpyAsync(b->buf.pf + ((size_t)PF_COOLDOWN * NUM_PADS + pad) * A + arena, &in->cooldown, 4, cudaMemcpyHostToDevice, b->stream));
-    RSG_CUDA(cudaMemcpyAsync(b->buf.pu + ((size_t)PU_CUR_LOCKED * NUM_PADS + pad) * A + arena, &zero, 4, cudaMemcpyHostToDevice, b->stream));
-    RSG_CUDA(cudaMemcpyAsync(b->buf.pu + ((size_t)PU_PREV_LOCKED * NUM_PADS + pad) * A + arena, &in->prev_locked_car_id, 4,
-                             cudaMemcpyHostToDevice, b->stream));
+    // one pad block of the arena record: cooldown, active, previous and current locked car
+    uint32_t words[PAD_WORDS];
+    std::memcpy(&words[PF_COOLDOWN], &in->cooldown, 4);
+    words[PF_COUNT + PU_ACTIVE] = in->is_active ? 1u : 0u;
+    words[PF_COUNT + PU_PREV_LOCKED] = in->prev_locked_car_id;
+    words[PF_COUNT + PU_CUR_LOCKED] = 0;
+    uint32_t* rec = b->buf.rec + (size_t)arena * rec_words(b->buf.MC);
+    RSG_CUDA(cudaMemcpyAsync(rec + rec_pad_f(0, (int)pad), words, sizeof(words), cudaMemcpyHostToDevice, b->stream));
     RSG_CUDA(cudaStreamSynchronize(b->stream));
     return RSG_OK;
 }
@@ -836,7 +831,7 @@ int rsg_step(rsg_batch* b, int ticks) {
     RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
     for (int done = 0; done < ticks;) {
         int n = std::min(chunk, ticks - done);
-        RSG_CUDA(launch_tick(b->buf, nullptr, n, 32, b->stream));
+        RSG_CUDA(launch_tick(b->buf, nullptr, n, b->warps_per_block, b->stream));
         done += n;
         if (b->buf.event_mask && (rc = drain_events(b))) return rc;
     }
@@ -850,7 +845,7 @@ int rsg_step_async(rsg_batch* b, const rsg_car_controls* d_controls, int ticks) 
     int rc;
     if ((rc = set_device(b))) return rc;
     RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
-    RSG_CUDA(launch_tick(b->buf, d_controls, ticks, 32, b->stream));
+    RSG_CUDA(launch_tick(b->buf, d_controls, ticks, b->warps_per_block, b->stream));
     return RSG_OK;
 }
 

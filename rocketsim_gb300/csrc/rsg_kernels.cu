@@ -17,12 +17,8 @@ static BatchView make_view(const BatchBuffers& b) {
     v.MC = b.MC;
     v.has_arena = b.has_arena;
     v.dt = b.dt;
-    v.cf = b.cf;
-    v.cu = b.cu;
-    v.bf = b.bf;
-    v.bu = b.bu;
-    v.pf = b.pf;
-    v.pu = b.pu;
+    v.rec = b.rec;
+    v.rec_words = rec_words(b.MC);
     v.au = b.au;
     v.cfgs = b.cfgs;
     v.events = (DevEvent*)b.events;
@@ -59,27 +55,46 @@ RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
     c.setf(F_CTRL_HB, k.handbrake != 0);
 }
 
-__global__ void __launch_bounds__(128) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls, int ticks) {
-    int ar = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ar >= bv.A) return;
-    Ctx a;
-    load_ctx(bv, ar, a);
+// One warp per arena: the arena's working set is carved out of dynamic shared memory
+// (smem_layout), loaded from its record, advanced `ticks` ticks and stored back.
+__global__ void __launch_bounds__(128) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
+                                                       int ticks) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ar = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (ar >= bv.A) return;  // whole warps leave together
+    const SmemLayout L = smem_layout(bv.MC);
+    Ctx& a = bind_ctx(smem + (size_t)warp * L.bytes, L, lane);
+    if (lane == 0) load_arena(bv, ar, a);
+    __syncwarp();
+    if (lane < a.ncars) load_car(bv, ar, a, lane);
+    load_pads(bv, ar, a, lane);
+    __syncwarp();
     for (int t = 0; t < ticks; t++) {
-        if (controls) {
-            const rsg_car_controls* k = controls + ((size_t)t * bv.A + ar) * bv.MC;
-            for (int i = 0; i < a.ncars; i++) apply_controls(a.cars[i], k[i]);
+        if (controls && lane < a.ncars) {
+            const rsg_car_controls k = controls[((size_t)t * bv.A + ar) * bv.MC + lane];
+            apply_controls(a.cars[lane], k);
         }
-        arena_tick(bv, a);
-        a.stepped = true;
+        __syncwarp();
+        arena_tick_warp(bv, a, lane);
     }
-    store_ctx(bv, ar, a);
+    if (lane == 0) store_arena(bv, ar, a);
+    if (lane < a.ncars) store_car(bv, ar, a, lane);
+    store_pads(bv, ar, a, lane);
 }
 
-cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int block, cudaStream_t st) {
+int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars).bytes; }
+
+cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int warps_per_block,
+                        cudaStream_t st) {
     if (b.A <= 0 || ticks <= 0) return cudaSuccess;
-    if (block <= 0 || block > 128) block = 64;
-    int grid = (b.A + block - 1) / block;
-    rsg_tick_kernel<<<grid, block, 0, st>>>(make_view(b), controls, ticks);
+    if (warps_per_block <= 0 || warps_per_block > 4) warps_per_block = 2;
+    const int per_arena = smem_layout(b.MC).bytes;
+    const int smem = per_arena * warps_per_block;
+    cudaError_t e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    int grid = (b.A + warps_per_block - 1) / warps_per_block;
+    rsg_tick_kernel<<<grid, 32 * warps_per_block, smem, st>>>(make_view(b), controls, ticks);
     return cudaGetLastError();
 }
 

@@ -23,13 +23,8 @@ struct DevMeshPtrs {
 struct BatchBuffers {
     int A, MC, has_arena;
     float dt;
-    float* cf;
-    uint32_t* cu;
-    float* bf;
-    uint32_t* bu;
-    float* pf;
-    uint32_t* pu;
-    uint32_t* au;
+    uint32_t* rec;  // A records of rec_words(MC) 32-bit words
+    uint32_t* au;   // [AU_COUNT][A]
     const CarCfgDev* cfgs;
     void* events;  // DevEvent[A * MAX_EVENTS_PER_ARENA]
     uint32_t event_mask;
@@ -39,9 +34,13 @@ struct BatchBuffers {
 
 constexpr int DEV_EVENT_BYTES = 24;
 
-// Advances every arena by `ticks` ticks.  `controls` (device, may be null) holds
-// [ticks][A][MC] rsg_car_controls applied before each tick.
-cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int block, cudaStream_t st);
+// Advances every arena by `ticks` ticks, one warp per arena and `warps_per_block`
+// arenas per block.  `controls` (device, may be null) holds [ticks][A][MC]
+// rsg_car_controls applied before each tick.
+cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int warps_per_block,
+                        cudaStream_t st);
+// Shared memory one arena needs in the tick kernel.
+int tick_smem_per_arena(int max_cars);
 
 // Gathers states of `n` (arena, slot) pairs (idx[2k], idx[2k+1]); idx == null means
 // all arenas x all slots in [arena][slot] order.  Slots beyond the arena's car count

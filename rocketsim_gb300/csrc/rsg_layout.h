@@ -1,13 +1,20 @@
-// rsg_layout.h -- structure-of-arrays layout of a batch of arenas in device memory.
+// rsg_layout.h -- layout of a batch of arenas in device memory.
 //
-// Every per-car quantity is an array of n_arenas * max_cars values indexed
-// [slot * n_arenas + arena]: a warp that handles 32 consecutive arenas reads 32
-// consecutive words of each field (coalesced 128-byte transactions).  Ball and
-// arena fields are indexed [arena]; pad fields [pad * n_arenas + arena].
-// Positions and velocities are kept in Bullet units (uu / 50) as the reference
-// keeps them inside btRigidBody.
+// Each arena's persistent state is one record of 32-bit words (ball, boost
+// pads, then one fixed-size block per car slot), records stored back to back.
+// One warp advances one arena and moves its record with contiguous loads and
+// stores.  A second, small array holds per-arena scalars field-major
+// ([field][arena]) so that the host can read one field of every arena (event
+// counts, error flags) with a single copy.  Positions and velocities are kept
+// in Bullet units (uu / 50) as the reference keeps them inside btRigidBody.
 #pragma once
 #include <cstdint>
+
+#if defined(__CUDACC__)
+#define RSG_LAYOUT_FN __host__ __device__ constexpr
+#else
+#define RSG_LAYOUT_FN constexpr
+#endif
 
 namespace rsg {
 
@@ -124,6 +131,22 @@ enum DeviceError : uint32_t {
 constexpr int MAX_CARS = 8;
 constexpr int NUM_PADS = 34;
 constexpr int MAX_EVENTS_PER_ARENA = 64;
+
+// ---- record word offsets
+constexpr int PAD_WORDS = 4;   // cooldown (f32), then PadU fields
+constexpr int CAR_WORDS = 96;  // CarF floats, then CarU words, one spare
+constexpr int REC_BALL = 0;
+constexpr int REC_PADS = REC_BALL + BF_COUNT + BU_COUNT;
+constexpr int REC_CARS = 160;
+static_assert(REC_PADS + NUM_PADS * PAD_WORDS <= REC_CARS, "record layout");
+static_assert(CF_COUNT + CU_COUNT <= CAR_WORDS, "car block");
+RSG_LAYOUT_FN int rec_words(int max_cars) { return REC_CARS + CAR_WORDS * max_cars; }
+RSG_LAYOUT_FN int rec_ball_f(int f) { return REC_BALL + f; }
+RSG_LAYOUT_FN int rec_ball_u(int f) { return REC_BALL + BF_COUNT + f; }
+RSG_LAYOUT_FN int rec_pad_f(int f, int pad) { return REC_PADS + pad * PAD_WORDS + f; }
+RSG_LAYOUT_FN int rec_pad_u(int f, int pad) { return REC_PADS + pad * PAD_WORDS + PF_COUNT + f; }
+RSG_LAYOUT_FN int rec_car_f(int f, int slot) { return REC_CARS + slot * CAR_WORDS + f; }
+RSG_LAYOUT_FN int rec_car_u(int f, int slot) { return REC_CARS + slot * CAR_WORDS + CF_COUNT + f; }
 
 // Per-car-config constants uploaded once (derived like Car::_BulletSetup, Car.cpp:195-292)
 struct CarCfgDev {

@@ -11,6 +11,7 @@
 #pragma once
 #include <cstdint>
 
+#include "../../include/rocketsim_gb300.h"
 #include "rsg_consts.cuh"
 #include "rsg_layout.h"
 #include "rsg_math.cuh"
@@ -54,13 +55,9 @@ struct BatchView {
     int A, MC;  // arenas, car slots per arena
     int has_arena;
     float dt;
-    float* cf;
-    uint32_t* cu;
-    float* bf;
-    uint32_t* bu;
-    float* pf;
-    uint32_t* pu;
-    uint32_t* au;
+    uint32_t* rec;  // A records of rec_words(MC) words
+    int rec_words;
+    uint32_t* au;   // [AU_COUNT][A]
     const CarCfgDev* cfgs;
     DevEvent* events;
     uint32_t event_mask;
@@ -71,10 +68,22 @@ struct BatchView {
 constexpr int OBJ_MESH = 0, OBJ_PLANE0 = 1, OBJ_BALL = 5, OBJ_CAR0 = 6;
 enum ActState { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
 
-constexpr int MAX_PAIRS = 96;
-constexpr int MAX_MANIFOLDS = 96;
-constexpr int MAX_POINTS = 64;
-constexpr int MAX_ROWS = MAX_POINTS + MAX_CARS + 1;
+// Per-arena capacities of the world-step scratch for `mc` car slots: every
+// dynamic object can pair with the mesh and the 4 planes and with every other
+// dynamic object; a manifold holds at most 4 points.
+constexpr int MAX_DYN = MAX_CARS + 1;
+constexpr int MAX_PAIRS = 5 * MAX_DYN + MAX_DYN * (MAX_CARS) / 2;
+struct ArenaCaps {
+    int pairs, points, rows;
+};
+RSG_HD ArenaCaps arena_caps(int mc) {
+    int nd = mc + 1;
+    ArenaCaps c;
+    c.pairs = 5 * nd + nd * (nd - 1) / 2;
+    c.points = 12 * nd;
+    c.rows = c.points + nd;
+    return c;
+}
 
 struct Body {
     Xf xf, interp;
@@ -160,28 +169,40 @@ struct Manifold {
     int8_t pt[4];
 };
 
+struct Row;
+struct SBody;
+
+// One arena's working state during a launch.  It lives in shared memory (one
+// region per warp); the arrays are carved out of the same region with sizes
+// from arena_caps(MC).
 struct Ctx {
-    DevEvent* ev;  // this arena's event slots
+    DevEvent* ev;         // this arena's event slots
     uint32_t event_mask;  // bit k set: record events of kind k
     uint64_t ball_ticks;
     int ncars;
     int order[MAX_CARS];
-    Car cars[MAX_CARS];
+    Car* cars;
     Body ball;
     V3 ball_cache;
-    Pad pads[NUM_PADS];
+    Pad* pads;
     uint64_t tick;
     uint32_t seq;
     bool stepped;
     uint32_t err;
     int nevents;
     float solver_dt;
+    int serial;  // the pre-tick of this tick runs car by car in update order
     // scratch of one world step
-    int npairs;
-    int8_t pair0[MAX_PAIRS], pair1[MAX_PAIRS];
-    int nman, npts;
-    Manifold man[MAX_MANIFOLDS];
-    MPoint pts[MAX_POINTS];
+    int npairs, cap_pairs;
+    int8_t* pair0;
+    int8_t* pair1;
+    int nman, npts, cap_pts;
+    struct Manifold* man;
+    MPoint* pts;
+    SBody* sb;
+    Row* rows_c;
+    Row* rows_f;
+    int cap_rows;
 
     RSG_D Body& body(int o) { return o == OBJ_BALL ? ball : cars[o - OBJ_CAR0].rb; }
 };
@@ -1012,21 +1033,10 @@ RSG_D void update_auto_roll(Car& c, int nwc) {  // Car::_UpdateAutoRoll (Car.cpp
 
 RSG_D void car_set_respawn(Car& c, int idx, float boost);
 
-RSG_DN void car_pre_tick(const BatchView& bv, Ctx& a, Car& c) {  // Car::_PreTickUpdate (Car.cpp:58-131)
+// Car::_PreTickUpdate (Car.cpp:58-131) after the four suspension rays: friction, wheels, air
+// control, jump, auto-flip, flip / double jump, auto-roll, suspension and boost.
+RSG_DN void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
     float dt = bv.dt;
-    for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
-    if (c.f(F_DEMOED)) {
-        c.demo_timer = rs_maxf(c.demo_timer - dt, 0);
-        if (c.demo_timer == 0) car_set_respawn(c, 0, RL::BOOST_SPAWN_AMOUNT);
-        c.rb.act = DISABLE_SIMULATION;
-        c.rb.no_contact_response = true;
-    } else {
-        c.rb.act = ACTIVE_TAG;
-        c.rb.no_contact_response = false;
-    }
-    if (c.f(F_DEMOED)) return;
-    for (int i = 0; i < 4; i++) update_wheel_transform(c, i);
-    for (int i = 0; i < 4; i++) ray_cast_wheel(bv, a, c, i);
     calc_friction_impulses(a, c, dt);
     bool pressed = c.f(F_CTRL_JUMP) && !c.f(F_LAST_JUMP);
     int nwc = 0;
@@ -1048,6 +1058,33 @@ RSG_DN void car_pre_tick(const BatchView& bv, Ctx& a, Car& c) {  // Car::_PreTic
     update_suspension(c, dt);
     apply_friction_impulses(c, dt);
     update_boost(c, dt);
+}
+
+// Start of Car::_PreTickUpdate for a car that is not demolished and was not at the last
+// pre-tick: control clamping, activation and the wheel transforms.
+RSG_D void car_pre_before_rays(Car& c) {
+    for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
+    c.rb.act = ACTIVE_TAG;
+    c.rb.no_contact_response = false;
+    for (int i = 0; i < 4; i++) update_wheel_transform(c, i);
+}
+
+RSG_DN void car_pre_tick(const BatchView& bv, Ctx& a, Car& c) {  // Car::_PreTickUpdate (Car.cpp:58-131)
+    float dt = bv.dt;
+    for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
+    if (c.f(F_DEMOED)) {
+        c.demo_timer = rs_maxf(c.demo_timer - dt, 0);
+        if (c.demo_timer == 0) car_set_respawn(c, 0, RL::BOOST_SPAWN_AMOUNT);
+        c.rb.act = DISABLE_SIMULATION;
+        c.rb.no_contact_response = true;
+    } else {
+        c.rb.act = ACTIVE_TAG;
+        c.rb.no_contact_response = false;
+    }
+    if (c.f(F_DEMOED)) return;
+    for (int i = 0; i < 4; i++) update_wheel_transform(c, i);
+    for (int i = 0; i < 4; i++) ray_cast_wheel(bv, a, c, i);
+    car_pre_after_rays(bv, a, c);
 }
 
 RSG_D void car_post_tick(Car& c, float dt) {  // Car::_PostTickUpdate (Car.cpp:133-163)
@@ -1192,7 +1229,7 @@ RSG_D int add_point(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1, V3 n, V3 pb
         idx = closest_axis4(r0, r1, r2, r3);
         if (idx < 0) idx = 0;
     } else {
-        if (a.npts >= MAX_POINTS) {
+        if (a.npts >= a.cap_pts) {
             a.err |= ERR_POINT_OVERFLOW;
             return -1;
         }
@@ -2280,7 +2317,7 @@ RSG_DN void convex_vs_plane(const BatchView& bv, Ctx& a, Manifold& m, const Xf& 
 // btAlignedObjectArray::quickSortInternal (B/LinearMath/btAlignedObjectArray.h:370-400) over manifold
 // indices keyed by island id; sub-ranges are disjoint, so an explicit stack gives the same result.
 RSG_D void island_quicksort(const Ctx& a, int* v, int n) {
-    int stk_lo[MAX_MANIFOLDS], stk_hi[MAX_MANIFOLDS];
+    int stk_lo[MAX_PAIRS], stk_hi[MAX_PAIRS];
     int sp = 0;
     stk_lo[sp] = 0;
     stk_hi[sp] = n - 1;
@@ -2307,8 +2344,10 @@ RSG_D void island_quicksort(const Ctx& a, int* v, int n) {
 // ---------------------------------------------------------------- solver
 // btSequentialImpulseConstraintSolver (B/BulletDynamics/ConstraintSolver/btSequentialImpulseConstraintSolver.cpp)
 // in RocketSim's configuration: 10 iterations, split impulse, no warm starting (manifolds are rebuilt
-// every tick), one friction direction, erp2 0.8.
-constexpr int SB_FIXED = MAX_CARS + 1;
+// every tick), one friction direction, erp2 0.8.  A row's body B is either a dynamic body (its
+// Jacobian on B is the negated normal) or the fixed body (zero); the constraint-force mixing term is
+// zero for every row RocketSim builds, so rows keep neither.
+constexpr int SB_FIXED = MAX_DYN;
 struct SBody {
     int obj;  // -1 fixed body
     V3 dlv, dav, push, turn;
@@ -2319,14 +2358,10 @@ struct SBody {
 struct Row {
     int8_t ba, bb, special;
     int16_t friction_index;
-    V3 n1, n2, rp1xn, rp2xn, angA, angB;
-    float jac_inv, rhs, rhs_pen, cfm, lo, hi, applied, applied_push, friction;
+    V3 n1, rp1xn, rp2xn, angA, angB;
+    float jac_inv, rhs, rhs_pen, applied, applied_push, friction;
 };
-struct Solver {
-    SBody b[MAX_CARS + 2];
-    int nc, nf;
-    Row c[MAX_ROWS], f[MAX_ROWS];
-};
+RSG_D V3 row_n2(const Row& r) { return r.bb == SB_FIXED ? V3(0, 0, 0) : -r.n1; }
 
 RSG_D void init_solver_body(Ctx& a, SBody& sb, int obj, float dt) {
     Body& b = a.body(obj);
@@ -2340,14 +2375,16 @@ RSG_D void init_solver_body(Ctx& a, SBody& sb, int obj, float dt) {
     sb.dlv = sb.dav = sb.push = sb.turn = V3(0, 0, 0);
 }
 
-RSG_D void setup_contact_row(Ctx& a, Solver& s, Row& r, int ia, int ib, const MPoint& cp, V3 rel1, V3 rel2, float dt) {
-    SBody& A = s.b[ia];
-    SBody& B = s.b[ib];
+RSG_D void setup_contact_row(Ctx& a, Row& r, int ia, int ib, const MPoint& cp, V3 rel1, V3 rel2, float dt) {
+    SBody& A = a.sb[ia];
+    SBody& B = a.sb[ib];
     Body* rb0 = A.obj >= 0 ? &a.body(A.obj) : nullptr;
     Body* rb1 = B.obj >= 0 ? &a.body(B.obj) : nullptr;
     float inv_dt = 1.f / dt;
     float cfm = 0.f * inv_dt;
     const float erp = 0.8f;  // m_erp2 (src/Sim/Arena/Arena.cpp:473-475)
+    r.ba = (int8_t)ia;
+    r.bb = (int8_t)ib;
     V3 ta0 = cross(rel1, cp.normal);
     r.angA = rb0 ? rb0->inv_inertia_world * ta0 : V3(0, 0, 0);
     V3 ta1 = cross(rel2, cp.normal);
@@ -2356,8 +2393,11 @@ RSG_D void setup_contact_row(Ctx& a, Solver& s, Row& r, int ia, int ib, const MP
     if (rb0) { V3 v = cross(r.angA, rel1); d0 = rb0->inv_mass + dot(cp.normal, v); }
     if (rb1) { V3 v = cross(-r.angB, rel2); d1 = rb1->inv_mass + dot(cp.normal, v); }
     r.jac_inv = 1.f / (d0 + d1 + cfm);
-    if (rb0) { r.n1 = cp.normal; r.rp1xn = ta0; } else { r.n1 = V3(0, 0, 0); r.rp1xn = V3(0, 0, 0); }
-    if (rb1) { r.n2 = -cp.normal; r.rp2xn = -ta1; } else { r.n2 = V3(0, 0, 0); r.rp2xn = V3(0, 0, 0); }
+    V3 n1 = rb0 ? cp.normal : V3(0, 0, 0);
+    V3 n2 = rb1 ? -cp.normal : V3(0, 0, 0);
+    r.n1 = n1;
+    r.rp1xn = rb0 ? ta0 : V3(0, 0, 0);
+    r.rp2xn = rb1 ? -ta1 : V3(0, 0, 0);
     float restitution = 0.f;
     float penetration = cp.dist + 0.f;
     {
@@ -2374,8 +2414,8 @@ RSG_D void setup_contact_row(Ctx& a, Solver& s, Row& r, int ia, int ib, const MP
     {
         V3 efA = A.obj >= 0 ? A.ext_f : V3(0, 0, 0), etA = A.obj >= 0 ? A.ext_t : V3(0, 0, 0);
         V3 efB = B.obj >= 0 ? B.ext_f : V3(0, 0, 0), etB = B.obj >= 0 ? B.ext_t : V3(0, 0, 0);
-        float v1 = dot(r.n1, A.lv + efA) + dot(r.rp1xn, A.av + etA);
-        float v2 = dot(r.n2, B.lv + efB) + dot(r.rp2xn, B.av + etB);
+        float v1 = dot(n1, A.lv + efA) + dot(r.rp1xn, A.av + etA);
+        float v2 = dot(n2, B.lv + efB) + dot(r.rp2xn, B.av + etB);
         float rel_vel = v1 + v2;
         float pos_err = 0.f;
         float vel_err = restitution - rel_vel;
@@ -2390,16 +2430,13 @@ RSG_D void setup_contact_row(Ctx& a, Solver& s, Row& r, int ia, int ib, const MP
             r.rhs = vel_imp;
             r.rhs_pen = pen_imp;
         }
-        r.cfm = cfm * r.jac_inv;
-        r.lo = 0;
-        r.hi = 1e10f;
     }
     r.special = cp.special;
 }
 
-RSG_D void setup_friction_row(Ctx& a, Solver& s, Row& r, V3 n, int ia, int ib, float friction, V3 rel1, V3 rel2) {
-    SBody& A = s.b[ia];
-    SBody& B = s.b[ib];
+RSG_D void setup_friction_row(Ctx& a, Row& r, V3 n, int ia, int ib, float friction, V3 rel1, V3 rel2) {
+    SBody& A = a.sb[ia];
+    SBody& B = a.sb[ib];
     Body* b0 = A.obj >= 0 ? &a.body(A.obj) : nullptr;
     Body* b1 = B.obj >= 0 ? &a.body(B.obj) : nullptr;
     r.ba = (int8_t)ia;
@@ -2408,41 +2445,38 @@ RSG_D void setup_friction_row(Ctx& a, Solver& s, Row& r, V3 n, int ia, int ib, f
     r.friction = friction;
     r.applied = 0;
     r.applied_push = 0;
+    V3 n1 = b0 ? n : V3(0, 0, 0), n2 = b1 ? -n : V3(0, 0, 0);
+    r.n1 = n1;
     if (b0) {
-        r.n1 = n;
-        V3 t = cross(rel1, r.n1);
+        V3 t = cross(rel1, n1);
         r.rp1xn = t;
         r.angA = b0->inv_inertia_world * t;
     } else {
-        r.n1 = r.rp1xn = r.angA = V3(0, 0, 0);
+        r.rp1xn = r.angA = V3(0, 0, 0);
     }
     if (b1) {
-        r.n2 = -n;
-        V3 t = cross(rel2, r.n2);
+        V3 t = cross(rel2, n2);
         r.rp2xn = t;
         r.angB = b1->inv_inertia_world * t;
     } else {
-        r.n2 = r.rp2xn = r.angB = V3(0, 0, 0);
+        r.rp2xn = r.angB = V3(0, 0, 0);
     }
     float d0 = 0, d1 = 0;
     if (b0) { V3 v = cross(r.angA, rel1); d0 = b0->inv_mass + dot(n, v); }
     if (b1) { V3 v = cross(-r.angB, rel2); d1 = b1->inv_mass + dot(n, v); }
     r.jac_inv = 1.f / (d0 + d1);
-    float v1 = dot(r.n1, b0 ? A.lv + A.ext_f : V3(0, 0, 0)) + dot(r.rp1xn, b0 ? A.av : V3(0, 0, 0));
-    float v2 = dot(r.n2, b1 ? B.lv + B.ext_f : V3(0, 0, 0)) + dot(r.rp2xn, b1 ? B.av : V3(0, 0, 0));
+    float v1 = dot(n1, b0 ? A.lv + A.ext_f : V3(0, 0, 0)) + dot(r.rp1xn, b0 ? A.av : V3(0, 0, 0));
+    float v2 = dot(n2, b1 ? B.lv + B.ext_f : V3(0, 0, 0)) + dot(r.rp2xn, b1 ? B.av : V3(0, 0, 0));
     float rel_vel = v1 + v2;
     float vel_imp = (0.f - rel_vel) * r.jac_inv;
     r.rhs = 0.f + vel_imp;
     r.rhs_pen = 0.f;
-    r.cfm = 0.f;
-    r.lo = -r.friction;
-    r.hi = r.friction;
 }
 
 // convertContactInner friction part (btSequentialImpulseConstraintSolver.cpp:1071-1162)
-RSG_D void add_friction(Ctx& a, Solver& s, int ia, int ib, V3 normal, float friction, V3 rel1, V3 rel2, int fidx) {
-    SBody& A = s.b[ia];
-    SBody& B = s.b[ib];
+RSG_D void add_friction(Ctx& a, int& nf, int ia, int ib, V3 normal, float friction, V3 rel1, V3 rel2, int fidx) {
+    SBody& A = a.sb[ia];
+    SBody& B = a.sb[ib];
     V3 v1 = A.obj >= 0 ? A.lv + A.ext_f + cross(A.av + A.ext_t, rel1) : V3(0, 0, 0);
     V3 v2 = B.obj >= 0 ? B.lv + B.ext_f + cross(B.av + B.ext_t, rel2) : V3(0, 0, 0);
     V3 vel = v1 - v2;
@@ -2456,56 +2490,58 @@ RSG_D void add_friction(Ctx& a, Solver& s, int ia, int ib, V3 normal, float fric
         V3 d2;
         plane_space(normal, dir, d2);
     }
-    Row& fr = s.f[s.nf++];
+    Row& fr = a.rows_f[nf++];
     fr.friction_index = (int16_t)fidx;
-    setup_friction_row(a, s, fr, dir, ia, ib, friction, rel1, rel2);
+    setup_friction_row(a, fr, dir, ia, ib, friction, rel1, rel2);
 }
 
-RSG_D void solve_row(Solver& s, Row& c, bool lower_only) {  // gResolveSingleConstraintRow{Generic,LowerLimit}
-    SBody& A = s.b[c.ba];
-    SBody& B = s.b[c.bb];
-    float d = c.rhs - c.applied * c.cfm;
+// gResolveSingleConstraintRowGeneric / LowerLimit with the row's limits passed in
+RSG_D void solve_row(Ctx& a, Row& c, float lo, float hi, bool lower_only) {
+    SBody& A = a.sb[c.ba];
+    SBody& B = a.sb[c.bb];
+    V3 n2 = row_n2(c);
+    float d = c.rhs - c.applied * 0.f;
     float d1 = simd_dot(c.n1, A.dlv) + simd_dot(c.rp1xn, A.dav);
-    float d2 = simd_dot(c.n2, B.dlv) + simd_dot(c.rp2xn, B.dav);
+    float d2 = simd_dot(n2, B.dlv) + simd_dot(c.rp2xn, B.dav);
     d -= d1 * c.jac_inv;
     d -= d2 * c.jac_inv;
     float sum = c.applied + d;
-    if (sum < c.lo) { d = c.lo - c.applied; c.applied = c.lo; }
-    else if (!lower_only && sum > c.hi) { d = c.hi - c.applied; c.applied = c.hi; }
+    if (sum < lo) { d = lo - c.applied; c.applied = lo; }
+    else if (!lower_only && sum > hi) { d = hi - c.applied; c.applied = hi; }
     else c.applied = sum;
     if (A.obj >= 0) { A.dlv += c.n1 * A.inv_mass * d; A.dav += c.angA * d; }
-    if (B.obj >= 0) { B.dlv += c.n2 * B.inv_mass * d; B.dav += c.angB * d; }
+    if (B.obj >= 0) { B.dlv += n2 * B.inv_mass * d; B.dav += c.angB * d; }
 }
 
-RSG_D float solve_split(Solver& s, Row& c) {  // gResolveSplitPenetrationImpulse_sse2
+RSG_D float solve_split(Ctx& a, Row& c) {  // gResolveSplitPenetrationImpulse_sse2
     if (!c.rhs_pen) return 0.f;
-    SBody& A = s.b[c.ba];
-    SBody& B = s.b[c.bb];
-    float d = c.rhs_pen - c.applied_push * c.cfm;
+    SBody& A = a.sb[c.ba];
+    SBody& B = a.sb[c.bb];
+    V3 n2 = row_n2(c);
+    float d = c.rhs_pen - c.applied_push * 0.f;
     float d1 = simd_dot(c.n1, A.push) + simd_dot(c.rp1xn, A.turn);
-    float d2 = simd_dot(c.n2, B.push) + simd_dot(c.rp2xn, B.turn);
+    float d2 = simd_dot(n2, B.push) + simd_dot(c.rp2xn, B.turn);
     d -= d1 * c.jac_inv;
     d -= d2 * c.jac_inv;
     float sum = c.applied_push + d;
-    if (sum < c.lo) { d = c.lo - c.applied_push; c.applied_push = c.lo; }
+    if (sum < 0.f) { d = 0.f - c.applied_push; c.applied_push = 0.f; }
     else c.applied_push = sum;
     if (A.obj >= 0) { A.push += c.n1 * A.inv_mass * d; A.turn += c.angA * d; }
-    if (B.obj >= 0) { B.push += c.n2 * B.inv_mass * d; B.turn += c.angB * d; }
+    if (B.obj >= 0) { B.push += n2 * B.inv_mass * d; B.turn += c.angB * d; }
     return (float)((double)d * (1. / (double)c.jac_inv));
 }
 
 // Solves one batch: `bodies` are dynamic object ids in island order, `mans` manifold indices in
 // sorted island order (btSequentialImpulseConstraintSolver::solveGroup)
 RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, float dt) {
-    Solver s;
-    s.nc = s.nf = 0;
-    int sb_of[MAX_CARS + 1];
-    for (int i = 0; i <= MAX_CARS; i++) sb_of[i] = -1;
+    int nc = 0, nf = 0;
+    int sb_of[MAX_DYN];
+    for (int i = 0; i < MAX_DYN; i++) sb_of[i] = -1;
     for (int i = 0; i < nb; i++) {
-        init_solver_body(a, s.b[i], bodies[i], dt);
+        init_solver_body(a, a.sb[i], bodies[i], dt);
         sb_of[bodies[i] - OBJ_BALL] = i;
     }
-    SBody& fixed = s.b[SB_FIXED];
+    SBody& fixed = a.sb[SB_FIXED];
     fixed.obj = -1;
     fixed.xf = xf_identity();
     fixed.inv_mass = 0;
@@ -2518,14 +2554,12 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
         for (int j = 0; j < m.n; j++) {
             const MPoint& cp = a.pts[m.pt[j]];
             if (!(cp.dist <= BT_LARGE)) continue;
-            if (s.nc >= MAX_ROWS) { a.err |= ERR_ROW_OVERFLOW; continue; }
-            Row& r = s.c[s.nc];
-            r.ba = (int8_t)ia;
-            r.bb = (int8_t)ib;
+            if (nc >= a.cap_rows) { a.err |= ERR_ROW_OVERFLOW; continue; }
+            Row& r = a.rows_c[nc];
             V3 rel1 = cp.pos_a - obj_xf(a, m.body0).o;
             V3 rel2 = cp.pos_b - obj_xf(a, m.body1).o;
-            setup_contact_row(a, s, r, ia, ib, cp, rel1, rel2, dt);
-            r.friction_index = (int16_t)s.nf;
+            setup_contact_row(a, r, ia, ib, cp, rel1, rel2, dt);
+            r.friction_index = (int16_t)nf;
             if (cp.special) {
                 for (int k = 0; k < 2; k++) {
                     int o = k ? m.body1 : m.body0;
@@ -2539,8 +2573,8 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
                     }
                 }
             }
-            int fidx = s.nc++;
-            add_friction(a, s, ia, ib, cp.normal, cp.friction, rel1, rel2, fidx);
+            int fidx = nc++;
+            add_friction(a, nf, ia, ib, cp.normal, cp.friction, rel1, rel2, fidx);
         }
     }
     // RocketSim's averaged ball-world contact (convertContactSpecial,
@@ -2556,16 +2590,14 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
             tmp.friction = b.sp_friction;
             tmp.restitution = b.sp_restitution;
             tmp.special = false;
-            if (s.nc < MAX_ROWS) {
-                Row& r = s.c[s.nc];
-                r.ba = (int8_t)i;
-                r.bb = (int8_t)SB_FIXED;
+            if (nc < a.cap_rows) {
+                Row& r = a.rows_c[nc];
                 V3 rel1 = nrm * -dist, rel2(0, 0, 0);
-                setup_contact_row(a, s, r, i, SB_FIXED, tmp, rel1, rel2, dt);
-                int fidx = s.nc;
-                r.friction_index = (int16_t)s.nf;
-                s.nc++;
-                add_friction(a, s, i, SB_FIXED, tmp.normal, tmp.friction, rel1, rel2, fidx);
+                setup_contact_row(a, r, i, SB_FIXED, tmp, rel1, rel2, dt);
+                int fidx = nc;
+                r.friction_index = (int16_t)nf;
+                nc++;
+                add_friction(a, nf, i, SB_FIXED, tmp.normal, tmp.friction, rel1, rel2, fidx);
             } else {
                 a.err |= ERR_ROW_OVERFLOW;
             }
@@ -2577,31 +2609,27 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
     const int ITER = 10;
     for (int it = 0; it < ITER; it++) {
         float lsr = 0;
-        for (int k = 0; k < s.nc; k++) {
-            float res = solve_split(s, s.c[k]);
+        for (int k = 0; k < nc; k++) {
+            float res = solve_split(a, a.rows_c[k]);
             float r2 = res * res;
             lsr = lsr < r2 ? r2 : lsr;
         }
         if (lsr <= 0.f || it >= ITER - 1) break;
     }
     for (int it = 0; it < ITER; it++) {
-        for (int k = 0; k < s.nc; k++) {
-            if (s.c[k].special) continue;
-            solve_row(s, s.c[k], true);
+        for (int k = 0; k < nc; k++) {
+            if (a.rows_c[k].special) continue;
+            solve_row(a, a.rows_c[k], 0.f, 1e10f, true);
         }
-        for (int k = 0; k < s.nf; k++) {
-            Row& f = s.f[k];
-            float total = s.c[f.friction_index].applied;
-            if (total > 0.f) {
-                f.lo = -(f.friction * total);
-                f.hi = f.friction * total;
-                solve_row(s, f, false);
-            }
+        for (int k = 0; k < nf; k++) {
+            Row& f = a.rows_f[k];
+            float total = a.rows_c[f.friction_index].applied;
+            if (total > 0.f) solve_row(a, f, -(f.friction * total), f.friction * total, false);
         }
     }
     // writeBackBodies (btSequentialImpulseConstraintSolver.cpp:1878-1904)
     for (int i = 0; i < nb; i++) {
-        SBody& sb = s.b[i];
+        SBody& sb = a.sb[i];
         Body& b = a.body(sb.obj);
         sb.lv += sb.dlv;
         sb.av += sb.dav;
@@ -2621,41 +2649,13 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
 // (src/Sim/Arena/Arena.cpp:731, B/BulletDynamics/Dynamics/btDiscreteDynamicsWorld.cpp:360-450)
 RSG_D uint32_t grid_cell_index(const DevGrid& g, int i, int j, int k) { return (uint32_t)(i * g.ny * g.nz + j * g.nz + k); }
 
-RSG_D void update_bp_aabb(const BatchView& bv, Ctx& a, int obj) {  // updateSingleAabb + btRSBroadphase::setAabb
-    V3 mn, mx, mn2, mx2;
-    Body& b = a.body(obj);
-    if (obj == OBJ_BALL) {
-        ball_aabb(b.xf, mn, mx);
-        ball_aabb(b.interp, mn2, mx2);
-    } else {
-        Car& c = a.cars[obj - OBJ_CAR0];
-        car_compound_aabb(c, b.xf, mn, mx);
-        car_compound_aabb(c, b.interp, mn2, mx2);
-    }
-    V3 th(0.02f, 0.02f, 0.02f);
-    mn -= th; mx += th;
-    mn2 -= th; mx2 += th;
-    mn = vmin(mn, mn2);
-    mx = vmax(mx, mx2);
-    b.bp_min = mn;
-    b.bp_max = mx;
-    int i, j, k;
-    grid_idx(bv.grid, mn, i, j, k);
-    uint32_t nidx = grid_cell_index(bv.grid, i, j, k);
-    if (b.cell != nidx) {
-        b.cell = nidx;
-        b.ci = i; b.cj = j; b.ck = k;
-        b.cell_seq = a.seq++;
-    }
-}
-
 RSG_D bool has_pair(const Ctx& a, int x, int y) {
     for (int p = 0; p < a.npairs; p++)
         if ((a.pair0[p] == x && a.pair1[p] == y) || (a.pair0[p] == y && a.pair1[p] == x)) return true;
     return false;
 }
 RSG_D void add_pair(Ctx& a, int x, int y) {
-    if (a.npairs >= MAX_PAIRS) { a.err |= ERR_PAIR_OVERFLOW; return; }
+    if (a.npairs >= a.cap_pairs) { a.err |= ERR_PAIR_OVERFLOW; return; }
     a.pair0[a.npairs] = (int8_t)x;
     a.pair1[a.npairs] = (int8_t)y;
     a.npairs++;
@@ -2670,22 +2670,58 @@ RSG_D Manifold& new_manifold(Ctx& a, int b0, int b1, float breaking) {
     return m;
 }
 
-RSG_DN void step_world(const BatchView& bv, Ctx& a) {
+// Phase 1 of a world step, one lane per dynamic object (ball = lane 0, cars = lanes 1..): gravity,
+// damping and predicted transform, broadphase AABB and voxel cell.  Cell changes take their sequence
+// numbers in object order (a ballot prefix count), like the reference's serial AABB update.
+RSG_D void step_bodies_pre(const BatchView& bv, Ctx& a, int lane) {
     const float dt = bv.dt;
-    const int nd = 1 + a.ncars;  // dynamic objects: ball, then cars in AddCar order
-    // applyGravity (btDiscreteDynamicsWorld.cpp:265-277)
-    for (int d = 0; d < nd; d++) {
-        Body& b = a.body(OBJ_BALL + d);
+    const int nd = 1 + a.ncars;
+    bool changed = false;
+    if (lane < nd) {
+        Body& b = a.body(OBJ_BALL + lane);
+        // applyGravity (btDiscreteDynamicsWorld.cpp:265-277)
         if (b.is_active()) b.total_force += V3(0, 0, RL::GRAVITY_Z * RL::UU_TO_BT) * (1.f / b.inv_mass);
-    }
-    // predictUnconstraintMotion (btDiscreteDynamicsWorld.cpp:1029-1044)
-    for (int d = 0; d < nd; d++) {
-        Body& b = a.body(OBJ_BALL + d);
+        // predictUnconstraintMotion (btDiscreteDynamicsWorld.cpp:1029-1044)
         b.lin_vel *= powf(1.f - b.lin_damping, dt);
         b.ang_vel *= powf(1.f - 0.f, dt);
         integrate_transform(b.xf, b.lin_vel, b.ang_vel, dt, b.no_rot, b.interp);
+        // updateSingleAabb + btRSBroadphase::setAabb
+        V3 mn, mx, mn2, mx2;
+        if (lane == 0) {
+            ball_aabb(b.xf, mn, mx);
+            ball_aabb(b.interp, mn2, mx2);
+        } else {
+            Car& c = a.cars[lane - 1];
+            car_compound_aabb(c, b.xf, mn, mx);
+            car_compound_aabb(c, b.interp, mn2, mx2);
+        }
+        V3 th(0.02f, 0.02f, 0.02f);
+        mn -= th; mx += th;
+        mn2 -= th; mx2 += th;
+        mn = vmin(mn, mn2);
+        mx = vmax(mx, mx2);
+        b.bp_min = mn;
+        b.bp_max = mx;
+        int i, j, k;
+        grid_idx(bv.grid, mn, i, j, k);
+        uint32_t nidx = grid_cell_index(bv.grid, i, j, k);
+        if (b.cell != nidx) {
+            changed = true;
+            b.cell = nidx;
+            b.ci = i; b.cj = j; b.ck = k;
+        }
     }
-    for (int d = 0; d < nd; d++) update_bp_aabb(bv, a, OBJ_BALL + d);
+    unsigned mask = __ballot_sync(0xffffffffu, changed);
+    if (changed) a.body(OBJ_BALL + lane).cell_seq = a.seq + __popc(mask & ((1u << lane) - 1u));
+    __syncwarp();
+    if (lane == 0) a.seq += __popc(mask);
+    __syncwarp();
+}
+
+// Phase 2 of a world step, on one lane: pairs, narrow phase, islands and the solver.
+RSG_DN void step_collide(const BatchView& bv, Ctx& a) {
+    const float dt = bv.dt;
+    const int nd = 1 + a.ncars;
     // calculateOverlappingPairs (btRSBroadphase.cpp:392-468)
     a.npairs = 0;
     V3 mesh_mn, mesh_mx;
@@ -2866,7 +2902,7 @@ RSG_DN void step_world(const BatchView& bv, Ctx& a) {
             }
         }
     }
-    int island_mans[MAX_MANIFOLDS];
+    int island_mans[MAX_PAIRS];
     int nim = 0;
     for (int mi = 0; mi < a.nman; mi++) {
         Manifold& m = a.man[mi];
@@ -2887,7 +2923,7 @@ RSG_DN void step_world(const BatchView& bv, Ctx& a) {
     if (nim > 1) island_quicksort(a, island_mans, nim);
     // processIslands: bodies and manifolds of awake islands, solved as one batch
     int bodies[MAX_CARS + 1], nb = 0;
-    int solve_mans[MAX_MANIFOLDS], nsm = 0;
+    int solve_mans[MAX_PAIRS], nsm = 0;
     for (int id = 0; id < nd; id++) {
         bool present = false, sleeping = true;
         for (int i = 0; i < nd; i++)
@@ -2903,8 +2939,14 @@ RSG_DN void step_world(const BatchView& bv, Ctx& a) {
     }
     a.solver_dt = dt;
     if (nb > 0) solve(a, bodies, nb, solve_mans, nsm, dt);
+}
+
+// Phase 3 of a world step, one lane per dynamic object: integration, activation, force reset.
+RSG_D void step_bodies_post(const BatchView& bv, Ctx& a, int lane) {
+    const float dt = bv.dt;
+    const int nd = 1 + a.ncars;
     // integrateTransforms (btDiscreteDynamicsWorld.cpp:889-991)
-    for (int d = 0; d < nd; d++) {
+    for (int d = lane; d < nd; d += 32) {
         Body& b = a.body(OBJ_BALL + d);
         if (b.is_active()) {
             Xf nt;
@@ -2913,12 +2955,9 @@ RSG_DN void step_world(const BatchView& bv, Ctx& a) {
             b.xf = nt;
             b.update_inertia();
         }
-    }
-    // updateActivationState (btDiscreteDynamicsWorld.cpp:516-551).  The deactivation timer can only
-    // move a body to WANTS_DEACTIVATION, which the next tick overwrites before anything reads it,
-    // so it is not carried between ticks.
-    for (int d = 0; d < nd; d++) {
-        Body& b = a.body(OBJ_BALL + d);
+        // updateActivationState (btDiscreteDynamicsWorld.cpp:516-551).  The deactivation timer can
+        // only move a body to WANTS_DEACTIVATION, which the next tick overwrites before anything
+        // reads it, so it is not carried between ticks.
         if (b.act == ISLAND_SLEEPING || b.act == DISABLE_DEACTIVATION) {
         } else if (len2(b.lin_vel) < 0.8f * 0.8f && len2(b.ang_vel) < 1.f * 1.f) {
         } else {
@@ -2984,89 +3023,136 @@ RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Si
             }
 }
 
-// Arena::Step, one tick (src/Sim/Arena/Arena.cpp:689-756)
-RSG_DN void arena_tick(const BatchView& bv, Ctx& a) {
-    Body& ball = a.ball;
-    bool ball_off = ball.act == DISABLE_DEACTIVATION || ball.act == DISABLE_SIMULATION;
-    if (len2(ball.lin_vel) == 0 && len2(ball.ang_vel) == 0) {
-        if (!ball_off) ball.act = ISLAND_SLEEPING;
-    } else {
-        if (!ball_off) ball.act = ACTIVE_TAG;
+// Arena::Step, one tick (src/Sim/Arena/Arena.cpp:689-756), run by the 32 lanes of one warp.
+//
+// Work that is independent in the reference runs on separate lanes: the 16 suspension rays, the
+// per-car logic after the rays, per-body integration and the boost pads.  Two situations make the
+// cars depend on each other within the pre-tick, and then it runs car by car in update order
+// like the reference: a car that is or just was demolished (its pre-tick changes its transform and
+// collision response, which later cars' rays must see and earlier cars' rays must not), and a wheel
+// resting on another car (its friction reads that car's velocity after that car's pre-tick).
+// Collision detection, islands and the solver run on lane 0.
+RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
+    const unsigned FULL = 0xffffffffu;
+    if (lane == 0) {
+        Body& ball = a.ball;
+        bool ball_off = ball.act == DISABLE_DEACTIVATION || ball.act == DISABLE_SIMULATION;
+        if (len2(ball.lin_vel) == 0 && len2(ball.ang_vel) == 0) {
+            if (!ball_off) ball.act = ISLAND_SLEEPING;
+        } else {
+            if (!ball_off) ball.act = ACTIVE_TAG;
+        }
+        int serial = 0;
+        for (int i = 0; i < a.ncars; i++) serial |= a.cars[i].f(F_DEMOED) || a.cars[i].rb.no_contact_response;
+        a.serial = serial;
     }
-    bool ball_only = a.ncars == 0;
-    for (int k = 0; k < a.ncars; k++) car_pre_tick(bv, a, a.cars[a.order[k]]);
-    if (bv.has_arena && !ball_only)
-        for (int i = 0; i < NUM_PADS; i++) {  // BoostPad::_PreTickUpdate (src/Sim/BoostPad/BoostPad.cpp:51-60)
+    __syncwarp();
+    if (a.serial) {
+        if (lane == 0)
+            for (int k = 0; k < a.ncars; k++) car_pre_tick(bv, a, a.cars[a.order[k]]);
+    } else {
+        if (lane < a.ncars) car_pre_before_rays(a.cars[lane]);
+        __syncwarp();
+        bool on_car = false;
+        if (lane < 4 * a.ncars) {
+            Car& c = a.cars[lane >> 2];
+            ray_cast_wheel(bv, a, c, lane & 3);
+            on_car = c.w[lane & 3].ground >= OBJ_CAR0;
+        }
+        bool any_on_car = __any_sync(FULL, on_car);
+        __syncwarp();
+        if (any_on_car) {
+            if (lane == 0)
+                for (int k = 0; k < a.ncars; k++) car_pre_after_rays(bv, a, a.cars[a.order[k]]);
+        } else if (lane < a.ncars) {
+            car_pre_after_rays(bv, a, a.cars[lane]);
+        }
+    }
+    __syncwarp();
+    if (bv.has_arena && a.ncars > 0)
+        for (int i = lane; i < NUM_PADS; i += 32) {  // BoostPad::_PreTickUpdate (src/Sim/BoostPad/BoostPad.cpp:51-60)
             Pad& p = a.pads[i];
             if (p.cooldown > 0) p.cooldown = rs_maxf(p.cooldown - bv.dt, 0);
             p.active = (p.cooldown == 0);
             p.cur_locked = -1;
         }
-    step_world(bv, a);
-    for (int k = 0; k < a.ncars; k++) {
-        int ci = a.order[k];
-        car_post_tick(a.cars[ci], bv.dt);
-        car_finish_physics(a.cars[ci]);
-        if (bv.has_arena) grid_check(a, ci);
+    __syncwarp();
+    step_bodies_pre(bv, a, lane);
+    if (lane == 0) step_collide(bv, a);
+    __syncwarp();
+    step_bodies_post(bv, a, lane);
+    __syncwarp();
+    if (lane < a.ncars) {
+        car_post_tick(a.cars[lane], bv.dt);
+        car_finish_physics(a.cars[lane]);
     }
-    if (bv.has_arena && !ball_only)
-        for (int i = 0; i < NUM_PADS; i++) {  // BoostPad::_PostTickUpdate (src/Sim/BoostPad/BoostPad.cpp:88-105)
-            Pad& p = a.pads[i];
-            uint32_t locked = 0;
-            if (p.cur_locked >= 0) {
-                Car& c = a.cars[p.cur_locked];
-                locked = c.id;
-                if (p.active) {
-                    bool big = i < 6;
-                    c.boost = rs_minf(c.boost + (big ? RL::PAD_BOOST_BIG : RL::PAD_BOOST_SMALL), RL::BOOST_MAX);
-                    p.active = false;
-                    p.cooldown = big ? RL::PAD_COOLDOWN_BIG : RL::PAD_COOLDOWN_SMALL;
+    __syncwarp();
+    if (lane == 0) {
+        if (bv.has_arena)
+            for (int k = 0; k < a.ncars; k++) grid_check(a, a.order[k]);
+        if (bv.has_arena && a.ncars > 0)
+            for (int i = 0; i < NUM_PADS; i++) {  // BoostPad::_PostTickUpdate (src/Sim/BoostPad/BoostPad.cpp:88-105)
+                Pad& p = a.pads[i];
+                uint32_t locked = 0;
+                if (p.cur_locked >= 0) {
+                    Car& c = a.cars[p.cur_locked];
+                    locked = c.id;
+                    if (p.active) {
+                        bool big = i < 6;
+                        c.boost = rs_minf(c.boost + (big ? RL::PAD_BOOST_BIG : RL::PAD_BOOST_SMALL), RL::BOOST_MAX);
+                        p.active = false;
+                        p.cooldown = big ? RL::PAD_COOLDOWN_BIG : RL::PAD_COOLDOWN_SMALL;
+                    }
                 }
+                p.prev_locked = locked;
             }
-            p.prev_locked = locked;
+        Body& ball = a.ball;
+        {  // Ball::_FinishPhysicsTick (src/Sim/Ball/Ball.cpp:117-143)
+            if (!is_zero(a.ball_cache)) {
+                ball.lin_vel += a.ball_cache;
+                a.ball_cache = V3(0, 0, 0);
+            }
+            V3 v = ball.lin_vel, w = ball.ang_vel;
+            const float ms = RL::BALL_MAX_SPEED * RL::UU_TO_BT;
+            if (len2(v) > ms * ms) v = normalized(v) * ms;
+            if (len2(w) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) w = normalized(w) * RL::BALL_MAX_ANG_SPEED;
+            ball.lin_vel = v;
+            ball.ang_vel = w;
+            a.ball_ticks++;
         }
-    {  // Ball::_FinishPhysicsTick (src/Sim/Ball/Ball.cpp:117-143)
-        if (!is_zero(a.ball_cache)) {
-            ball.lin_vel += a.ball_cache;
-            a.ball_cache = V3(0, 0, 0);
+        if (bv.has_arena && ball_scored(a)) {
+            uint32_t team = (-(a.ball.xf.o.y) < 0) ? 0u : 1u;  // RS_TEAM_FROM_Y(-y)
+            push_event(a, RSG_EVENT_GOAL, team, 0, 0);
         }
-        V3 v = ball.lin_vel, w = ball.ang_vel;
-        const float ms = RL::BALL_MAX_SPEED * RL::UU_TO_BT;
-        if (len2(v) > ms * ms) v = normalized(v) * ms;
-        if (len2(w) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) w = normalized(w) * RL::BALL_MAX_ANG_SPEED;
-        ball.lin_vel = v;
-        ball.ang_vel = w;
-        a.ball_ticks++;
+        a.tick++;
+        a.stepped = true;
     }
-    if (bv.has_arena && ball_scored(a)) {
-        uint32_t team = (-(a.ball.xf.o.y) < 0) ? 0u : 1u;  // RS_TEAM_FROM_Y(-y)
-        push_event(a, RSG_EVENT_GOAL, team, 0, 0);
-    }
-    a.tick++;
+    __syncwarp();
 }
 
-// ---------------------------------------------------------------- SoA load / store
+// ---------------------------------------------------------------- record load / store
 RSG_D uint32_t pack_cell(int i, int j, int k) { return (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16); }
 
-struct SoA {  // address helpers for one arena
+struct SoA {  // field accessors of one arena's record and scalars
     const BatchView& bv;
     int ar;
-    RSG_D float& cf(int f, int s) const { return bv.cf[((size_t)f * bv.MC + s) * bv.A + ar]; }
-    RSG_D uint32_t& cu(int f, int s) const { return bv.cu[((size_t)f * bv.MC + s) * bv.A + ar]; }
-    RSG_D float& bf(int f) const { return bv.bf[(size_t)f * bv.A + ar]; }
-    RSG_D uint32_t& bu(int f) const { return bv.bu[(size_t)f * bv.A + ar]; }
-    RSG_D float& pf(int f, int p) const { return bv.pf[((size_t)f * NUM_PADS + p) * bv.A + ar]; }
-    RSG_D uint32_t& pu(int f, int p) const { return bv.pu[((size_t)f * NUM_PADS + p) * bv.A + ar]; }
+    RSG_D uint32_t* r() const { return bv.rec + (size_t)ar * bv.rec_words; }
+    RSG_D float& cf(int f, int s) const { return reinterpret_cast<float*>(r())[rec_car_f(f, s)]; }
+    RSG_D uint32_t& cu(int f, int s) const { return r()[rec_car_u(f, s)]; }
+    RSG_D float& bf(int f) const { return reinterpret_cast<float*>(r())[rec_ball_f(f)]; }
+    RSG_D uint32_t& bu(int f) const { return r()[rec_ball_u(f)]; }
+    RSG_D float& pf(int f, int p) const { return reinterpret_cast<float*>(r())[rec_pad_f(f, p)]; }
+    RSG_D uint32_t& pu(int f, int p) const { return r()[rec_pad_u(f, p)]; }
     RSG_D uint32_t& au(int f) const { return bv.au[(size_t)f * bv.A + ar]; }
     RSG_D V3 v3(int f, int s) const { return V3(cf(f, s), cf(f + 1, s), cf(f + 2, s)); }
     RSG_D void set_v3(int f, int s, V3 v) const { cf(f, s) = v.x; cf(f + 1, s) = v.y; cf(f + 2, s) = v.z; }
     RSG_D M3 m3(int f, int s) const {
         M3 m;
-        for (int r = 0; r < 3; r++) m.r[r] = v3(f + 3 * r, s);
+        for (int r_ = 0; r_ < 3; r_++) m.r[r_] = v3(f + 3 * r_, s);
         return m;
     }
     RSG_D void set_m3(int f, int s, const M3& m) const {
-        for (int r = 0; r < 3; r++) set_v3(f + 3 * r, s, m.r[r]);
+        for (int r_ = 0; r_ < 3; r_++) set_v3(f + 3 * r_, s, m.r[r_]);
     }
 };
 
@@ -3093,7 +3179,7 @@ RSG_D void body_common(Body& b) {
     b.update_inertia();
 }
 
-RSG_DN void load_ctx(const BatchView& bv, int ar, Ctx& a) {
+RSG_DN void load_arena(const BatchView& bv, int ar, Ctx& a) {  // scalars and ball (one lane)
     SoA s{bv, ar};
     a.ev = bv.events ? bv.events + (size_t)ar * MAX_EVENTS_PER_ARENA : nullptr;
     a.event_mask = bv.event_mask;
@@ -3130,7 +3216,11 @@ RSG_DN void load_ctx(const BatchView& bv, int ar, Ctx& a) {
     a.ball_ticks = (uint64_t)s.bu(BU_TICKS_LO) | ((uint64_t)s.bu(BU_TICKS_HI) << 32);
     a.ball_cache = V3(0, 0, 0);
     // cars (Car::_BulletSetup, src/Sim/Car/Car.cpp:195-292, derived per config on the host)
-    for (int i = 0; i < a.ncars; i++) {
+}
+
+RSG_DN void load_car(const BatchView& bv, int ar, Ctx& a, int i) {  // one car slot (one lane per car)
+    SoA s{bv, ar};
+    {
         Car& c = a.cars[i];
         c.cfg = bv.cfgs + s.cu(CU_CFG, i);
         c.obj = OBJ_CAR0 + i;
@@ -3189,7 +3279,11 @@ RSG_DN void load_ctx(const BatchView& bv, int ar, Ctx& a) {
         }
         c.vel_cache = s.v3(CF_VEL_CACHE, i);
     }
-    for (int p = 0; p < NUM_PADS; p++) {
+}
+
+RSG_D void load_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
+    SoA s{bv, ar};
+    for (int p = lane; p < NUM_PADS; p += 32) {
         Pad& pd = a.pads[p];
         pd.active = s.pu(PU_ACTIVE, p) != 0;
         pd.cooldown = s.pf(PF_COOLDOWN, p);
@@ -3198,7 +3292,7 @@ RSG_DN void load_ctx(const BatchView& bv, int ar, Ctx& a) {
     }
 }
 
-RSG_DN void store_ctx(const BatchView& bv, int ar, Ctx& a) {
+RSG_DN void store_arena(const BatchView& bv, int ar, Ctx& a) {
     SoA s{bv, ar};
     s.au(AU_TICK_LO) = (uint32_t)a.tick;
     s.au(AU_TICK_HI) = (uint32_t)(a.tick >> 32);
@@ -3219,7 +3313,11 @@ RSG_DN void store_ctx(const BatchView& bv, int ar, Ctx& a) {
     s.bu(BU_CELL_SEQ) = b.cell_seq;
     s.bu(BU_TICKS_LO) = (uint32_t)a.ball_ticks;
     s.bu(BU_TICKS_HI) = (uint32_t)(a.ball_ticks >> 32);
-    for (int i = 0; i < a.ncars; i++) {
+}
+
+RSG_DN void store_car(const BatchView& bv, int ar, Ctx& a, int i) {
+    SoA s{bv, ar};
+    {
         Car& c = a.cars[i];
         c.setf(F_NO_RESPONSE, c.rb.no_contact_response);
         s.cu(CU_FLAGS, i) = c.flags;
@@ -3269,13 +3367,59 @@ RSG_DN void store_ctx(const BatchView& bv, int ar, Ctx& a) {
         }
         s.set_v3(CF_VEL_CACHE, i, c.vel_cache);
     }
-    for (int p = 0; p < NUM_PADS; p++) {
+}
+
+RSG_D void store_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
+    SoA s{bv, ar};
+    for (int p = lane; p < NUM_PADS; p += 32) {
         Pad& pd = a.pads[p];
         s.pu(PU_ACTIVE, p) = pd.active ? 1u : 0u;
         s.pf(PF_COOLDOWN, p) = pd.cooldown;
         s.pu(PU_PREV_LOCKED, p) = pd.prev_locked;
         s.pu(PU_CUR_LOCKED, p) = (uint32_t)(pd.cur_locked + 1);
     }
+}
+
+// ---------------------------------------------------------------- shared-memory carve-out
+// Byte offsets of one arena's working set inside its warp's shared-memory region.
+struct SmemLayout {
+    int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, bytes;
+    ArenaCaps caps;
+};
+RSG_HD int align16(int x) { return (x + 15) & ~15; }
+RSG_HD SmemLayout smem_layout(int mc) {
+    SmemLayout L;
+    L.caps = arena_caps(mc);
+    int o = align16((int)sizeof(Ctx));
+    L.cars = o;   o = align16(o + (int)sizeof(Car) * mc);
+    L.pads = o;   o = align16(o + (int)sizeof(Pad) * NUM_PADS);
+    L.pair0 = o;  o = align16(o + L.caps.pairs);
+    L.pair1 = o;  o = align16(o + L.caps.pairs);
+    L.man = o;    o = align16(o + (int)sizeof(Manifold) * L.caps.pairs);
+    L.pts = o;    o = align16(o + (int)sizeof(MPoint) * L.caps.points);
+    L.sb = o;     o = align16(o + (int)sizeof(SBody) * (MAX_DYN + 1));
+    L.rows_c = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
+    L.rows_f = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
+    L.bytes = o;
+    return L;
+}
+// Lane 0 writes the carve-out pointers; the caller synchronises the warp before use.
+RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane) {
+    Ctx& a = *reinterpret_cast<Ctx*>(base);
+    if (lane != 0) return a;
+    a.cars = reinterpret_cast<Car*>(base + L.cars);
+    a.pads = reinterpret_cast<Pad*>(base + L.pads);
+    a.pair0 = reinterpret_cast<int8_t*>(base + L.pair0);
+    a.pair1 = reinterpret_cast<int8_t*>(base + L.pair1);
+    a.man = reinterpret_cast<Manifold*>(base + L.man);
+    a.pts = reinterpret_cast<MPoint*>(base + L.pts);
+    a.sb = reinterpret_cast<SBody*>(base + L.sb);
+    a.rows_c = reinterpret_cast<Row*>(base + L.rows_c);
+    a.rows_f = reinterpret_cast<Row*>(base + L.rows_f);
+    a.cap_pairs = L.caps.pairs;
+    a.cap_pts = L.caps.points;
+    a.cap_rows = L.caps.rows;
+    return a;
 }
 
 }  // namespace rsg
