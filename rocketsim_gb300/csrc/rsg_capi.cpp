@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -417,6 +418,10 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
         delete b;
         fail(RSG_ERR_STATE, "the mesh was loaded on another device");
         return nullptr;
+    }
+    if (const char* w = std::getenv("RSG_TICK_WARPS_PER_BLOCK")) {  // launch-shape override for tuning runs
+        int v = std::atoi(w);
+        if (v >= 1 && v <= 4) b->warps_per_block = v;
     }
     BatchBuffers& B = b->buf;
     B.A = (int)n_arenas;
