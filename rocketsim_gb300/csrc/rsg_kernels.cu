@@ -494,3 +494,13 @@ cudaError_t launch_demolish(const BatchBuffers& b, uint32_t arena, uint32_t slot
 }
 
 }  // namespace rsg
+
+#if defined(RSG_PHASE_TIMERS)
+extern "C" int rsg_phase_read(unsigned long long* out) {
+    return (int)cudaMemcpyFromSymbol(out, rsg::g_phase_cycles, sizeof(unsigned long long) * 16);
+}
+extern "C" int rsg_phase_reset() {
+    unsigned long long z[16] = {0};
+    return (int)cudaMemcpyToSymbol(rsg::g_phase_cycles, z, sizeof(z));
+}
+#endif

@@ -26,6 +26,23 @@ namespace rsg {
 #define RSG_DN __device__ __noinline__
 
 __constant__ Curve c_curves[CV_COUNT] = RSG_CURVES_INIT;
+
+// Optional per-phase cycle counters of lane 0 (compiled in only with -DRSG_PHASE_TIMERS).
+#if defined(RSG_PHASE_TIMERS)
+__device__ unsigned long long g_phase_cycles[16];
+#define RSG_PHASE_BEGIN long long rsg_t_last_ = clock64()
+#define RSG_PHASE(i)                                                                   \
+    do {                                                                               \
+        if (lane == 0) {                                                               \
+            long long t_ = clock64();                                                  \
+            atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - rsg_t_last_));     \
+            rsg_t_last_ = t_;                                                          \
+        }                                                                              \
+    } while (0)
+#else
+#define RSG_PHASE_BEGIN
+#define RSG_PHASE(i)
+#endif
 __constant__ float c_pad_locs[NUM_PADS][3] = RSG_PAD_LOCS_INIT;
 __constant__ float c_respawn_locs[4][2] = {{-2304, -4608}, {-2688, -4608}, {2304, -4608}, {2688, -4608}};
 
@@ -203,6 +220,16 @@ struct Ctx {
     Row* rows_c;
     Row* rows_f;
     int cap_rows;
+    // narrow-phase work lists: pair kinds, flattened candidate offsets, mesh candidates per
+    // dynamic object, and the results of one round of candidate tests
+    int8_t* pkind;
+    int16_t* flat_off;
+    int16_t* flat_n;
+    int* cand_tri;
+    int16_t* cand_n;
+    struct CandRes* cand_res;
+    int nflat;
+    uint32_t warn;
 
     RSG_D Body& body(int o) { return o == OBJ_BALL ? ball : cars[o - OBJ_CAR0].rb; }
 };
@@ -2215,12 +2242,21 @@ RSG_D Xf obj_xf(Ctx& a, int o) {
 }
 
 // Convex object (ball sphere or car box) against the arena mesh: btConvexConcaveCollisionAlgorithm
-// (B/.../CollisionDispatch/btConvexConcaveCollisionAlgorithm.cpp:71-250)
-RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, const Xf& conv_xf, const Convex& cshape) {
+// (B/.../CollisionDispatch/btConvexConcaveCollisionAlgorithm.cpp:71-250).  It is split in two: the
+// BVH query with the per-triangle AABB and plane early-outs (which triangles reach a detector, in
+// BVH order), and the detector run on one triangle.  Results are committed to the manifold in
+// BVH order.
+struct CandRes {
+    V3 n, p;
+    float d;
+    int valid;
+};
+constexpr int MESH_SEG = 64;  // candidate triangles kept per mesh pair before falling back to lane 0
+
+template <class F>
+RSG_D void mesh_candidates(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking, F&& emit) {
     V3 mn, mx;
     cshape.aabb(conv_xf, mn, mx);
-    Xf x0 = a.body(m.body0).xf, x1 = obj_xf(a, m.body1);
-    float fr = combined_friction(a, OBJ_MESH, conv), re = combined_restitution(a, OBJ_MESH, conv);
     M3 inv_basis = inverse(conv_xf.b);
     mesh_query_aabb(bv.mesh, mn, mx, [&](int t) {
         V3 tv[3];
@@ -2236,7 +2272,6 @@ RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, c
         }
         {  // early out on the triangle plane
             V3 tn = normalized(cross(tv[1] - tv[0], tv[2] - tv[0]));
-            float thr = m.breaking;
             for (int side = 0; side < 2; side++) {
                 V3 dir = side ? -tn : tn;
                 V3 ld = inv_basis * dir;
@@ -2252,31 +2287,59 @@ RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, c
                 }
                 V3 wp = xf_apply(conv_xf, lp);
                 float pp = dot(dir, wp), pt = dot(dir, tv[0]);
-                if (pt - pp > thr) return;
+                if (pt - pp > breaking) return;
             }
         }
-        if (cshape.type == 1) {
-            V3 point, nrm;
-            float depth;
-            if (sphere_triangle(conv_xf.o, cshape.margin, tv, m.breaking, point, nrm, depth)) {
-                int idx = add_point(a, m, x0, x1, nrm, point, depth, fr, re);
-                if (idx >= 0) contact_added(bv, a, m, idx, t);
-            }
-        } else {
-            Convex tri;
-            tri.type = 2;
-            tri.margin = 0.f;
-            tri.he = V3(0, 0, 0);
-            for (int k = 0; k < 3; k++) tri.tv[k] = tv[k];
-            float md = cshape.margin + tri.margin + m.breaking;
-            GjkOut g = gjk(cshape, conv_xf, tri, xf_identity(), md * md);
-            if (g.epa_needed) a.err |= WARN_EPA_SKIPPED;
-            if (g.valid) {
-                int idx = add_point(a, m, x0, x1, g.normal, g.point_on_b, g.dist, fr, re);
-                if (idx >= 0) contact_added(bv, a, m, idx, t);
-            }
-        }
+        emit(t);
     });
+}
+
+RSG_DN CandRes mesh_candidate_test(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking, int t,
+                                   uint32_t& warn) {
+    V3 tv[3];
+    tri_load(bv.mesh, t, tv);
+    CandRes r;
+    if (cshape.type == 1) {
+        float depth;
+        V3 point, nrm;
+        r.valid = sphere_triangle(conv_xf.o, cshape.margin, tv, breaking, point, nrm, depth);
+        r.n = nrm;
+        r.p = point;
+        r.d = depth;
+    } else {
+        Convex tri;
+        tri.type = 2;
+        tri.margin = 0.f;
+        tri.he = V3(0, 0, 0);
+        for (int k = 0; k < 3; k++) tri.tv[k] = tv[k];
+        float md = cshape.margin + tri.margin + breaking;
+        GjkOut g = gjk(cshape, conv_xf, tri, xf_identity(), md * md);
+        if (g.epa_needed) warn |= WARN_EPA_SKIPPED;
+        r.valid = g.valid;
+        r.n = g.normal;
+        r.p = g.point_on_b;
+        r.d = g.dist;
+    }
+    return r;
+}
+
+RSG_D void commit_mesh_contact(const BatchView& bv, Ctx& a, Manifold& m, const Xf& x0, const Xf& x1, float fr, float re,
+                               const CandRes& r, int t) {
+    if (!r.valid) return;
+    int idx = add_point(a, m, x0, x1, r.n, r.p, r.d, fr, re);
+    if (idx >= 0) contact_added(bv, a, m, idx, t);
+}
+
+// Whole pair on one lane (used when a pair has more candidates than its segment holds)
+RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, const Xf& conv_xf, const Convex& cshape) {
+    Xf x0 = a.body(m.body0).xf, x1 = obj_xf(a, m.body1);
+    float fr = combined_friction(a, OBJ_MESH, conv), re = combined_restitution(a, OBJ_MESH, conv);
+    uint32_t warn = 0;
+    mesh_candidates(bv, conv_xf, cshape, m.breaking, [&](int t) {
+        CandRes r = mesh_candidate_test(bv, conv_xf, cshape, m.breaking, t, warn);
+        commit_mesh_contact(bv, a, m, x0, x1, fr, re, r, t);
+    });
+    a.err |= warn;
     refresh(a, m, x0, x1);
 }
 
@@ -2718,11 +2781,15 @@ RSG_D void step_bodies_pre(const BatchView& bv, Ctx& a, int lane) {
     __syncwarp();
 }
 
-// Phase 2 of a world step, on one lane: pairs, narrow phase, islands and the solver.
-RSG_DN void step_collide(const BatchView& bv, Ctx& a) {
-    const float dt = bv.dt;
+// Phase 2 of a world step: broadphase pairs (lane 0), narrow phase (candidate tests on all
+// lanes, results committed in pair order by lane 0), islands and the solver (lane 0).
+enum PairKind : int8_t { PK_SKIP = 0, PK_BALL_MESH, PK_BALL_PLANE, PK_CAR_MESH, PK_CAR_PLANE, PK_CAR_BALL, PK_CAR_CAR };
+
+constexpr float BALL_BREAKING = (BALL_RADIUS_BT + 0.08f) * 0.02f;  // getAngularMotionDisc * gContactBreakingThreshold
+
+// calculateOverlappingPairs (btRSBroadphase.cpp:392-468) and the dispatcher's choice of algorithm
+RSG_DN void build_pairs(const BatchView& bv, Ctx& a) {
     const int nd = 1 + a.ncars;
-    // calculateOverlappingPairs (btRSBroadphase.cpp:392-468)
     a.npairs = 0;
     V3 mesh_mn, mesh_mx;
     if (bv.has_arena) {
@@ -2755,118 +2822,298 @@ RSG_DN void step_collide(const BatchView& bv, Ctx& a) {
             }
         }
     }
-    // dispatchAllCollisionPairs: one manifold per pair with a collision algorithm, in pair order
-    a.nman = 0;
-    a.npts = 0;
     for (int pi = 0; pi < a.npairs; pi++) {
         int o0 = a.pair0[pi], o1 = a.pair1[pi];
+        int8_t k = PK_SKIP;
         bool act0 = is_static_obj(o0) ? false : a.body(o0).is_active();
         bool act1 = a.body(o1).is_active();
-        if (!act0 && !act1) continue;  // btCollisionDispatcher::needsCollision
-        if (is_static_obj(o0)) {
-            if (o1 == OBJ_BALL) {
-                Convex sph;
-                sph.type = 1;
-                sph.margin = BALL_RADIUS_BT;
-                sph.he = V3(0, 0, 0);
-                Manifold& m = new_manifold(a, OBJ_BALL, o0, (BALL_RADIUS_BT + 0.08f) * 0.02f);
-                if (o0 == OBJ_MESH) convex_vs_mesh(bv, a, m, OBJ_BALL, a.ball.xf, sph);
-                else convex_vs_plane(bv, a, m, a.ball.xf, sph, o0);
-            } else {
+        if (act0 || act1) {  // btCollisionDispatcher::needsCollision
+            if (is_static_obj(o0)) {
+                if (o1 == OBJ_BALL) {
+                    k = o0 == OBJ_MESH ? PK_BALL_MESH : PK_BALL_PLANE;
+                } else {
+                    Car& c = a.cars[o1 - OBJ_CAR0];
+                    Xf cx;
+                    car_child_xf(c, cx);
+                    V3 bmn, bmx, omn, omx;
+                    car_box_aabb(c, cx, bmn, bmx);
+                    if (o0 == OBJ_MESH) mesh_aabb(bv.mesh, omn, omx);
+                    else {
+                        PlaneC pl;
+                        plane_const(o0 - OBJ_PLANE0, pl);
+                        omn = pl.raw_min;
+                        omx = pl.raw_max;
+                    }
+                    if (aabb_overlap(bmn, bmx, omn, omx)) k = o0 == OBJ_MESH ? PK_CAR_MESH : PK_CAR_PLANE;
+                }
+            } else if (o0 == OBJ_BALL) {
                 Car& c = a.cars[o1 - OBJ_CAR0];
                 Xf cx;
                 car_child_xf(c, cx);
-                Convex box;
-                box.type = 0;
-                box.he = car_he(c);
-                box.margin = c.cfg->margin;
-                V3 bmn, bmx, omn, omx;
+                V3 bmn, bmx, smn, smx;
                 car_box_aabb(c, cx, bmn, bmx);
-                if (o0 == OBJ_MESH) mesh_aabb(bv.mesh, omn, omx);
-                else {
-                    PlaneC pl;
-                    plane_const(o0 - OBJ_PLANE0, pl);
-                    omn = pl.raw_min;
-                    omx = pl.raw_max;
-                }
-                if (aabb_overlap(bmn, bmx, omn, omx)) {
-                    Manifold& m = new_manifold(a, o1, o0, c.cfg->breaking);
-                    if (o0 == OBJ_MESH) convex_vs_mesh(bv, a, m, o1, cx, box);
-                    else convex_vs_plane(bv, a, m, cx, box, o0);
-                }
-            }
-        } else if (o0 == OBJ_BALL) {
-            // ball sphere vs the car compound's box child: GJK, manifold (car, ball)
-            Car& c = a.cars[o1 - OBJ_CAR0];
-            Xf cx;
-            car_child_xf(c, cx);
-            V3 bmn, bmx, smn, smx;
-            car_box_aabb(c, cx, bmn, bmx);
-            ball_aabb(a.ball.xf, smn, smx);
-            if (aabb_overlap(bmn, bmx, smn, smx)) {
-                float bt = (BALL_RADIUS_BT + 0.08f) * 0.02f;
-                Manifold& m = new_manifold(a, o1, OBJ_BALL, c.cfg->breaking < bt ? c.cfg->breaking : bt);
-                Convex box;
-                box.type = 0;
-                box.he = car_he(c);
-                box.margin = c.cfg->margin;
-                Convex sph;
-                sph.type = 1;
-                sph.margin = BALL_RADIUS_BT;
-                sph.he = V3(0, 0, 0);
-                float md = box.margin + sph.margin + m.breaking;
-                GjkOut g = gjk(box, cx, sph, a.ball.xf, md * md);
-                if (g.epa_needed) a.err |= WARN_EPA_SKIPPED;
-                Xf x0 = c.rb.xf, x1 = a.ball.xf;
-                if (g.valid) {
-                    float fr = combined_friction(a, OBJ_BALL, o1), re = combined_restitution(a, OBJ_BALL, o1);
-                    int idx = add_point(a, m, x0, x1, g.normal, g.point_on_b, g.dist, fr, re);
-                    if (idx >= 0) contact_added(bv, a, m, idx, -1);
-                }
-                refresh(a, m, x0, x1);
-            }
-        } else {
-            // car vs car: btCompoundCompoundCollisionAlgorithm (btCompoundCompoundCollisionAlgorithm.cpp:213-330)
-            // over each car's single box child, then btBoxBoxCollisionAlgorithm with its own manifold.  The
-            // pair's algorithm runs with the later-added car as body 0.
-            int ca = o1, cb = o0;
-            Car& c0 = a.cars[ca - OBJ_CAR0];
-            Car& c1 = a.cars[cb - OBJ_CAR0];
-            V3 h0 = car_he(c0) + V3(c0.cfg->margin, c0.cfg->margin, c0.cfg->margin);
-            V3 h1 = car_he(c1) + V3(c1.cfg->margin, c1.cfg->margin, c1.cfg->margin);
-            Xf l0 = xf_identity(), l1 = xf_identity();
-            l0.o = V3(c0.cfg->off[0], c0.cfg->off[1], c0.cfg->off[2]);
-            l1.o = V3(c1.cfg->off[0], c1.cfg->off[1], c1.cfg->off[2]);
-            V3 amn, amx, bmn, bmx, rmn, rmx;
-            transform_aabb(car_he(c0), c0.cfg->margin, l0, amn, amx);
-            transform_aabb(car_he(c1), c1.cfg->margin, l1, bmn, bmx);
-            Xf rel = xf_mul(xf_inverse(c0.rb.xf), c1.rb.xf);
-            transform_aabb_mm(bmn, bmx, rel, rmn, rmx);
-            bool root = (amn.x <= rmx.x) && (amx.x >= rmn.x) && (amn.y <= rmx.y) && (amx.y >= rmn.y) &&
-                        (amn.z <= rmx.z) && (amx.z >= rmn.z);
-            if (root) {
-                Xf w0, w1;
-                car_child_xf(c0, w0);
-                car_child_xf(c1, w1);
-                V3 m0, x0v, m1, x1v;
-                car_box_aabb(c0, w0, m0, x0v);
-                car_box_aabb(c1, w1, m1, x1v);
-                if (aabb_overlap(m0, x0v, m1, x1v)) {
-                    float br = c0.cfg->breaking < c1.cfg->breaking ? c0.cfg->breaking : c1.cfg->breaking;
-                    Manifold& m = new_manifold(a, ca, cb, br);
-                    V3 nrm;
-                    BoxHit hits[4];
-                    int nh = box_box(w0.o, w0.b, h0, w1.o, w1.b, h1, nrm, hits);
-                    float fr = combined_friction(a, ca, cb), re = combined_restitution(a, ca, cb);
-                    for (int k = 0; k < nh; k++) {
-                        int idx = add_point(a, m, c0.rb.xf, c1.rb.xf, -nrm, hits[k].point, -hits[k].depth, fr, re);
-                        if (idx >= 0) contact_added(bv, a, m, idx, -1);
-                    }
-                    refresh(a, m, c0.rb.xf, c1.rb.xf);
-                }
+                ball_aabb(a.ball.xf, smn, smx);
+                if (aabb_overlap(bmn, bmx, smn, smx)) k = PK_CAR_BALL;
+            } else {
+                k = PK_CAR_CAR;
             }
         }
+        a.pkind[pi] = k;
     }
+}
+
+// collision shape of a dynamic object against static geometry
+RSG_D void dyn_shape(Ctx& a, int o, Xf& xf, Convex& sh, float& breaking) {
+    sh.he = V3(0, 0, 0);
+    if (o == OBJ_BALL) {
+        xf = a.ball.xf;
+        sh.type = 1;
+        sh.margin = BALL_RADIUS_BT;
+        breaking = BALL_BREAKING;
+    } else {
+        Car& c = a.cars[o - OBJ_CAR0];
+        car_child_xf(c, xf);
+        sh.type = 0;
+        sh.he = car_he(c);
+        sh.margin = c.cfg->margin;
+        breaking = c.cfg->breaking;
+    }
+}
+
+// the car-ball detector: GJK between the car's box child and the ball sphere
+RSG_D CandRes car_ball_test(Ctx& a, int car_obj, uint32_t& warn) {
+    Car& c = a.cars[car_obj - OBJ_CAR0];
+    Xf cx;
+    car_child_xf(c, cx);
+    Convex box;
+    box.type = 0;
+    box.he = car_he(c);
+    box.margin = c.cfg->margin;
+    Convex sph;
+    sph.type = 1;
+    sph.margin = BALL_RADIUS_BT;
+    sph.he = V3(0, 0, 0);
+    float br = c.cfg->breaking < BALL_BREAKING ? c.cfg->breaking : BALL_BREAKING;
+    float md = box.margin + sph.margin + br;
+    GjkOut g = gjk(box, cx, sph, a.ball.xf, md * md);
+    if (g.epa_needed) warn |= WARN_EPA_SKIPPED;
+    CandRes r;
+    r.valid = g.valid;
+    r.n = g.normal;
+    r.p = g.point_on_b;
+    r.d = g.dist;
+    return r;
+}
+
+RSG_D bool pair_has_candidates(const Ctx& a, int p) {
+    int k = a.pkind[p];
+    return ((k == PK_BALL_MESH || k == PK_CAR_MESH) && a.cand_n[a.pair1[p] - OBJ_BALL] >= 0) || k == PK_CAR_BALL;
+}
+
+// car vs car: btCompoundCompoundCollisionAlgorithm (btCompoundCompoundCollisionAlgorithm.cpp:213-330)
+// over each car's single box child, then btBoxBoxCollisionAlgorithm with its own manifold.  The
+// pair's algorithm runs with the later-added car as body 0.
+RSG_DN void car_car_pair(const BatchView& bv, Ctx& a, int o0, int o1) {
+    int ca = o1, cb = o0;
+    Car& c0 = a.cars[ca - OBJ_CAR0];
+    Car& c1 = a.cars[cb - OBJ_CAR0];
+    V3 h0 = car_he(c0) + V3(c0.cfg->margin, c0.cfg->margin, c0.cfg->margin);
+    V3 h1 = car_he(c1) + V3(c1.cfg->margin, c1.cfg->margin, c1.cfg->margin);
+    Xf l0 = xf_identity(), l1 = xf_identity();
+    l0.o = V3(c0.cfg->off[0], c0.cfg->off[1], c0.cfg->off[2]);
+    l1.o = V3(c1.cfg->off[0], c1.cfg->off[1], c1.cfg->off[2]);
+    V3 amn, amx, bmn, bmx, rmn, rmx;
+    transform_aabb(car_he(c0), c0.cfg->margin, l0, amn, amx);
+    transform_aabb(car_he(c1), c1.cfg->margin, l1, bmn, bmx);
+    Xf rel = xf_mul(xf_inverse(c0.rb.xf), c1.rb.xf);
+    transform_aabb_mm(bmn, bmx, rel, rmn, rmx);
+    bool root = (amn.x <= rmx.x) && (amx.x >= rmn.x) && (amn.y <= rmx.y) && (amx.y >= rmn.y) && (amn.z <= rmx.z) &&
+                (amx.z >= rmn.z);
+    if (!root) return;
+    Xf w0, w1;
+    car_child_xf(c0, w0);
+    car_child_xf(c1, w1);
+    V3 m0, x0v, m1, x1v;
+    car_box_aabb(c0, w0, m0, x0v);
+    car_box_aabb(c1, w1, m1, x1v);
+    if (!aabb_overlap(m0, x0v, m1, x1v)) return;
+    float br = c0.cfg->breaking < c1.cfg->breaking ? c0.cfg->breaking : c1.cfg->breaking;
+    Manifold& m = new_manifold(a, ca, cb, br);
+    V3 nrm;
+    BoxHit hits[4];
+    int nh = box_box(w0.o, w0.b, h0, w1.o, w1.b, h1, nrm, hits);
+    float fr = combined_friction(a, ca, cb), re = combined_restitution(a, ca, cb);
+    for (int k = 0; k < nh; k++) {
+        int idx = add_point(a, m, c0.rb.xf, c1.rb.xf, -nrm, hits[k].point, -hits[k].depth, fr, re);
+        if (idx >= 0) contact_added(bv, a, m, idx, -1);
+    }
+    refresh(a, m, c0.rb.xf, c1.rb.xf);
+}
+
+// Lane 0's walk over the pairs in order (btCollisionDispatcher::dispatchAllCollisionPairs): pairs
+// without candidates are processed when reached; a pair with candidates takes their results as
+// the rounds deliver them.
+struct CommitState {
+    int p, j, mi;
+    Xf x0, x1;
+    float fr, re;
+};
+RSG_DN void commit_sweep(const BatchView& bv, Ctx& a, CommitState& cs, int base, int f_end) {
+    while (cs.p < a.npairs) {
+        const int p = cs.p, k = a.pkind[p];
+        const int o0 = a.pair0[p], o1 = a.pair1[p];
+        if (!pair_has_candidates(a, p)) {
+            if (k == PK_BALL_MESH || k == PK_CAR_MESH) {  // more candidates than a segment holds
+                Xf xf;
+                Convex sh;
+                float br;
+                dyn_shape(a, o1, xf, sh, br);
+                Manifold& m = new_manifold(a, o1, o0, br);
+                convex_vs_mesh(bv, a, m, o1, xf, sh);
+            } else if (k == PK_BALL_PLANE || k == PK_CAR_PLANE) {
+                Xf xf;
+                Convex sh;
+                float br;
+                dyn_shape(a, o1, xf, sh, br);
+                Manifold& m = new_manifold(a, o1, o0, br);
+                convex_vs_plane(bv, a, m, xf, sh, o0);
+            } else if (k == PK_CAR_CAR) {
+                car_car_pair(bv, a, o0, o1);
+            }
+            cs.p++;
+            continue;
+        }
+        const int n = a.flat_n[p];
+        if (cs.j == 0) {
+            if (k == PK_CAR_BALL) {
+                float cb = a.cars[o1 - OBJ_CAR0].cfg->breaking;
+                cs.mi = a.nman;
+                new_manifold(a, o1, OBJ_BALL, cb < BALL_BREAKING ? cb : BALL_BREAKING);
+                cs.x0 = a.body(o1).xf;
+                cs.x1 = a.ball.xf;
+                cs.fr = combined_friction(a, OBJ_BALL, o1);
+                cs.re = combined_restitution(a, OBJ_BALL, o1);
+            } else {
+                Xf xf;
+                Convex sh;
+                float br;
+                dyn_shape(a, o1, xf, sh, br);
+                cs.mi = a.nman;
+                new_manifold(a, o1, o0, br);
+                cs.x0 = a.body(o1).xf;
+                cs.x1 = obj_xf(a, o0);
+                cs.fr = combined_friction(a, OBJ_MESH, o1);
+                cs.re = combined_restitution(a, OBJ_MESH, o1);
+            }
+        }
+        Manifold& m = a.man[cs.mi];
+        while (cs.j < n) {
+            const int f = a.flat_off[p] + cs.j;
+            if (f >= f_end) return;  // the next round delivers it
+            const CandRes& r = a.cand_res[f - base];
+            if (k == PK_CAR_BALL) {
+                if (r.valid) {
+                    int idx = add_point(a, m, cs.x0, cs.x1, r.n, r.p, r.d, cs.fr, cs.re);
+                    if (idx >= 0) contact_added(bv, a, m, idx, -1);
+                }
+            } else {
+                int t = a.cand_tri[(o1 - OBJ_BALL) * MESH_SEG + cs.j];
+                commit_mesh_contact(bv, a, m, cs.x0, cs.x1, cs.fr, cs.re, r, t);
+            }
+            cs.j++;
+        }
+        refresh(a, m, cs.x0, cs.x1);
+        cs.p++;
+        cs.j = 0;
+    }
+}
+
+RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a);
+
+RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
+    RSG_PHASE_BEGIN;
+    if (lane == 0) {
+        build_pairs(bv, a);
+        a.nman = 0;
+        a.npts = 0;
+        a.warn = 0;
+    }
+    __syncwarp();
+    uint32_t warn = 0;
+    // candidate triangles of each mesh pair, one lane per pair, in BVH order
+    for (int p = lane; p < a.npairs; p += 32) {
+        int k = a.pkind[p];
+        if (k == PK_BALL_MESH || k == PK_CAR_MESH) {
+            int o = a.pair1[p];
+            Xf xf;
+            Convex sh;
+            float br;
+            dyn_shape(a, o, xf, sh, br);
+            int* out = a.cand_tri + (o - OBJ_BALL) * MESH_SEG;
+            int n = 0;
+            mesh_candidates(bv, xf, sh, br, [&](int t) {
+                if (n < MESH_SEG) out[n] = t;
+                n++;
+            });
+            a.cand_n[o - OBJ_BALL] = (int16_t)(n <= MESH_SEG ? n : -1);
+        }
+    }
+    __syncwarp();
+    RSG_PHASE(4);
+    if (lane == 0) {
+        int total = 0;
+        for (int p = 0; p < a.npairs; p++) {
+            int n = 0;
+            if (pair_has_candidates(a, p)) n = a.pkind[p] == PK_CAR_BALL ? 1 : a.cand_n[a.pair1[p] - OBJ_BALL];
+            a.flat_off[p] = (int16_t)total;
+            a.flat_n[p] = (int16_t)n;
+            total += n;
+        }
+        a.nflat = total;
+    }
+    __syncwarp();
+    // rounds of 32 candidate tests, then lane 0 commits them in pair order
+    CommitState cs;
+    cs.p = 0;
+    cs.j = 0;
+    cs.mi = 0;
+    const int nflat = a.nflat;
+    for (int base = 0; base < nflat; base += 32) {
+        const int f = base + lane;
+        if (f < nflat) {
+            int p = 0;
+            while (!(f >= a.flat_off[p] && f < a.flat_off[p] + a.flat_n[p])) p++;
+            const int o1 = a.pair1[p];
+            if (a.pkind[p] == PK_CAR_BALL) {
+                a.cand_res[lane] = car_ball_test(a, o1, warn);
+            } else {
+                Xf xf;
+                Convex sh;
+                float br;
+                dyn_shape(a, o1, xf, sh, br);
+                int t = a.cand_tri[(o1 - OBJ_BALL) * MESH_SEG + (f - a.flat_off[p])];
+                a.cand_res[lane] = mesh_candidate_test(bv, xf, sh, br, t, warn);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) commit_sweep(bv, a, cs, base, base + 32 < nflat ? base + 32 : nflat);
+        __syncwarp();
+    }
+    if (warn) atomicOr(&a.warn, warn);
+    __syncwarp();
+    RSG_PHASE(5);
+    if (lane == 0) {
+        commit_sweep(bv, a, cs, nflat, nflat);
+        a.err |= a.warn;
+    }
+    RSG_PHASE(6);
+    if (lane == 0) step_collide_tail(bv, a);
+    RSG_PHASE(7);
+}
+
+RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a) {
+    const float dt = bv.dt;
+    const int nd = 1 + a.ncars;
     // islands (btSimulationIslandManager, STATIC_SIMULATION_ISLAND_OPTIMIZATION)
     int uf_id[MAX_CARS + 1], uf_sz[MAX_CARS + 1], tag[MAX_CARS + 1];
     for (int i = 0; i < nd; i++) { uf_id[i] = i; uf_sz[i] = 1; }
@@ -3014,13 +3261,13 @@ RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Si
     int iy = (int)(cp.y / SY + (CY / 2));
     int i0 = ix - 1 > 0 ? ix - 1 : 0, i1 = ix + 1 < CX - 1 ? ix + 1 : CX - 1;
     int j0 = iy - 1 > 0 ? iy - 1 : 0, j1 = iy + 1 < CY - 1 ? iy + 1 : CY - 1;
-    for (int i = i0; i <= i1; i++)
-        for (int j = j0; j <= j1; j++)
-            for (int k = 0; k < NUM_PADS; k++) {
-                int px = (int)(c_pad_locs[k][0] / SX + (CX / 2));
-                int py = (int)(c_pad_locs[k][1] / SY + (CY / 2));
-                if (px == i && py == j) pad_check(a, a.pads[k], k, ci);
-            }
+    // Every pad lies in exactly one grid cell and a check only touches that pad, so visiting the
+    // pads of the 3x3 neighbourhood in pad order equals the reference's cell-by-cell visit.
+    for (int k = 0; k < NUM_PADS; k++) {
+        int px = (int)(c_pad_locs[k][0] / SX + (CX / 2));
+        int py = (int)(c_pad_locs[k][1] / SY + (CY / 2));
+        if (px >= i0 && px <= i1 && py >= j0 && py <= j1) pad_check(a, a.pads[k], k, ci);
+    }
 }
 
 // Arena::Step, one tick (src/Sim/Arena/Arena.cpp:689-756), run by the 32 lanes of one warp.
@@ -3034,6 +3281,7 @@ RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Si
 // Collision detection, islands and the solver run on lane 0.
 RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
     const unsigned FULL = 0xffffffffu;
+    RSG_PHASE_BEGIN;
     if (lane == 0) {
         Body& ball = a.ball;
         bool ball_off = ball.act == DISABLE_DEACTIVATION || ball.act == DISABLE_SIMULATION;
@@ -3069,6 +3317,7 @@ RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
         }
     }
     __syncwarp();
+    RSG_PHASE(0);
     if (bv.has_arena && a.ncars > 0)
         for (int i = lane; i < NUM_PADS; i += 32) {  // BoostPad::_PreTickUpdate (src/Sim/BoostPad/BoostPad.cpp:51-60)
             Pad& p = a.pads[i];
@@ -3078,8 +3327,10 @@ RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
         }
     __syncwarp();
     step_bodies_pre(bv, a, lane);
-    if (lane == 0) step_collide(bv, a);
+    RSG_PHASE(1);
+    step_collide_warp(bv, a, lane);
     __syncwarp();
+    RSG_PHASE(2);
     step_bodies_post(bv, a, lane);
     __syncwarp();
     if (lane < a.ncars) {
@@ -3128,6 +3379,7 @@ RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
         a.stepped = true;
     }
     __syncwarp();
+    RSG_PHASE(3);
 }
 
 // ---------------------------------------------------------------- record load / store
@@ -3383,7 +3635,7 @@ RSG_D void store_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
 // ---------------------------------------------------------------- shared-memory carve-out
 // Byte offsets of one arena's working set inside its warp's shared-memory region.
 struct SmemLayout {
-    int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, bytes;
+    int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, bytes;
     ArenaCaps caps;
 };
 RSG_HD int align16(int x) { return (x + 15) & ~15; }
@@ -3400,6 +3652,12 @@ RSG_HD SmemLayout smem_layout(int mc) {
     L.sb = o;     o = align16(o + (int)sizeof(SBody) * (MAX_DYN + 1));
     L.rows_c = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
     L.rows_f = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
+    L.pkind = o;  o = align16(o + L.caps.pairs);
+    L.flat_off = o; o = align16(o + 2 * L.caps.pairs);
+    L.flat_n = o; o = align16(o + 2 * L.caps.pairs);
+    L.cand_tri = o; o = align16(o + 4 * MESH_SEG * (mc + 1));
+    L.cand_n = o; o = align16(o + 2 * (mc + 1));
+    L.cand_res = o; o = align16(o + (int)sizeof(CandRes) * 32);
     L.bytes = o;
     return L;
 }
@@ -3416,6 +3674,12 @@ RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane) {
     a.sb = reinterpret_cast<SBody*>(base + L.sb);
     a.rows_c = reinterpret_cast<Row*>(base + L.rows_c);
     a.rows_f = reinterpret_cast<Row*>(base + L.rows_f);
+    a.pkind = reinterpret_cast<int8_t*>(base + L.pkind);
+    a.flat_off = reinterpret_cast<int16_t*>(base + L.flat_off);
+    a.flat_n = reinterpret_cast<int16_t*>(base + L.flat_n);
+    a.cand_tri = reinterpret_cast<int*>(base + L.cand_tri);
+    a.cand_n = reinterpret_cast<int16_t*>(base + L.cand_n);
+    a.cand_res = reinterpret_cast<CandRes*>(base + L.cand_res);
     a.cap_pairs = L.caps.pairs;
     a.cap_pts = L.caps.points;
     a.cap_rows = L.caps.rows;
