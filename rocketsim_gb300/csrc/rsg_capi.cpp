@@ -421,7 +421,7 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
     }
     if (const char* w = std::getenv("RSG_TICK_WARPS_PER_BLOCK")) {  // launch-shape override for tuning runs
         int v = std::atoi(w);
-        if (v >= 1 && v <= 4) b->warps_per_block = v;
+        if (v >= 1 && v <= 8) b->warps_per_block = v;
     }
     BatchBuffers& B = b->buf;
     B.A = (int)n_arenas;

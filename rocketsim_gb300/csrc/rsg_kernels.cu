@@ -56,31 +56,51 @@ RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
 }
 
 // One warp per arena: the arena's working set is carved out of dynamic shared memory
-// (smem_layout), loaded from its record, advanced `ticks` ticks and stored back.
-__global__ void __launch_bounds__(128) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
+// (smem_layout), loaded from its record, advanced `ticks` ticks and stored back.  The warps of a
+// block step through the parts of a tick together (block-wide barriers between parts), which keeps
+// the instruction working set of an SM to one part of the tick at a time.
+__global__ void __launch_bounds__(256) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
                                                        int ticks) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ar = blockIdx.x * (blockDim.x >> 5) + warp;
-    if (ar >= bv.A) return;  // whole warps leave together
+    const bool active = ar < bv.A;  // warp-uniform; idle warps still take part in the barriers
     const SmemLayout L = smem_layout(bv.MC);
     Ctx& a = bind_ctx(smem + (size_t)warp * L.bytes, L, lane);
-    if (lane == 0) load_arena(bv, ar, a);
-    __syncwarp();
-    if (lane < a.ncars) load_car(bv, ar, a, lane);
-    load_pads(bv, ar, a, lane);
-    __syncwarp();
-    for (int t = 0; t < ticks; t++) {
-        if (controls && lane < a.ncars) {
-            const rsg_car_controls k = controls[((size_t)t * bv.A + ar) * bv.MC + lane];
-            apply_controls(a.cars[lane], k);
-        }
+    if (active) {
+        if (lane == 0) load_arena(bv, ar, a);
         __syncwarp();
-        arena_tick_warp(bv, a, lane);
+        if (lane < a.ncars) load_car(bv, ar, a, lane);
+        load_pads(bv, ar, a, lane);
+        __syncwarp();
     }
-    if (lane == 0) store_arena(bv, ar, a);
-    if (lane < a.ncars) store_car(bv, ar, a, lane);
-    store_pads(bv, ar, a, lane);
+    RSG_PHASE_BEGIN;
+    for (int t = 0; t < ticks; t++) {
+        if (active) {
+            if (controls && lane < a.ncars) {
+                const rsg_car_controls k = controls[((size_t)t * bv.A + ar) * bv.MC + lane];
+                apply_controls(a.cars[lane], k);
+            }
+            __syncwarp();
+            tick_pre(bv, a, lane);
+        }
+        __syncthreads();
+        RSG_PHASE(0);
+        if (active) step_bodies_pre(bv, a, lane);
+        __syncthreads();
+        RSG_PHASE(1);
+        if (active) step_collide_warp(bv, a, lane);
+        __syncthreads();
+        RSG_PHASE(2);
+        if (active) tick_post(bv, a, lane);
+        __syncthreads();
+        RSG_PHASE(3);
+    }
+    if (active) {
+        if (lane == 0) store_arena(bv, ar, a);
+        if (lane < a.ncars) store_car(bv, ar, a, lane);
+        store_pads(bv, ar, a, lane);
+    }
 }
 
 int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars).bytes; }
@@ -88,7 +108,9 @@ int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars).bytes; }
 cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int warps_per_block,
                         cudaStream_t st) {
     if (b.A <= 0 || ticks <= 0) return cudaSuccess;
-    if (warps_per_block <= 0 || warps_per_block > 4) warps_per_block = 2;
+    if (warps_per_block <= 0 || warps_per_block > 8) warps_per_block = 2;
+    // the block must fit in shared memory
+    while (warps_per_block > 1 && smem_layout(b.MC).bytes * warps_per_block > 227 * 1024) warps_per_block--;
     const int per_arena = smem_layout(b.MC).bytes;
     const int smem = per_arena * warps_per_block;
     cudaError_t e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

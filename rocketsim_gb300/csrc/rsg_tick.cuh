@@ -228,9 +228,6 @@ struct Ctx {
     int* cand_tri;
     int16_t* cand_n;
     struct CandRes* cand_res;
-    uint16_t* qbox;    // [MAX_DYN][6] quantized query box of each mesh pair (min, max)
-    int16_t* hdr_list; // [MAX_DYN][HDR_LIST] overlapping subtree headers in header order
-    int16_t* hdr_n;    // [MAX_DYN], -1 when the list overflowed
     int nflat;
     uint32_t warn;
 
@@ -316,42 +313,26 @@ RSG_D bool qov(const uint16_t* a0, const uint16_t* a1, const uint16_t* b0, const
     return o;
 }
 
-// walkStacklessQuantizedTreeCacheFriendly (btQuantizedBvh.cpp:551-575): subtree headers in order,
-// the nodes of each overlapping subtree in order.
-RSG_D void subtree_load(const DevMesh& m, int s, uint16_t qmin[3], uint16_t qmax[3], int& root, int& size) {
-    const Subtree* st = m.sub + s;
-    for (int k = 0; k < 3; k++) {
-        qmin[k] = __ldg(&st->qmin[k]);
-        qmax[k] = __ldg(&st->qmax[k]);
-    }
-    root = __ldg(&st->root);
-    size = __ldg(&st->size);
-}
-template <class F>
-RSG_D void subtree_walk(const DevMesh& m, const uint16_t* qa, const uint16_t* qb, int root, int size, F&& f) {
-    int cur = root, end = root + size;
-    while (cur < end) {
-        uint16_t nmin[3], nmax[3];
-        int esc;
-        node_load(m, cur, nmin, nmax, esc);
-        bool ov = qov(qa, qb, nmin, nmax);
-        bool leaf = esc >= 0;
-        if (leaf && ov) f(esc);
-        if (ov || leaf) cur++;
-        else cur += -esc;
-    }
-}
+// walkStacklessQuantizedTreeCacheFriendly (btQuantizedBvh.cpp:551-575)
 template <class F>
 RSG_D void mesh_query_aabb(const DevMesh& m, V3 mn, V3 mx, F&& f) {
     uint16_t qa[3], qb[3];
     quantize_clamp(m, qa, mn, false);
     quantize_clamp(m, qb, mx, true);
     for (int s = 0; s < m.nsub; s++) {
-        uint16_t smin[3], smax[3];
-        int root, size;
-        subtree_load(m, s, smin, smax, root, size);
-        if (!qov(qa, qb, smin, smax)) continue;
-        subtree_walk(m, qa, qb, root, size, f);
+        Subtree st = m.sub[s];
+        if (!qov(qa, qb, st.qmin, st.qmax)) continue;
+        int cur = st.root, end = st.root + st.size;
+        while (cur < end) {
+            uint16_t nmin[3], nmax[3];
+            int esc;
+            node_load(m, cur, nmin, nmax, esc);
+            bool ov = qov(qa, qb, nmin, nmax);
+            bool leaf = esc >= 0;
+            if (leaf && ov) f(esc);
+            if (ov || leaf) cur++;
+            else cur += -esc;
+        }
     }
 }
 
@@ -595,7 +576,7 @@ RSG_D void wheel_ws(Car& c, int i) {  // btVehicleRL::updateWheelTransformsWS (b
     w.dir_ws = c.rb.xf.b * V3(0, 0, -1);
     w.axle_ws = c.rb.xf.b * V3(0, -1, 0);
 }
-RSG_DN void update_wheel_transform(Car& c, int i) {  // btVehicleRL::updateWheelTransform (btVehicleRL.cpp:66-94)
+RSG_D void update_wheel_transform(Car& c, int i) {  // btVehicleRL::updateWheelTransform (btVehicleRL.cpp:66-94)
     wheel_ws(c, i);
     WheelRT& w = c.w[i];
     V3 up = -w.dir_ws;
@@ -630,7 +611,7 @@ RSG_D float resolve_single_collision(Ctx& a, Body& b1, int obj2, V3 pos, V3 n, f
     return 0.f > imp ? 0.f : imp;
 }
 
-RSG_DN void ray_cast_wheel(const BatchView& bv, Ctx& a, Car& c, int i) {  // btVehicleRL::rayCast (btVehicleRL.cpp:120-209)
+RSG_D void ray_cast_wheel(const BatchView& bv, Ctx& a, Car& c, int i) {  // btVehicleRL::rayCast (btVehicleRL.cpp:120-209)
     wheel_ws(c, i);
     WheelRT& w = c.w[i];
     int fb = i < 2 ? 0 : 1;
@@ -703,7 +684,7 @@ RSG_D float resolve_single_bilateral(Ctx& a, Body& b1, V3 pos, int obj2, V3 norm
     return -0.2f * dot(normal, v1 - v2) * jinv;
 }
 
-RSG_DN void calc_friction_impulses(Ctx& a, Car& c, float dt) {  // btVehicleRL::calcFrictionImpulses (btVehicleRL.cpp:306-380)
+RSG_D void calc_friction_impulses(Ctx& a, Car& c, float dt) {  // btVehicleRL::calcFrictionImpulses (btVehicleRL.cpp:306-380)
     float fscale = (1.f / c.rb.inv_mass) / 3;
     for (int i = 0; i < 4; i++) {
         WheelRT& w = c.w[i];
@@ -754,7 +735,7 @@ RSG_D V3 upwards_from_wheels(const Car& c) {  // btVehicleRL.cpp:397-410
     return safe_normalized(sum);
 }
 
-RSG_DN void update_suspension(Car& c, float dt) {  // btVehicleRL.cpp:270-303
+RSG_D void update_suspension(Car& c, float dt) {  // btVehicleRL.cpp:270-303
     for (int i = 0; i < 4; i++) {
         WheelRT& w = c.w[i];
         if (w.in_contact) {
@@ -796,7 +777,7 @@ RSG_D float rs_minf(float a, float b) { return (a < b) ? a : b; }
 RSG_D float rs_clampf(float v, float lo, float hi) { return rs_minf(rs_maxf(v, lo), hi); }
 RSG_D int rs_sgn(float v) { return (v > 0) - (v < 0); }
 
-RSG_DN void update_wheels(Car& c, float dt, int nwc, float fwd_speed) {  // Car::_UpdateWheels (Car.cpp:339-484)
+RSG_D void update_wheels(Car& c, float dt, int nwc, float fwd_speed) {  // Car::_UpdateWheels (Car.cpp:339-484)
     float absfs = fabsf(fwd_speed);
     bool world_contact = false;
     for (int i = 0; i < 4; i++) world_contact |= c.w[i].contact_world;
@@ -918,7 +899,7 @@ RSG_D void update_jump(Car& c, float dt, bool pressed) {  // Car::_UpdateJump (C
     if (c.f(F_JUMPING) || c.f(F_HAS_JUMPED)) c.jump_time += dt;
 }
 
-RSG_DN void update_air_torque(Car& c, bool update_air_control) {  // Car::_UpdateAirTorque (Car.cpp:584-669)
+RSG_D void update_air_torque(Car& c, bool update_air_control) {  // Car::_UpdateAirTorque (Car.cpp:584-669)
     V3 pitch_right = -c.right(), yaw_up = c.up(), roll_fwd = -c.fwd();
     bool do_air = false;
     if (c.f(F_FLIPPING)) c.setf(F_FLIPPING, c.f(F_HAS_FLIPPED) && c.flip_time < RL::FLIP_TORQUE_TIME);
@@ -967,7 +948,7 @@ RSG_DN void update_air_torque(Car& c, bool update_air_control) {  // Car::_Updat
     if (c.ctrl[0] != 0) c.rb.total_force += c.fwd() * c.ctrl[0] * RL::THROTTLE_AIR_ACCEL * RL::UU_TO_BT * RL::CAR_MASS_BT;
 }
 
-RSG_DN void update_double_jump_or_flip(Car& c, float dt, bool pressed, float fwd_speed) {  // Car.cpp:671-781
+RSG_D void update_double_jump_or_flip(Car& c, float dt, bool pressed, float fwd_speed) {  // Car.cpp:671-781
     if (c.f(F_ON_GROUND)) {
         c.setf(F_HAS_DJ, false);
         c.setf(F_HAS_FLIPPED, false);
@@ -1042,7 +1023,7 @@ RSG_D float roll_from_rot(const M3& m) {  // Angle::FromRotMat roll (MathTypes.c
     return -roll;
 }
 
-RSG_DN void update_auto_flip(Car& c, float dt, bool pressed) {  // Car::_UpdateAutoFlip (Car.cpp:783-817)
+RSG_D void update_auto_flip(Car& c, float dt, bool pressed) {  // Car::_UpdateAutoFlip (Car.cpp:783-817)
     if (pressed && c.f(F_WC_CONTACT) && c.wc_normal.z > RL::CAR_AUTOFLIP_NORMZ_THRESH) {
         float roll = roll_from_rot(c.rot);
         float ar = fabsf(roll);
@@ -1064,7 +1045,7 @@ RSG_DN void update_auto_flip(Car& c, float dt, bool pressed) {  // Car::_UpdateA
     }
 }
 
-RSG_DN void update_auto_roll(Car& c, int nwc) {  // Car::_UpdateAutoRoll (Car.cpp:819-853)
+RSG_D void update_auto_roll(Car& c, int nwc) {  // Car::_UpdateAutoRoll (Car.cpp:819-853)
     V3 gup = nwc > 0 ? upwards_from_wheels(c) : c.wc_normal;
     V3 gdown = -gup;
     V3 f = c.fwd(), r = c.right();
@@ -1077,7 +1058,7 @@ RSG_DN void update_auto_roll(Car& c, int nwc) {  // Car::_UpdateAutoRoll (Car.cp
     c.rb.total_torque += inverse(c.rb.inv_inertia_world) * ((tdf * ftf) + (tdr * rtf)) * RL::CAR_AUTOROLL_TORQUE;
 }
 
-RSG_DN void car_set_respawn(Car& c, int idx, float boost);
+RSG_D void car_set_respawn(Car& c, int idx, float boost);
 
 // Car::_PreTickUpdate (Car.cpp:58-131) after the four suspension rays: friction, wheels, air
 // control, jump, auto-flip, flip / double jump, auto-roll, suspension and boost.
@@ -1108,7 +1089,7 @@ RSG_DN void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
 
 // Start of Car::_PreTickUpdate for a car that is not demolished and was not at the last
 // pre-tick: control clamping, activation and the wheel transforms.
-RSG_DN void car_pre_before_rays(Car& c) {
+RSG_D void car_pre_before_rays(Car& c) {
     for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
     c.rb.act = ACTIVE_TAG;
     c.rb.no_contact_response = false;
@@ -1133,7 +1114,7 @@ RSG_DN void car_pre_tick(const BatchView& bv, Ctx& a, Car& c) {  // Car::_PreTic
     car_pre_after_rays(bv, a, c);
 }
 
-RSG_DN void car_post_tick(Car& c, float dt) {  // Car::_PostTickUpdate (Car.cpp:133-163)
+RSG_D void car_post_tick(Car& c, float dt) {  // Car::_PostTickUpdate (Car.cpp:133-163)
     if (c.f(F_DEMOED)) return;
     c.rot = c.rb.xf.b;
     float sp2 = len2(c.rb.lin_vel * RL::BT_TO_UU);
@@ -1152,7 +1133,7 @@ RSG_DN void car_post_tick(Car& c, float dt) {  // Car::_PostTickUpdate (Car.cpp:
     c.setf(F_LAST_HB, c.f(F_CTRL_HB));
 }
 
-RSG_DN void car_finish_physics(Car& c) {  // Car::_FinishPhysicsTick (Car.cpp:165-193)
+RSG_D void car_finish_physics(Car& c) {  // Car::_FinishPhysicsTick (Car.cpp:165-193)
     if (c.f(F_DEMOED)) return;
     if (!is_zero(c.vel_cache)) {
         c.rb.lin_vel += c.vel_cache;
@@ -1167,7 +1148,7 @@ RSG_DN void car_finish_physics(Car& c) {  // Car::_FinishPhysicsTick (Car.cpp:16
     c.ticks_since++;
 }
 
-RSG_DN void car_set_respawn(Car& c, int idx, float boost) {  // Car::Respawn (Car.cpp:43-56) + SetState
+RSG_D void car_set_respawn(Car& c, int idx, float boost) {  // Car::Respawn (Car.cpp:43-56) + SetState
     float team_sign = c.f(F_TEAM_ORANGE) ? -1.f : 1.f;
     V3 pos(c_respawn_locs[idx][0], c_respawn_locs[idx][1] * team_sign, RL::CAR_RESPAWN_Z);
     float yaw = (float)((double)(float)(3.14159265358979323846 / 2) + (c.f(F_TEAM_ORANGE) ? 3.14159265358979323846 : 0));
@@ -1225,7 +1206,7 @@ RSG_D void mesh_aabb(const DevMesh& m, V3& mn, V3& mx) {  // btTriangleMeshShape
 }
 
 // btTransformUtil::integrateTransform (B/LinearMath/btTransformUtil.h:37-80)
-RSG_DN void integrate_transform(const Xf& cur, V3 lv, V3 av, float dt, bool no_rot, Xf& out) {
+RSG_D void integrate_transform(const Xf& cur, V3 lv, V3 av, float dt, bool no_rot, Xf& out) {
     out.o = cur.o + lv * dt;
     if (no_rot) { out.b = cur.b; return; }
     const float ANGULAR_MOTION_THRESHOLD = 0.5f * HALF_PI_F;
@@ -1245,7 +1226,7 @@ RSG_DN void integrate_transform(const Xf& cur, V3 lv, V3 av, float dt, bool no_r
 
 // ---------------------------------------------------------------- contact manifolds
 // btManifoldResult::addContactPoint (B/.../CollisionDispatch/btManifoldResult.cpp:109-194)
-RSG_DN int add_point(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1, V3 n, V3 pb, float depth, float friction,
+RSG_D int add_point(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1, V3 n, V3 pb, float depth, float friction,
                     float restitution) {
     if (depth > m.breaking) return -1;
     V3 pa = pb + n * depth;
@@ -1287,7 +1268,7 @@ RSG_DN int add_point(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1, V3 n, V3 p
 }
 
 // btPersistentManifold::refreshContactPoints (btPersistentManifold.cpp:263-318)
-RSG_DN void refresh(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1) {
+RSG_D void refresh(Ctx& a, Manifold& m, const Xf& x0, const Xf& x1) {
     for (int i = m.n - 1; i >= 0; i--) {
         MPoint& p = a.pts[m.pt[i]];
         p.pos_a = xf_apply(x0, p.local_a);
@@ -2271,18 +2252,13 @@ struct CandRes {
     int valid;
 };
 constexpr int MESH_SEG = 64;  // candidate triangles kept per mesh pair before falling back to lane 0
-constexpr int HDR_LIST = 24;  // overlapping BVH subtree headers kept per mesh query
 
-// Candidate triangles of a mesh query in BVH order.  `hdrs` (may be null) lists, in header
-// order, the subtree headers that overlap the query box; without it every header is tested.
-// Candidates with rank in [skip, skip + cap) are written to `out`; the return value is the total.
-RSG_DN int mesh_gather(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking,
-                       const int16_t* hdrs, int nh, int* out, int cap, int skip) {
+template <class F>
+RSG_D void mesh_candidates(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking, F&& emit) {
     V3 mn, mx;
     cshape.aabb(conv_xf, mn, mx);
     M3 inv_basis = inverse(conv_xf.b);
-    int n = 0;
-    auto visit = [&](int t) {
+    mesh_query_aabb(bv.mesh, mn, mx, [&](int t) {
         V3 tv[3];
         tri_load(bv.mesh, t, tv);
         // TestTriangleAgainstAabb2 (z, x, y)
@@ -2314,21 +2290,8 @@ RSG_DN int mesh_gather(const BatchView& bv, const Xf& conv_xf, const Convex& csh
                 if (pt - pp > breaking) return;
             }
         }
-        if (n >= skip && n < skip + cap) out[n - skip] = t;
-        n++;
-    };
-    uint16_t qa[3], qb[3];
-    quantize_clamp(bv.mesh, qa, mn, false);
-    quantize_clamp(bv.mesh, qb, mx, true);
-    const int count = hdrs ? nh : bv.mesh.nsub;
-    for (int i = 0; i < count; i++) {
-        uint16_t smin[3], smax[3];
-        int root, size;
-        subtree_load(bv.mesh, hdrs ? hdrs[i] : i, smin, smax, root, size);
-        if (!hdrs && !qov(qa, qb, smin, smax)) continue;
-        subtree_walk(bv.mesh, qa, qb, root, size, visit);
-    }
-    return n;
+        emit(t);
+    });
 }
 
 RSG_DN CandRes mesh_candidate_test(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking, int t,
@@ -2367,23 +2330,15 @@ RSG_D void commit_mesh_contact(const BatchView& bv, Ctx& a, Manifold& m, const X
     if (idx >= 0) contact_added(bv, a, m, idx, t);
 }
 
-// Whole pair on one lane, used when a pair has more candidates than its segment holds: the
-// candidates are gathered again chunk by chunk into `buf` (MESH_SEG entries) and committed in order.
-RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, const Xf& conv_xf, const Convex& cshape,
-                           int* buf) {
+// Whole pair on one lane (used when a pair has more candidates than its segment holds)
+RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, const Xf& conv_xf, const Convex& cshape) {
     Xf x0 = a.body(m.body0).xf, x1 = obj_xf(a, m.body1);
     float fr = combined_friction(a, OBJ_MESH, conv), re = combined_restitution(a, OBJ_MESH, conv);
     uint32_t warn = 0;
-    for (int skip = 0;; skip += MESH_SEG) {
-        int total = mesh_gather(bv, conv_xf, cshape, m.breaking, nullptr, 0, buf, MESH_SEG, skip);
-        int end = total < skip + MESH_SEG ? total : skip + MESH_SEG;
-        for (int k = skip; k < end; k++) {
-            int t = buf[k - skip];
-            CandRes r = mesh_candidate_test(bv, conv_xf, cshape, m.breaking, t, warn);
-            commit_mesh_contact(bv, a, m, x0, x1, fr, re, r, t);
-        }
-        if (total <= skip + MESH_SEG) break;
-    }
+    mesh_candidates(bv, conv_xf, cshape, m.breaking, [&](int t) {
+        CandRes r = mesh_candidate_test(bv, conv_xf, cshape, m.breaking, t, warn);
+        commit_mesh_contact(bv, a, m, x0, x1, fr, re, r, t);
+    });
     a.err |= warn;
     refresh(a, m, x0, x1);
 }
@@ -2483,7 +2438,7 @@ RSG_D void init_solver_body(Ctx& a, SBody& sb, int obj, float dt) {
     sb.dlv = sb.dav = sb.push = sb.turn = V3(0, 0, 0);
 }
 
-RSG_DN void setup_contact_row(Ctx& a, Row& r, int ia, int ib, const MPoint& cp, V3 rel1, V3 rel2, float dt) {
+RSG_D void setup_contact_row(Ctx& a, Row& r, int ia, int ib, const MPoint& cp, V3 rel1, V3 rel2, float dt) {
     SBody& A = a.sb[ia];
     SBody& B = a.sb[ib];
     Body* rb0 = A.obj >= 0 ? &a.body(A.obj) : nullptr;
@@ -2542,7 +2497,7 @@ RSG_DN void setup_contact_row(Ctx& a, Row& r, int ia, int ib, const MPoint& cp, 
     r.special = cp.special;
 }
 
-RSG_DN void setup_friction_row(Ctx& a, Row& r, V3 n, int ia, int ib, float friction, V3 rel1, V3 rel2) {
+RSG_D void setup_friction_row(Ctx& a, Row& r, V3 n, int ia, int ib, float friction, V3 rel1, V3 rel2) {
     SBody& A = a.sb[ia];
     SBody& B = a.sb[ib];
     Body* b0 = A.obj >= 0 ? &a.body(A.obj) : nullptr;
@@ -2582,7 +2537,7 @@ RSG_DN void setup_friction_row(Ctx& a, Row& r, V3 n, int ia, int ib, float frict
 }
 
 // convertContactInner friction part (btSequentialImpulseConstraintSolver.cpp:1071-1162)
-RSG_DN void add_friction(Ctx& a, int& nf, int ia, int ib, V3 normal, float friction, V3 rel1, V3 rel2, int fidx) {
+RSG_D void add_friction(Ctx& a, int& nf, int ia, int ib, V3 normal, float friction, V3 rel1, V3 rel2, int fidx) {
     SBody& A = a.sb[ia];
     SBody& B = a.sb[ib];
     V3 v1 = A.obj >= 0 ? A.lv + A.ext_f + cross(A.av + A.ext_t, rel1) : V3(0, 0, 0);
@@ -2604,7 +2559,7 @@ RSG_DN void add_friction(Ctx& a, int& nf, int ia, int ib, V3 normal, float frict
 }
 
 // gResolveSingleConstraintRowGeneric / LowerLimit with the row's limits passed in
-RSG_DN void solve_row(Ctx& a, Row& c, float lo, float hi, bool lower_only) {
+RSG_D void solve_row(Ctx& a, Row& c, float lo, float hi, bool lower_only) {
     SBody& A = a.sb[c.ba];
     SBody& B = a.sb[c.bb];
     V3 n2 = row_n2(c);
@@ -2621,7 +2576,7 @@ RSG_DN void solve_row(Ctx& a, Row& c, float lo, float hi, bool lower_only) {
     if (B.obj >= 0) { B.dlv += n2 * B.inv_mass * d; B.dav += c.angB * d; }
 }
 
-RSG_DN float solve_split(Ctx& a, Row& c) {  // gResolveSplitPenetrationImpulse_sse2
+RSG_D float solve_split(Ctx& a, Row& c) {  // gResolveSplitPenetrationImpulse_sse2
     if (!c.rhs_pen) return 0.f;
     SBody& A = a.sb[c.ba];
     SBody& B = a.sb[c.bb];
@@ -3014,7 +2969,7 @@ RSG_DN void commit_sweep(const BatchView& bv, Ctx& a, CommitState& cs, int base,
                 float br;
                 dyn_shape(a, o1, xf, sh, br);
                 Manifold& m = new_manifold(a, o1, o0, br);
-                convex_vs_mesh(bv, a, m, o1, xf, sh, a.cand_tri + (o1 - OBJ_BALL) * MESH_SEG);
+                convex_vs_mesh(bv, a, m, o1, xf, sh);
             } else if (k == PK_BALL_PLANE || k == PK_CAR_PLANE) {
                 Xf xf;
                 Convex sh;
@@ -3085,66 +3040,22 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     }
     __syncwarp();
     uint32_t warn = 0;
-    // quantized query box of each mesh pair (one lane per pair)
-    unsigned qmask = 0;
-    for (int p = lane; p < a.npairs; p += 32) {
-        int k = a.pkind[p];
-        if (k == PK_BALL_MESH || k == PK_CAR_MESH) {
-            int d = a.pair1[p] - OBJ_BALL;
-            Xf xf;
-            Convex sh;
-            float br;
-            dyn_shape(a, a.pair1[p], xf, sh, br);
-            V3 mn, mx;
-            sh.aabb(xf, mn, mx);
-            quantize_clamp(bv.mesh, a.qbox + d * 6, mn, false);
-            quantize_clamp(bv.mesh, a.qbox + d * 6 + 3, mx, true);
-            qmask |= 1u << d;
-        }
-    }
-    qmask = __reduce_or_sync(0xffffffffu, qmask);
-    __syncwarp();
-    // subtree headers against every query box, 32 headers at a time; each query keeps the
-    // overlapping headers in header order
-    if (qmask) {
-        int cnt[MAX_DYN];
-        for (int d = 0; d < MAX_DYN; d++) cnt[d] = 0;
-        const int nsub = bv.mesh.nsub;
-        for (int base = 0; base < nsub; base += 32) {
-            const int h = base + lane;
-            uint16_t smin[3], smax[3];
-            int root = 0, size = 0;
-            if (h < nsub) subtree_load(bv.mesh, h, smin, smax, root, size);
-            for (int d = 0; d < MAX_DYN; d++) {
-                if (!((qmask >> d) & 1u)) continue;
-                bool ov = h < nsub && qov(a.qbox + d * 6, a.qbox + d * 6 + 3, smin, smax);
-                unsigned m = __ballot_sync(0xffffffffu, ov);
-                if (ov) {
-                    int pos = cnt[d] + __popc(m & ((1u << lane) - 1u));
-                    if (pos < HDR_LIST) a.hdr_list[d * HDR_LIST + pos] = (int16_t)h;
-                }
-                cnt[d] += __popc(m);
-            }
-        }
-        if (lane == 0)
-            for (int d = 0; d < MAX_DYN; d++)
-                if ((qmask >> d) & 1u) a.hdr_n[d] = (int16_t)(cnt[d] <= HDR_LIST ? cnt[d] : -1);
-    }
-    __syncwarp();
     // candidate triangles of each mesh pair, one lane per pair, in BVH order
     for (int p = lane; p < a.npairs; p += 32) {
         int k = a.pkind[p];
         if (k == PK_BALL_MESH || k == PK_CAR_MESH) {
             int o = a.pair1[p];
-            int d = o - OBJ_BALL;
             Xf xf;
             Convex sh;
             float br;
             dyn_shape(a, o, xf, sh, br);
-            int nh = a.hdr_n[d];
-            int n = mesh_gather(bv, xf, sh, br, nh >= 0 ? a.hdr_list + d * HDR_LIST : nullptr, nh, a.cand_tri + d * MESH_SEG,
-                                MESH_SEG, 0);
-            a.cand_n[d] = (int16_t)(n <= MESH_SEG ? n : -1);
+            int* out = a.cand_tri + (o - OBJ_BALL) * MESH_SEG;
+            int n = 0;
+            mesh_candidates(bv, xf, sh, br, [&](int t) {
+                if (n < MESH_SEG) out[n] = t;
+                n++;
+            });
+            a.cand_n[o - OBJ_BALL] = (int16_t)(n <= MESH_SEG ? n : -1);
         }
     }
     __syncwarp();
@@ -3339,7 +3250,7 @@ RSG_D void pad_check(Ctx& a, Pad& p, int pi, int ci) {  // BoostPad::_CheckColli
     if (col) p.cur_locked = ci;
 }
 
-RSG_DN void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25)
+RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25)
     Car& c = a.cars[ci];
     if (c.f(F_DEMOED) || c.boost >= RL::BOOST_MAX) return;
     V3 cp = c.rb.xf.o * RL::BT_TO_UU;
@@ -3359,7 +3270,9 @@ RSG_DN void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/S
     }
 }
 
-// Arena::Step, one tick (src/Sim/Arena/Arena.cpp:689-756), run by the 32 lanes of one warp.
+// Arena::Step, one tick (src/Sim/Arena/Arena.cpp:689-756), run by the 32 lanes of one warp in four
+// parts (tick_pre, step_bodies_pre, step_collide_warp, tick_post); the kernel puts a block-wide
+// barrier between the parts so that the warps of a block run the same code at the same time.
 //
 // Work that is independent in the reference runs on separate lanes: the 16 suspension rays, the
 // per-car logic after the rays, per-body integration and the boost pads.  Two situations make the
@@ -3368,9 +3281,9 @@ RSG_DN void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/S
 // collision response, which later cars' rays must see and earlier cars' rays must not), and a wheel
 // resting on another car (its friction reads that car's velocity after that car's pre-tick).
 // Collision detection, islands and the solver run on lane 0.
-RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
+// Start of a tick: ball activation, car pre-ticks, boost pad pre-ticks.
+RSG_DN void tick_pre(const BatchView& bv, Ctx& a, int lane) {
     const unsigned FULL = 0xffffffffu;
-    RSG_PHASE_BEGIN;
     if (lane == 0) {
         Body& ball = a.ball;
         bool ball_off = ball.act == DISABLE_DEACTIVATION || ball.act == DISABLE_SIMULATION;
@@ -3406,7 +3319,6 @@ RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
         }
     }
     __syncwarp();
-    RSG_PHASE(0);
     if (bv.has_arena && a.ncars > 0)
         for (int i = lane; i < NUM_PADS; i += 32) {  // BoostPad::_PreTickUpdate (src/Sim/BoostPad/BoostPad.cpp:51-60)
             Pad& p = a.pads[i];
@@ -3415,11 +3327,10 @@ RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
             p.cur_locked = -1;
         }
     __syncwarp();
-    step_bodies_pre(bv, a, lane);
-    RSG_PHASE(1);
-    step_collide_warp(bv, a, lane);
-    __syncwarp();
-    RSG_PHASE(2);
+}
+
+// End of a tick: integration, car post-ticks, pads, ball clamp, goal.
+RSG_DN void tick_post(const BatchView& bv, Ctx& a, int lane) {
     step_bodies_post(bv, a, lane);
     __syncwarp();
     if (lane < a.ncars) {
@@ -3468,7 +3379,6 @@ RSG_DN void arena_tick_warp(const BatchView& bv, Ctx& a, int lane) {
         a.stepped = true;
     }
     __syncwarp();
-    RSG_PHASE(3);
 }
 
 // ---------------------------------------------------------------- record load / store
@@ -3724,8 +3634,7 @@ RSG_D void store_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
 // ---------------------------------------------------------------- shared-memory carve-out
 // Byte offsets of one arena's working set inside its warp's shared-memory region.
 struct SmemLayout {
-    int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, qbox,
-        hdr_list, hdr_n, bytes;
+    int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, bytes;
     ArenaCaps caps;
 };
 RSG_HD int align16(int x) { return (x + 15) & ~15; }
@@ -3748,9 +3657,6 @@ RSG_HD SmemLayout smem_layout(int mc) {
     L.cand_tri = o; o = align16(o + 4 * MESH_SEG * (mc + 1));
     L.cand_n = o; o = align16(o + 2 * (mc + 1));
     L.cand_res = o; o = align16(o + (int)sizeof(CandRes) * 32);
-    L.qbox = o; o = align16(o + 2 * 6 * MAX_DYN);
-    L.hdr_list = o; o = align16(o + 2 * HDR_LIST * MAX_DYN);
-    L.hdr_n = o; o = align16(o + 2 * MAX_DYN);
     L.bytes = o;
     return L;
 }
@@ -3773,9 +3679,6 @@ RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane) {
     a.cand_tri = reinterpret_cast<int*>(base + L.cand_tri);
     a.cand_n = reinterpret_cast<int16_t*>(base + L.cand_n);
     a.cand_res = reinterpret_cast<CandRes*>(base + L.cand_res);
-    a.qbox = reinterpret_cast<uint16_t*>(base + L.qbox);
-    a.hdr_list = reinterpret_cast<int16_t*>(base + L.hdr_list);
-    a.hdr_n = reinterpret_cast<int16_t*>(base + L.hdr_n);
     a.cap_pairs = L.caps.pairs;
     a.cap_pts = L.caps.points;
     a.cap_rows = L.caps.rows;
