@@ -228,6 +228,9 @@ struct Ctx {
     int* cand_tri;
     int16_t* cand_n;
     struct CandRes* cand_res;
+    uint16_t* qbox;    // [MAX_DYN][6] quantized query box of each mesh pair (min, max)
+    int16_t* hdr_list; // [MAX_DYN][HDR_LIST] overlapping subtree headers in header order
+    int16_t* hdr_n;    // [MAX_DYN], -1 when the list overflowed
     int nflat;
     uint32_t warn;
 
@@ -313,26 +316,42 @@ RSG_D bool qov(const uint16_t* a0, const uint16_t* a1, const uint16_t* b0, const
     return o;
 }
 
-// walkStacklessQuantizedTreeCacheFriendly (btQuantizedBvh.cpp:551-575)
+// walkStacklessQuantizedTreeCacheFriendly (btQuantizedBvh.cpp:551-575): subtree headers in order,
+// the nodes of each overlapping subtree in order.
+RSG_D void subtree_load(const DevMesh& m, int s, uint16_t qmin[3], uint16_t qmax[3], int& root, int& size) {
+    const Subtree* st = m.sub + s;
+    for (int k = 0; k < 3; k++) {
+        qmin[k] = __ldg(&st->qmin[k]);
+        qmax[k] = __ldg(&st->qmax[k]);
+    }
+    root = __ldg(&st->root);
+    size = __ldg(&st->size);
+}
+template <class F>
+RSG_D void subtree_walk(const DevMesh& m, const uint16_t* qa, const uint16_t* qb, int root, int size, F&& f) {
+    int cur = root, end = root + size;
+    while (cur < end) {
+        uint16_t nmin[3], nmax[3];
+        int esc;
+        node_load(m, cur, nmin, nmax, esc);
+        bool ov = qov(qa, qb, nmin, nmax);
+        bool leaf = esc >= 0;
+        if (leaf && ov) f(esc);
+        if (ov || leaf) cur++;
+        else cur += -esc;
+    }
+}
 template <class F>
 RSG_D void mesh_query_aabb(const DevMesh& m, V3 mn, V3 mx, F&& f) {
     uint16_t qa[3], qb[3];
     quantize_clamp(m, qa, mn, false);
     quantize_clamp(m, qb, mx, true);
     for (int s = 0; s < m.nsub; s++) {
-        Subtree st = m.sub[s];
-        if (!qov(qa, qb, st.qmin, st.qmax)) continue;
-        int cur = st.root, end = st.root + st.size;
-        while (cur < end) {
-            uint16_t nmin[3], nmax[3];
-            int esc;
-            node_load(m, cur, nmin, nmax, esc);
-            bool ov = qov(qa, qb, nmin, nmax);
-            bool leaf = esc >= 0;
-            if (leaf && ov) f(esc);
-            if (ov || leaf) cur++;
-            else cur += -esc;
-        }
+        uint16_t smin[3], smax[3];
+        int root, size;
+        subtree_load(m, s, smin, smax, root, size);
+        if (!qov(qa, qb, smin, smax)) continue;
+        subtree_walk(m, qa, qb, root, size, f);
     }
 }
 
@@ -2252,13 +2271,17 @@ struct CandRes {
     int valid;
 };
 constexpr int MESH_SEG = 64;  // candidate triangles kept per mesh pair before falling back to lane 0
+constexpr int HDR_LIST = 24;  // overlapping BVH subtree headers kept per mesh query
 
+// `hdrs` (may be null) lists, in header order, the subtree headers that overlap the query box;
+// without it every header is tested.
 template <class F>
-RSG_D void mesh_candidates(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking, F&& emit) {
+RSG_D void mesh_candidates(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking,
+                           const int16_t* hdrs, int nh, F&& emit) {
     V3 mn, mx;
     cshape.aabb(conv_xf, mn, mx);
     M3 inv_basis = inverse(conv_xf.b);
-    mesh_query_aabb(bv.mesh, mn, mx, [&](int t) {
+    auto visit = [&](int t) {
         V3 tv[3];
         tri_load(bv.mesh, t, tv);
         // TestTriangleAgainstAabb2 (z, x, y)
@@ -2291,7 +2314,20 @@ RSG_D void mesh_candidates(const BatchView& bv, const Xf& conv_xf, const Convex&
             }
         }
         emit(t);
-    });
+    };
+    if (!hdrs) {
+        mesh_query_aabb(bv.mesh, mn, mx, visit);
+        return;
+    }
+    uint16_t qa[3], qb[3];
+    quantize_clamp(bv.mesh, qa, mn, false);
+    quantize_clamp(bv.mesh, qb, mx, true);
+    for (int i = 0; i < nh; i++) {
+        uint16_t smin[3], smax[3];
+        int root, size;
+        subtree_load(bv.mesh, hdrs[i], smin, smax, root, size);
+        subtree_walk(bv.mesh, qa, qb, root, size, visit);
+    }
 }
 
 RSG_DN CandRes mesh_candidate_test(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking, int t,
@@ -2335,7 +2371,7 @@ RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, c
     Xf x0 = a.body(m.body0).xf, x1 = obj_xf(a, m.body1);
     float fr = combined_friction(a, OBJ_MESH, conv), re = combined_restitution(a, OBJ_MESH, conv);
     uint32_t warn = 0;
-    mesh_candidates(bv, conv_xf, cshape, m.breaking, [&](int t) {
+    mesh_candidates(bv, conv_xf, cshape, m.breaking, nullptr, 0, [&](int t) {
         CandRes r = mesh_candidate_test(bv, conv_xf, cshape, m.breaking, t, warn);
         commit_mesh_contact(bv, a, m, x0, x1, fr, re, r, t);
     });
@@ -3040,22 +3076,70 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     }
     __syncwarp();
     uint32_t warn = 0;
+    // quantized query box of each mesh pair (one lane per pair)
+    unsigned qmask = 0;
+    for (int p = lane; p < a.npairs; p += 32) {
+        int k = a.pkind[p];
+        if (k == PK_BALL_MESH || k == PK_CAR_MESH) {
+            int d = a.pair1[p] - OBJ_BALL;
+            Xf xf;
+            Convex sh;
+            float br;
+            dyn_shape(a, a.pair1[p], xf, sh, br);
+            V3 mn, mx;
+            sh.aabb(xf, mn, mx);
+            quantize_clamp(bv.mesh, a.qbox + d * 6, mn, false);
+            quantize_clamp(bv.mesh, a.qbox + d * 6 + 3, mx, true);
+            qmask |= 1u << d;
+        }
+    }
+    qmask = __reduce_or_sync(0xffffffffu, qmask);
+    __syncwarp();
+    // subtree headers against every query box, 32 headers at a time; each query keeps the
+    // overlapping headers in header order
+    if (qmask) {
+        int cnt[MAX_DYN];
+        for (int d = 0; d < MAX_DYN; d++) cnt[d] = 0;
+        const int nsub = bv.mesh.nsub;
+        for (int base = 0; base < nsub; base += 32) {
+            const int h = base + lane;
+            uint16_t smin[3], smax[3];
+            int root = 0, size = 0;
+            if (h < nsub) subtree_load(bv.mesh, h, smin, smax, root, size);
+            for (int d = 0; d < MAX_DYN; d++) {
+                if (!((qmask >> d) & 1u)) continue;
+                bool ov = h < nsub && qov(a.qbox + d * 6, a.qbox + d * 6 + 3, smin, smax);
+                unsigned m = __ballot_sync(0xffffffffu, ov);
+                if (ov) {
+                    int pos = cnt[d] + __popc(m & ((1u << lane) - 1u));
+                    if (pos < HDR_LIST) a.hdr_list[d * HDR_LIST + pos] = (int16_t)h;
+                }
+                cnt[d] += __popc(m);
+            }
+        }
+        if (lane == 0)
+            for (int d = 0; d < MAX_DYN; d++)
+                if ((qmask >> d) & 1u) a.hdr_n[d] = (int16_t)(cnt[d] <= HDR_LIST ? cnt[d] : -1);
+    }
+    __syncwarp();
     // candidate triangles of each mesh pair, one lane per pair, in BVH order
     for (int p = lane; p < a.npairs; p += 32) {
         int k = a.pkind[p];
         if (k == PK_BALL_MESH || k == PK_CAR_MESH) {
             int o = a.pair1[p];
+            int d = o - OBJ_BALL;
             Xf xf;
             Convex sh;
             float br;
             dyn_shape(a, o, xf, sh, br);
-            int* out = a.cand_tri + (o - OBJ_BALL) * MESH_SEG;
+            int* out = a.cand_tri + d * MESH_SEG;
             int n = 0;
-            mesh_candidates(bv, xf, sh, br, [&](int t) {
+            int nh = a.hdr_n[d];
+            mesh_candidates(bv, xf, sh, br, nh >= 0 ? a.hdr_list + d * HDR_LIST : nullptr, nh, [&](int t) {
                 if (n < MESH_SEG) out[n] = t;
                 n++;
             });
-            a.cand_n[o - OBJ_BALL] = (int16_t)(n <= MESH_SEG ? n : -1);
+            a.cand_n[d] = (int16_t)(n <= MESH_SEG ? n : -1);
         }
     }
     __syncwarp();
@@ -3634,7 +3718,8 @@ RSG_D void store_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
 // ---------------------------------------------------------------- shared-memory carve-out
 // Byte offsets of one arena's working set inside its warp's shared-memory region.
 struct SmemLayout {
-    int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, bytes;
+    int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, qbox,
+        hdr_list, hdr_n, bytes;
     ArenaCaps caps;
 };
 RSG_HD int align16(int x) { return (x + 15) & ~15; }
@@ -3657,6 +3742,9 @@ RSG_HD SmemLayout smem_layout(int mc) {
     L.cand_tri = o; o = align16(o + 4 * MESH_SEG * (mc + 1));
     L.cand_n = o; o = align16(o + 2 * (mc + 1));
     L.cand_res = o; o = align16(o + (int)sizeof(CandRes) * 32);
+    L.qbox = o; o = align16(o + 2 * 6 * MAX_DYN);
+    L.hdr_list = o; o = align16(o + 2 * HDR_LIST * MAX_DYN);
+    L.hdr_n = o; o = align16(o + 2 * MAX_DYN);
     L.bytes = o;
     return L;
 }
@@ -3679,6 +3767,9 @@ RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane) {
     a.cand_tri = reinterpret_cast<int*>(base + L.cand_tri);
     a.cand_n = reinterpret_cast<int16_t*>(base + L.cand_n);
     a.cand_res = reinterpret_cast<CandRes*>(base + L.cand_res);
+    a.qbox = reinterpret_cast<uint16_t*>(base + L.qbox);
+    a.hdr_list = reinterpret_cast<int16_t*>(base + L.hdr_list);
+    a.hdr_n = reinterpret_cast<int16_t*>(base + L.hdr_n);
     a.cap_pairs = L.caps.pairs;
     a.cap_pts = L.caps.points;
     a.cap_rows = L.caps.rows;
