@@ -74,17 +74,20 @@ __global__ void __launch_bounds__(256) rsg_tick_kernel(BatchView bv, const rsg_c
         load_pads(bv, ar, a, lane);
         __syncwarp();
     }
+    const int wpb = blockDim.x >> 5;
+    int nact = bv.A - blockIdx.x * wpb;
+    nact = nact < wpb ? nact : wpb;
+    const BlockArenas B{smem, L.bytes, nact};
     RSG_PHASE_BEGIN;
     for (int t = 0; t < ticks; t++) {
-        if (active) {
-            if (controls && lane < a.ncars) {
-                const rsg_car_controls k = controls[((size_t)t * bv.A + ar) * bv.MC + lane];
-                apply_controls(a.cars[lane], k);
+        if (controls)
+            for (int u = threadIdx.x; u < nact * bv.MC; u += blockDim.x) {
+                const int w = u / bv.MC, k = u % bv.MC;
+                Ctx& aw = B(w);
+                if (k < aw.ncars) apply_controls(aw.cars[k], controls[((size_t)t * bv.A + blockIdx.x * wpb + w) * bv.MC + k]);
             }
-            __syncwarp();
-            tick_pre(bv, a, lane);
-        }
         __syncthreads();
+        block_tick_pre(bv, B, threadIdx.x, blockDim.x);
         RSG_PHASE(0);
         if (active) step_bodies_pre(bv, a, lane);
         __syncthreads();
@@ -92,8 +95,7 @@ __global__ void __launch_bounds__(256) rsg_tick_kernel(BatchView bv, const rsg_c
         if (active) step_collide_warp(bv, a, lane);
         __syncthreads();
         RSG_PHASE(2);
-        if (active) tick_post(bv, a, lane);
-        __syncthreads();
+        block_tick_post(bv, B, threadIdx.x, blockDim.x);
         RSG_PHASE(3);
     }
     if (active) {

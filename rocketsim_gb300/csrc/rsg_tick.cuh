@@ -209,6 +209,7 @@ struct Ctx {
     int nevents;
     float solver_dt;
     int serial;  // the pre-tick of this tick runs car by car in update order
+    int on_car;  // a wheel rests on another car: the car logic after the rays runs in update order
     // scratch of one world step
     int npairs, cap_pairs;
     int8_t* pair0;
@@ -3365,10 +3366,25 @@ RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Si
 // collision response, which later cars' rays must see and earlier cars' rays must not), and a wheel
 // resting on another car (its friction reads that car's velocity after that car's pre-tick).
 // Collision detection, islands and the solver run on lane 0.
-// Start of a tick: ball activation, car pre-ticks, boost pad pre-ticks.
-RSG_DN void tick_pre(const BatchView& bv, Ctx& a, int lane) {
-    const unsigned FULL = 0xffffffffu;
-    if (lane == 0) {
+// The arenas of one block (one warp each), addressed by their index in the block.
+struct BlockArenas {
+    unsigned char* base;
+    int bytes;  // shared memory per arena
+    int nact;   // arenas of this block that exist
+    RSG_D Ctx& operator()(int w) const { return *reinterpret_cast<Ctx*>(base + (size_t)w * bytes); }
+};
+
+// Start of a tick for every arena of the block, the work spread over the block's threads by
+// unit: arena, car, wheel, pad.  In the reference these run car by car; the units here are
+// independent (a car's rays read only positions, cells and collision flags of other cars, none
+// of which a pre-tick changes), except in the two situations that fall back to the reference's
+// order for the whole arena: a car that is or just was demolished (its pre-tick moves it and
+// changes its collision response, which earlier cars' rays must not see), and a wheel resting on
+// another car (its friction reads that car's velocity after that car's pre-tick).
+RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, int nthreads) {
+    const int MC = bv.MC;
+    for (int w = tid; w < B.nact; w += nthreads) {
+        Ctx& a = B(w);
         Body& ball = a.ball;
         bool ball_off = ball.act == DISABLE_DEACTIVATION || ball.act == DISABLE_SIMULATION;
         if (len2(ball.lin_vel) == 0 && len2(ball.ang_vel) == 0) {
@@ -3379,80 +3395,186 @@ RSG_DN void tick_pre(const BatchView& bv, Ctx& a, int lane) {
         int serial = 0;
         for (int i = 0; i < a.ncars; i++) serial |= a.cars[i].f(F_DEMOED) || a.cars[i].rb.no_contact_response;
         a.serial = serial;
+        a.on_car = 0;
     }
-    __syncwarp();
-    if (a.serial) {
-        if (lane == 0)
-            for (int k = 0; k < a.ncars; k++) car_pre_tick(bv, a, a.cars[a.order[k]]);
-    } else {
-        if (lane < a.ncars) car_pre_before_rays(a.cars[lane]);
-        __syncwarp();
-        bool on_car = false;
-        if (lane < 4 * a.ncars) {
-            Car& c = a.cars[lane >> 2];
-            ray_cast_wheel(bv, a, c, lane & 3);
-            on_car = c.w[lane & 3].ground >= OBJ_CAR0;
-        }
-        bool any_on_car = __any_sync(FULL, on_car);
-        __syncwarp();
-        if (any_on_car) {
-            if (lane == 0)
-                for (int k = 0; k < a.ncars; k++) car_pre_after_rays(bv, a, a.cars[a.order[k]]);
-        } else if (lane < a.ncars) {
-            car_pre_after_rays(bv, a, a.cars[lane]);
+    __syncthreads();
+    for (int u = tid; u < B.nact * MC; u += nthreads) {
+        Ctx& a = B(u / MC);
+        int k = u % MC;
+        if (k >= a.ncars) continue;
+        if (a.serial) {
+            if (k == 0)
+                for (int kk = 0; kk < a.ncars; kk++) car_pre_tick(bv, a, a.cars[a.order[kk]]);
+        } else {
+            car_pre_before_rays(a.cars[k]);
         }
     }
-    __syncwarp();
-    if (bv.has_arena && a.ncars > 0)
-        for (int i = lane; i < NUM_PADS; i += 32) {  // BoostPad::_PreTickUpdate (src/Sim/BoostPad/BoostPad.cpp:51-60)
-            Pad& p = a.pads[i];
+    __syncthreads();
+    for (int u = tid; u < B.nact * MC * 4; u += nthreads) {
+        Ctx& a = B(u / (MC * 4));
+        int r = u % (MC * 4), k = r >> 2, wh = r & 3;
+        if (a.serial || k >= a.ncars) continue;
+        ray_cast_wheel(bv, a, a.cars[k], wh);
+        if (a.cars[k].w[wh].ground >= OBJ_CAR0) a.on_car = 1;
+    }
+    __syncthreads();
+    for (int u = tid; u < B.nact * MC; u += nthreads) {
+        Ctx& a = B(u / MC);
+        int k = u % MC;
+        if (a.serial || k >= a.ncars) continue;
+        if (a.on_car) {
+            if (k == 0)
+                for (int kk = 0; kk < a.ncars; kk++) car_pre_after_rays(bv, a, a.cars[a.order[kk]]);
+        } else {
+            car_pre_after_rays(bv, a, a.cars[k]);
+        }
+    }
+    if (bv.has_arena)
+        for (int u = tid; u < B.nact * NUM_PADS; u += nthreads) {  // BoostPad::_PreTickUpdate (BoostPad.cpp:51-60)
+            Ctx& a = B(u / NUM_PADS);
+            if (a.ncars == 0) continue;
+            Pad& p = a.pads[u % NUM_PADS];
             if (p.cooldown > 0) p.cooldown = rs_maxf(p.cooldown - bv.dt, 0);
             p.active = (p.cooldown == 0);
             p.cur_locked = -1;
         }
-    __syncwarp();
+    __syncthreads();
 }
 
-// End of a tick: integration, car post-ticks, pads, ball clamp, goal.
-RSG_DN void tick_post(const BatchView& bv, Ctx& a, int lane) {
-    step_bodies_post(bv, a, lane);
-    __syncwarp();
-    if (lane < a.ncars) {
-        car_post_tick(a.cars[lane], bv.dt);
-        car_finish_physics(a.cars[lane]);
+// Body integration and activation (btDiscreteDynamicsWorld.cpp:516-551, 889-991) of one body.
+RSG_DN void body_post(Body& b, float dt) {
+    if (b.is_active()) {
+        Xf nt;
+        integrate_transform(b.xf, b.lin_vel, b.ang_vel, dt, b.no_rot, nt);
+        b.interp = nt;
+        b.xf = nt;
+        b.update_inertia();
     }
-    __syncwarp();
-    if (lane == 0) {
-        if (bv.has_arena)
-            for (int k = 0; k < a.ncars; k++) grid_check(a, a.order[k]);
-        if (bv.has_arena && a.ncars > 0)
-            for (int i = 0; i < NUM_PADS; i++) {  // BoostPad::_PostTickUpdate (src/Sim/BoostPad/BoostPad.cpp:88-105)
-                Pad& p = a.pads[i];
-                uint32_t locked = 0;
-                if (p.cur_locked >= 0) {
-                    Car& c = a.cars[p.cur_locked];
-                    locked = c.id;
-                    if (p.active) {
-                        bool big = i < 6;
-                        c.boost = rs_minf(c.boost + (big ? RL::PAD_BOOST_BIG : RL::PAD_BOOST_SMALL), RL::BOOST_MAX);
-                        p.active = false;
-                        p.cooldown = big ? RL::PAD_COOLDOWN_BIG : RL::PAD_COOLDOWN_SMALL;
-                    }
-                }
-                p.prev_locked = locked;
+    // The deactivation timer can only move a body to WANTS_DEACTIVATION, which the next tick
+    // overwrites before anything reads it, so it is not carried between ticks.
+    if (b.act == ISLAND_SLEEPING || b.act == DISABLE_DEACTIVATION) {
+    } else if (len2(b.lin_vel) < 0.8f * 0.8f && len2(b.ang_vel) < 1.f * 1.f) {
+    } else {
+        if (b.act != DISABLE_DEACTIVATION && b.act != DISABLE_SIMULATION) b.act = 0;
+    }
+    bool wants = b.act != DISABLE_DEACTIVATION && (b.act == ISLAND_SLEEPING || b.act == WANTS_DEACTIVATION);
+    if (wants) {
+        if (b.act == ISLAND_SLEEPING) { b.ang_vel = V3(0, 0, 0); b.lin_vel = V3(0, 0, 0); }
+    } else {
+        if (b.act != DISABLE_DEACTIVATION && b.act != DISABLE_SIMULATION) b.act = ACTIVE_TAG;
+    }
+    b.total_force = V3(0, 0, 0);  // clearForces
+    b.total_torque = V3(0, 0, 0);
+}
+
+// The pad grid test of one (pad, car): BoostPadGrid::CheckCollision's cell neighbourhood
+// (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25) and BoostPad::_CheckCollide (BoostPad.cpp:62-86).
+RSG_D bool pad_touches(Ctx& a, const Pad& p, int pi, int ci) {
+    Car& c = a.cars[ci];
+    if (c.f(F_DEMOED) || c.boost >= RL::BOOST_MAX) return false;
+    V3 cpu = c.rb.xf.o * RL::BT_TO_UU;
+    const float EXT_Z = RL::PAD_CYL_HEIGHT + 250.f;
+    if (cpu.z > EXT_Z) return false;
+    const int CX = 8, CY = 10, SX = (int)(4096.f / (CX / 2)), SY = (int)(5120.f / (CY / 2));
+    int ix = (int)(cpu.x / SX + (CX / 2));
+    int iy = (int)(cpu.y / SY + (CY / 2));
+    int px = (int)(c_pad_locs[pi][0] / SX + (CX / 2));
+    int py = (int)(c_pad_locs[pi][1] / SY + (CY / 2));
+    int i0 = ix - 1 > 0 ? ix - 1 : 0, i1 = ix + 1 < CX - 1 ? ix + 1 : CX - 1;
+    int j0 = iy - 1 > 0 ? iy - 1 : 0, j1 = iy + 1 < CY - 1 ? iy + 1 : CY - 1;
+    if (px < i0 || px > i1 || py < j0 || py > j1) return false;
+    V3 cp = c.rb.xf.o;
+    bool big = pi < 6;
+    V3 pos_bt = V3(c_pad_locs[pi][0], c_pad_locs[pi][1], c_pad_locs[pi][2]) * RL::UU_TO_BT;
+    if (p.prev_locked == c.id) {
+        V3 mn, mx;
+        car_compound_aabb(c, c.rb.xf, mn, mx);
+        float br = (big ? RL::PAD_BOX_RAD_BIG : RL::PAD_BOX_RAD_SMALL) * RL::UU_TO_BT;
+        V3 bmin = pos_bt - V3(br, br, 0);
+        V3 bmax = pos_bt + V3(br, br, RL::PAD_BOX_HEIGHT * RL::UU_TO_BT);
+        bool gt = (bmax.x > mn.x) && (bmax.y > mn.y) && (bmax.z > mn.z);
+        bool lt = (bmin.x < mx.x) && (bmin.y < mx.y) && (bmin.z < mx.z);
+        return gt && lt;
+    }
+    float rad = (big ? RL::PAD_CYL_RAD_BIG : RL::PAD_CYL_RAD_SMALL) * RL::UU_TO_BT;
+    float dx = cp.x - pos_bt.x, dy = cp.y - pos_bt.y;
+    if (dx * dx + dy * dy < rad * rad) return fabsf(cp.z - pos_bt.z) < (RL::PAD_CYL_HEIGHT * RL::UU_TO_BT);
+    return false;
+}
+
+// End of a tick for every arena of the block: integration, car post-ticks, boost pads, ball
+// clamp, goal.  The pad pass of the reference (each car in update order marks the pads it
+// touches, the last one wins; then each pad in order gives boost to its car) is done per pad
+// and per car, which gives the same result because a pad's outcome depends only on the cars and
+// a car's boost only on its pads taken in pad order.
+RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, int nthreads) {
+    const int MC = bv.MC, NB = MC + 1;
+    for (int u = tid; u < B.nact * NB; u += nthreads) {
+        Ctx& a = B(u / NB);
+        int d = u % NB;
+        if (d > a.ncars) continue;
+        body_post(a.body(OBJ_BALL + d), bv.dt);
+    }
+    __syncthreads();
+    for (int u = tid; u < B.nact * MC; u += nthreads) {
+        Ctx& a = B(u / MC);
+        int k = u % MC;
+        if (k >= a.ncars) continue;
+        car_post_tick(a.cars[k], bv.dt);
+        car_finish_physics(a.cars[k]);
+    }
+    __syncthreads();
+    if (bv.has_arena) {
+        for (int u = tid; u < B.nact * NUM_PADS; u += nthreads) {  // which car each pad is locked to
+            Ctx& a = B(u / NUM_PADS);
+            int pi = u % NUM_PADS;
+            Pad& p = a.pads[pi];
+            for (int kk = 0; kk < a.ncars; kk++)
+                if (pad_touches(a, p, pi, a.order[kk])) p.cur_locked = a.order[kk];
+        }
+        __syncthreads();
+        for (int u = tid; u < B.nact * MC; u += nthreads) {  // BoostPad::_PostTickUpdate boost, in pad order
+            Ctx& a = B(u / MC);
+            int k = u % MC;
+            if (k >= a.ncars) continue;
+            Car& c = a.cars[k];
+            for (int i = 0; i < NUM_PADS; i++) {
+                const Pad& p = a.pads[i];
+                if (p.cur_locked == k && p.active)
+                    c.boost = rs_minf(c.boost + (i < 6 ? RL::PAD_BOOST_BIG : RL::PAD_BOOST_SMALL), RL::BOOST_MAX);
             }
+        }
+        __syncthreads();
+        for (int u = tid; u < B.nact * NUM_PADS; u += nthreads) {  // BoostPad::_PostTickUpdate (BoostPad.cpp:88-105)
+            Ctx& a = B(u / NUM_PADS);
+            if (a.ncars == 0) continue;
+            int i = u % NUM_PADS;
+            Pad& p = a.pads[i];
+            uint32_t locked = 0;
+            if (p.cur_locked >= 0) {
+                locked = a.cars[p.cur_locked].id;
+                if (p.active) {
+                    p.active = false;
+                    p.cooldown = i < 6 ? RL::PAD_COOLDOWN_BIG : RL::PAD_COOLDOWN_SMALL;
+                }
+            }
+            p.prev_locked = locked;
+        }
+    }
+    for (int w = tid; w < B.nact; w += nthreads) {
+        Ctx& a = B(w);
         Body& ball = a.ball;
         {  // Ball::_FinishPhysicsTick (src/Sim/Ball/Ball.cpp:117-143)
             if (!is_zero(a.ball_cache)) {
                 ball.lin_vel += a.ball_cache;
                 a.ball_cache = V3(0, 0, 0);
             }
-            V3 v = ball.lin_vel, w = ball.ang_vel;
+            V3 v = ball.lin_vel, wv = ball.ang_vel;
             const float ms = RL::BALL_MAX_SPEED * RL::UU_TO_BT;
             if (len2(v) > ms * ms) v = normalized(v) * ms;
-            if (len2(w) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) w = normalized(w) * RL::BALL_MAX_ANG_SPEED;
+            if (len2(wv) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) wv = normalized(wv) * RL::BALL_MAX_ANG_SPEED;
             ball.lin_vel = v;
-            ball.ang_vel = w;
+            ball.ang_vel = wv;
             a.ball_ticks++;
         }
         if (bv.has_arena && ball_scored(a)) {
@@ -3462,7 +3584,7 @@ RSG_DN void tick_post(const BatchView& bv, Ctx& a, int lane) {
         a.tick++;
         a.stepped = true;
     }
-    __syncwarp();
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------- record load / store
