@@ -173,7 +173,7 @@ static_assert(sizeof(DevEventHost) == DEV_EVENT_BYTES, "event record");
 struct rsg_batch {
     int game_mode = 0;
     int device = 0;
-    int warps_per_block = 4;  // arenas per block of the tick kernel
+    int warps_per_block = 8;  // arenas per block of the tick kernel
     BatchBuffers buf{};
     cudaStream_t stream = nullptr;
     std::vector<CarCfgDev> cfgs;
