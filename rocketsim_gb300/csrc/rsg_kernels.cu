@@ -92,7 +92,8 @@ __global__ void __launch_bounds__(256) rsg_tick_kernel(BatchView bv, const rsg_c
         if (active) step_bodies_pre(bv, a, lane);
         __syncthreads();
         RSG_PHASE(1);
-        block_collide(bv, B, a, active, lane, threadIdx.x, blockDim.x);
+        if (active) step_collide_warp(bv, a, lane);
+        __syncthreads();
         RSG_PHASE(2);
         block_tick_post(bv, B, threadIdx.x, blockDim.x);
         RSG_PHASE(3);

@@ -188,12 +188,6 @@ struct Manifold {
 
 struct Row;
 struct SBody;
-// Position of the in-order sweep over the pairs that commits narrow-phase results.
-struct CommitState {
-    int p, j, mi;
-    Xf x0, x1;
-    float fr, re;
-};
 
 // One arena's working state during a launch.  It lives in shared memory (one
 // region per warp); the arrays are carved out of the same region with sizes
@@ -240,7 +234,6 @@ struct Ctx {
     int16_t* hdr_n;    // [MAX_DYN], -1 when the list overflowed
     int nflat;
     uint32_t warn;
-    struct CommitState cs;  // where lane 0's in-order sweep over the pairs stopped
 
     RSG_D Body& body(int o) { return o == OBJ_BALL ? ball : cars[o - OBJ_CAR0].rb; }
 };
@@ -2994,17 +2987,14 @@ RSG_DN void car_car_pair(const BatchView& bv, Ctx& a, int o0, int o1) {
     refresh(a, m, c0.rb.xf, c1.rb.xf);
 }
 
-// The arenas of one block (one warp each), addressed by their index in the block.
-struct BlockArenas {
-    unsigned char* base;
-    int bytes;  // shared memory per arena
-    int nact;   // arenas of this block that exist
-    RSG_D Ctx& operator()(int w) const { return *reinterpret_cast<Ctx*>(base + (size_t)w * bytes); }
-};
-
 // Lane 0's walk over the pairs in order (btCollisionDispatcher::dispatchAllCollisionPairs): pairs
 // without candidates are processed when reached; a pair with candidates takes their results as
 // the rounds deliver them.
+struct CommitState {
+    int p, j, mi;
+    Xf x0, x1;
+    float fr, re;
+};
 RSG_DN void commit_sweep(const BatchView& bv, Ctx& a, CommitState& cs, int base, int f_end) {
     while (cs.p < a.npairs) {
         const int p = cs.p, k = a.pkind[p];
@@ -3077,10 +3067,15 @@ RSG_DN void commit_sweep(const BatchView& bv, Ctx& a, CommitState& cs, int base,
 
 RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a);
 
-// Narrow phase of one arena on the 32 lanes of its warp; the pair list (build_pairs) exists and
-// the commit state is left in the context for the final sweep.
 RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     RSG_PHASE_BEGIN;
+    if (lane == 0) {
+        build_pairs(bv, a);
+        a.nman = 0;
+        a.npts = 0;
+        a.warn = 0;
+    }
+    __syncwarp();
     uint32_t warn = 0;
     // quantized query box of each mesh pair (one lane per pair)
     unsigned qmask = 0;
@@ -3190,34 +3185,15 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
         __syncwarp();
     }
     if (warn) atomicOr(&a.warn, warn);
-    if (lane == 0) a.cs = cs;
     __syncwarp();
     RSG_PHASE(5);
-}
-
-// World-step collision work of every arena of the block: pair lists (one thread per arena),
-// narrow phase (one warp per arena), then the rest of the pair sweep, islands and the solver
-// (one thread per arena).
-RSG_DN void block_collide(const BatchView& bv, const BlockArenas& B, Ctx& own, bool active, int lane, int tid,
-                          int nthreads) {
-    for (int w = tid; w < B.nact; w += nthreads) {
-        Ctx& a = B(w);
-        build_pairs(bv, a);
-        a.nman = 0;
-        a.npts = 0;
-        a.warn = 0;
-    }
-    __syncthreads();
-    if (active) step_collide_warp(bv, own, lane);
-    __syncthreads();
-    for (int w = tid; w < B.nact; w += nthreads) {
-        Ctx& a = B(w);
-        CommitState cs = a.cs;
-        commit_sweep(bv, a, cs, a.nflat, a.nflat);
+    if (lane == 0) {
+        commit_sweep(bv, a, cs, nflat, nflat);
         a.err |= a.warn;
-        step_collide_tail(bv, a);
     }
-    __syncthreads();
+    RSG_PHASE(6);
+    if (lane == 0) step_collide_tail(bv, a);
+    RSG_PHASE(7);
 }
 
 RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a) {
@@ -3390,6 +3366,14 @@ RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Si
 // collision response, which later cars' rays must see and earlier cars' rays must not), and a wheel
 // resting on another car (its friction reads that car's velocity after that car's pre-tick).
 // Collision detection, islands and the solver run on lane 0.
+// The arenas of one block (one warp each), addressed by their index in the block.
+struct BlockArenas {
+    unsigned char* base;
+    int bytes;  // shared memory per arena
+    int nact;   // arenas of this block that exist
+    RSG_D Ctx& operator()(int w) const { return *reinterpret_cast<Ctx*>(base + (size_t)w * bytes); }
+};
+
 // Start of a tick for every arena of the block, the work spread over the block's threads by
 // unit: arena, car, wheel, pad.  In the reference these run car by car; the units here are
 // independent (a car's rays read only positions, cells and collision flags of other cars, none
