@@ -136,6 +136,8 @@ PROTOTYPES = {
     "rsg_set_bump_callback": (i32, [vp, BUMP_FN, vp]),
     "rsg_set_ball_hit_callback": (i32, [vp, BALL_HIT_FN, vp]),
     "rsg_get_device_flags": (i32, [vp, P(u32)]),
+    "rsg_air_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp]),
+    "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
 }
 
 _LIB = None
