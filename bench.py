@@ -15,6 +15,12 @@ memory (rsg_set_controls_all), rsg_step(8), and every car, ball and pad state
 read back to host memory (rsg_get_all_states).  The L2 cache is flushed
 (a 256 MiB device write) between timed steps.
 
+The same line carries ``adjoint``: gradient steps (forward with checkpoints,
+loss, hand-written adjoint backward) of 60-tick air-control rollouts over
+8192 instances, replayed as one captured CUDA graph (and eagerly), their
+relative error against FP64 central finite differences on a few instances,
+and the backward / forward cost ratio of the C-ABI calls.
+
 ``--impl reference`` times the CPU implementation of the same tick on the
 host cores instead: the reference library built from its sources when it is
 loadable on this machine, else the CPU restatement of it (oracle/).
@@ -358,6 +364,169 @@ def run_gpu(args, rank: int, world: int):
     }
 
 
+# ---------------------------------------------------------------- adjoint (air phase)
+ADJ_TICKS = 60
+ADJ_WORKLOAD = ("air-phase adjoint: 8192 instances x (1 airborne Octane + ball), 60 ticks, controls "
+                "pitch/yaw/roll in [-1, 1] and relaxed boost in [0, 1], checkpoints every 16 ticks")
+
+
+def adjoint_case(n: int, seed: int):
+    """Air-phase differentiation workload: car at 400..1600 uu, |v| <= 1500 uu/s of uniform
+    direction, uniformly random orientation, at rest rotationally; the ball point 300..1500 uu away
+    with |v| <= 500 uu/s; controls uniform (|u| >= 1e-3 so no input sits on the |u| kink of the
+    damping); a seeded target orientation per instance.  Bullet units (1 BT = 50 uu)."""
+    rng = np.random.default_rng(seed)
+    s = np.zeros((n, 24), np.float32)
+    s[:, 0:2] = rng.uniform(-3000, 3000, (n, 2)) / 50.0
+    s[:, 2] = rng.uniform(400, 1600, n) / 50.0
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    s[:, 3:6] = d * rng.uniform(0, 1500, (n, 1)) / 50.0
+
+    def rot(k):
+        q = rng.normal(size=(k, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        x, y, z, w = q.T
+        return np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                         2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                         2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], 1)
+    s[:, 9:18] = rot(n)
+    off = rng.normal(size=(n, 3))
+    off *= (rng.uniform(300, 1500, n) / np.linalg.norm(off, axis=1))[:, None]
+    s[:, 18:21] = s[:, 0:3] + off / 50.0
+    bd = rng.normal(size=(n, 3))
+    bd /= np.linalg.norm(bd, axis=1, keepdims=True)
+    s[:, 21:24] = bd * rng.uniform(0, 500, (n, 1)) / 50.0
+    u = rng.uniform(1e-3, 1.0, (ADJ_TICKS, n, 4)) * rng.choice([-1.0, 1.0], (ADJ_TICKS, n, 4))
+    u[..., 3] = rng.uniform(1e-3, 1.0 - 1e-3, (ADJ_TICKS, n))
+    return s, u.astype(np.float32), rot(n).reshape(n, 3, 3).astype(np.float32)
+
+
+def run_adjoint(args, dev: int):
+    """Gradient steps of the air-phase workload: forward with checkpoints, loss, adjoint backward."""
+    import torch
+    from rocketsim_gb300 import adjoint
+
+    n = args.adj_instances
+    s, u, target = adjoint_case(n, 4321)
+    ds = torch.from_numpy(s).to(f"cuda:{dev}")
+    du = torch.from_numpy(u).to(f"cuda:{dev}").requires_grad_(True)
+    tgt = torch.from_numpy(target).to(f"cuda:{dev}")
+
+    def grad_step():
+        du.grad = None
+        fin = adjoint.air_rollout(ds, du, ckpt_every=16)
+        adjoint.aim_loss(fin, tgt).sum().backward()
+
+    for _ in range(args.warmup):
+        grad_step()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        du.grad = None
+        ev[k][0].record()
+        fin = adjoint.air_rollout(ds, du, ckpt_every=16)
+        ev[k][1].record()
+        adjoint.aim_loss(fin, tgt).sum().backward()
+        ev[k][2].record()
+    torch.cuda.synchronize()
+    fwd = [a.elapsed_time(b) for a, b, _ in ev]
+    bwd = [b.elapsed_time(c) for _, b, c in ev]
+    total_ms = sum(a.elapsed_time(c) for a, _, c in ev)
+    grads_per_s = n * args.steps / (total_ms / 1e3)
+    # plain forward (no checkpoints) for the cost ratio
+    with torch.no_grad():
+        adjoint.air_rollout(ds, du.detach())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            adjoint.air_rollout(ds, du.detach())
+        e1.record()
+        torch.cuda.synchronize()
+        plain_fwd_ms = e0.elapsed_time(e1) / args.steps
+    eager_grads_per_s = grads_per_s
+    # the same gradient step captured once as a CUDA graph and replayed (a training loop's form:
+    # the controls and the gradient are static tensors updated in place)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            grad_step()
+    torch.cuda.current_stream().wait_stream(side)
+    du.grad = None
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        fin_g = adjoint.air_rollout(ds, du, ckpt_every=16)
+        adjoint.aim_loss(fin_g, tgt).sum().backward()
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        gev[k][0].record()
+        graph.replay()
+        gev[k][1].record()
+    torch.cuda.synchronize()
+    graph_ms = [a.elapsed_time(b) for a, b in gev]
+    grads_per_s = n * args.steps / (sum(graph_ms) / 1e3)
+    g_gpu = du.grad[:, :args.adj_check].detach().cpu().numpy().astype(np.float64)
+    # the two C-ABI calls alone (no torch loss): forward with checkpoints, adjoint backward
+    import ctypes as C
+    from rocketsim_gb300 import abi
+    from rocketsim_gb300.arena import car_config
+    lib = abi.load(build_if_missing=False)
+    cfg = car_config(abi.CAR_OCTANE)
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    ck = torch.empty(((ADJ_TICKS + 15) // 16, n, 24), device=ds.device)
+    fin = torch.empty_like(ds)
+    gfin = torch.randn_like(ds)
+    gu = torch.empty_like(du)
+    nb = C.c_size_t()
+    abi.check(lib.rsg_air_backward_workspace_size(n, ADJ_TICKS, C.byref(nb)), "workspace size")
+    work = torch.empty(nb.value, dtype=torch.uint8, device=ds.device)
+    strm = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    kf, kb = [], []
+    for k in range(args.warmup + args.steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        abi.check(lib.rsg_air_forward(C.byref(cfg), 120.0, n, ADJ_TICKS, P(ds), P(du), P(fin), P(ck), 16, strm),
+                  "rsg_air_forward")
+        e[1].record()
+        abi.check(lib.rsg_air_backward(C.byref(cfg), 120.0, n, ADJ_TICKS, P(du), P(ck), 16, P(gfin), P(gu), None,
+                                       P(work), nb.value, strm), "rsg_air_backward")
+        e[2].record()
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            kf.append(e[0].elapsed_time(e[1]))
+            kb.append(e[1].elapsed_time(e[2]))
+    return {"value": grads_per_s, "ms_per_step": sum(graph_ms) / args.steps,
+            "eager_value": eager_grads_per_s, "eager_ms_per_step": total_ms / args.steps,
+            "ms_forward_ckpt": statistics.median(fwd), "ms_forward_plain": plain_fwd_ms,
+            "ms_backward": statistics.median(bwd),
+            "backward_over_forward": statistics.median(bwd) / plain_fwd_ms,
+            "kernel_ms_forward_ckpt": statistics.median(kf), "kernel_ms_backward": statistics.median(kb),
+            "kernel_backward_over_forward": statistics.median(kb) / plain_fwd_ms,
+            "workspace_bytes": nb.value,
+            "case": (s, u, target), "g_gpu": g_gpu}
+
+
+def adjoint_cpu_check(case, g_gpu: np.ndarray, k: int):
+    """FP64 central finite differences (step 1e-4) on the host for the first k instances: the
+    gradient reference (relative error of the GPU adjoint) and the CPU way to the same gradients."""
+    from oracle import air_fp64 as F
+    s, u, target = case
+    s64 = s[:k].astype(np.float64)
+    u64 = u[:, :k].astype(np.float64)
+    t64 = target[:k].astype(np.float64)
+    iinv = F.car_inv_inertia((120.507, 86.6994, 38.6591))
+    t0 = time.perf_counter()
+    gfd = F.fd_grad(s64, u64, iinv, 1.0 / 120.0, lambda f: F.aim_loss(f, t64), h=1e-4)
+    el = time.perf_counter() - t0
+    num = np.linalg.norm((g_gpu - gfd).transpose(1, 0, 2).reshape(k, -1), axis=1)
+    den = np.linalg.norm(gfd.transpose(1, 0, 2).reshape(k, -1), axis=1)
+    return float((num / den).max()), k / el, el
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -366,6 +535,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--arenas", type=int, default=4096)
     ap.add_argument("--cpu-seconds", type=float, default=1.5)
+    ap.add_argument("--adj-instances", type=int, default=8192)
+    ap.add_argument("--adj-check", type=int, default=4, help="instances checked against FP64 finite differences")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -405,6 +576,8 @@ def main():
     r = run_gpu(args, rank, world)
     if rank != 0:
         return
+    adj = run_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
+    adj_err, cpu_grads, cpu_el = adjoint_cpu_check(adj["case"], adj["g_gpu"], args.adj_check)
     single, _, _, kind = cpu_ticks_per_second(1, args.cpu_seconds)
     allc, n, el, _ = cpu_ticks_per_second(threads, args.cpu_seconds)
     line = {
@@ -419,6 +592,22 @@ def main():
                                    + reference_kind_note(kind)},
         "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "device_warn_flags": r["warn_flags_any"],
         "host": platform.machine(),
+        "adjoint": {
+            "metric": "adjoint grads/s", "value": adj["value"], "unit": "grads/s (60-tick air rollouts)",
+            "workload": ADJ_WORKLOAD, "rel_err_max_vs_fp64_fd": adj_err, "rel_err_instances": args.adj_check,
+            "ms_per_step": adj["ms_per_step"], "step": "forward + loss + backward captured as one CUDA graph",
+            "eager_value": adj["eager_value"], "eager_ms_per_step": adj["eager_ms_per_step"],
+            "ms_forward_with_checkpoints": adj["ms_forward_ckpt"],
+            "ms_forward_plain": adj["ms_forward_plain"], "ms_backward": adj["ms_backward"],
+            "backward_over_forward": adj["backward_over_forward"],
+            "c_abi_ms_forward_with_checkpoints": adj["kernel_ms_forward_ckpt"],
+            "c_abi_ms_backward": adj["kernel_ms_backward"],
+            "c_abi_backward_over_forward": adj["kernel_backward_over_forward"],
+            "workspace_bytes": adj["workspace_bytes"], "steps": args.steps, "warmup": args.warmup,
+            "gpu_launches_per_step": 3,
+            "cpu_baseline": {"value": cpu_grads, "unit": "grads/s", "cores": 1, "kind": "port",
+                             "sample": f"FP64 central differences of the numpy restatement, "
+                                       f"{args.adj_check} instances x 240 inputs x 2 rollouts ({cpu_el:.1f} s)"}},
     }
     print(json.dumps(line))
 

@@ -293,25 +293,29 @@ int rsg_set_ball_hit_callback(rsg_batch* batch, rsg_ball_hit_fn fn, void* user);
  * gravity; btTransformUtil::integrateTransform, btTransformUtil.h:37-80; the
  * clamps of Car::_FinishPhysicsTick, Car.cpp:165-193; ball drag and clamps,
  * Ball.cpp:117-143) for gradient-based control.  For boost inputs of exactly
- * 0 or 1 the forward equals rsg_step on an airborne car.
+ * 0 or 1 held over the rollout the forward equals rsg_step on an airborne car
+ * that touches nothing.
  *
  * All pointers are device pointers.  State: [n][24] floats per instance, Bullet
  * units: car position, velocity, angular velocity, basis rows (9), ball
  * position, ball velocity.  Controls: [ticks][n][4] = pitch, yaw, roll in
  * [-1, 1] and boost in [0, 1].  d_ckpt (may be NULL in the forward) receives
- * the state every ckpt_every ticks (1..32), [ceil(ticks / ckpt_every)][n][24];
- * the backward recomputes each segment from it.  d_grad_final is the gradient
- * of a loss with respect to the final state ([n][24]), d_grad_controls
- * receives the gradient with respect to the controls ([ticks][n][4]; an
- * input outside its range gets 0, one on its boundary passes the gradient)
- * and d_grad_state0 (may be NULL) the gradient with respect to the initial
- * state ([n][24]).  `stream` is a cudaStream_t or NULL; both calls are
- * asynchronous on it. */
+ * the state every ckpt_every (>= 1) ticks, [ceil(ticks / ckpt_every)][n][24];
+ * the backward recomputes all segments from it at once.  d_grad_final is the
+ * gradient of a loss with respect to the final state ([n][24]),
+ * d_grad_controls receives the gradient with respect to the controls
+ * ([ticks][n][4]; an input outside its range gets 0, one on its boundary
+ * passes the gradient) and d_grad_state0 (may be NULL) the gradient with
+ * respect to the initial state ([n][24]).  The backward needs a device
+ * workspace of rsg_air_backward_workspace_size bytes (152 bytes per instance
+ * and tick; RSG_ERR_ARG if smaller).  `stream` is a cudaStream_t or NULL;
+ * the calls are asynchronous on it. */
 int rsg_air_forward(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_state0,
                     const float* d_controls, float* d_final, float* d_ckpt, int ckpt_every, void* stream);
+int rsg_air_backward_workspace_size(int n, int ticks, size_t* bytes);
 int rsg_air_backward(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_controls,
                      const float* d_ckpt, int ckpt_every, const float* d_grad_final, float* d_grad_controls,
-                     float* d_grad_state0, void* stream);
+                     float* d_grad_state0, void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* Device flags of every arena after the last step ([n_arenas] words).  Bits 0-7
  * are capacity overflows (the step also returns RSG_ERR_DEVICE); bit 8 marks a

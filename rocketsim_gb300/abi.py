@@ -137,7 +137,8 @@ PROTOTYPES = {
     "rsg_set_ball_hit_callback": (i32, [vp, BALL_HIT_FN, vp]),
     "rsg_get_device_flags": (i32, [vp, P(u32)]),
     "rsg_air_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp]),
-    "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
+    "rsg_air_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
+    "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),
 }
 
 _LIB = None

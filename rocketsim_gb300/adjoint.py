@@ -5,8 +5,9 @@ under pitch/yaw/roll/boost controls, with nothing to touch (the air path of Aren
 src/Sim/Arena/Arena.cpp:689-756, for a car with no wheel, body or world contact).  The boost
 input is relaxed from {0, 1} to [0, 1] so that it has a gradient; for inputs of exactly 0 or 1
 the forward is the arena tick.  The backward runs the hand-written adjoint kernel: the forward
-stores the state every `ckpt_every` ticks and the backward recomputes each segment from its
-checkpoint, so memory is O(ticks / ckpt_every) states per instance.
+stores the state every `ckpt_every` ticks; the backward recomputes all segments from their
+checkpoints at once into a tape (152 bytes per instance and tick, from torch's allocator) and
+sweeps it in reverse.
 
 State vector, 24 floats per instance in Bullet units (1 BT = 50 uu): car position, velocity,
 angular velocity, basis rows (row r = (forward[r], right[r], up[r])), ball position, ball
@@ -31,7 +32,6 @@ from . import abi
 from .abi import BallState, CarConfig, CarState, check
 
 STATE = 24
-MAX_CKPT_EVERY = 32
 UU_TO_BT = np.float32(1.0 / 50.0)  # RLConst::UU_TO_BT, a float
 BT_TO_UU = np.float32(50.0)
 
@@ -68,8 +68,8 @@ class AirRollout(torch.autograd.Function):
         _check_tensor(controls, "controls", (ticks, n, 4))
         if state0.device != controls.device:
             raise ValueError("state0 and controls must be on the same device")
-        if not 1 <= ckpt_every <= MAX_CKPT_EVERY:
-            raise ValueError(f"ckpt_every must be in 1..{MAX_CKPT_EVERY}")
+        if ckpt_every < 1:
+            raise ValueError("ckpt_every must be >= 1")
         final = torch.empty_like(state0)
         need_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
         ckpt = None
@@ -96,10 +96,13 @@ class AirRollout(torch.autograd.Function):
         grad_final = grad_final.contiguous().to(torch.float32)
         grad_controls = torch.empty_like(controls)
         grad_state0 = torch.empty_like(grad_final) if ctx.needs_input_grad[0] else None
+        nbytes = C.c_size_t()
+        check(lib.rsg_air_backward_workspace_size(n, ticks, C.byref(nbytes)), "rsg_air_backward_workspace_size")
+        work = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, device=controls.device)
         with torch.cuda.device(controls.device):
             check(lib.rsg_air_backward(C.byref(ctx.car), ctx.tick_rate, n, ticks, _ptr(controls), _ptr(ckpt),
                                        ctx.ckpt_every, _ptr(grad_final), _ptr(grad_controls), _ptr(grad_state0),
-                                       _stream()), "rsg_air_backward")
+                                       _ptr(work), nbytes.value, _stream()), "rsg_air_backward")
         return grad_state0, (grad_controls if ctx.needs_input_grad[1] else None), None, None, None
 
 

@@ -10,16 +10,21 @@
 // operations in the same order as rsg_tick_kernel, so for boost inputs of exactly 0 or 1 it
 // reproduces the full tick of an airborne car.
 //
-// The adjoint kernel differentiates the same rollout in reverse: one thread per instance,
-// checkpoints every `ckpt_every` ticks written by the forward kernel, each segment recomputed
-// into a per-thread buffer and walked backwards.  Citations are <file>:<line> in the RocketSim
-// tree; B/ is libsrc/bullet3-3.24/.  The torque path uses
+// The adjoint runs in two launches.  The forward kernel stores the state every `ckpt_every`
+// ticks; the tape kernel recomputes every segment from its checkpoint at once (one thread per
+// instance and segment) and writes, per tick, what the reverse pass needs (the tick's
+// linearisation point) to a caller-provided workspace laid out [tick][word][instance]; the sweep
+// kernel (one thread per instance) then walks the ticks backwards through that tape, which it
+// prefetches a tick ahead.  The recompute is parallel in time and the serial chain holds only
+// the reverse tick.  Citations are <file>:<line> in the RocketSim tree; B/ is
+// libsrc/bullet3-3.24/.  The torque path uses
 // I_world_inv * inverse(I_world_inv) = identity, so the air-control torque reaches the angular
 // velocity as (torque - damping) * CAR_TORQUE_SCALE * dt.
 #include <cuda_runtime.h>
 
 #include "../../include/rocketsim_gb300.h"
 #include "rsg_consts.cuh"
+#include "rsg_kernels.h"
 #include "rsg_math.cuh"
 
 namespace rsg {
@@ -28,12 +33,20 @@ namespace air {
 #define RSG_AD RSG_HD
 
 constexpr int STATE = 24;  // per instance: car pos(3) vel(3) angvel(3) basis rows(9), ball pos(3) vel(3)
-constexpr int MAX_SEG = 32;
+constexpr int TAPE_WORDS = 38;  // per instance and tick, see put_tape
 
 struct Cfg {
     V3 iinv;   // car inverse inertia (local)
     float dt;
+    float car_damp, ball_damp;  // btRigidBody::applyDamping factors, filled on the device
 };
+
+// The damping factors are the same powf calls the arena tick makes every tick; computed once
+// per thread they give the same values.
+RSG_AD void fill_damping(Cfg& k) {
+    k.car_damp = powf(1.f - 0.f, k.dt);
+    k.ball_damp = powf(1.f - RL::BALL_DRAG, k.dt);
+}
 
 struct St {
     V3 p, v, w;
@@ -99,7 +112,7 @@ RSG_AD void car_tick(St& x, float4 u, const Cfg& k, Tape* tp) {
     // applyGravity, predictUnconstraintMotion (no car damping), solver write-back
     const float inv_mass = 1.f / RL::CAR_MASS_BT;
     total_force += V3(0, 0, RL::GRAVITY_Z * RL::UU_TO_BT) * (1.f / inv_mass);
-    V3 v = x.v * powf(1.f - 0.f, dt), w = x.w * powf(1.f - 0.f, dt);
+    V3 v = x.v * k.car_damp, w = x.w * k.car_damp;
     V3 ext_f = total_force * inv_mass * dt;
     V3 ext_t = total_torque * iw * dt;
     v = (v + V3(0, 0, 0)) + ext_f;
@@ -133,10 +146,11 @@ RSG_AD void car_tick(St& x, float4 u, const Cfg& k, Tape* tp) {
 }
 
 // One tick of the ball; returns its velocity before the speed clamp (what the adjoint needs).
-RSG_AD V3 ball_tick(St& x, float dt) {
+RSG_AD V3 ball_tick(St& x, const Cfg& k) {
+    const float dt = k.dt;
     const float mass = RL::BALL_MASS_BT, inv_mass = 1.f / mass;
     V3 force = V3(0, 0, 0) + V3(0, 0, RL::GRAVITY_Z * RL::UU_TO_BT) * (1.f / inv_mass);
-    V3 v = x.bv * powf(1.f - RL::BALL_DRAG, dt);
+    V3 v = x.bv * k.ball_damp;
     v = (v + V3(0, 0, 0)) + force * inv_mass * dt;
     x.bp = x.bp + v * dt;
     x.bv = clamp_len(v, RL::BALL_MAX_SPEED * RL::UU_TO_BT);
@@ -235,9 +249,9 @@ struct Adj {
 };
 
 // Reverse of ball_tick given the ball velocity before the clamp
-RSG_AD void ball_tick_bwd(V3 v1u, Adj& g, float dt) {
-    V3 gv1u = clamp_len_bwd(v1u, RL::BALL_MAX_SPEED * RL::UU_TO_BT, g.bv) + g.bp * dt;
-    g.bv = gv1u * powf(1.f - RL::BALL_DRAG, dt);
+RSG_AD void ball_tick_bwd(V3 v1u, Adj& g, const Cfg& k) {
+    V3 gv1u = clamp_len_bwd(v1u, RL::BALL_MAX_SPEED * RL::UU_TO_BT, g.bv) + g.bp * k.dt;
+    g.bv = gv1u * k.ball_damp;
 }
 
 // Reverse of car_tick: `g` holds the adjoint of the state after the tick and becomes the adjoint
@@ -278,8 +292,8 @@ RSG_AD float4 car_tick_bwd(const St& x0, float4 u, const Tape& t, Adj& g, const 
         }
     }
     M3 gB0 = q_from_m_bwd(x0.B, gq0);
-    // velocities before the step
-    g.v = gv1u;
+    // velocities before the step (the damping factor is exactly 1 for the car)
+    g.v = gv1u * k.car_damp;
     V3 X = gw1u * (RL::CAR_TORQUE_SCALE * dt);  // adjoint of (torque - damping)
     const M3& R = x0.B;
     V3 pr = -R.col(1), yu = R.col(2), rf = -R.col(0), f = R.col(0);
@@ -298,7 +312,7 @@ RSG_AD float4 car_tick_bwd(const St& x0, float4 u, const Tape& t, Adj& g, const 
     V3 gpr = X * (t.cp * RL::AIR_TORQUE_X) + gd * (wp * cpd) + x0.w * (gdp * cpd);
     V3 gyu = X * (t.cy * RL::AIR_TORQUE_Y) + gd * (wy * cyd) + x0.w * (gdy * cyd);
     V3 grf = X * (t.cr * RL::AIR_TORQUE_Z) + gd * (wr * crd) + x0.w * (gdr * crd);
-    g.w = gw1u + pr * (gdp * cpd) + yu * (gdy * cyd) + rf * (gdr * crd);
+    g.w = gw1u * k.car_damp + pr * (gdp * cpd) + yu * (gdy * cyd) + rf * (gdr * crd);
     V3 gc0 = gf - grf, gc1 = -gpr, gc2 = gyu;
     for (int r = 0; r < 3; r++) {
         gB0.r[r].x += gc0[r];
@@ -316,24 +330,95 @@ RSG_AD float4 car_tick_bwd(const St& x0, float4 u, const Tape& t, Adj& g, const 
     return gu;
 }
 
+// Tape of one tick of one instance, word w at tape[(t * TAPE_WORDS + w) * n + i]: the car basis
+// and angular velocity before the tick, its velocities before the clamps, the four orientation
+// quaternions of integrateTransform, the ball velocity before its clamp and the angular-clamp flag.
+struct TapeRef {
+    float* base;
+    size_t n;
+    RSG_AD float& operator[](int w) const { return base[(size_t)w * n]; }
+};
+RSG_AD void put_v3(const TapeRef& r, int w, V3 v) { r[w] = v.x; r[w + 1] = v.y; r[w + 2] = v.z; }
+RSG_AD void put_q(const TapeRef& r, int w, Q q) { r[w] = q.x; r[w + 1] = q.y; r[w + 2] = q.z; r[w + 3] = q.w; }
+RSG_AD V3 get_v3(const float* v, int w) { return V3(v[w], v[w + 1], v[w + 2]); }
+RSG_AD Q get_q(const float* v, int w) { return Q(v[w], v[w + 1], v[w + 2], v[w + 3]); }
+
+RSG_AD void put_tape(const TapeRef& r, const St& x0, const Tape& t, V3 ball_v1u) {
+    for (int a = 0; a < 3; a++) put_v3(r, 3 * a, x0.B.r[a]);
+    put_v3(r, 9, x0.w);
+    put_v3(r, 12, t.w1u);
+    put_v3(r, 15, t.v1u);
+    put_q(r, 18, t.q0);
+    put_q(r, 22, t.dq);
+    put_q(r, 26, t.qm);
+    put_q(r, 30, t.qn);
+    put_v3(r, 34, ball_v1u);
+    r[37] = t.ang_clamped ? 1.f : 0.f;
+}
+// Rebuilds the reverse pass's inputs from the tape words `v` and the tick's raw controls `u`.
+RSG_AD void get_tape(const float* v, float4 u, St& x0, Tape& t, V3& ball_v1u) {
+    for (int a = 0; a < 3; a++) x0.B.r[a] = get_v3(v, 3 * a);
+    x0.w = get_v3(v, 9);
+    t.w1u = get_v3(v, 12);
+    t.v1u = get_v3(v, 15);
+    t.q0 = get_q(v, 18);
+    t.dq = get_q(v, 22);
+    t.qm = get_q(v, 26);
+    t.qn = get_q(v, 30);
+    ball_v1u = get_v3(v, 34);
+    t.ang_clamped = v[37] != 0.f;
+    t.cp = clampf(u.x, -1, 1);
+    t.cy = clampf(u.y, -1, 1);
+    t.cr = clampf(u.z, -1, 1);
+    t.boost = clampf(u.w, 0, 1);
+}
+
 __global__ void air_forward_kernel(int n, int ticks, const float* __restrict__ state0, const float4* __restrict__ controls,
                                    float* __restrict__ final_state, float* __restrict__ ckpt, int ckpt_every, Cfg k) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    fill_damping(k);
     St x = load_state(state0 + (size_t)i * STATE);
+    float4 un = ticks > 0 ? controls[i] : make_float4(0, 0, 0, 0);
     for (int t = 0; t < ticks; t++) {
+        const float4 u = un;
+        if (t + 1 < ticks) un = controls[(size_t)(t + 1) * n + i];  // a tick ahead
         if (ckpt && t % ckpt_every == 0) store_state(ckpt + ((size_t)(t / ckpt_every) * n + i) * STATE, x);
-        car_tick(x, controls[(size_t)t * n + i], k, nullptr);
-        ball_tick(x, k.dt);
+        car_tick(x, u, k, nullptr);
+        ball_tick(x, k);
     }
     store_state(final_state + (size_t)i * STATE, x);
 }
 
-__global__ void air_backward_kernel(int n, int ticks, const float4* __restrict__ controls, const float* __restrict__ ckpt,
-                                    int ckpt_every, const float* __restrict__ grad_final, float4* __restrict__ grad_controls,
-                                    float* __restrict__ grad_state0, Cfg k) {
+// One thread per (segment, instance): recompute the segment from its checkpoint, writing the tape.
+__global__ void air_tape_kernel(int n, int ticks, const float4* __restrict__ controls, const float* __restrict__ ckpt,
+                                int ckpt_every, int nseg, float* __restrict__ tape, Cfg k) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nseg * n) return;
+    const int sgi = (int)(idx / n), i = (int)(idx % n);
+    fill_damping(k);
+    const int t0 = sgi * ckpt_every;
+    const int t1 = t0 + ckpt_every < ticks ? t0 + ckpt_every : ticks;
+    St x = load_state(ckpt + ((size_t)sgi * n + i) * STATE);
+    float4 un = controls[(size_t)t0 * n + i];
+    for (int t = t0; t < t1; t++) {
+        const float4 u = un;
+        if (t + 1 < t1) un = controls[(size_t)(t + 1) * n + i];
+        const St x0 = x;
+        Tape tp;
+        car_tick(x, u, k, &tp);
+        V3 bv = ball_tick(x, k);
+        put_tape(TapeRef{tape + (size_t)t * TAPE_WORDS * n + i, (size_t)n}, x0, tp, bv);
+    }
+}
+
+// One thread per instance: the reverse pass over all ticks, reading the tape a tick ahead.
+__global__ void air_sweep_kernel(int n, int ticks, const float4* __restrict__ controls, const float* __restrict__ tape,
+                                 const float* __restrict__ grad_final, float4* __restrict__ grad_controls,
+                                 float* __restrict__ grad_state0, Cfg k) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    fill_damping(k);
     Adj g;
     const float* gf = grad_final + (size_t)i * STATE;
     g.p = V3(gf[0], gf[1], gf[2]);
@@ -342,30 +427,36 @@ __global__ void air_backward_kernel(int n, int ticks, const float4* __restrict__
     for (int r = 0; r < 3; r++) g.B.r[r] = V3(gf[9 + 3 * r], gf[10 + 3 * r], gf[11 + 3 * r]);
     g.bp = V3(gf[18], gf[19], gf[20]);
     g.bv = V3(gf[21], gf[22], gf[23]);
-    St xs[MAX_SEG];
-    Tape tp[MAX_SEG];
-    V3 bv[MAX_SEG];
-    const int nseg = (ticks + ckpt_every - 1) / ckpt_every;
-    for (int sgi = nseg - 1; sgi >= 0; sgi--) {
-        const int t0 = sgi * ckpt_every;
-        const int t1 = t0 + ckpt_every < ticks ? t0 + ckpt_every : ticks;
-        St x = load_state(ckpt + ((size_t)sgi * n + i) * STATE);
-        for (int t = t0; t < t1; t++) {  // recompute the segment
-            xs[t - t0] = x;
-            car_tick(x, controls[(size_t)t * n + i], k, &tp[t - t0]);
-            bv[t - t0] = ball_tick(x, k.dt);
+    float nxt[TAPE_WORDS];
+    float4 un = make_float4(0, 0, 0, 0);
+    if (ticks > 0) {
+        const float* src = tape + (size_t)(ticks - 1) * TAPE_WORDS * n + i;
+#pragma unroll
+        for (int w = 0; w < TAPE_WORDS; w++) nxt[w] = src[(size_t)w * n];
+        un = controls[(size_t)(ticks - 1) * n + i];
+    }
+    for (int t = ticks - 1; t >= 0; t--) {
+        float cur[TAPE_WORDS];
+#pragma unroll
+        for (int w = 0; w < TAPE_WORDS; w++) cur[w] = nxt[w];
+        const float4 u = un;
+        if (t > 0) {  // a tick ahead
+            const float* src = tape + (size_t)(t - 1) * TAPE_WORDS * n + i;
+#pragma unroll
+            for (int w = 0; w < TAPE_WORDS; w++) nxt[w] = src[(size_t)w * n];
+            un = controls[(size_t)(t - 1) * n + i];
         }
-        for (int t = t1 - 1; t >= t0; t--) {
-            const size_t at = (size_t)t * n + i;
-            ball_tick_bwd(bv[t - t0], g, k.dt);
-            grad_controls[at] = car_tick_bwd(xs[t - t0], controls[at], tp[t - t0], g, k);
-        }
+        St x0;
+        Tape tp;
+        V3 bv;
+        get_tape(cur, u, x0, tp, bv);
+        ball_tick_bwd(bv, g, k);
+        grad_controls[(size_t)t * n + i] = car_tick_bwd(x0, u, tp, g, k);
     }
     if (grad_state0) {
-        float* o = grad_state0 + (size_t)i * STATE;
         St gs;
         gs.p = g.p; gs.v = g.v; gs.w = g.w; gs.B = g.B; gs.bp = g.bp; gs.bv = g.bv;
-        store_state(o, gs);
+        store_state(grad_state0 + (size_t)i * STATE, gs);
     }
 }
 
@@ -384,6 +475,7 @@ static Cfg make_cfg(const rsg_car_config* c, float tick_rate) {
     Cfg k;
     k.iinv = V3(1.f / inertia.x, 1.f / inertia.y, 1.f / inertia.z);
     k.dt = 1.f / tick_rate;
+    k.car_damp = k.ball_damp = 0.f;  // set by fill_damping on the device
     return k;
 }
 
@@ -392,33 +484,55 @@ static Cfg make_cfg(const rsg_car_config* c, float tick_rate) {
 
 using namespace rsg;
 
+static size_t tape_bytes(int n, int ticks) { return sizeof(float) * air::TAPE_WORDS * (size_t)n * (size_t)ticks; }
+
 extern "C" int rsg_air_forward(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_state0,
                                const float* d_controls, float* d_final, float* d_ckpt, int ckpt_every, void* stream) {
-    if (!car || n < 0 || ticks < 0 || !d_state0 || !d_controls || !d_final) return RSG_ERR_ARG;
-    if (d_ckpt && (ckpt_every < 1 || ckpt_every > air::MAX_SEG)) return RSG_ERR_ARG;
+    if (!car || n < 0 || ticks < 0 || !d_state0 || !d_controls || !d_final || !(tick_rate > 0.f))
+        return report_error(RSG_ERR_ARG, "rsg_air_forward: null pointer, negative size or tick_rate <= 0");
+    if (d_ckpt && ckpt_every < 1) return report_error(RSG_ERR_ARG, "rsg_air_forward: ckpt_every must be >= 1");
     if (n == 0) return RSG_OK;
     air::Cfg k = air::make_cfg(car, tick_rate);
-    air::air_forward_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+    air::air_forward_kernel<<<(n + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
         n, ticks, d_state0, reinterpret_cast<const float4*>(d_controls), d_final, d_ckpt, d_ckpt ? ckpt_every : 1, k);
-    return cudaGetLastError() == cudaSuccess ? RSG_OK : RSG_ERR_CUDA;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? RSG_OK : report_error(RSG_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" int rsg_air_backward_workspace_size(int n, int ticks, size_t* bytes) {
+    if (n < 0 || ticks < 0 || !bytes)
+        return report_error(RSG_ERR_ARG, "rsg_air_backward_workspace_size: negative size or null pointer");
+    *bytes = tape_bytes(n, ticks);
+    return RSG_OK;
 }
 
 extern "C" int rsg_air_backward(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_controls,
                                 const float* d_ckpt, int ckpt_every, const float* d_grad_final, float* d_grad_controls,
-                                float* d_grad_state0, void* stream) {
-    if (!car || n < 0 || ticks < 0 || !d_controls || !d_ckpt || !d_grad_final || !d_grad_controls) return RSG_ERR_ARG;
-    if (ckpt_every < 1 || ckpt_every > air::MAX_SEG) return RSG_ERR_ARG;
+                                float* d_grad_state0, void* d_workspace, size_t workspace_bytes, void* stream) {
+    if (!car || n < 0 || ticks < 0 || !d_controls || !d_ckpt || !d_grad_final || !d_grad_controls ||
+        !(tick_rate > 0.f))
+        return report_error(RSG_ERR_ARG, "rsg_air_backward: null pointer, negative size or tick_rate <= 0");
+    if (ckpt_every < 1) return report_error(RSG_ERR_ARG, "rsg_air_backward: ckpt_every must be >= 1");
     if (n == 0) return RSG_OK;
     if (ticks == 0) {  // the gradient passes straight through
         if (d_grad_state0)
             if (cudaMemcpyAsync(d_grad_state0, d_grad_final, sizeof(float) * air::STATE * (size_t)n,
                                 cudaMemcpyDeviceToDevice, (cudaStream_t)stream) != cudaSuccess)
-                return RSG_ERR_CUDA;
+                return report_error(RSG_ERR_CUDA, "rsg_air_backward: copy of the gradient failed");
         return RSG_OK;
     }
+    if (!d_workspace || workspace_bytes < tape_bytes(n, ticks))
+        return report_error(RSG_ERR_ARG, "rsg_air_backward: workspace missing or smaller than "
+                                         "rsg_air_backward_workspace_size");
     air::Cfg k = air::make_cfg(car, tick_rate);
-    air::air_backward_kernel<<<(n + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
-        n, ticks, reinterpret_cast<const float4*>(d_controls), d_ckpt, ckpt_every, d_grad_final,
+    const int nseg = (ticks + ckpt_every - 1) / ckpt_every;
+    const long long tape_threads = (long long)nseg * n;
+    float* tape = static_cast<float*>(d_workspace);
+    air::air_tape_kernel<<<(unsigned)((tape_threads + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+        n, ticks, reinterpret_cast<const float4*>(d_controls), d_ckpt, ckpt_every, nseg, tape, k);
+    air::air_sweep_kernel<<<(n + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
+        n, ticks, reinterpret_cast<const float4*>(d_controls), tape, d_grad_final,
         reinterpret_cast<float4*>(d_grad_controls), d_grad_state0, k);
-    return cudaGetLastError() == cudaSuccess ? RSG_OK : RSG_ERR_CUDA;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? RSG_OK : report_error(RSG_ERR_CUDA, cudaGetErrorString(e));
 }

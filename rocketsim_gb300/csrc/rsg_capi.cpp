@@ -32,6 +32,13 @@ int fail(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
 }
+}  // namespace
+
+namespace rsg {
+int report_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace rsg
+
+namespace {
 int cuda_fail(cudaError_t e, const char* what) {
     return fail(RSG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }

@@ -42,6 +42,9 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
 // Shared memory one arena needs in the tick kernel.
 int tick_smem_per_arena(int max_cars);
 
+// Records `msg` as the calling thread's last error (rsg_get_last_error) and returns `code`.
+int report_error(int code, const char* msg);
+
 // Gathers states of `n` (arena, slot) pairs (idx[2k], idx[2k+1]); idx == null means
 // all arenas x all slots in [arena][slot] order.  Slots beyond the arena's car count
 // are not written.  Cars/balls/pads outputs are device arrays; any may be null.

@@ -105,7 +105,7 @@ def _fd_check(torch, seed, n, ticks, ckpt_every, fast=False):
     return s, u, target, gs, iinv, loss
 
 
-@pytest.mark.parametrize("ckpt_every", [1, 7, 16, 32])
+@pytest.mark.parametrize("ckpt_every", [1, 7, 16, 60, 100])
 def test_air_control_gradient_matches_fp64_fd(torch_cuda, ckpt_every):
     _fd_check(torch_cuda, 11, 12, 60, ckpt_every)
 
@@ -144,14 +144,26 @@ def test_air_c_abi_direct_and_errors(torch_cuda):
     assert lib.rsg_air_forward(C.byref(cfg), 120.0, 5, 9, P(ds), P(du), P(fin), P(ck), 4, None) == abi.OK
     gfin = torch.ones_like(ds)
     gu = torch.empty_like(du)
-    assert lib.rsg_air_backward(C.byref(cfg), 120.0, 5, 9, P(du), P(ck), 4, P(gfin), P(gu), None, None) == abi.OK
+    nb = C.c_size_t()
+    assert lib.rsg_air_backward_workspace_size(5, 9, C.byref(nb)) == abi.OK
+    assert nb.value == 152 * 5 * 9
+    work = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    assert lib.rsg_air_backward(C.byref(cfg), 120.0, 5, 9, P(du), P(ck), 4, P(gfin), P(gu), None, P(work), nb.value,
+                                None) == abi.OK
     torch.cuda.synchronize()
-    ref = adjoint.air_rollout(ds, du, cfg, ckpt_every=4)
+    du2 = du.clone().requires_grad_(True)
+    ref = adjoint.air_rollout(ds, du2, cfg, ckpt_every=4)
     assert torch.equal(ref, fin)
+    ref.backward(gfin)
+    assert torch.equal(du2.grad, gu)
     # argument errors come back as RSG_ERR_ARG, nothing is launched
-    assert lib.rsg_air_forward(C.byref(cfg), 120.0, 5, 9, P(ds), P(du), P(fin), P(ck), 33, None) == abi.ERR_ARG
+    assert lib.rsg_air_forward(C.byref(cfg), 120.0, 5, 9, P(ds), P(du), P(fin), P(ck), 0, None) == abi.ERR_ARG
     assert lib.rsg_air_forward(C.byref(cfg), 120.0, -1, 9, P(ds), P(du), P(fin), None, 4, None) == abi.ERR_ARG
-    assert lib.rsg_air_backward(C.byref(cfg), 120.0, 5, 9, P(du), None, 4, P(gfin), P(gu), None, None) == abi.ERR_ARG
+    assert lib.rsg_air_forward(C.byref(cfg), 0.0, 5, 9, P(ds), P(du), P(fin), None, 4, None) == abi.ERR_ARG
+    assert lib.rsg_air_backward(C.byref(cfg), 120.0, 5, 9, P(du), None, 4, P(gfin), P(gu), None, P(work), nb.value,
+                                None) == abi.ERR_ARG
+    assert lib.rsg_air_backward(C.byref(cfg), 120.0, 5, 9, P(du), P(ck), 4, P(gfin), P(gu), None, P(work),
+                                nb.value - 1, None) == abi.ERR_ARG
     with pytest.raises(ValueError):
         adjoint.air_rollout(torch.from_numpy(s), torch.from_numpy(u))
     with pytest.raises(ValueError):
