@@ -317,6 +317,21 @@ int rsg_air_backward(const rsg_car_config* car, float tick_rate, int n, int tick
                      const float* d_ckpt, int ckpt_every, const float* d_grad_final, float* d_grad_controls,
                      float* d_grad_state0, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* rsg_air_backward for callers that cannot allocate device memory (a plugin
+ * whose host program owns the device memory through its own allocator, or a
+ * control loop that cannot afford the synchronisation cudaMalloc/cudaFree may
+ * cause).  No counterpart in the reference.  Same arguments and results as
+ * rsg_air_backward without the workspace: the tape lives in a 16 MiB static
+ * device array, so n * ticks must be at most 110376 (RSG_ERR_ARG with a
+ * message otherwise, nothing launched).  All calls on a device share that
+ * array: calls whose kernels overlap on the GPU race, so order them on one
+ * stream.  Nothing in it must start at zero.  The first call on each device
+ * looks up the array's address (with that device current); make it before any
+ * stream capture. */
+int rsg_air_backward_noalloc(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_controls,
+                             const float* d_ckpt, int ckpt_every, const float* d_grad_final, float* d_grad_controls,
+                             float* d_grad_state0, void* stream);
+
 /* Device flags of every arena after the last step ([n_arenas] words).  Bits 0-7
  * are capacity overflows (the step also returns RSG_ERR_DEVICE); bit 8 marks a
  * box contact deeper than GJK resolves and bit 9 overlapping car boxes, two

@@ -139,6 +139,7 @@ PROTOTYPES = {
     "rsg_air_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp]),
     "rsg_air_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
     "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),
+    "rsg_air_backward_noalloc": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
 }
 
 _LIB = None

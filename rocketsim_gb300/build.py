@@ -20,7 +20,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "librsg_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-SOURCES = ["rsg_kernels.cu", "rsg_air.cu", "rsg_capi.cpp", "rsg_mesh.cpp"]
+SOURCES = ["rsg_kernels.cu", "rsg_air.cu", "rsg_air_noalloc.cu", "rsg_capi.cpp", "rsg_mesh.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 
