@@ -58,6 +58,8 @@ struct MeshStore {
     Subtree* sub = nullptr;
     TriInfo* info = nullptr;
     uint8_t* cells = nullptr;
+    uint32_t* lg_start = nullptr;
+    QNode* lg_leaf = nullptr;
 };
 std::mutex g_mesh_mutex;
 MeshStore g_soccar;
@@ -70,6 +72,12 @@ DevMeshPtrs mesh_ptrs(const MeshStore& m) {
     p.sub = m.sub;
     p.info = m.info;
     p.cells = m.cells;
+    p.lg_start = m.lg_start;
+    p.lg_leaf = m.lg_leaf;
+    for (int k = 0; k < 3; k++) {
+        p.lg_shift[k] = m.host.lg_shift[k];
+        p.lg_n[k] = m.host.lg_n[k];
+    }
     p.ntri = m.host.ntri;
     p.nnodes = m.host.cur_node;
     p.nsub = (int)m.host.subtrees.size();
@@ -372,6 +380,8 @@ int rsg_init_from_mem(int game_mode, const uint8_t* const* mesh_files, const uin
     if ((rc = upload(m.sub, m.host.subtrees, "mesh subtrees")) != RSG_OK) return rc;
     if ((rc = upload(m.info, m.host.info, "mesh edge info")) != RSG_OK) return rc;
     if ((rc = upload(m.cells, m.host.mesh_cells, "mesh cells")) != RSG_OK) return rc;
+    if ((rc = upload(m.lg_start, m.host.lg_start, "mesh leaf grid")) != RSG_OK) return rc;
+    if ((rc = upload(m.lg_leaf, m.host.lg_leaf, "mesh leaf grid")) != RSG_OK) return rc;
     m.ready = true;
     g_soccar = std::move(m);
     return RSG_OK;

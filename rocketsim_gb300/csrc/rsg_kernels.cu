@@ -28,6 +28,12 @@ static BatchView make_view(const BatchBuffers& b) {
     v.mesh.sub = b.mesh.sub;
     v.mesh.info = b.mesh.info;
     v.mesh.cells = b.mesh.cells;
+    v.mesh.lg_start = b.mesh.lg_start;
+    v.mesh.lg_leaf = b.mesh.lg_leaf;
+    for (int k = 0; k < 3; k++) {
+        v.mesh.lg_shift[k] = b.mesh.lg_shift[k];
+        v.mesh.lg_n[k] = b.mesh.lg_n[k];
+    }
     v.mesh.ntri = b.mesh.ntri;
     v.mesh.nnodes = b.mesh.nnodes;
     v.mesh.nsub = b.mesh.nsub;
@@ -59,7 +65,7 @@ RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
 // (smem_layout), loaded from its record, advanced `ticks` ticks and stored back.  The warps of a
 // block step through the parts of a tick together (block-wide barriers between parts), which keeps
 // the instruction working set of an SM to one part of the tick at a time.
-__global__ void __launch_bounds__(256) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
+__global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
                                                        int ticks) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

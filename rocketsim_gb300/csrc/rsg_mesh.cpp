@@ -272,6 +272,40 @@ struct Builder {
 
 }  // namespace
 
+// Leaf grid over the quantized BVH space, cells of about 2.5 Bullet units per axis (a power of
+// two quanta, so a quantized coordinate's cell is a shift).
+void build_leaf_grid(HostMesh& m) {
+    for (int k = 0; k < 3; k++) {
+        float quanta = 2.5f * m.quant[k];
+        int sh = 4;
+        while (sh < 15 && (float)(1 << (sh + 1)) <= quanta * 1.41421356f) sh++;
+        m.lg_shift[k] = sh;
+        m.lg_n[k] = (65535 >> sh) + 1;
+    }
+    const size_t ncell = (size_t)m.lg_n[0] * m.lg_n[1] * m.lg_n[2];
+    std::vector<uint32_t> count(ncell + 1, 0);
+    auto each_cell = [&](const QNode& q, auto&& fn) {
+        int c0[3], c1[3];
+        for (int k = 0; k < 3; k++) { c0[k] = q.qmin[k] >> m.lg_shift[k]; c1[k] = q.qmax[k] >> m.lg_shift[k]; }
+        for (int x = c0[0]; x <= c1[0]; x++)
+            for (int y = c0[1]; y <= c1[1]; y++)
+                for (int z = c0[2]; z <= c1[2]; z++) fn(((size_t)x * m.lg_n[1] + y) * m.lg_n[2] + z);
+    };
+    for (int j = 0; j < m.cur_node; j++)
+        if (m.nodes[j].esc_or_tri >= 0) each_cell(m.nodes[j], [&](size_t c) { count[c + 1]++; });
+    for (size_t c = 0; c < ncell; c++) count[c + 1] += count[c];
+    m.lg_start = count;
+    m.lg_leaf.assign(count[ncell], QNode{});
+    std::vector<uint32_t> fill(count.begin(), count.end() - 1);
+    for (int j = 0; j < m.cur_node; j++)  // node order, so every cell's list is sorted
+        if (m.nodes[j].esc_or_tri >= 0)
+            each_cell(m.nodes[j], [&](size_t c) {
+                QNode q = m.nodes[j];
+                q.esc_or_tri = j;
+                m.lg_leaf[fill[c]++] = q;
+            });
+}
+
 bool build_mesh(const uint8_t* data, uint64_t len, HostMesh& m, std::string& err) {
     if (!data || len < 8) { err = "mesh file too short"; return false; }
     int32_t nt, nv;
@@ -326,6 +360,7 @@ bool build_mesh(const uint8_t* data, uint64_t len, HostMesh& m, std::string& err
     m.nodes.resize(m.cur_node);
     b.edge_info();
     b.cells();
+    build_leaf_grid(m);
     return true;
 }
 

@@ -47,6 +47,12 @@ struct HostMesh {
     std::vector<Subtree> subtrees;
     std::vector<TriInfo> info;
     std::vector<uint8_t> mesh_cells;  // broadphase cells where the mesh proxy is registered
+    // Leaf grid: a uniform grid over the BVH's quantized space (cell = quantized coordinate >>
+    // lg_shift per axis) listing, per cell and in node order, the leaf nodes whose quantized box
+    // touches the cell.  A query box's leaves are then found without walking the tree.
+    int lg_shift[3] = {0, 0, 0}, lg_n[3] = {0, 0, 0};
+    std::vector<uint32_t> lg_start;  // ncells + 1 offsets into lg_leaf
+    std::vector<QNode> lg_leaf;      // copies of the leaf nodes with esc_or_tri = the node's index
 };
 
 // Parses one .cmf file (src/CollisionMeshFile/CollisionMeshFile.cpp:11-61) and

@@ -39,9 +39,21 @@ __device__ unsigned long long g_phase_cycles[16];
             rsg_t_last_ = t_;                                                          \
         }                                                                              \
     } while (0)
+// Block-level sub-steps, timed on thread 0 after each barrier, weighted by the block's arenas.
+#define RSG_SUB_BEGIN long long rsg_s_last_ = clock64()
+#define RSG_SUB(i)                                                                                  \
+    do {                                                                                            \
+        if (tid == 0) {                                                                             \
+            long long t_ = clock64();                                                               \
+            atomicAdd(&g_phase_cycles[i], (unsigned long long)((t_ - rsg_s_last_) * B.nact));       \
+            rsg_s_last_ = t_;                                                                       \
+        }                                                                                           \
+    } while (0)
 #else
 #define RSG_PHASE_BEGIN
 #define RSG_PHASE(i)
+#define RSG_SUB_BEGIN
+#define RSG_SUB(i)
 #endif
 __constant__ float c_pad_locs[NUM_PADS][3] = RSG_PAD_LOCS_INIT;
 __constant__ float c_respawn_locs[4][2] = {{-2304, -4608}, {-2688, -4608}, {2304, -4608}, {2688, -4608}};
@@ -52,9 +64,13 @@ struct DevMesh {
     const Subtree* sub;
     const TriInfo* info;
     const uint8_t* cells;
+    const uint32_t* lg_start;  // leaf grid (see HostMesh): per-cell offsets into lg_leaf
+    const QNode* lg_leaf;
+    int lg_shift[3], lg_n[3];
     int ntri, nnodes, nsub;
     V3 bvh_min, bvh_max, quant, aabb_min, aabb_max;
 };
+static_assert(sizeof(QNode) == 16, "leaf grid records are read as uint4");
 struct DevGrid {
     V3 mn;
     float cell;
@@ -356,42 +372,117 @@ RSG_D void mesh_query_aabb(const DevMesh& m, V3 mn, V3 mx, F&& f) {
     }
 }
 
-// walkStacklessQuantizedTreeAgainstRay (btQuantizedBvh.cpp:436-548)
+// walkStacklessQuantizedTreeAgainstRay (btQuantizedBvh.cpp:436-548).  A node is entered when its
+// quantized box overlaps the ray's and the ray meets its unquantized box (btRayAabb2); the
+// triangles reported are the leaves that pass both tests, in node order.  The leaf grid gives that
+// same set without the walk: a leaf that passes overlaps the ray's quantized box, so it is listed
+// in one of the cells that box touches (it is taken from the first such cell only), and its
+// ancestors pass whenever it does (their boxes contain its box).  The accepted leaves are sorted
+// back into node order; more than RAY_GRID_MAX of them falls back to the walk.
+struct RaySlab {
+    V3 src, inv;
+    float lambda_max;
+    unsigned sg0, sg1, sg2;
+    uint16_t qa[3], qb[3];
+};
+RSG_D void ray_slab_setup(const DevMesh& m, V3 src, V3 dst, RaySlab& r) {
+    V3 dir = safe_normalized(dst - src);
+    r.src = src;
+    r.lambda_max = dot(dir, dst - src);
+    r.inv = V3(dir.x == 0.f ? BT_LARGE : 1.f / dir.x, dir.y == 0.f ? BT_LARGE : 1.f / dir.y,
+               dir.z == 0.f ? BT_LARGE : 1.f / dir.z);
+    r.sg0 = r.inv.x < 0.f;
+    r.sg1 = r.inv.y < 0.f;
+    r.sg2 = r.inv.z < 0.f;
+    quantize_clamp(m, r.qa, vmin(src, dst), false);
+    quantize_clamp(m, r.qb, vmax(src, dst), true);
+}
+RSG_D bool ray_node_test(const DevMesh& m, const RaySlab& r, const uint16_t* nmin, const uint16_t* nmax) {
+    if (!qov(r.qa, r.qb, nmin, nmax)) return false;
+    V3 b0 = unquantize(m, nmin), b1 = unquantize(m, nmax);
+    const V3 src = r.src, inv = r.inv;
+    float tmin = ((r.sg0 ? b1 : b0).x - src.x) * inv.x;
+    float tmax = ((r.sg0 ? b0 : b1).x - src.x) * inv.x;
+    float tymin = ((r.sg1 ? b1 : b0).y - src.y) * inv.y;
+    float tymax = ((r.sg1 ? b0 : b1).y - src.y) * inv.y;
+    if ((tmin > tymax) || (tymin > tmax)) return false;
+    if (tymin > tmin) tmin = tymin;
+    if (tymax < tmax) tmax = tymax;
+    float tzmin = ((r.sg2 ? b1 : b0).z - src.z) * inv.z;
+    float tzmax = ((r.sg2 ? b0 : b1).z - src.z) * inv.z;
+    if ((tmin > tzmax) || (tzmin > tmax)) return false;
+    if (tzmin > tmin) tmin = tzmin;
+    if (tzmax < tmax) tmax = tzmax;
+    return (tmin < r.lambda_max) && (tmax > 0.f);
+}
+constexpr int RAY_GRID_MAX = 16;
+// The leaves a ray reports, from the leaf grid, in node order: their count, or -1 when there are
+// more than RAY_GRID_MAX (the caller then walks the tree).
+RSG_DN int ray_grid_leaves(const DevMesh& m, const RaySlab& r, int* node) {
+    int c0[3], c1[3];
+    for (int k = 0; k < 3; k++) {
+        c0[k] = r.qa[k] >> m.lg_shift[k];
+        c1[k] = r.qb[k] >> m.lg_shift[k];
+    }
+    int n = 0;
+    const uint4* recs = reinterpret_cast<const uint4*>(m.lg_leaf);
+    for (int x = c0[0]; x <= c1[0]; x++)
+        for (int y = c0[1]; y <= c1[1]; y++)
+            for (int z = c0[2]; z <= c1[2]; z++) {
+                const uint32_t cell = ((uint32_t)x * m.lg_n[1] + y) * m.lg_n[2] + z;
+                const uint32_t beg = __ldg(m.lg_start + cell), end = __ldg(m.lg_start + cell + 1);
+                for (uint32_t e0 = beg; e0 < end; e0 += 4) {
+                    uint4 rec[4];  // four leaf boxes in flight at once
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        if (e0 + i < end) rec[i] = __ldg(recs + e0 + i);
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        if (e0 + i >= end) continue;
+                        uint16_t nmin[3], nmax[3];
+                        nmin[0] = rec[i].x & 0xffff; nmin[1] = rec[i].x >> 16; nmin[2] = rec[i].y & 0xffff;
+                        nmax[0] = rec[i].y >> 16; nmax[1] = rec[i].z & 0xffff; nmax[2] = rec[i].z >> 16;
+                        const int j = (int)rec[i].w;
+                        // the leaf's first cell inside the ray's cell range
+                        int fx = nmin[0] >> m.lg_shift[0], fy = nmin[1] >> m.lg_shift[1];
+                        int fz = nmin[2] >> m.lg_shift[2];
+                        if ((fx > c0[0] ? fx : c0[0]) != x || (fy > c0[1] ? fy : c0[1]) != y ||
+                            (fz > c0[2] ? fz : c0[2]) != z)
+                            continue;
+                        if (!ray_node_test(m, r, nmin, nmax)) continue;
+                        if (n == RAY_GRID_MAX) return -1;
+                        int p = n++;  // insertion in node order
+                        while (p > 0 && node[p - 1] > j) { node[p] = node[p - 1]; p--; }
+                        node[p] = j;
+                    }
+                }
+            }
+    return n;
+}
 template <class F>
 RSG_D void mesh_query_ray(const DevMesh& m, V3 src, V3 dst, F&& f) {
-    V3 dir = safe_normalized(dst - src);
-    float lambda_max = dot(dir, dst - src);
-    V3 inv(dir.x == 0.f ? BT_LARGE : 1.f / dir.x, dir.y == 0.f ? BT_LARGE : 1.f / dir.y,
-           dir.z == 0.f ? BT_LARGE : 1.f / dir.z);
-    unsigned sg0 = inv.x < 0.f, sg1 = inv.y < 0.f, sg2 = inv.z < 0.f;
-    uint16_t qa[3], qb[3];
-    quantize_clamp(m, qa, vmin(src, dst), false);
-    quantize_clamp(m, qb, vmax(src, dst), true);
+    RaySlab r;
+    ray_slab_setup(m, src, dst, r);
+    if (m.lg_start) {
+        int node[RAY_GRID_MAX];
+        const int n = ray_grid_leaves(m, r, node);
+        if (n >= 0) {
+            for (int i = 0; i < n; i++) {
+                uint16_t nmin[3], nmax[3];
+                int tri;
+                node_load(m, node[i], nmin, nmax, tri);
+                f(tri);
+            }
+            return;
+        }
+    }
     int cur = 0;
     while (cur < m.nnodes) {
         uint16_t nmin[3], nmax[3];
         int esc;
         node_load(m, cur, nmin, nmax, esc);
-        bool rayov = false;
         bool leaf = esc >= 0;
-        if (qov(qa, qb, nmin, nmax)) {
-            V3 b0 = unquantize(m, nmin), b1 = unquantize(m, nmax);
-            float tmin = ((sg0 ? b1 : b0).x - src.x) * inv.x;
-            float tmax = ((sg0 ? b0 : b1).x - src.x) * inv.x;
-            float tymin = ((sg1 ? b1 : b0).y - src.y) * inv.y;
-            float tymax = ((sg1 ? b0 : b1).y - src.y) * inv.y;
-            if (!((tmin > tymax) || (tymin > tmax))) {
-                if (tymin > tmin) tmin = tymin;
-                if (tymax < tmax) tmax = tymax;
-                float tzmin = ((sg2 ? b1 : b0).z - src.z) * inv.z;
-                float tzmax = ((sg2 ? b0 : b1).z - src.z) * inv.z;
-                if (!((tmin > tzmax) || (tzmin > tmax))) {
-                    if (tzmin > tmin) tmin = tzmin;
-                    if (tzmax < tmax) tmax = tzmax;
-                    rayov = (tmin < lambda_max) && (tmax > 0.f);
-                }
-            }
-        }
+        bool rayov = ray_node_test(m, r, nmin, nmax);
         if (leaf && rayov) f(esc);
         if (rayov || leaf) cur++;
         else cur += -esc;
@@ -3383,6 +3474,7 @@ struct BlockArenas {
 // another car (its friction reads that car's velocity after that car's pre-tick).
 RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, int nthreads) {
     const int MC = bv.MC;
+    RSG_SUB_BEGIN;
     for (int w = tid; w < B.nact; w += nthreads) {
         Ctx& a = B(w);
         Body& ball = a.ball;
@@ -3398,6 +3490,7 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
         a.on_car = 0;
     }
     __syncthreads();
+    RSG_SUB(8);
     for (int u = tid; u < B.nact * MC; u += nthreads) {
         Ctx& a = B(u / MC);
         int k = u % MC;
@@ -3410,6 +3503,7 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
         }
     }
     __syncthreads();
+    RSG_SUB(9);
     for (int u = tid; u < B.nact * MC * 4; u += nthreads) {
         Ctx& a = B(u / (MC * 4));
         int r = u % (MC * 4), k = r >> 2, wh = r & 3;
@@ -3418,6 +3512,7 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
         if (a.cars[k].w[wh].ground >= OBJ_CAR0) a.on_car = 1;
     }
     __syncthreads();
+    RSG_SUB(10);
     for (int u = tid; u < B.nact * MC; u += nthreads) {
         Ctx& a = B(u / MC);
         int k = u % MC;
@@ -3439,6 +3534,7 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
             p.cur_locked = -1;
         }
     __syncthreads();
+    RSG_SUB(11);
 }
 
 // Body integration and activation (btDiscreteDynamicsWorld.cpp:516-551, 889-991) of one body.
@@ -3507,7 +3603,32 @@ RSG_D bool pad_touches(Ctx& a, const Pad& p, int pi, int ci) {
 // touches, the last one wins; then each pad in order gives boost to its car) is done per pad
 // and per car, which gives the same result because a pad's outcome depends only on the cars and
 // a car's boost only on its pads taken in pad order.
+// Tick end of one arena: Ball::_FinishPhysicsTick, the goal event, the tick counters.
+RSG_D void arena_post(const BatchView& bv, Ctx& a) {
+    Body& ball = a.ball;
+    {  // Ball::_FinishPhysicsTick (src/Sim/Ball/Ball.cpp:117-143)
+        if (!is_zero(a.ball_cache)) {
+            ball.lin_vel += a.ball_cache;
+            a.ball_cache = V3(0, 0, 0);
+        }
+        V3 v = ball.lin_vel, wv = ball.ang_vel;
+        const float ms = RL::BALL_MAX_SPEED * RL::UU_TO_BT;
+        if (len2(v) > ms * ms) v = normalized(v) * ms;
+        if (len2(wv) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) wv = normalized(wv) * RL::BALL_MAX_ANG_SPEED;
+        ball.lin_vel = v;
+        ball.ang_vel = wv;
+        a.ball_ticks++;
+    }
+    if (bv.has_arena && ball_scored(a)) {
+        uint32_t team = (-(a.ball.xf.o.y) < 0) ? 0u : 1u;  // RS_TEAM_FROM_Y(-y)
+        push_event(a, RSG_EVENT_GOAL, team, 0, 0);
+    }
+    a.tick++;
+    a.stepped = true;
+}
+
 RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, int nthreads) {
+    RSG_SUB_BEGIN;
     const int MC = bv.MC, NB = MC + 1;
     for (int u = tid; u < B.nact * NB; u += nthreads) {
         Ctx& a = B(u / NB);
@@ -3516,6 +3637,7 @@ RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, 
         body_post(a.body(OBJ_BALL + d), bv.dt);
     }
     __syncthreads();
+    RSG_SUB(12);
     for (int u = tid; u < B.nact * MC; u += nthreads) {
         Ctx& a = B(u / MC);
         int k = u % MC;
@@ -3524,6 +3646,7 @@ RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, 
         car_finish_physics(a.cars[k]);
     }
     __syncthreads();
+    RSG_SUB(13);
     if (bv.has_arena) {
         for (int u = tid; u < B.nact * NUM_PADS; u += nthreads) {  // which car each pad is locked to
             Ctx& a = B(u / NUM_PADS);
@@ -3561,30 +3684,9 @@ RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, 
             p.prev_locked = locked;
         }
     }
-    for (int w = tid; w < B.nact; w += nthreads) {
-        Ctx& a = B(w);
-        Body& ball = a.ball;
-        {  // Ball::_FinishPhysicsTick (src/Sim/Ball/Ball.cpp:117-143)
-            if (!is_zero(a.ball_cache)) {
-                ball.lin_vel += a.ball_cache;
-                a.ball_cache = V3(0, 0, 0);
-            }
-            V3 v = ball.lin_vel, wv = ball.ang_vel;
-            const float ms = RL::BALL_MAX_SPEED * RL::UU_TO_BT;
-            if (len2(v) > ms * ms) v = normalized(v) * ms;
-            if (len2(wv) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) wv = normalized(wv) * RL::BALL_MAX_ANG_SPEED;
-            ball.lin_vel = v;
-            ball.ang_vel = wv;
-            a.ball_ticks++;
-        }
-        if (bv.has_arena && ball_scored(a)) {
-            uint32_t team = (-(a.ball.xf.o.y) < 0) ? 0u : 1u;  // RS_TEAM_FROM_Y(-y)
-            push_event(a, RSG_EVENT_GOAL, team, 0, 0);
-        }
-        a.tick++;
-        a.stepped = true;
-    }
+    for (int w = tid; w < B.nact; w += nthreads) arena_post(bv, B(w));
     __syncthreads();
+    RSG_SUB(14);
 }
 
 // ---------------------------------------------------------------- record load / store
