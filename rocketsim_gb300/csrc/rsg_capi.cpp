@@ -58,8 +58,9 @@ struct MeshStore {
     Subtree* sub = nullptr;
     TriInfo* info = nullptr;
     uint8_t* cells = nullptr;
-    uint32_t* lg_start = nullptr;
-    QNode* lg_leaf = nullptr;
+    QNode* lg_block = nullptr;
+    QNode* lg_over = nullptr;
+    QNode* sub_grp = nullptr;
 };
 std::mutex g_mesh_mutex;
 MeshStore g_soccar;
@@ -72,8 +73,10 @@ DevMeshPtrs mesh_ptrs(const MeshStore& m) {
     p.sub = m.sub;
     p.info = m.info;
     p.cells = m.cells;
-    p.lg_start = m.lg_start;
-    p.lg_leaf = m.lg_leaf;
+    p.lg_block = m.host.lg_block.empty() ? nullptr : m.lg_block;
+    p.lg_over = m.lg_over;
+    p.sub_grp = m.sub_grp;
+    p.nsub_grp = (int)m.host.sub_groups.size();
     for (int k = 0; k < 3; k++) {
         p.lg_shift[k] = m.host.lg_shift[k];
         p.lg_n[k] = m.host.lg_n[k];
@@ -380,8 +383,9 @@ int rsg_init_from_mem(int game_mode, const uint8_t* const* mesh_files, const uin
     if ((rc = upload(m.sub, m.host.subtrees, "mesh subtrees")) != RSG_OK) return rc;
     if ((rc = upload(m.info, m.host.info, "mesh edge info")) != RSG_OK) return rc;
     if ((rc = upload(m.cells, m.host.mesh_cells, "mesh cells")) != RSG_OK) return rc;
-    if ((rc = upload(m.lg_start, m.host.lg_start, "mesh leaf grid")) != RSG_OK) return rc;
-    if ((rc = upload(m.lg_leaf, m.host.lg_leaf, "mesh leaf grid")) != RSG_OK) return rc;
+    if ((rc = upload(m.lg_block, m.host.lg_block, "mesh leaf grid")) != RSG_OK) return rc;
+    if ((rc = upload(m.lg_over, m.host.lg_over, "mesh leaf grid")) != RSG_OK) return rc;
+    if ((rc = upload(m.sub_grp, m.host.sub_groups, "mesh subtree groups")) != RSG_OK) return rc;
     m.ready = true;
     g_soccar = std::move(m);
     return RSG_OK;

@@ -28,8 +28,10 @@ static BatchView make_view(const BatchBuffers& b) {
     v.mesh.sub = b.mesh.sub;
     v.mesh.info = b.mesh.info;
     v.mesh.cells = b.mesh.cells;
-    v.mesh.lg_start = b.mesh.lg_start;
-    v.mesh.lg_leaf = b.mesh.lg_leaf;
+    v.mesh.lg_block = b.mesh.lg_block;
+    v.mesh.lg_over = b.mesh.lg_over;
+    v.mesh.sub_grp = b.mesh.sub_grp;
+    v.mesh.nsub_grp = b.mesh.nsub_grp;
     for (int k = 0; k < 3; k++) {
         v.mesh.lg_shift[k] = b.mesh.lg_shift[k];
         v.mesh.lg_n[k] = b.mesh.lg_n[k];
@@ -66,15 +68,28 @@ RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
 // block step through the parts of a tick together (block-wide barriers between parts), which keeps
 // the instruction working set of an SM to one part of the tick at a time.
 __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
-                                                       int ticks) {
+                                                          int ticks, int hdr_cache) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ar = blockIdx.x * (blockDim.x >> 5) + warp;
     const bool active = ar < bv.A;  // warp-uniform; idle warps still take part in the barriers
     const SmemLayout L = smem_layout(bv.MC);
     Ctx& a = bind_ctx(smem + (size_t)warp * L.bytes, L, lane);
+    // the BVH subtree headers, read by every narrow-phase query, copied once into the block's
+    // shared memory behind the arenas when they fit
+    const Subtree* sub = bv.mesh.sub;
+    if (hdr_cache) {
+        uint32_t* dst = reinterpret_cast<uint32_t*>(smem + (size_t)(blockDim.x >> 5) * L.bytes);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(bv.mesh.sub);
+        for (int i = threadIdx.x; i < bv.mesh.nsub * 5; i += blockDim.x) dst[i] = __ldg(src + i);
+        sub = reinterpret_cast<const Subtree*>(dst);
+        __syncthreads();
+    }
     if (active) {
-        if (lane == 0) load_arena(bv, ar, a);
+        if (lane == 0) {
+            load_arena(bv, ar, a);
+            a.sub = sub;
+        }
         __syncwarp();
         if (lane < a.ncars) load_car(bv, ar, a, lane);
         load_pads(bv, ar, a, lane);
@@ -120,11 +135,18 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
     // the block must fit in shared memory
     while (warps_per_block > 1 && smem_layout(b.MC).bytes * warps_per_block > 227 * 1024) warps_per_block--;
     const int per_arena = smem_layout(b.MC).bytes;
-    const int smem = per_arena * warps_per_block;
+    int smem = per_arena * warps_per_block;
+    // the header copy is made only when it costs no block per SM (228 KB of shared memory per SM,
+    // 1 KB of it reserved per block)
+    const int hdr_bytes = b.mesh.sub ? b.mesh.nsub * (int)sizeof(Subtree) : 0;
+    const int sm_smem = 228 * 1024;
+    const int blocks_without = sm_smem / (smem + 1024), blocks_with = sm_smem / (smem + hdr_bytes + 1024);
+    const int hdr_cache = (hdr_bytes > 0 && smem + hdr_bytes <= 227 * 1024 && blocks_with >= blocks_without) ? 1 : 0;
+    if (hdr_cache) smem += hdr_bytes;
     cudaError_t e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     int grid = (b.A + warps_per_block - 1) / warps_per_block;
-    rsg_tick_kernel<<<grid, 32 * warps_per_block, smem, st>>>(make_view(b), controls, ticks);
+    rsg_tick_kernel<<<grid, 32 * warps_per_block, smem, st>>>(make_view(b), controls, ticks, hdr_cache);
     return cudaGetLastError();
 }
 
@@ -527,10 +549,10 @@ cudaError_t launch_demolish(const BatchBuffers& b, uint32_t arena, uint32_t slot
 
 #if defined(RSG_PHASE_TIMERS)
 extern "C" int rsg_phase_read(unsigned long long* out) {
-    return (int)cudaMemcpyFromSymbol(out, rsg::g_phase_cycles, sizeof(unsigned long long) * 16);
+    return (int)cudaMemcpyFromSymbol(out, rsg::g_phase_cycles, sizeof(unsigned long long) * 64);
 }
 extern "C" int rsg_phase_reset() {
-    unsigned long long z[16] = {0};
+    unsigned long long z[64] = {0};
     return (int)cudaMemcpyToSymbol(rsg::g_phase_cycles, z, sizeof(z));
 }
 #endif

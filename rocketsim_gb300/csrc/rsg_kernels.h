@@ -15,8 +15,10 @@ struct DevMeshPtrs {
     const Subtree* sub;
     const TriInfo* info;
     const uint8_t* cells;
-    const uint32_t* lg_start;
-    const QNode* lg_leaf;
+    const QNode* lg_block;
+    const QNode* lg_over;
+    const QNode* sub_grp;
+    int nsub_grp;
     int lg_shift[3], lg_n[3];
     int ntri, nnodes, nsub;
     V3 bvh_min, bvh_max, quant, aabb_min, aabb_max;

@@ -272,38 +272,47 @@ struct Builder {
 
 }  // namespace
 
-// Leaf grid over the quantized BVH space, cells of about 2.5 Bullet units per axis (a power of
-// two quanta, so a quantized coordinate's cell is a shift).
+// Leaf grid over the quantized BVH space, cells of about RSG_LEAF_GRID_CELL Bullet units per axis
+// (a power of two quanta, so a quantized coordinate's cell is a shift).
+#ifndef RSG_LEAF_GRID_CELL
+#define RSG_LEAF_GRID_CELL 2.5f
+#endif
 void build_leaf_grid(HostMesh& m) {
+    m.lg_block.clear();
+    m.lg_over.clear();
+    if (m.ntri > 65535) return;
     for (int k = 0; k < 3; k++) {
-        float quanta = 2.5f * m.quant[k];
+        float quanta = RSG_LEAF_GRID_CELL * m.quant[k];
         int sh = 4;
         while (sh < 15 && (float)(1 << (sh + 1)) <= quanta * 1.41421356f) sh++;
         m.lg_shift[k] = sh;
         m.lg_n[k] = (65535 >> sh) + 1;
     }
     const size_t ncell = (size_t)m.lg_n[0] * m.lg_n[1] * m.lg_n[2];
-    std::vector<uint32_t> count(ncell + 1, 0);
-    auto each_cell = [&](const QNode& q, auto&& fn) {
+    std::vector<std::vector<QNode>> cells(ncell);
+    int rank = 0;
+    for (int j = 0; j < m.cur_node; j++) {  // node order, so every cell's list is sorted
+        if (m.nodes[j].esc_or_tri < 0) continue;
+        QNode q = m.nodes[j];
+        q.esc_or_tri = (int32_t)(((uint32_t)rank << 16) | (uint32_t)m.nodes[j].esc_or_tri);
+        rank++;
         int c0[3], c1[3];
         for (int k = 0; k < 3; k++) { c0[k] = q.qmin[k] >> m.lg_shift[k]; c1[k] = q.qmax[k] >> m.lg_shift[k]; }
         for (int x = c0[0]; x <= c1[0]; x++)
             for (int y = c0[1]; y <= c1[1]; y++)
-                for (int z = c0[2]; z <= c1[2]; z++) fn(((size_t)x * m.lg_n[1] + y) * m.lg_n[2] + z);
-    };
-    for (int j = 0; j < m.cur_node; j++)
-        if (m.nodes[j].esc_or_tri >= 0) each_cell(m.nodes[j], [&](size_t c) { count[c + 1]++; });
-    for (size_t c = 0; c < ncell; c++) count[c + 1] += count[c];
-    m.lg_start = count;
-    m.lg_leaf.assign(count[ncell], QNode{});
-    std::vector<uint32_t> fill(count.begin(), count.end() - 1);
-    for (int j = 0; j < m.cur_node; j++)  // node order, so every cell's list is sorted
-        if (m.nodes[j].esc_or_tri >= 0)
-            each_cell(m.nodes[j], [&](size_t c) {
-                QNode q = m.nodes[j];
-                q.esc_or_tri = j;
-                m.lg_leaf[fill[c]++] = q;
-            });
+                for (int z = c0[2]; z <= c1[2]; z++) cells[((size_t)x * m.lg_n[1] + y) * m.lg_n[2] + z].push_back(q);
+    }
+    m.lg_block.assign(ncell * 4, QNode{});
+    for (size_t c = 0; c < ncell; c++) {
+        const std::vector<QNode>& v = cells[c];
+        QNode& hdr = m.lg_block[c * 4];
+        uint32_t words[4] = {(uint32_t)v.size(), (uint32_t)m.lg_over.size(), 0, 0};
+        std::memcpy(&hdr, words, sizeof(words));
+        for (size_t i = 0; i < v.size(); i++) {
+            if (i < 3) m.lg_block[c * 4 + 1 + i] = v[i];
+            else m.lg_over.push_back(v[i]);
+        }
+    }
 }
 
 bool build_mesh(const uint8_t* data, uint64_t len, HostMesh& m, std::string& err) {
@@ -361,6 +370,18 @@ bool build_mesh(const uint8_t* data, uint64_t len, HostMesh& m, std::string& err
     b.edge_info();
     b.cells();
     build_leaf_grid(m);
+    m.sub_groups.clear();
+    for (size_t g = 0; g < m.subtrees.size(); g += 32) {
+        QNode q{};
+        for (int k = 0; k < 3; k++) { q.qmin[k] = 0xffff; q.qmax[k] = 0; }
+        for (size_t h = g; h < m.subtrees.size() && h < g + 32; h++)
+            for (int k = 0; k < 3; k++) {
+                q.qmin[k] = std::min(q.qmin[k], m.subtrees[h].qmin[k]);
+                q.qmax[k] = std::max(q.qmax[k], m.subtrees[h].qmax[k]);
+            }
+        q.esc_or_tri = (int32_t)g;
+        m.sub_groups.push_back(q);
+    }
     return true;
 }
 

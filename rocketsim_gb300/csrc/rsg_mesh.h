@@ -45,14 +45,19 @@ struct HostMesh {
     std::vector<QNode> nodes;
     int cur_node = 0;
     std::vector<Subtree> subtrees;
+    std::vector<QNode> sub_groups;  // quantized box around each run of 32 subtree headers
     std::vector<TriInfo> info;
     std::vector<uint8_t> mesh_cells;  // broadphase cells where the mesh proxy is registered
     // Leaf grid: a uniform grid over the BVH's quantized space (cell = quantized coordinate >>
     // lg_shift per axis) listing, per cell and in node order, the leaf nodes whose quantized box
     // touches the cell.  A query box's leaves are then found without walking the tree.
+    // Each cell is a 64-byte block: a header (leaf count, offset of the leaves past the first three
+    // in lg_over) and the first three leaf records.  A record is the leaf's quantized box with
+    // esc_or_tri = (the leaf's rank in node order << 16) | its triangle index.  Empty when the mesh
+    // has more than 65535 triangles (queries then walk the tree).
     int lg_shift[3] = {0, 0, 0}, lg_n[3] = {0, 0, 0};
-    std::vector<uint32_t> lg_start;  // ncells + 1 offsets into lg_leaf
-    std::vector<QNode> lg_leaf;      // copies of the leaf nodes with esc_or_tri = the node's index
+    std::vector<QNode> lg_block;  // 4 QNode-sized slots per cell: header, three records
+    std::vector<QNode> lg_over;   // the remaining records of every cell, cell by cell
 };
 
 // Parses one .cmf file (src/CollisionMeshFile/CollisionMeshFile.cpp:11-61) and

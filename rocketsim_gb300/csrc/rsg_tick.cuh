@@ -29,7 +29,7 @@ __constant__ Curve c_curves[CV_COUNT] = RSG_CURVES_INIT;
 
 // Optional per-phase cycle counters of lane 0 (compiled in only with -DRSG_PHASE_TIMERS).
 #if defined(RSG_PHASE_TIMERS)
-__device__ unsigned long long g_phase_cycles[16];
+__device__ unsigned long long g_phase_cycles[64];
 #define RSG_PHASE_BEGIN long long rsg_t_last_ = clock64()
 #define RSG_PHASE(i)                                                                   \
     do {                                                                               \
@@ -38,6 +38,14 @@ __device__ unsigned long long g_phase_cycles[16];
             atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - rsg_t_last_));     \
             rsg_t_last_ = t_;                                                          \
         }                                                                              \
+    } while (0)
+// Sub-steps of lane-0-only code.
+#define RSG_L0_BEGIN long long rsg_l_last_ = clock64()
+#define RSG_L0(i)                                                                                   \
+    do {                                                                                            \
+        long long t_ = clock64();                                                                   \
+        atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - rsg_l_last_));                      \
+        rsg_l_last_ = t_;                                                                           \
     } while (0)
 // Block-level sub-steps, timed on thread 0 after each barrier, weighted by the block's arenas.
 #define RSG_SUB_BEGIN long long rsg_s_last_ = clock64()
@@ -54,6 +62,8 @@ __device__ unsigned long long g_phase_cycles[16];
 #define RSG_PHASE(i)
 #define RSG_SUB_BEGIN
 #define RSG_SUB(i)
+#define RSG_L0_BEGIN
+#define RSG_L0(i)
 #endif
 __constant__ float c_pad_locs[NUM_PADS][3] = RSG_PAD_LOCS_INIT;
 __constant__ float c_respawn_locs[4][2] = {{-2304, -4608}, {-2688, -4608}, {2304, -4608}, {2688, -4608}};
@@ -64,13 +74,16 @@ struct DevMesh {
     const Subtree* sub;
     const TriInfo* info;
     const uint8_t* cells;
-    const uint32_t* lg_start;  // leaf grid (see HostMesh): per-cell offsets into lg_leaf
-    const QNode* lg_leaf;
+    const QNode* lg_block;  // leaf grid (see HostMesh): 64-byte cell blocks
+    const QNode* lg_over;
+    const QNode* sub_grp;  // box of each run of 32 subtree headers
+    int nsub_grp;
     int lg_shift[3], lg_n[3];
     int ntri, nnodes, nsub;
     V3 bvh_min, bvh_max, quant, aabb_min, aabb_max;
 };
 static_assert(sizeof(QNode) == 16, "leaf grid records are read as uint4");
+static_assert(sizeof(Subtree) == 20, "subtree headers are read as five words");
 struct DevGrid {
     V3 mn;
     float cell;
@@ -225,6 +238,7 @@ struct Ctx {
     int nevents;
     float solver_dt;
     int serial;  // the pre-tick of this tick runs car by car in update order
+    const Subtree* sub;  // BVH subtree headers (the block's shared-memory copy when there is one)
     int on_car;  // a wheel rests on another car: the car logic after the rays runs in update order
     // scratch of one world step
     int npairs, cap_pairs;
@@ -306,6 +320,12 @@ RSG_D void node_load(const DevMesh& m, int i, uint16_t qmin[3], uint16_t qmax[3]
     esc = n.esc_or_tri;
 #endif
 }
+RSG_D void node_load_ptr(const QNode* base, int i, uint16_t qmin[3], uint16_t qmax[3], int& w) {
+    const uint4 raw = __ldg(reinterpret_cast<const uint4*>(base) + i);
+    qmin[0] = raw.x & 0xffff; qmin[1] = raw.x >> 16; qmin[2] = raw.y & 0xffff;
+    qmax[0] = raw.y >> 16; qmax[1] = raw.z & 0xffff; qmax[2] = raw.z >> 16;
+    w = (int)raw.w;
+}
 RSG_D void quantize(const DevMesh& m, uint16_t* out, V3 p, bool is_max) {
     V3 v = (p - m.bvh_min) * m.quant;
     if (is_max) {
@@ -343,6 +363,14 @@ RSG_D void subtree_load(const DevMesh& m, int s, uint16_t qmin[3], uint16_t qmax
     }
     root = __ldg(&st->root);
     size = __ldg(&st->size);
+}
+RSG_D void subtree_load_at(const Subtree* st, uint16_t qmin[3], uint16_t qmax[3], int& root, int& size) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(st);
+    uint32_t w0 = w[0], w1 = w[1], w2 = w[2];
+    qmin[0] = w0 & 0xffff; qmin[1] = w0 >> 16; qmin[2] = w1 & 0xffff;
+    qmax[0] = w1 >> 16; qmax[1] = w2 & 0xffff; qmax[2] = w2 >> 16;
+    root = (int)w[3];
+    size = (int)w[4];
 }
 template <class F>
 RSG_D void subtree_walk(const DevMesh& m, const uint16_t* qa, const uint16_t* qb, int root, int size, F&& f) {
@@ -415,34 +443,40 @@ RSG_D bool ray_node_test(const DevMesh& m, const RaySlab& r, const uint16_t* nmi
     if (tzmax < tmax) tmax = tzmax;
     return (tmin < r.lambda_max) && (tmax > 0.f);
 }
-constexpr int RAY_GRID_MAX = 16;
-// The leaves a ray reports, from the leaf grid, in node order: their count, or -1 when there are
-// more than RAY_GRID_MAX (the caller then walks the tree).
-RSG_DN int ray_grid_leaves(const DevMesh& m, const RaySlab& r, int* node) {
+constexpr int RAY_GRID_MAX = 6;
+// The triangles a ray reports, from the leaf grid, in node order: their count (keys in key[]:
+// (rank << 16) | triangle, sorted by rank), or -1 when there are more than RAY_GRID_MAX (the caller
+// then walks the tree).  key[] is indexed statically so it stays in registers.
+RSG_D int ray_grid_tris(const DevMesh& m, const RaySlab& r, int (&key)[RAY_GRID_MAX]) {
     int c0[3], c1[3];
     for (int k = 0; k < 3; k++) {
         c0[k] = r.qa[k] >> m.lg_shift[k];
         c1[k] = r.qb[k] >> m.lg_shift[k];
     }
     int n = 0;
-    const uint4* recs = reinterpret_cast<const uint4*>(m.lg_leaf);
+    const uint4* blocks = reinterpret_cast<const uint4*>(m.lg_block);
+    const uint4* over = reinterpret_cast<const uint4*>(m.lg_over);
     for (int x = c0[0]; x <= c1[0]; x++)
         for (int y = c0[1]; y <= c1[1]; y++)
             for (int z = c0[2]; z <= c1[2]; z++) {
                 const uint32_t cell = ((uint32_t)x * m.lg_n[1] + y) * m.lg_n[2] + z;
-                const uint32_t beg = __ldg(m.lg_start + cell), end = __ldg(m.lg_start + cell + 1);
-                for (uint32_t e0 = beg; e0 < end; e0 += 4) {
-                    uint4 rec[4];  // four leaf boxes in flight at once
+                uint4 rec[4];  // the cell's block: header and three records, one round trip
 #pragma unroll
-                    for (int i = 0; i < 4; i++)
-                        if (e0 + i < end) rec[i] = __ldg(recs + e0 + i);
+                for (int i = 0; i < 4; i++) rec[i] = __ldg(blocks + (size_t)cell * 4 + i);
+                const uint32_t count = rec[0].x, off = rec[0].y;
+                for (uint32_t e0 = 0; e0 < count; e0 += 3) {
+                    if (e0 > 0) {  // records past the block, three at a time
 #pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        if (e0 + i >= end) continue;
+                        for (int i = 0; i < 3; i++)
+                            if (e0 + i < count) rec[1 + i] = __ldg(over + off + (e0 - 3) + i);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 3; i++) {
+                        if (e0 + i >= count) continue;
                         uint16_t nmin[3], nmax[3];
-                        nmin[0] = rec[i].x & 0xffff; nmin[1] = rec[i].x >> 16; nmin[2] = rec[i].y & 0xffff;
-                        nmax[0] = rec[i].y >> 16; nmax[1] = rec[i].z & 0xffff; nmax[2] = rec[i].z >> 16;
-                        const int j = (int)rec[i].w;
+                        nmin[0] = rec[1 + i].x & 0xffff; nmin[1] = rec[1 + i].x >> 16; nmin[2] = rec[1 + i].y & 0xffff;
+                        nmax[0] = rec[1 + i].y >> 16; nmax[1] = rec[1 + i].z & 0xffff; nmax[2] = rec[1 + i].z >> 16;
+                        const int kv = (int)rec[1 + i].w;
                         // the leaf's first cell inside the ray's cell range
                         int fx = nmin[0] >> m.lg_shift[0], fy = nmin[1] >> m.lg_shift[1];
                         int fz = nmin[2] >> m.lg_shift[2];
@@ -451,9 +485,16 @@ RSG_DN int ray_grid_leaves(const DevMesh& m, const RaySlab& r, int* node) {
                             continue;
                         if (!ray_node_test(m, r, nmin, nmax)) continue;
                         if (n == RAY_GRID_MAX) return -1;
-                        int p = n++;  // insertion in node order
-                        while (p > 0 && node[p - 1] > j) { node[p] = node[p - 1]; p--; }
-                        node[p] = j;
+                        // insertion by rank (node order) with static indices: shift the larger keys up
+                        int v = kv;
+#pragma unroll
+                        for (int q = 0; q < RAY_GRID_MAX; q++) {
+                            if (q < n && key[q] > v) { int t = key[q]; key[q] = v; v = t; }
+                        }
+#pragma unroll
+                        for (int q = 0; q < RAY_GRID_MAX; q++)
+                            if (q == n) key[q] = v;
+                        n++;
                     }
                 }
             }
@@ -461,20 +502,32 @@ RSG_DN int ray_grid_leaves(const DevMesh& m, const RaySlab& r, int* node) {
 }
 template <class F>
 RSG_D void mesh_query_ray(const DevMesh& m, V3 src, V3 dst, F&& f) {
+#if defined(RSG_PHASE_TIMERS)
+    long long qt_ = clock64();
+#define RSG_QT(i) do { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - qt_)); qt_ = t_; } while (0)
+#else
+#define RSG_QT(i)
+#endif
     RaySlab r;
     ray_slab_setup(m, src, dst, r);
-    if (m.lg_start) {
-        int node[RAY_GRID_MAX];
-        const int n = ray_grid_leaves(m, r, node);
+    RSG_QT(35);
+    if (m.lg_block) {
+        int key[RAY_GRID_MAX];
+        const int n = ray_grid_tris(m, r, key);
+        RSG_QT(36);
         if (n >= 0) {
-            for (int i = 0; i < n; i++) {
-                uint16_t nmin[3], nmax[3];
-                int tri;
-                node_load(m, node[i], nmin, nmax, tri);
-                f(tri);
-            }
+#pragma unroll
+            for (int i = 0; i < RAY_GRID_MAX; i++)
+                if (i < n) f(key[i] & 0xffff);
+            RSG_QT(37);
+#if defined(RSG_PHASE_TIMERS)
+            atomicAdd(&g_phase_cycles[38], (unsigned long long)n);
+#endif
             return;
         }
+#if defined(RSG_PHASE_TIMERS)
+        atomicAdd(&g_phase_cycles[39], 1ull);
+#endif
     }
     int cur = 0;
     while (cur < m.nnodes) {
@@ -624,6 +677,12 @@ RSG_D void car_child_xf(const Car& c, Xf& out) {
 RSG_D V3 car_he(const Car& c) { return V3(c.cfg->he[0], c.cfg->he[1], c.cfg->he[2]); }
 
 RSG_DN RayHit cast_ray(const BatchView& bv, Ctx& a, V3 from, V3 to, int self_obj) {
+#if defined(RSG_PHASE_TIMERS)
+    long long ct_ = clock64();
+#define RSG_CT(i) do { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - ct_)); ct_ = t_; } while (0)
+#else
+#define RSG_CT(i)
+#endif
     RayHit r;
     r.hit = false;
     float frac = 1.f;
@@ -636,13 +695,24 @@ RSG_DN RayHit cast_ray(const BatchView& bv, Ctx& a, V3 from, V3 to, int self_obj
             V3 n;
             if (ray_triangle(from, to, tv, frac, n)) { obj = OBJ_MESH; nrm = n; }
         });
+        RSG_CT(32);
         for (int p = 0; p < 4; p++) {
+            // ray_plane's triangles lie in the plane and need the ray's ends on both sides of it
+            // (da * db < 0 in ray_triangle); ends more than 0.01 on one side cannot hit
+            const float H = RL::ARENA_HEIGHT * RL::UU_TO_BT, EX = RL::ARENA_EXTENT_X * RL::UU_TO_BT;
+            float sa, sb;
+            if (p == 0) { sa = from.z; sb = to.z; }
+            else if (p == 1) { sa = H - from.z; sb = H - to.z; }
+            else if (p == 2) { sa = from.x + EX; sb = to.x + EX; }
+            else { sa = EX - from.x; sb = EX - to.x; }
+            if ((sa > 0.01f && sb > 0.01f) || (sa < -0.01f && sb < -0.01f)) continue;
             PlaneC pl;
             plane_const(p, pl);
             V3 n;
             if (ray_plane(pl, from, to, frac, n)) { obj = OBJ_PLANE0 + p; nrm = n; }
         }
     }
+    RSG_CT(33);
     int ci, cj, ck;
     grid_idx(bv.grid, from, ci, cj, ck);
     int dyn[MAX_CARS + 1];
@@ -662,6 +732,7 @@ RSG_DN RayHit cast_ray(const BatchView& bv, Ctx& a, V3 from, V3 to, int self_obj
             if (ray_box(from, to, bx, he, frac, n)) { obj = o; nrm = n; }
         }
     }
+    RSG_CT(34);
     if (obj < 0) return r;
     if (!is_static_obj(obj) && a.body(obj).no_contact_response) return r;
     r.hit = true;
@@ -1174,8 +1245,15 @@ RSG_D void car_set_respawn(Car& c, int idx, float boost);
 // Car::_PreTickUpdate (Car.cpp:58-131) after the four suspension rays: friction, wheels, air
 // control, jump, auto-flip, flip / double jump, auto-roll, suspension and boost.
 RSG_DN void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
+#if defined(RSG_PHASE_TIMERS)
+    long long ft_ = clock64();
+#define RSG_FT(i) do { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - ft_)); ft_ = t_; } while (0)
+#else
+#define RSG_FT(i)
+#endif
     float dt = bv.dt;
     calc_friction_impulses(a, c, dt);
+    RSG_FT(40);
     bool pressed = c.f(F_CTRL_JUMP) && !c.f(F_LAST_JUMP);
     int nwc = 0;
     for (int i = 0; i < 4; i++) {
@@ -1186,6 +1264,7 @@ RSG_DN void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
     c.setf(F_ON_GROUND, nwc >= 3);
     float fwd_speed = dot(c.rb.lin_vel, c.rb.xf.b.col(0)) * RL::BT_TO_UU;
     update_wheels(c, dt, nwc, fwd_speed);
+    RSG_FT(41);
     if (nwc < 3) update_air_torque(c, nwc == 0);
     else c.setf(F_FLIPPING, false);
     update_jump(c, dt, pressed);
@@ -1193,9 +1272,13 @@ RSG_DN void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
     update_double_jump_or_flip(c, dt, pressed, fwd_speed);
     if (c.ctrl[0] && ((nwc > 0 && nwc < 4) || c.f(F_WC_CONTACT))) update_auto_roll(c, nwc);
     c.setf(F_WC_CONTACT, false);
+    RSG_FT(42);
     update_suspension(c, dt);
+    RSG_FT(43);
     apply_friction_impulses(c, dt);
+    RSG_FT(44);
     update_boost(c, dt);
+    RSG_FT(45);
 }
 
 // Start of Car::_PreTickUpdate for a car that is not demolished and was not at the last
@@ -2369,7 +2452,7 @@ constexpr int HDR_LIST = 24;  // overlapping BVH subtree headers kept per mesh q
 // without it every header is tested.
 template <class F>
 RSG_D void mesh_candidates(const BatchView& bv, const Xf& conv_xf, const Convex& cshape, float breaking,
-                           const int16_t* hdrs, int nh, F&& emit) {
+                           const Subtree* subs, const int16_t* hdrs, int nh, F&& emit) {
     V3 mn, mx;
     cshape.aabb(conv_xf, mn, mx);
     M3 inv_basis = inverse(conv_xf.b);
@@ -2417,7 +2500,7 @@ RSG_D void mesh_candidates(const BatchView& bv, const Xf& conv_xf, const Convex&
     for (int i = 0; i < nh; i++) {
         uint16_t smin[3], smax[3];
         int root, size;
-        subtree_load(bv.mesh, hdrs[i], smin, smax, root, size);
+        subtree_load_at(subs + hdrs[i], smin, smax, root, size);
         subtree_walk(bv.mesh, qa, qb, root, size, visit);
     }
 }
@@ -2463,7 +2546,7 @@ RSG_DN void convex_vs_mesh(const BatchView& bv, Ctx& a, Manifold& m, int conv, c
     Xf x0 = a.body(m.body0).xf, x1 = obj_xf(a, m.body1);
     float fr = combined_friction(a, OBJ_MESH, conv), re = combined_restitution(a, OBJ_MESH, conv);
     uint32_t warn = 0;
-    mesh_candidates(bv, conv_xf, cshape, m.breaking, nullptr, 0, [&](int t) {
+    mesh_candidates(bv, conv_xf, cshape, m.breaking, a.sub, nullptr, 0, [&](int t) {
         CandRes r = mesh_candidate_test(bv, conv_xf, cshape, m.breaking, t, warn);
         commit_mesh_contact(bv, a, m, x0, x1, fr, re, r, t);
     });
@@ -2507,8 +2590,8 @@ RSG_DN void convex_vs_plane(const BatchView& bv, Ctx& a, Manifold& m, const Xf& 
 
 // btAlignedObjectArray::quickSortInternal (B/LinearMath/btAlignedObjectArray.h:370-400) over manifold
 // indices keyed by island id; sub-ranges are disjoint, so an explicit stack gives the same result.
-RSG_D void island_quicksort(const Ctx& a, int* v, int n) {
-    int stk_lo[MAX_PAIRS], stk_hi[MAX_PAIRS];
+// stk_lo / stk_hi: scratch of at least n entries each
+RSG_D void island_quicksort(const Ctx& a, int* v, int n, int* stk_lo, int* stk_hi) {
     int sp = 0;
     stk_lo[sp] = 0;
     stk_hi[sp] = n - 1;
@@ -2725,6 +2808,7 @@ RSG_D float solve_split(Ctx& a, Row& c) {  // gResolveSplitPenetrationImpulse_ss
 // Solves one batch: `bodies` are dynamic object ids in island order, `mans` manifold indices in
 // sorted island order (btSequentialImpulseConstraintSolver::solveGroup)
 RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, float dt) {
+    RSG_L0_BEGIN;
     int nc = 0, nf = 0;
     int sb_of[MAX_DYN];
     for (int i = 0; i < MAX_DYN; i++) sb_of[i] = -1;
@@ -2797,6 +2881,7 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
             b.sp_total_normal = V3(0, 0, 0);
         }
     }
+    RSG_L0(19);
     const int ITER = 10;
     for (int it = 0; it < ITER; it++) {
         float lsr = 0;
@@ -2807,6 +2892,7 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
         }
         if (lsr <= 0.f || it >= ITER - 1) break;
     }
+    RSG_L0(20);
     for (int it = 0; it < ITER; it++) {
         for (int k = 0; k < nc; k++) {
             if (a.rows_c[k].special) continue;
@@ -2818,6 +2904,7 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
             if (total > 0.f) solve_row(a, f, -(f.friction * total), f.friction * total, false);
         }
     }
+    RSG_L0(21);
     // writeBackBodies (btSequentialImpulseConstraintSolver.cpp:1878-1904)
     for (int i = 0; i < nb; i++) {
         SBody& sb = a.sb[i];
@@ -2990,6 +3077,113 @@ RSG_DN void build_pairs(const BatchView& bv, Ctx& a) {
     }
 }
 
+// build_pairs spread over the warp, one lane per dynamic object: each lane lists its object's
+// pairs in the order the serial loop adds them, drops the dynamic pairs that an earlier object
+// already added (the serial loop's has_pair), and the lists are concatenated in object order.
+RSG_D int8_t classify_pair(const BatchView& bv, Ctx& a, int o0, int o1) {
+    int8_t k = PK_SKIP;
+    bool act0 = is_static_obj(o0) ? false : a.body(o0).is_active();
+    bool act1 = a.body(o1).is_active();
+    if (act0 || act1) {  // btCollisionDispatcher::needsCollision
+        if (is_static_obj(o0)) {
+            if (o1 == OBJ_BALL) {
+                k = o0 == OBJ_MESH ? PK_BALL_MESH : PK_BALL_PLANE;
+            } else {
+                Car& c = a.cars[o1 - OBJ_CAR0];
+                Xf cx;
+                car_child_xf(c, cx);
+                V3 bmn, bmx, omn, omx;
+                car_box_aabb(c, cx, bmn, bmx);
+                if (o0 == OBJ_MESH) mesh_aabb(bv.mesh, omn, omx);
+                else {
+                    PlaneC pl;
+                    plane_const(o0 - OBJ_PLANE0, pl);
+                    omn = pl.raw_min;
+                    omx = pl.raw_max;
+                }
+                if (aabb_overlap(bmn, bmx, omn, omx)) k = o0 == OBJ_MESH ? PK_CAR_MESH : PK_CAR_PLANE;
+            }
+        } else if (o0 == OBJ_BALL) {
+            Car& c = a.cars[o1 - OBJ_CAR0];
+            Xf cx;
+            car_child_xf(c, cx);
+            V3 bmn, bmx, smn, smx;
+            car_box_aabb(c, cx, bmn, bmx);
+            ball_aabb(a.ball.xf, smn, smx);
+            if (aabb_overlap(bmn, bmx, smn, smx)) k = PK_CAR_BALL;
+        } else {
+            k = PK_CAR_CAR;
+        }
+    }
+    return k;
+}
+RSG_D void build_pairs_warp(const BatchView& bv, Ctx& a, int lane) {
+    const int nd = 1 + a.ncars;
+    constexpr int LMAX = 5 + MAX_DYN;
+    int8_t l0[LMAX], l1[LMAX];
+    int n = 0, ncd = 0;
+    int cd[MAX_CARS + 1];
+    const int o = OBJ_BALL + lane;
+    if (lane < nd) ncd = cell_dyn_list(a, a.body(o).ci, a.body(o).cj, a.body(o).ck, cd);
+    if (lane < nd) {
+        Body& b = a.body(o);
+        if (bv.has_arena) {
+            V3 mesh_mn, mesh_mx;
+            mesh_aabb(bv.mesh, mesh_mn, mesh_mx);
+            mesh_mn -= V3(0.02f, 0.02f, 0.02f);
+            mesh_mx += V3(0.02f, 0.02f, 0.02f);
+            if (bv.mesh.cells[b.cell] && aabb_overlap(b.bp_min, b.bp_max, mesh_mn, mesh_mx)) {
+                l0[n] = OBJ_MESH; l1[n] = (int8_t)o; n++;
+            }
+            for (int p = 0; p < 4; p++) {
+                PlaneC pl;
+                plane_const(p, pl);
+                if (aabb_overlap(b.bp_min, b.bp_max, pl.bp_min, pl.bp_max)) {
+                    l0[n] = (int8_t)(OBJ_PLANE0 + p); l1[n] = (int8_t)o; n++;
+                }
+            }
+        }
+    }
+    int ncd_lane[MAX_DYN];
+    for (int d = 0; d < MAX_DYN; d++) ncd_lane[d] = __shfl_sync(0xffffffffu, ncd, d);
+    if (lane < nd && ncd > 1) {
+        Body& b = a.body(o);
+        for (int qi = 0; qi < ncd; qi++) {
+            int q = cd[qi];
+            if (q == o) continue;
+            Body& bq = a.body(q);
+            if (!aabb_overlap(b.bp_min, b.bp_max, bq.bp_min, bq.bp_max)) continue;
+            // added already while the earlier object q listed its own pairs?
+            bool earlier = q < o && ncd_lane[q - OBJ_BALL] > 1 && dyn_registered(b, bq.ci, bq.cj, bq.ck);
+            if (earlier) continue;
+            l0[n] = (int8_t)(o < q ? o : q);
+            l1[n] = (int8_t)(o < q ? q : o);
+            n++;
+        }
+    }
+    // concatenate in object order
+    int off = n;
+    for (int d = 1; d < 32; d <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, off, d);
+        if (lane >= d) off += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, off, 31);
+    off -= n;
+    for (int i = 0; i < n; i++) {
+        int at = off + i;
+        if (at >= a.cap_pairs) break;
+        a.pair0[at] = l0[i];
+        a.pair1[at] = l1[i];
+        a.pkind[at] = classify_pair(bv, a, l0[i], l1[i]);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        a.npairs = total < a.cap_pairs ? total : a.cap_pairs;
+        if (total > a.cap_pairs) a.err |= ERR_PAIR_OVERFLOW;
+    }
+    __syncwarp();
+}
+
 // collision shape of a dynamic object against static geometry
 RSG_D void dyn_shape(Ctx& a, int o, Xf& xf, Convex& sh, float& breaking) {
     sh.he = V3(0, 0, 0);
@@ -3160,13 +3354,20 @@ RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a);
 
 RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     RSG_PHASE_BEGIN;
+#if defined(RSG_PHASE_TIMERS)
+    long long rsg_w_ = clock64();
+#define RSG_W(i) do { if (lane == 0) { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - rsg_w_)); rsg_w_ = t_; } } while (0)
+#else
+#define RSG_W(i)
+#endif
+    build_pairs_warp(bv, a, lane);
     if (lane == 0) {
-        build_pairs(bv, a);
         a.nman = 0;
         a.npts = 0;
         a.warn = 0;
     }
     __syncwarp();
+    RSG_W(22);
     uint32_t warn = 0;
     // quantized query box of each mesh pair (one lane per pair)
     unsigned qmask = 0;
@@ -3187,26 +3388,47 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     }
     qmask = __reduce_or_sync(0xffffffffu, qmask);
     __syncwarp();
+    RSG_W(23);
     // subtree headers against every query box, 32 headers at a time; each query keeps the
-    // overlapping headers in header order
+    // overlapping headers in header order.  A run of 32 headers is scanned only for the queries
+    // that overlap the box around the whole run.
     if (qmask) {
         int cnt[MAX_DYN];
         for (int d = 0; d < MAX_DYN; d++) cnt[d] = 0;
-        const int nsub = bv.mesh.nsub;
-        for (int base = 0; base < nsub; base += 32) {
-            const int h = base + lane;
-            uint16_t smin[3], smax[3];
-            int root = 0, size = 0;
-            if (h < nsub) subtree_load(bv.mesh, h, smin, smax, root, size);
-            for (int d = 0; d < MAX_DYN; d++) {
-                if (!((qmask >> d) & 1u)) continue;
-                bool ov = h < nsub && qov(a.qbox + d * 6, a.qbox + d * 6 + 3, smin, smax);
-                unsigned m = __ballot_sync(0xffffffffu, ov);
-                if (ov) {
-                    int pos = cnt[d] + __popc(m & ((1u << lane) - 1u));
-                    if (pos < HDR_LIST) a.hdr_list[d * HDR_LIST + pos] = (int16_t)h;
+        const int nsub = bv.mesh.nsub, ngrp = bv.mesh.nsub_grp;
+        for (int gbase = 0; gbase < ngrp; gbase += 32) {
+            unsigned gm[MAX_DYN];
+            {
+                const int g = gbase + lane;
+                uint16_t gmin[3], gmax[3];
+                int gfirst = 0;
+                if (g < ngrp) node_load_ptr(bv.mesh.sub_grp, g, gmin, gmax, gfirst);
+                for (int d = 0; d < MAX_DYN; d++) {
+                    gm[d] = 0;
+                    if (!((qmask >> d) & 1u)) continue;
+                    bool ov = g < ngrp && qov(a.qbox + d * 6, a.qbox + d * 6 + 3, gmin, gmax);
+                    gm[d] = __ballot_sync(0xffffffffu, ov);
                 }
-                cnt[d] += __popc(m);
+            }
+            unsigned any = 0;
+            for (int d = 0; d < MAX_DYN; d++) any |= gm[d];
+            while (any) {
+                const int gi = __ffs(any) - 1;
+                any &= any - 1;
+                const int h = (gbase + gi) * 32 + lane;
+                uint16_t smin[3], smax[3];
+                int root = 0, size = 0;
+                if (h < nsub) subtree_load_at(a.sub + h, smin, smax, root, size);
+                for (int d = 0; d < MAX_DYN; d++) {
+                    if (!((gm[d] >> gi) & 1u)) continue;
+                    bool ov = h < nsub && qov(a.qbox + d * 6, a.qbox + d * 6 + 3, smin, smax);
+                    unsigned m = __ballot_sync(0xffffffffu, ov);
+                    if (ov) {
+                        int pos = cnt[d] + __popc(m & ((1u << lane) - 1u));
+                        if (pos < HDR_LIST) a.hdr_list[d * HDR_LIST + pos] = (int16_t)h;
+                    }
+                    cnt[d] += __popc(m);
+                }
             }
         }
         if (lane == 0)
@@ -3214,6 +3436,7 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
                 if ((qmask >> d) & 1u) a.hdr_n[d] = (int16_t)(cnt[d] <= HDR_LIST ? cnt[d] : -1);
     }
     __syncwarp();
+    RSG_W(24);
     // candidate triangles of each mesh pair, one lane per pair, in BVH order
     for (int p = lane; p < a.npairs; p += 32) {
         int k = a.pkind[p];
@@ -3227,7 +3450,7 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
             int* out = a.cand_tri + d * MESH_SEG;
             int n = 0;
             int nh = a.hdr_n[d];
-            mesh_candidates(bv, xf, sh, br, nh >= 0 ? a.hdr_list + d * HDR_LIST : nullptr, nh, [&](int t) {
+            mesh_candidates(bv, xf, sh, br, a.sub, nh >= 0 ? a.hdr_list + d * HDR_LIST : nullptr, nh, [&](int t) {
                 if (n < MESH_SEG) out[n] = t;
                 n++;
             });
@@ -3287,80 +3510,147 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     RSG_PHASE(7);
 }
 
+// Register-array helpers for the at most MAX_DYN dynamic objects of an arena (unrolled selects
+// keep the small arrays out of local memory).
+RSG_D int rget(const int (&v)[MAX_DYN], int i) {
+    int r = 0;
+#pragma unroll
+    for (int k = 0; k < MAX_DYN; k++) r = (k == i) ? v[k] : r;
+    return r;
+}
+RSG_D void rset(int (&v)[MAX_DYN], int i, int x) {
+#pragma unroll
+    for (int k = 0; k < MAX_DYN; k++) v[k] = (k == i) ? x : v[k];
+}
+
 RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a) {
+    RSG_L0_BEGIN;
     const float dt = bv.dt;
     const int nd = 1 + a.ncars;
-    // islands (btSimulationIslandManager, STATIC_SIMULATION_ISLAND_OPTIMIZATION)
-    int uf_id[MAX_CARS + 1], uf_sz[MAX_CARS + 1], tag[MAX_CARS + 1];
-    for (int i = 0; i < nd; i++) { uf_id[i] = i; uf_sz[i] = 1; }
-    auto find = [&](int x) { while (x != uf_id[x]) x = uf_id[x]; return x; };
-    auto merges = [&](int o) { return !is_static_obj(o) && !a.body(o).no_contact_response; };
-    for (int pi = 0; pi < a.npairs; pi++) {
-        int p0 = a.pair0[pi], p1 = a.pair1[pi];
-        if (merges(p0) && merges(p1)) {
-            int i = find(p0 - OBJ_BALL), j = find(p1 - OBJ_BALL);
+    RSG_L0(50);
+    // per-body activation state and contact response, read once
+    int act[MAX_DYN];
+    unsigned resp = 0;
+#pragma unroll
+    for (int i = 0; i < MAX_DYN; i++) {
+        act[i] = 0;
+        if (i < nd) {
+            const Body& b = a.body(OBJ_BALL + i);
+            act[i] = b.act;
+            if (!b.no_contact_response) resp |= 1u << i;
+        }
+    }
+    // islands (btSimulationIslandManager, STATIC_SIMULATION_ISLAND_OPTIMIZATION): union by size
+    // over the broadphase pairs in order
+    RSG_L0(51);
+    int tag[MAX_DYN];
+#pragma unroll
+    for (int i = 0; i < MAX_DYN; i++) tag[i] = i < nd ? i : -1;
+    bool merging = false;  // any pair of two responding dynamic objects?
+    for (int pi = 0; pi < a.npairs && !merging; pi++) {
+        int p0 = a.pair0[pi];
+        if (is_static_obj(p0)) continue;
+        merging = ((resp >> (p0 - OBJ_BALL)) & 1u) && ((resp >> (a.pair1[pi] - OBJ_BALL)) & 1u);
+    }
+    if (merging) {
+        int uf_id[MAX_DYN], uf_sz[MAX_DYN];
+        for (int i = 0; i < nd; i++) { uf_id[i] = i; uf_sz[i] = 1; }
+        auto find = [&](int x) { while (x != uf_id[x]) x = uf_id[x]; return x; };
+        for (int pi = 0; pi < a.npairs; pi++) {
+            int p0 = a.pair0[pi];
+            if (is_static_obj(p0)) continue;
+            int d0 = p0 - OBJ_BALL, d1 = a.pair1[pi] - OBJ_BALL;
+            if (!((resp >> d0) & 1u) || !((resp >> d1) & 1u)) continue;
+            int i = find(d0), j = find(d1);
             if (i == j) continue;
             if (uf_sz[i] < uf_sz[j]) { uf_id[i] = j; uf_sz[j] += uf_sz[i]; }
             else { uf_id[j] = i; uf_sz[i] += uf_sz[j]; }
         }
+        int t[MAX_DYN];
+        for (int i = 0; i < nd; i++) t[i] = find(i);
+#pragma unroll
+        for (int i = 0; i < MAX_DYN; i++)
+            if (i < nd) tag[i] = t[i];
     }
-    for (int i = 0; i < nd; i++) tag[i] = find(i);
+    RSG_L0(52);
     // buildIslands: activation per island, island ids ascending
-    for (int id = 0; id < nd; id++) {
-        bool present = false, all_sleeping = true;
-        for (int i = 0; i < nd; i++) {
-            if (tag[i] != id) continue;
-            present = true;
-            int st = a.body(OBJ_BALL + i).act;
-            if (st == ACTIVE_TAG || st == DISABLE_DEACTIVATION) { all_sleeping = false; break; }
-        }
-        if (!present) continue;
-        for (int i = 0; i < nd; i++) {
-            if (tag[i] != id) continue;
-            Body& b = a.body(OBJ_BALL + i);
-            if (all_sleeping) {
-                if (b.act != DISABLE_DEACTIVATION && b.act != DISABLE_SIMULATION) b.act = ISLAND_SLEEPING;
-            } else if (b.act == ISLAND_SLEEPING) {
-                b.act = WANTS_DEACTIVATION;
+    if (!merging) {  // every body is its own island
+#pragma unroll
+        for (int i = 0; i < MAX_DYN; i++)
+            if (i < nd && act[i] != ACTIVE_TAG && act[i] != DISABLE_DEACTIVATION && act[i] != DISABLE_SIMULATION)
+                act[i] = ISLAND_SLEEPING;
+    } else {
+        int ta[MAX_DYN], aa[MAX_DYN];
+        for (int i = 0; i < MAX_DYN; i++) { ta[i] = rget(tag, i); aa[i] = rget(act, i); }
+        for (int id = 0; id < nd; id++) {
+            bool present = false, all_sleeping = true;
+            for (int i = 0; i < nd; i++)
+                if (ta[i] == id) {
+                    present = true;
+                    if (aa[i] == ACTIVE_TAG || aa[i] == DISABLE_DEACTIVATION) all_sleeping = false;
+                }
+            if (!present) continue;
+            for (int i = 0; i < nd; i++) {
+                if (ta[i] != id) continue;
+                if (all_sleeping) {
+                    if (aa[i] != DISABLE_DEACTIVATION && aa[i] != DISABLE_SIMULATION) aa[i] = ISLAND_SLEEPING;
+                } else if (aa[i] == ISLAND_SLEEPING) {
+                    aa[i] = WANTS_DEACTIVATION;
+                }
             }
         }
+#pragma unroll
+        for (int i = 0; i < MAX_DYN; i++) act[i] = aa[i];
     }
-    int island_mans[MAX_PAIRS];
+#pragma unroll
+    for (int i = 0; i < MAX_DYN; i++)
+        if (i < nd) a.body(OBJ_BALL + i).act = act[i];
+    RSG_L0(53);
+    // the tail's lists live in the candidate-triangle scratch, free once the narrow phase is done
+    int* island_mans = a.cand_tri;
+    int* solve_mans = island_mans + a.cap_pairs;
+    int* qs_lo = solve_mans + a.cap_pairs;
+    int* qs_hi = qs_lo + a.cap_pairs;
+    int* bodies = qs_hi + a.cap_pairs;
     int nim = 0;
     for (int mi = 0; mi < a.nman; mi++) {
         Manifold& m = a.man[mi];
-        int s0 = is_static_obj(m.body0) ? ISLAND_SLEEPING : a.body(m.body0).act;
-        int s1 = is_static_obj(m.body1) ? ISLAND_SLEEPING : a.body(m.body1).act;
+        const int b0 = m.body0, b1 = m.body1;
+        const bool st0 = is_static_obj(b0), st1 = is_static_obj(b1);
+        int s0 = st0 ? ISLAND_SLEEPING : rget(act, b0 - OBJ_BALL);
+        int s1 = st1 ? ISLAND_SLEEPING : rget(act, b1 - OBJ_BALL);
         if (s0 != ISLAND_SLEEPING || s1 != ISLAND_SLEEPING) {
-            bool r0 = is_static_obj(m.body0) ? true : !a.body(m.body0).no_contact_response;
-            bool r1 = is_static_obj(m.body1) ? true : !a.body(m.body1).no_contact_response;
-            bool resp = r0 && r1 && (!is_static_obj(m.body0) || !is_static_obj(m.body1));
-            if (resp) {
-                int i0 = is_static_obj(m.body0) ? -1 : tag[m.body0 - OBJ_BALL];
-                int i1 = is_static_obj(m.body1) ? -1 : tag[m.body1 - OBJ_BALL];
+            bool r0 = st0 ? true : ((resp >> (b0 - OBJ_BALL)) & 1u);
+            bool r1 = st1 ? true : ((resp >> (b1 - OBJ_BALL)) & 1u);
+            if (r0 && r1 && (!st0 || !st1)) {
+                int i0 = st0 ? -1 : rget(tag, b0 - OBJ_BALL);
+                int i1 = st1 ? -1 : rget(tag, b1 - OBJ_BALL);
                 m.island = (int8_t)(i0 >= 0 ? i0 : i1);
                 island_mans[nim++] = mi;
             }
         }
     }
-    if (nim > 1) island_quicksort(a, island_mans, nim);
-    // processIslands: bodies and manifolds of awake islands, solved as one batch
-    int bodies[MAX_CARS + 1], nb = 0;
-    int solve_mans[MAX_PAIRS], nsm = 0;
-    for (int id = 0; id < nd; id++) {
-        bool present = false, sleeping = true;
-        for (int i = 0; i < nd; i++)
-            if (tag[i] == id) {
-                present = true;
-                if (a.body(OBJ_BALL + i).is_active()) sleeping = false;
-            }
-        if (!present || sleeping) continue;
-        for (int i = 0; i < nd; i++)
+    RSG_L0(16);
+    if (nim > 1) island_quicksort(a, island_mans, nim, qs_lo, qs_hi);
+    RSG_L0(17);
+    // processIslands: bodies and manifolds of awake islands, solved as one batch.  The sorted
+    // manifold list is in island order, so one pass keeps each awake island's manifolds in order.
+    unsigned awake = 0;
+#pragma unroll
+    for (int i = 0; i < MAX_DYN; i++)
+        if (tag[i] >= 0 && act[i] != ISLAND_SLEEPING && act[i] != DISABLE_SIMULATION) awake |= 1u << tag[i];
+    int nb = 0, nsm = 0;
+#pragma unroll
+    for (int id = 0; id < MAX_DYN; id++) {
+        if (!((awake >> id) & 1u)) continue;
+#pragma unroll
+        for (int i = 0; i < MAX_DYN; i++)
             if (tag[i] == id) bodies[nb++] = OBJ_BALL + i;
-        for (int k = 0; k < nim; k++)
-            if (a.man[island_mans[k]].island == id) solve_mans[nsm++] = island_mans[k];
     }
+    for (int k = 0; k < nim; k++)
+        if ((awake >> a.man[island_mans[k]].island) & 1u) solve_mans[nsm++] = island_mans[k];
     a.solver_dt = dt;
+    RSG_L0(18);
     if (nb > 0) solve(a, bodies, nb, solve_mans, nsm, dt);
 }
 
@@ -3508,7 +3798,18 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
         Ctx& a = B(u / (MC * 4));
         int r = u % (MC * 4), k = r >> 2, wh = r & 3;
         if (a.serial || k >= a.ncars) continue;
+#if defined(RSG_PHASE_TIMERS)
+        long long rt0_ = clock64();
+#endif
         ray_cast_wheel(bv, a, a.cars[k], wh);
+#if defined(RSG_PHASE_TIMERS)
+        {
+            long long dtw = clock64() - rt0_;
+            atomicAdd(&g_phase_cycles[25], (unsigned long long)dtw);
+            atomicAdd(&g_phase_cycles[26], 1ull);
+            atomicMax(&g_phase_cycles[27], (unsigned long long)dtw);
+        }
+#endif
         if (a.cars[k].w[wh].ground >= OBJ_CAR0) a.on_car = 1;
     }
     __syncthreads();
@@ -3521,7 +3822,18 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
             if (k == 0)
                 for (int kk = 0; kk < a.ncars; kk++) car_pre_after_rays(bv, a, a.cars[a.order[kk]]);
         } else {
+#if defined(RSG_PHASE_TIMERS)
+            long long at0_ = clock64();
+#endif
             car_pre_after_rays(bv, a, a.cars[k]);
+#if defined(RSG_PHASE_TIMERS)
+            {
+                long long dtc = clock64() - at0_;
+                atomicAdd(&g_phase_cycles[28], (unsigned long long)dtc);
+                atomicAdd(&g_phase_cycles[29], 1ull);
+                atomicMax(&g_phase_cycles[30], (unsigned long long)dtc);
+            }
+#endif
         }
     }
     if (bv.has_arena)
@@ -3963,7 +4275,10 @@ RSG_HD SmemLayout smem_layout(int mc) {
     L.pkind = o;  o = align16(o + L.caps.pairs);
     L.flat_off = o; o = align16(o + 2 * L.caps.pairs);
     L.flat_n = o; o = align16(o + 2 * L.caps.pairs);
-    L.cand_tri = o; o = align16(o + 4 * MESH_SEG * (mc + 1));
+    {  // candidate triangles; reused by the island / solver lists after the narrow phase
+        int words = MESH_SEG * (mc + 1), tail = 4 * L.caps.pairs + MAX_DYN;
+        L.cand_tri = o; o = align16(o + 4 * (words > tail ? words : tail));
+    }
     L.cand_n = o; o = align16(o + 2 * (mc + 1));
     L.cand_res = o; o = align16(o + (int)sizeof(CandRes) * 32);
     L.qbox = o; o = align16(o + 2 * 6 * MAX_DYN);
