@@ -82,18 +82,27 @@ struct Curve {
     int n;
     float x[6], y[6];
 };
+// LinearPieceCurve::GetOutput: the first point above `in` and a linear interpolation from the
+// point before it.  The segment is selected without early returns so that threads evaluating
+// different segments share one interpolation.
 RSG_HD float curve_eval(const Curve& c, float in, float def = 1) {
-    if (c.n == 0) return def;
+    const int n = c.n;
+    if (n == 0) return def;
     if (in <= c.x[0]) return c.y[0];
-    for (int i = 1; i < c.n; i++) {
-        if (c.x[i] > in) {
-            float range = c.x[i] - c.x[i - 1];
-            float diff = c.y[i] - c.y[i - 1];
-            float f = (in - c.x[i - 1]) / range;
-            return c.y[i - 1] + diff * f;
+    float xa = 0, xb = 0, ya = 0, yb = 0;
+    bool found = false;
+#pragma unroll
+    for (int i = 1; i < 6; i++) {
+        if (!found && i < n && c.x[i] > in) {
+            xa = c.x[i - 1]; xb = c.x[i]; ya = c.y[i - 1]; yb = c.y[i];
+            found = true;
         }
     }
-    return c.y[c.n - 1];
+    if (!found) return c.y[n - 1];
+    float range = xb - xa;
+    float diff = yb - ya;
+    float f = (in - xa) / range;
+    return ya + diff * f;
 }
 
 // Curve table (RLConst.h:388-503)

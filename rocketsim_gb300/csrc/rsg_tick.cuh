@@ -460,42 +460,30 @@ RSG_D int ray_grid_tris(const DevMesh& m, const RaySlab& r, int (&key)[RAY_GRID_
         for (int y = c0[1]; y <= c1[1]; y++)
             for (int z = c0[2]; z <= c1[2]; z++) {
                 const uint32_t cell = ((uint32_t)x * m.lg_n[1] + y) * m.lg_n[2] + z;
-                uint4 rec[4];  // the cell's block: header and three records, one round trip
+                const uint4 hdr = __ldg(blocks + (size_t)cell * 4);
+                const uint32_t count = hdr.x, off = hdr.y;
+                for (uint32_t e = 0; e < count; e++) {  // one compact loop: the block's line stays in L1
+                    const uint4 rec = e < 3 ? __ldg(blocks + (size_t)cell * 4 + 1 + e) : __ldg(over + off + (e - 3));
+                    uint16_t nmin[3], nmax[3];
+                    nmin[0] = rec.x & 0xffff; nmin[1] = rec.x >> 16; nmin[2] = rec.y & 0xffff;
+                    nmax[0] = rec.y >> 16; nmax[1] = rec.z & 0xffff; nmax[2] = rec.z >> 16;
+                    // the leaf's first cell inside the ray's cell range
+                    int fx = nmin[0] >> m.lg_shift[0], fy = nmin[1] >> m.lg_shift[1], fz = nmin[2] >> m.lg_shift[2];
+                    if ((fx > c0[0] ? fx : c0[0]) != x || (fy > c0[1] ? fy : c0[1]) != y ||
+                        (fz > c0[2] ? fz : c0[2]) != z)
+                        continue;
+                    if (!ray_node_test(m, r, nmin, nmax)) continue;
+                    if (n == RAY_GRID_MAX) return -1;
+                    // insertion by rank (node order) with static indices: shift the larger keys up
+                    int v = (int)rec.w;
 #pragma unroll
-                for (int i = 0; i < 4; i++) rec[i] = __ldg(blocks + (size_t)cell * 4 + i);
-                const uint32_t count = rec[0].x, off = rec[0].y;
-                for (uint32_t e0 = 0; e0 < count; e0 += 3) {
-                    if (e0 > 0) {  // records past the block, three at a time
-#pragma unroll
-                        for (int i = 0; i < 3; i++)
-                            if (e0 + i < count) rec[1 + i] = __ldg(over + off + (e0 - 3) + i);
+                    for (int q = 0; q < RAY_GRID_MAX; q++) {
+                        if (q < n && key[q] > v) { int t = key[q]; key[q] = v; v = t; }
                     }
 #pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        if (e0 + i >= count) continue;
-                        uint16_t nmin[3], nmax[3];
-                        nmin[0] = rec[1 + i].x & 0xffff; nmin[1] = rec[1 + i].x >> 16; nmin[2] = rec[1 + i].y & 0xffff;
-                        nmax[0] = rec[1 + i].y >> 16; nmax[1] = rec[1 + i].z & 0xffff; nmax[2] = rec[1 + i].z >> 16;
-                        const int kv = (int)rec[1 + i].w;
-                        // the leaf's first cell inside the ray's cell range
-                        int fx = nmin[0] >> m.lg_shift[0], fy = nmin[1] >> m.lg_shift[1];
-                        int fz = nmin[2] >> m.lg_shift[2];
-                        if ((fx > c0[0] ? fx : c0[0]) != x || (fy > c0[1] ? fy : c0[1]) != y ||
-                            (fz > c0[2] ? fz : c0[2]) != z)
-                            continue;
-                        if (!ray_node_test(m, r, nmin, nmax)) continue;
-                        if (n == RAY_GRID_MAX) return -1;
-                        // insertion by rank (node order) with static indices: shift the larger keys up
-                        int v = kv;
-#pragma unroll
-                        for (int q = 0; q < RAY_GRID_MAX; q++) {
-                            if (q < n && key[q] > v) { int t = key[q]; key[q] = v; v = t; }
-                        }
-#pragma unroll
-                        for (int q = 0; q < RAY_GRID_MAX; q++)
-                            if (q == n) key[q] = v;
-                        n++;
-                    }
+                    for (int q = 0; q < RAY_GRID_MAX; q++)
+                        if (q == n) key[q] = v;
+                    n++;
                 }
             }
     return n;
@@ -3640,12 +3628,15 @@ RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a) {
     for (int i = 0; i < MAX_DYN; i++)
         if (tag[i] >= 0 && act[i] != ISLAND_SLEEPING && act[i] != DISABLE_SIMULATION) awake |= 1u << tag[i];
     int nb = 0, nsm = 0;
-#pragma unroll
-    for (int id = 0; id < MAX_DYN; id++) {
-        if (!((awake >> id) & 1u)) continue;
-#pragma unroll
-        for (int i = 0; i < MAX_DYN; i++)
-            if (tag[i] == id) bodies[nb++] = OBJ_BALL + i;
+    if (!merging) {  // island id == body index
+        for (int i = 0; i < nd; i++)
+            if ((awake >> i) & 1u) bodies[nb++] = OBJ_BALL + i;
+    } else {
+        for (int id = 0; id < nd; id++) {
+            if (!((awake >> id) & 1u)) continue;
+            for (int i = 0; i < nd; i++)
+                if (rget(tag, i) == id) bodies[nb++] = OBJ_BALL + i;
+        }
     }
     for (int k = 0; k < nim; k++)
         if ((awake >> a.man[island_mans[k]].island) & 1u) solve_mans[nsm++] = island_mans[k];
@@ -3755,6 +3746,10 @@ struct BlockArenas {
     RSG_D Ctx& operator()(int w) const { return *reinterpret_cast<Ctx*>(base + (size_t)w * bytes); }
 };
 
+// Thread `tid` of `nthreads` takes unit (tid % 32) * warps + tid / 32: consecutive units land in
+// different warps.  Every unit count here is at most nthreads (32 wheel slots per arena).
+RSG_D int spread_unit(int tid, int nthreads) { return (tid & 31) * (nthreads >> 5) + (tid >> 5); }
+
 // Start of a tick for every arena of the block, the work spread over the block's threads by
 // unit: arena, car, wheel, pad.  In the reference these run car by car; the units here are
 // independent (a car's rays read only positions, cells and collision flags of other cars, none
@@ -3781,23 +3776,26 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
     }
     __syncthreads();
     RSG_SUB(8);
-    for (int u = tid; u < B.nact * MC; u += nthreads) {
+    {  // units spread over the block's warps (a few per warp): less divergence, more warps at work
+        const int u = spread_unit(tid, nthreads);
         Ctx& a = B(u / MC);
         int k = u % MC;
-        if (k >= a.ncars) continue;
+        if (u < B.nact * MC && k < a.ncars) {
         if (a.serial) {
             if (k == 0)
                 for (int kk = 0; kk < a.ncars; kk++) car_pre_tick(bv, a, a.cars[a.order[kk]]);
         } else {
             car_pre_before_rays(a.cars[k]);
         }
+        }
     }
     __syncthreads();
     RSG_SUB(9);
-    for (int u = tid; u < B.nact * MC * 4; u += nthreads) {
+    {
+        const int u = spread_unit(tid, nthreads);
         Ctx& a = B(u / (MC * 4));
         int r = u % (MC * 4), k = r >> 2, wh = r & 3;
-        if (a.serial || k >= a.ncars) continue;
+        if (u < B.nact * MC * 4 && !a.serial && k < a.ncars) {
 #if defined(RSG_PHASE_TIMERS)
         long long rt0_ = clock64();
 #endif
@@ -3811,13 +3809,15 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
         }
 #endif
         if (a.cars[k].w[wh].ground >= OBJ_CAR0) a.on_car = 1;
+        }
     }
     __syncthreads();
     RSG_SUB(10);
-    for (int u = tid; u < B.nact * MC; u += nthreads) {
+    {
+        const int u = spread_unit(tid, nthreads);
         Ctx& a = B(u / MC);
         int k = u % MC;
-        if (a.serial || k >= a.ncars) continue;
+        if (u < B.nact * MC && !a.serial && k < a.ncars) {
         if (a.on_car) {
             if (k == 0)
                 for (int kk = 0; kk < a.ncars; kk++) car_pre_after_rays(bv, a, a.cars[a.order[kk]]);
@@ -3834,6 +3834,7 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
                 atomicMax(&g_phase_cycles[30], (unsigned long long)dtc);
             }
 #endif
+        }
         }
     }
     if (bv.has_arena)
