@@ -854,9 +854,10 @@ RSG_D float resolve_single_bilateral(Ctx& a, Body& b1, V3 pos, int obj2, V3 norm
     return -0.2f * dot(normal, v1 - v2) * jinv;
 }
 
-RSG_D void calc_friction_impulses(Ctx& a, Car& c, float dt) {  // btVehicleRL::calcFrictionImpulses (btVehicleRL.cpp:306-380)
+// btVehicleRL::calcFrictionImpulses (btVehicleRL.cpp:306-380) for wheel i (wheels are independent)
+RSG_D void calc_friction_impulse(Ctx& a, Car& c, float dt, int i) {
     float fscale = (1.f / c.rb.inv_mass) / 3;
-    for (int i = 0; i < 4; i++) {
+    {
         WheelRT& w = c.w[i];
         if (w.ground >= 0) {
             V3 axle = w.wbasis.col(1);
@@ -905,8 +906,9 @@ RSG_D V3 upwards_from_wheels(const Car& c) {  // btVehicleRL.cpp:397-410
     return safe_normalized(sum);
 }
 
-RSG_D void update_suspension(Car& c, float dt) {  // btVehicleRL.cpp:270-303
-    for (int i = 0; i < 4; i++) {
+// btVehicleRL::updateSuspension (btVehicleRL.cpp:270-303): the force of wheel i
+RSG_D void suspension_force(Car& c, int i) {
+    {
         WheelRT& w = c.w[i];
         if (w.in_contact) {
             int fb = i < 2 ? 0 : 1;
@@ -919,6 +921,9 @@ RSG_D void update_suspension(Car& c, float dt) {  // btVehicleRL.cpp:270-303
             w.susp_force = 0;
         }
     }
+}
+// ... and the suspension impulses on the chassis, wheel by wheel in order
+RSG_D void apply_suspension(Car& c, float dt) {
     for (int i = 0; i < 4; i++) {
         WheelRT& w = c.w[i];
         if (w.susp_force != 0) {
@@ -947,16 +952,25 @@ RSG_D float rs_minf(float a, float b) { return (a < b) ? a : b; }
 RSG_D float rs_clampf(float v, float lo, float hi) { return rs_minf(rs_maxf(v, lo), hi); }
 RSG_D int rs_sgn(float v) { return (v > 0) - (v < 0); }
 
-RSG_D void update_wheels(Car& c, float dt, int nwc, float fwd_speed) {  // Car::_UpdateWheels (Car.cpp:339-484)
+// Car::_UpdateWheels (Car.cpp:339-484) in three parts: the car's handbrake, engine, brake and steer
+// (computed by every thread of the car's group, stored by `store`), each wheel's friction curves,
+// and the sticky force.
+struct WheelsCommon {
+    float absfs, real_throttle;
+    bool world_contact;
+};
+RSG_D WheelsCommon update_wheels_car(Car& c, float dt, int nwc, float fwd_speed, float hb, bool store) {
+    WheelsCommon wc;
     float absfs = fabsf(fwd_speed);
     bool world_contact = false;
     for (int i = 0; i < 4; i++) world_contact |= c.w[i].contact_world;
-    if (c.f(F_CTRL_HB)) c.handbrake += RL::POWERSLIDE_RISE_RATE * dt;
-    else c.handbrake -= RL::POWERSLIDE_FALL_RATE * dt;
-    c.handbrake = rs_clampf(c.handbrake, 0, 1);
+    if (c.f(F_CTRL_HB)) hb += RL::POWERSLIDE_RISE_RATE * dt;
+    else hb -= RL::POWERSLIDE_FALL_RATE * dt;
+    hb = rs_clampf(hb, 0, 1);
     float real_throttle = c.ctrl[0];
     float real_brake = 0;
     if (c.f(F_CTRL_BOOST) && c.boost > 0) real_throttle = 1;
+    float engine, brake, steer;
     {
         float dss = curve_eval(c_curves[CV_DRIVE_TORQUE], absfs);
         float eng = real_throttle;
@@ -973,49 +987,61 @@ RSG_D void update_wheels(Car& c, float dt, int nwc, float fwd_speed) {  // Car::
             }
         }
         if (nwc < 3) dss /= 4;
-        c.engine = eng * (RL::THROTTLE_TORQUE_AMOUNT * RL::UU_TO_BT) * dss;
-        c.brake = real_brake * (RL::BRAKE_TORQUE_AMOUNT * RL::UU_TO_BT);
+        engine = eng * (RL::THROTTLE_TORQUE_AMOUNT * RL::UU_TO_BT) * dss;
+        brake = real_brake * (RL::BRAKE_TORQUE_AMOUNT * RL::UU_TO_BT);
     }
     {
         bool tw = c.cfg->three_wheels != 0;
-        float steer = curve_eval(c_curves[tw ? CV_STEER_3W : CV_STEER], absfs);
-        if (c.handbrake) steer += (curve_eval(c_curves[CV_POWERSLIDE_STEER], absfs) - steer) * c.handbrake;
+        steer = curve_eval(c_curves[tw ? CV_STEER_3W : CV_STEER], absfs);
+        if (hb) steer += (curve_eval(c_curves[CV_POWERSLIDE_STEER], absfs) - steer) * hb;
         steer *= c.ctrl[1];
+    }
+    if (store) {
+        c.handbrake = hb;
+        c.engine = engine;
+        c.brake = brake;
         c.steer = steer;
     }
-    for (int i = 0; i < 4; i++) {
-        WheelRT& w = c.w[i];
-        if (w.ground >= 0) {
-            V3 vel = c.rb.lin_vel, av = c.rb.ang_vel;
-            V3 lat = w.wbasis.col(1);
-            V3 lng = cross(lat, w.contact_normal);
-            float in = 0;
-            V3 wd = w.hard_point - c.rb.xf.o;
-            V3 cv = (cross(av, wd) + vel) * RL::BT_TO_UU;
-            float base = fabsf(dot(cv, lat));
-            if (base > 5) in = base / (fabsf(dot(cv, lng)) + base);
-            bool tw = c.cfg->three_wheels != 0;
-            float latf = curve_eval(c_curves[tw ? CV_LAT_FRIC_3W : CV_LAT_FRIC], in);
-            float longf = curve_eval(c_curves[CV_LONG_FRIC], in);
-            if (c.handbrake) {
-                float hb = c.handbrake;
-                latf *= (curve_eval(c_curves[CV_HB_LAT], in) - 1) * hb + 1;
-                longf *= (curve_eval(c_curves[CV_HB_LONG], in) - 1) * hb + 1;
-            } else {
-                longf = 1;
-            }
-            if (!(real_throttle != 0)) {
-                float ns = curve_eval(c_curves[CV_NON_STICKY], w.contact_normal.z);
-                latf *= ns;
-                longf *= ns;
-            }
-            c.latf[i] = latf;
-            c.longf[i] = longf;
+    wc.absfs = absfs;
+    wc.real_throttle = real_throttle;
+    wc.world_contact = world_contact;
+    return wc;
+}
+// reads the handbrake stored by update_wheels_car
+RSG_D void update_wheel_friction(Car& c, const WheelsCommon& wc, int i) {
+    WheelRT& w = c.w[i];
+    if (w.ground >= 0) {
+        V3 vel = c.rb.lin_vel, av = c.rb.ang_vel;
+        V3 lat = w.wbasis.col(1);
+        V3 lng = cross(lat, w.contact_normal);
+        float in = 0;
+        V3 wd = w.hard_point - c.rb.xf.o;
+        V3 cv = (cross(av, wd) + vel) * RL::BT_TO_UU;
+        float base = fabsf(dot(cv, lat));
+        if (base > 5) in = base / (fabsf(dot(cv, lng)) + base);
+        bool tw = c.cfg->three_wheels != 0;
+        float latf = curve_eval(c_curves[tw ? CV_LAT_FRIC_3W : CV_LAT_FRIC], in);
+        float longf = curve_eval(c_curves[CV_LONG_FRIC], in);
+        if (c.handbrake) {
+            float hb = c.handbrake;
+            latf *= (curve_eval(c_curves[CV_HB_LAT], in) - 1) * hb + 1;
+            longf *= (curve_eval(c_curves[CV_HB_LONG], in) - 1) * hb + 1;
+        } else {
+            longf = 1;
         }
+        if (!(wc.real_throttle != 0)) {
+            float ns = curve_eval(c_curves[CV_NON_STICKY], w.contact_normal.z);
+            latf *= ns;
+            longf *= ns;
+        }
+        c.latf[i] = latf;
+        c.longf[i] = longf;
     }
-    if (world_contact) {
+}
+RSG_D void update_wheels_sticky(Car& c, const WheelsCommon& wc) {
+    if (wc.world_contact) {
         V3 updir = upwards_from_wheels(c);
-        bool full = (real_throttle != 0) || (absfs > RL::STOPPING_FORWARD_VEL);
+        bool full = (wc.real_throttle != 0) || (wc.absfs > RL::STOPPING_FORWARD_VEL);
         float sfs = c.cfg->three_wheels ? 0 : 0.5f;
         if (full) sfs += 1 - fabsf(updir.z);
         c.rb.total_force += updir * sfs * (RL::GRAVITY_Z * RL::UU_TO_BT) * RL::CAR_MASS_BT;
@@ -1232,41 +1258,60 @@ RSG_D void car_set_respawn(Car& c, int idx, float boost);
 
 // Car::_PreTickUpdate (Car.cpp:58-131) after the four suspension rays: friction, wheels, air
 // control, jump, auto-flip, flip / double jump, auto-roll, suspension and boost.
-RSG_DN void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
+// The rest of Car::_PreTickUpdate after the suspension rays (btVehicleRL::updateVehicleSecond and
+// the car logic, Car.cpp:96-131), by a group of `gsize` threads of one warp (1 or 4; `wl` is the
+// thread's place in it, `gmask` the group's lanes): the wheel-wise parts run one wheel per thread,
+// everything that touches the whole car runs on wl == 0 in the reference's order.
+RSG_DN void car_pre_after_rays_grp(const BatchView& bv, Ctx& a, Car& c, int wl, int gsize, unsigned gmask) {
 #if defined(RSG_PHASE_TIMERS)
     long long ft_ = clock64();
-#define RSG_FT(i) do { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - ft_)); ft_ = t_; } while (0)
+#define RSG_FT(i) do { if (wl == 0) { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - ft_)); ft_ = t_; } } while (0)
 #else
 #define RSG_FT(i)
 #endif
     float dt = bv.dt;
-    calc_friction_impulses(a, c, dt);
+    for (int i = wl; i < 4; i += gsize) calc_friction_impulse(a, c, dt, i);
     RSG_FT(40);
     bool pressed = c.f(F_CTRL_JUMP) && !c.f(F_LAST_JUMP);
     int nwc = 0;
-    for (int i = 0; i < 4; i++) {
-        bool ic = c.w[i].in_contact;
-        c.setf(F_WHEEL0 << i, ic);
-        nwc += ic;
-    }
-    c.setf(F_ON_GROUND, nwc >= 3);
+    for (int i = 0; i < 4; i++) nwc += c.w[i].in_contact;
     float fwd_speed = dot(c.rb.lin_vel, c.rb.xf.b.col(0)) * RL::BT_TO_UU;
-    update_wheels(c, dt, nwc, fwd_speed);
+    const float hb_before = c.handbrake;
+    __syncwarp(gmask);  // every thread has read the state the car part below changes
+    WheelsCommon wc = update_wheels_car(c, dt, nwc, fwd_speed, hb_before, wl == 0);
+    if (wl == 0) {
+        for (int i = 0; i < 4; i++) c.setf(F_WHEEL0 << i, c.w[i].in_contact);
+        c.setf(F_ON_GROUND, nwc >= 3);
+    }
+    __syncwarp(gmask);
+    for (int i = wl; i < 4; i += gsize) update_wheel_friction(c, wc, i);
+    __syncwarp(gmask);
     RSG_FT(41);
-    if (nwc < 3) update_air_torque(c, nwc == 0);
-    else c.setf(F_FLIPPING, false);
-    update_jump(c, dt, pressed);
-    update_auto_flip(c, dt, pressed);
-    update_double_jump_or_flip(c, dt, pressed, fwd_speed);
-    if (c.ctrl[0] && ((nwc > 0 && nwc < 4) || c.f(F_WC_CONTACT))) update_auto_roll(c, nwc);
-    c.setf(F_WC_CONTACT, false);
+    if (wl == 0) {
+        update_wheels_sticky(c, wc);
+        if (nwc < 3) update_air_torque(c, nwc == 0);
+        else c.setf(F_FLIPPING, false);
+        update_jump(c, dt, pressed);
+        update_auto_flip(c, dt, pressed);
+        update_double_jump_or_flip(c, dt, pressed, fwd_speed);
+        if (c.ctrl[0] && ((nwc > 0 && nwc < 4) || c.f(F_WC_CONTACT))) update_auto_roll(c, nwc);
+        c.setf(F_WC_CONTACT, false);
+    }
     RSG_FT(42);
-    update_suspension(c, dt);
+    for (int i = wl; i < 4; i += gsize) suspension_force(c, i);
+    __syncwarp(gmask);
     RSG_FT(43);
-    apply_friction_impulses(c, dt);
-    RSG_FT(44);
-    update_boost(c, dt);
-    RSG_FT(45);
+    if (wl == 0) {
+        apply_suspension(c, dt);
+        apply_friction_impulses(c, dt);
+        RSG_FT(44);
+        update_boost(c, dt);
+        RSG_FT(45);
+    }
+    __syncwarp(gmask);
+}
+RSG_D void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
+    car_pre_after_rays_grp(bv, a, c, 0, 1, 1u << (threadIdx.x & 31));
 }
 
 // Start of Car::_PreTickUpdate for a car that is not demolished and was not at the last
@@ -3813,28 +3858,30 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
     }
     __syncthreads();
     RSG_SUB(10);
-    {
-        const int u = spread_unit(tid, nthreads);
+    {  // four threads per car (one per wheel), cars spread over the warps
+        const int nw = nthreads >> 5, lane = tid & 31, g = lane >> 2, wl = lane & 3;
+        const int u = g * nw + (tid >> 5);
+        const unsigned gmask = 0xfu << (4 * g);
         Ctx& a = B(u / MC);
         int k = u % MC;
         if (u < B.nact * MC && !a.serial && k < a.ncars) {
-        if (a.on_car) {
-            if (k == 0)
-                for (int kk = 0; kk < a.ncars; kk++) car_pre_after_rays(bv, a, a.cars[a.order[kk]]);
-        } else {
+            if (a.on_car) {
+                if (k == 0)
+                    for (int kk = 0; kk < a.ncars; kk++) car_pre_after_rays_grp(bv, a, a.cars[a.order[kk]], wl, 4, gmask);
+            } else {
 #if defined(RSG_PHASE_TIMERS)
-            long long at0_ = clock64();
+                long long at0_ = clock64();
 #endif
-            car_pre_after_rays(bv, a, a.cars[k]);
+                car_pre_after_rays_grp(bv, a, a.cars[k], wl, 4, gmask);
 #if defined(RSG_PHASE_TIMERS)
-            {
-                long long dtc = clock64() - at0_;
-                atomicAdd(&g_phase_cycles[28], (unsigned long long)dtc);
-                atomicAdd(&g_phase_cycles[29], 1ull);
-                atomicMax(&g_phase_cycles[30], (unsigned long long)dtc);
+                if (wl == 0) {
+                    long long dtc = clock64() - at0_;
+                    atomicAdd(&g_phase_cycles[28], (unsigned long long)dtc);
+                    atomicAdd(&g_phase_cycles[29], 1ull);
+                    atomicMax(&g_phase_cycles[30], (unsigned long long)dtc);
+                }
+#endif
             }
-#endif
-        }
         }
     }
     if (bv.has_arena)
