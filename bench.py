@@ -274,10 +274,11 @@ def run_gpu(args, rank: int, world: int):
             import torch.distributed as dist
             dist.barrier()
 
-    # ---- value: device-resident inputs, one launch per step
+    # ---- value: device-resident inputs, one launch per step.  The warm-up steps also let the
+    # batch's block-shape tuner finish its trials (each trial is read after its launch completes).
     for s in range(args.warmup):
         batch.step_async(d_seq[s].data_ptr(), TICKS_PER_STEP)
-    batch.sync()
+        batch.sync()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = ClockSampler(dev)

@@ -192,6 +192,16 @@ struct rsg_batch {
     int game_mode = 0;
     int device = 0;
     int warps_per_block = 8;  // arenas per block of the tick kernel
+    // block-shape tuner: candidate arenas-per-block values tried on the first launches, each
+    // timed with a pair of events that is read without blocking on a later launch
+    bool tuning = false;
+    std::vector<int> tune_cand;
+    std::vector<double> tune_ms_per_tick;  // < 0: not measured yet
+    int tune_next = 0;                     // next candidate to launch
+    int tune_pending = -1;                 // candidate whose events are in flight
+    int tune_pending_ticks = 0;
+    int tune_skip = 1;  // launches before the first trial (the first launch also loads the module)
+    cudaEvent_t tune_ev[2] = {nullptr, nullptr};
     BatchBuffers buf{};
     cudaStream_t stream = nullptr;
     std::vector<CarCfgDev> cfgs;
@@ -408,6 +418,79 @@ int rsg_get_car_config_preset(int preset, rsg_car_config* out) {
     return RSG_OK;
 }
 
+namespace {
+
+// Candidate arenas-per-block values for the tick kernel: the ones that reach the fewest waves of
+// blocks over the device's SMs (one block per SM: the tick kernel's shared memory allows no
+// more), largest first.  Arenas never depend on the block they share, so any shape gives the
+// same results and the first real launches can serve as the trials.
+void setup_tuner(rsg_batch* b, int A, int MC) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess || sms <= 0) return;
+    const int per_arena = tick_smem_per_arena(MC);
+    int best_waves = 1 << 30;
+    std::vector<std::pair<int, int>> opts;  // (waves, wpb)
+    for (int w = 8; w >= 4; w--) {
+        if (per_arena * w > 227 * 1024) continue;
+        int blocks = (A + w - 1) / w;
+        int waves = (blocks + sms - 1) / sms;
+        opts.push_back({waves, w});
+        best_waves = std::min(best_waves, waves);
+    }
+    for (auto& o : opts)
+        if (o.first == best_waves) b->tune_cand.push_back(o.second);
+    if (b->tune_cand.size() <= 1) {
+        if (!b->tune_cand.empty()) b->warps_per_block = b->tune_cand[0];
+        return;
+    }
+    if (cudaEventCreate(&b->tune_ev[0]) != cudaSuccess || cudaEventCreate(&b->tune_ev[1]) != cudaSuccess) return;
+    b->tune_ms_per_tick.assign(b->tune_cand.size(), -1.0);
+    b->tuning = true;
+}
+
+// Collects a finished trial (without waiting) and chooses the shape of the next launch.
+void tuner_before_launch(rsg_batch* b) {
+    if (!b->tuning) return;
+    if (b->tune_pending >= 0 && cudaEventQuery(b->tune_ev[1]) == cudaSuccess) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, b->tune_ev[0], b->tune_ev[1]) == cudaSuccess && b->tune_pending_ticks > 0)
+            b->tune_ms_per_tick[b->tune_pending] = ms / b->tune_pending_ticks;
+        b->tune_pending = -1;
+    }
+    bool all = true;
+    for (double v : b->tune_ms_per_tick) all = all && v >= 0;
+    if (all) {
+        size_t best = 0;
+        for (size_t i = 1; i < b->tune_cand.size(); i++)
+            if (b->tune_ms_per_tick[i] < b->tune_ms_per_tick[best]) best = i;
+        b->warps_per_block = b->tune_cand[best];
+        b->tuning = false;
+        return;
+    }
+    if (b->tune_pending < 0 && b->tune_next < (int)b->tune_cand.size())
+        b->warps_per_block = b->tune_cand[b->tune_next];
+}
+
+// Launches `ticks` ticks, timing the launch when it is a trial of the tuner.
+cudaError_t tuned_launch(rsg_batch* b, const rsg_car_controls* controls, int ticks) {
+    if (b->tuning && b->tune_skip > 0) {
+        b->tune_skip--;
+        return launch_tick(b->buf, controls, ticks, b->warps_per_block, b->stream);
+    }
+    tuner_before_launch(b);
+    const bool trial = b->tuning && b->tune_pending < 0 && b->tune_next < (int)b->tune_cand.size();
+    if (trial) cudaEventRecord(b->tune_ev[0], b->stream);
+    cudaError_t e = launch_tick(b->buf, controls, ticks, b->warps_per_block, b->stream);
+    if (trial && e == cudaSuccess) {
+        cudaEventRecord(b->tune_ev[1], b->stream);
+        b->tune_pending = b->tune_next++;
+        b->tune_pending_ticks = ticks;
+    }
+    return e;
+}
+
+}  // namespace
+
 rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate) {
     if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_THE_VOID) {
         fail(RSG_ERR_ARG, "game mode not supported (soccar and the void only)");
@@ -440,9 +523,11 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
         fail(RSG_ERR_STATE, "the mesh was loaded on another device");
         return nullptr;
     }
-    if (const char* w = std::getenv("RSG_TICK_WARPS_PER_BLOCK")) {  // launch-shape override for tuning runs
+    if (const char* w = std::getenv("RSG_TICK_WARPS_PER_BLOCK")) {  // fixed launch shape, no tuning
         int v = std::atoi(w);
         if (v >= 1 && v <= 8) b->warps_per_block = v;
+    } else {
+        setup_tuner(b, (int)n_arenas, (int)max_cars_per_arena);
     }
     BatchBuffers& B = b->buf;
     B.A = (int)n_arenas;
@@ -506,6 +591,8 @@ void rsg_batch_destroy(rsg_batch* b) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
+    for (cudaEvent_t e : b->tune_ev)
+        if (e) cudaEventDestroy(e);
     delete b;
 }
 
@@ -857,7 +944,7 @@ int rsg_step(rsg_batch* b, int ticks) {
     RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
     for (int done = 0; done < ticks;) {
         int n = std::min(chunk, ticks - done);
-        RSG_CUDA(launch_tick(b->buf, nullptr, n, b->warps_per_block, b->stream));
+        RSG_CUDA(tuned_launch(b, nullptr, n));
         done += n;
         if (b->buf.event_mask && (rc = drain_events(b))) return rc;
     }
@@ -871,7 +958,7 @@ int rsg_step_async(rsg_batch* b, const rsg_car_controls* d_controls, int ticks) 
     int rc;
     if ((rc = set_device(b))) return rc;
     RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
-    RSG_CUDA(launch_tick(b->buf, d_controls, ticks, b->warps_per_block, b->stream));
+    RSG_CUDA(tuned_launch(b, d_controls, ticks));
     return RSG_OK;
 }
 
