@@ -51,5 +51,24 @@ def test_portable_restatement_within_tolerance(golden):
         for t in (1, 8):
             cars, ball, _ = snaps[t - 1]
             check_continuous(cars, ball, golden.cars_at(si, t), golden.ball_at(si, t), t, f"scenario {si}")
-        epa = golden.epa_tick(si)
-        check_discrete(golden, si, snaps, 120 if epa < 0 else epa)
+        check_discrete(golden, si, snaps, 120)
+
+
+@pytest.mark.skipif(platform.machine() not in ("x86_64", "AMD64"), reason="SSE emulation build is x86 only")
+def test_sse_restatement_bit_exact_through_epa(golden):
+    """Scenarios where the reference runs Bullet's GJK-EPA penetration solver: the restatement
+    follows it bit for bit over every one of the 120 ticks (the reference run live here)."""
+    import os
+    ref_so = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "librsref.so")
+    if not os.path.exists(ref_so):
+        pytest.skip("reference library not built here")
+    epa_scenarios = [si for si in range(golden.S) if golden.epa_tick(si) >= 0]
+    assert epa_scenarios
+    for si in epa_scenarios:
+        ref = play("ref", golden, si, 120)
+        got = play("oracle_sse", golden, si, 120)
+        for t in range(120):
+            for f in ("pos", "vel", "ang_vel", "rot_mat"):
+                assert got[t][0][f].tobytes() == ref[t][0][f].tobytes(), f"scenario {si} tick {t + 1} car {f}"
+            for f in ("pos", "vel", "ang_vel"):
+                assert got[t][1][f].tobytes() == ref[t][1][f].tobytes(), f"scenario {si} tick {t + 1} ball {f}"
