@@ -543,6 +543,11 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
         cudaMemset(*p, 0, bytes);
         return true;
     };
+    if (cudaError_t pe = ensure_epa_pool(); pe != cudaSuccess) {
+        delete b;
+        cuda_fail(pe, "EPA work pool");
+        return nullptr;
+    }
     cudaError_t se = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (se != cudaSuccess) {
         cuda_fail(se, "cudaStreamCreateWithFlags");

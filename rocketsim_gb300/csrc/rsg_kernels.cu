@@ -4,6 +4,8 @@
 // rsg_tick_kernel: one thread advances one arena by `ticks` ticks (load the
 // arena's SoA state, run the ticks in registers / local memory, store it back).
 // Arenas are independent, so the grid is simply ceil(A / block) blocks.
+#include <mutex>
+
 #include "rsg_kernels.h"
 #include "rsg_tick.cuh"
 
@@ -127,6 +129,30 @@ __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rs
 }
 
 int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars).bytes; }
+
+// The EPA work-slot pool of the current device, made once per device for the process.
+cudaError_t ensure_epa_pool() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return cudaSuccess;
+    const int nslots = 1024;
+    uint32_t* locks = nullptr;
+    epa::Slot* slots = nullptr;
+    if ((e = cudaMalloc((void**)&locks, sizeof(uint32_t) * nslots)) != cudaSuccess) return e;
+    if ((e = cudaMemset(locks, 0, sizeof(uint32_t) * nslots)) != cudaSuccess) return e;
+    if ((e = cudaMalloc((void**)&slots, sizeof(epa::Slot) * nslots)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(epa::g_epa_lock, &locks, sizeof(locks))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(epa::g_epa_slots, &slots, sizeof(slots))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(epa::g_epa_nslots, &nslots, sizeof(nslots))) != cudaSuccess) return e;
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
+    done[dev] = true;
+    return cudaSuccess;
+}
 
 cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int warps_per_block,
                         cudaStream_t st) {

@@ -47,6 +47,9 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
 // Shared memory one arena needs in the tick kernel.
 int tick_smem_per_arena(int max_cars);
 
+// Allocates the current device's pool of EPA work slots (once per device; about 14 MB).
+cudaError_t ensure_epa_pool();
+
 // Records `msg` as the calling thread's last error (rsg_get_last_error) and returns `code`.
 int report_error(int code, const char* msg);
 

@@ -1864,11 +1864,15 @@ struct Simplex {
     RSG_D void points(V3& p1, V3& p2) { update(); p1 = cP1; p2 = cP2; }
 };
 
+}  // namespace rsg
+#include "rsg_epa.cuh"
+namespace rsg {
+
 struct GjkOut {
     bool valid;
     V3 normal, point_on_b;
     float dist;
-    bool epa_needed;
+    bool epa_needed;  // the pair needed EPA and no work slot was free (WARN_EPA_SKIPPED)
 };
 
 RSG_DN GjkOut gjk(const Convex& A, const Xf& ta_in, const Convex& B, const Xf& tb_in, float max_dist2) {
@@ -1929,8 +1933,45 @@ RSG_DN GjkOut gjk(const Convex& A, const Xf& ta_in, const Convex& B, const Xf& t
     }
     bool catch_deg = degenerate && ((distance + margin) < 0.01f);
     if (!is_valid || catch_deg) {
-        out.epa_needed = true;
-        if (!is_valid) return out;
+        // penetration depth (btGjkPairDetector.cpp:850-922)
+        const int slot = epa::acquire_slot();
+        if (slot < 0) {
+            out.epa_needed = true;
+            if (!is_valid) return out;
+        } else {
+            V3 sep_axis(0, 0, 0), tA, tB;
+            const bool valid2 = epa::calc_pen_depth(A, ta, B, tb, epa::g_epa_slots + slot, sep_axis, tA, tB);
+            epa::release_slot(slot);
+            if (valid2) {
+                V3 tn = tB - tA;
+                float l2 = len2(tn);
+                if (l2 <= SIMD_EPS * SIMD_EPS) {
+                    tn = sep_axis;
+                    l2 = len2(sep_axis);
+                }
+                if (l2 > SIMD_EPS * SIMD_EPS) {
+                    tn = tn / sqrtf(l2);
+                    const float d2 = -len(tA - tB);
+                    if (!is_valid || (d2 < distance)) {
+                        distance = d2;
+                        pA = tA;
+                        pB = tB;
+                        normalInB = tn;
+                        is_valid = true;
+                    }
+                }
+            } else if (len2(sep_axis) > 0.f) {
+                const float d2 = len(tA - tB) - margin;
+                if (!is_valid || (d2 < distance)) {
+                    distance = d2;
+                    pA = tA - sep_axis * mA;
+                    pB = tB + sep_axis * mB;
+                    normalInB = normalized(sep_axis);
+                    is_valid = true;
+                }
+            }
+            if (!is_valid) return out;
+        }
     }
     if (is_valid && ((distance < 0) || (distance * distance < max_dist2))) {
         V3 amn, amx, bmn, bmx;  // m_fixContactNormalDirection

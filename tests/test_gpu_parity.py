@@ -38,13 +38,37 @@ def test_gpu_matches_reference_golden(golden):
         for t in (1, 8):
             cars, ball, _ = snaps[t - 1][si]
             check_continuous(cars, ball, golden.cars_at(si, t), golden.ball_at(si, t), t, f"golden scenario {si}")
-        epa = golden.epa_tick(si)
-        for t in range(120 if epa < 0 else epa):
+        for t in range(120):
             cars, ball, pads = snaps[t][si]
             np.testing.assert_array_equal(discrete_car(cars).astype(np.float32), golden.disc_cars(si)[t],
                                           err_msg=f"golden scenario {si} tick {t + 1}: car discrete state")
             np.testing.assert_array_equal(discrete_pads(pads).astype(np.float32), golden.disc_pads(si)[t],
                                           err_msg=f"golden scenario {si} tick {t + 1}: pads")
+    batch.close()
+
+
+def test_gpu_follows_restatement_through_epa(golden):
+    """The golden scenarios where the reference runs Bullet's GJK-EPA: the GPU tick (EPA in a pooled
+    work slot) against the portable restatement over all 120 ticks, continuous state within the
+    8-tick tolerance at the EPA tick and 8 ticks after it, discrete state equal every tick, and no
+    arena flagged for a skipped EPA."""
+    epa_scenarios = [si for si in range(golden.S) if golden.epa_tick(si) >= 0]
+    assert epa_scenarios
+    scs = [golden.scenarios[si] for si in epa_scenarios]
+    batch, snaps = play_gpu(scs, 120)
+    flags = batch.device_flags()
+    assert not (int(np.bitwise_or.reduce(flags)) & 0x100), flags
+    for k, si in enumerate(epa_scenarios):
+        ref = []
+        a, _ = run_cpu("oracle", scs[k], 120, lambda t, a, ids: ref.append(cpu_snapshot(a, ids)))
+        a.close()
+        e = golden.epa_tick(si)
+        for t in (e + 1, min(e + 8, 120)):
+            cars, ball, _ = snaps[t - 1][k]
+            check_continuous(cars, ball, ref[t - 1][0], ref[t - 1][1], 8, f"epa scenario {si} tick {t}")
+        for t in range(120):
+            np.testing.assert_array_equal(discrete_car(snaps[t][k][0]), discrete_car(ref[t][0]),
+                                          err_msg=f"epa scenario {si} tick {t + 1}")
     batch.close()
 
 
@@ -64,19 +88,15 @@ def test_gpu_matches_restatement_random():
     batch, snaps = play_gpu(scs, 120)
     for si, sc in enumerate(scs):
         ref = []
-        first_epa = [-1]
 
         def rec(t, a, ids):
             ref.append(cpu_snapshot(a, ids))
-            if first_epa[0] < 0 and a.counters()[3] > 0:
-                first_epa[0] = t
         a, _ = run_cpu("oracle", sc, 120, rec)
         a.close()
         for t in (1, 8):
             cars, ball, _ = snaps[t - 1][si]
             check_continuous(cars, ball, ref[t - 1][0], ref[t - 1][1], t, f"random scenario {si}")
-        until = 120 if first_epa[0] < 0 else first_epa[0]
-        for t in range(until):
+        for t in range(120):
             np.testing.assert_array_equal(discrete_car(snaps[t][si][0]), discrete_car(ref[t][0]),
                                           err_msg=f"random scenario {si} tick {t + 1}")
             np.testing.assert_array_equal(discrete_pads(snaps[t][si][2]), discrete_pads(ref[t][2]),
