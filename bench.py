@@ -19,7 +19,8 @@ The same line carries ``adjoint``: gradient steps (forward with checkpoints,
 loss, hand-written adjoint backward) of 60-tick air-control rollouts over
 8192 instances, replayed as one captured CUDA graph (and eagerly), their
 relative error against FP64 central finite differences on a few instances,
-and the backward / forward cost ratio of the C-ABI calls.
+and the backward / forward cost ratio of the C-ABI calls; and ``ground_adjoint``:
+the same for 120-tick ground-driving rollouts (eager steps).
 
 ``--impl reference`` times the CPU implementation of the same tick on the
 host cores instead: the reference library built from its sources when it is
@@ -548,6 +549,156 @@ def adjoint_cpu_check(case, g_gpu: np.ndarray, k: int):
     return float((num / den).max()), k / el, el
 
 
+# ---------------------------------------------------------------- adjoint (ground driving)
+GROUND_TICKS = 120
+GROUND_SETTLE = 24
+GROUND_WORKLOAD = ("ground-driving adjoint: 8192 instances x (1 Octane on the floor + ball), 120 ticks, controls "
+                   "throttle/steer in [-1, 1] and relaxed boost in [0, 1], checkpoints every 16 ticks")
+
+
+def _smooth_controls(rng, ticks: int, n: int, lo: float, hi: float, knots: int = 4) -> np.ndarray:
+    """[ticks, n] piecewise-linear signals through `knots` uniform values in [lo, hi] per instance."""
+    vals = rng.uniform(lo, hi, (knots, n))
+    pos = np.arange(ticks) / max(ticks - 1, 1) * (knots - 1)
+    k = np.minimum(pos.astype(int), knots - 2)
+    f = (pos - k)[:, None]
+    return vals[k] * (1 - f) + vals[k + 1] * f
+
+
+def ground_adjoint_case(n: int, seed: int, dev: str):
+    """Ground-driving workload: an Octane on the floor within 800 uu of the centre, random heading,
+    forward speed 0..1200 uu/s, settled for 24 ticks at throttle 0.5 by the rollout itself; smooth
+    random controls inside the ranges; a drive_loss target 50..150 uu from where an uncontrolled
+    rollout would end and a random target heading.  Bullet units."""
+    import torch
+    from rocketsim_gb300 import adjoint
+    rng = np.random.default_rng(seed)
+    s = np.zeros((n, 39), np.float32)
+    yaw = rng.uniform(0, 2 * np.pi, n)
+    c, si = np.cos(yaw), np.sin(yaw)
+    s[:, 0:2] = rng.uniform(-800, 800, (n, 2)) / 50.0
+    s[:, 2] = 17.0 / 50.0
+    speed = rng.uniform(0, 1200, n) / 50.0
+    s[:, 3], s[:, 4] = speed * c, speed * si
+    s[:, 9:18] = np.stack([c, -si, np.zeros(n), si, c, np.zeros(n), np.zeros(n), np.zeros(n), np.ones(n)], 1)
+    s[:, 33:36] = np.array([2500.0, -3500.0, 1200.0]) / 50.0
+    s[:, 36:39] = rng.uniform(-300, 300, (n, 3)) / 50.0
+    settle = np.zeros((GROUND_SETTLE, n, 4), np.float32)
+    settle[..., 0] = 0.5
+    with torch.no_grad():
+        s = adjoint.ground_rollout(torch.from_numpy(s).to(dev), torch.from_numpy(settle).to(dev)).cpu().numpy()
+    u = np.zeros((GROUND_TICKS, n, 4), np.float32)
+    u[..., 0] = _smooth_controls(rng, GROUND_TICKS, n, 0.3, 0.9)
+    u[..., 1] = _smooth_controls(rng, GROUND_TICKS, n, -0.6, 0.6)
+    u[..., 2] = _smooth_controls(rng, GROUND_TICKS, n, 0.2, 0.8)
+    ang = rng.uniform(0, 2 * np.pi, n)
+    target_xy = s[:, 0:2] + s[:, 3:5] * (GROUND_TICKS / 120.0) + \
+        np.stack([np.cos(ang), np.sin(ang)], 1) * rng.uniform(1, 3, (n, 1))
+    ang = rng.uniform(0, 2 * np.pi, n)
+    target_dir = np.stack([np.cos(ang), np.sin(ang), np.zeros(n)], 1)
+    return s, u, target_xy.astype(np.float32), target_dir.astype(np.float32)
+
+
+def run_ground_adjoint(args, dev: int):
+    """Gradient steps of the ground-driving workload, eager: forward with checkpoints, loss, backward."""
+    import ctypes as C
+    import torch
+    from rocketsim_gb300 import abi, adjoint
+    from rocketsim_gb300.arena import car_config
+    n = args.adj_instances
+    d = f"cuda:{dev}"
+    s, u, txy, tdir = ground_adjoint_case(n, 2468, d)
+    ds = torch.from_numpy(s).to(d)
+    du = torch.from_numpy(u).to(d).requires_grad_(True)
+    t_xy, t_dir = torch.from_numpy(txy).to(d), torch.from_numpy(tdir).to(d)
+
+    def grad_step():
+        du.grad = None
+        fin, flags = adjoint.ground_rollout(ds, du, ckpt_every=16, return_flags=True)
+        adjoint.drive_loss(fin, t_xy, t_dir).sum().backward()
+        return flags
+
+    for _ in range(args.warmup):
+        flags = grad_step()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        du.grad = None
+        ev[k][0].record()
+        fin = adjoint.ground_rollout(ds, du, ckpt_every=16)
+        ev[k][1].record()
+        adjoint.drive_loss(fin, t_xy, t_dir).sum().backward()
+        ev[k][2].record()
+    torch.cuda.synchronize()
+    fwd = [a.elapsed_time(b) for a, b, _ in ev]
+    bwd = [b.elapsed_time(c) for _, b, c in ev]
+    total_ms = sum(a.elapsed_time(c) for a, _, c in ev)
+    g_gpu = du.grad[:, :args.adj_check].detach().cpu().numpy().astype(np.float64)
+    with torch.no_grad():
+        adjoint.ground_rollout(ds, du.detach())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            adjoint.ground_rollout(ds, du.detach())
+        e1.record()
+        torch.cuda.synchronize()
+        plain_fwd_ms = e0.elapsed_time(e1) / args.steps
+    # the C-ABI calls alone
+    lib = abi.load(build_if_missing=False)
+    cfg = car_config(abi.CAR_OCTANE)
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    ck = torch.empty(((GROUND_TICKS + 15) // 16, n, 39), device=d)
+    fin = torch.empty_like(ds)
+    gfin = torch.randn_like(ds)
+    gu = torch.empty_like(du)
+    nb = C.c_size_t()
+    abi.check(lib.rsg_ground_backward_workspace_size(n, GROUND_TICKS, C.byref(nb)), "workspace size")
+    work = torch.empty(nb.value, dtype=torch.uint8, device=d)
+    strm = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    kf, kb = [], []
+    for k in range(args.warmup + args.steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        abi.check(lib.rsg_ground_forward(C.byref(cfg), 120.0, n, GROUND_TICKS, P(ds), P(du), P(fin), P(ck), 16, None,
+                                         strm), "rsg_ground_forward")
+        e[1].record()
+        abi.check(lib.rsg_ground_backward(C.byref(cfg), 120.0, n, GROUND_TICKS, P(du), P(ck), 16, P(gfin), P(gu),
+                                          None, P(work), nb.value, strm), "rsg_ground_backward")
+        e[2].record()
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            kf.append(e[0].elapsed_time(e[1]))
+            kb.append(e[1].elapsed_time(e[2]))
+    return {"value": n * args.steps / (total_ms / 1e3), "ms_per_step": total_ms / args.steps,
+            "ms_forward_ckpt": statistics.median(fwd), "ms_forward_plain": plain_fwd_ms,
+            "ms_backward": statistics.median(bwd), "backward_over_forward": statistics.median(bwd) / plain_fwd_ms,
+            "kernel_ms_forward_ckpt": statistics.median(kf), "kernel_ms_backward": statistics.median(kb),
+            "workspace_bytes": nb.value, "flagged_instances": int((flags != 0).sum()),
+            "case": (s, u, txy, tdir), "g_gpu": g_gpu}
+
+
+GROUND_FD_TICKS = (0, 30, 60, 90, 110, 119)
+
+
+def ground_cpu_check(case, g_gpu: np.ndarray, k: int):
+    """FP64 central finite differences (step 1e-4) of the ground restatement for the first k
+    instances at six ticks x three controls: the relative error of the GPU adjoint and the CPU's
+    rate of such gradient entries."""
+    from oracle import ground_fp64 as Gr
+    s, u, txy, tdir = case
+    s64, u64 = s[:k].astype(np.float64), u[:, :k].astype(np.float64)
+    which = [(t, c) for t in GROUND_FD_TICKS for c in range(3)]
+    t0 = time.perf_counter()
+    gfd = Gr.fd_grad(s64, u64, Gr.car_geometry(), 1.0 / 120.0,
+                     lambda f: Gr.drive_loss(f, txy[:k].astype(np.float64), tdir[:k].astype(np.float64)),
+                     h=1e-4, which=which)
+    el = time.perf_counter() - t0
+    a = np.stack([g_gpu[t, :k, c] for t, c in which], 1)
+    b = np.stack([gfd[t, :, c] for t, c in which], 1)
+    rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
+    return float(rel.max()), k * len(which) / el, el, len(which)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -599,6 +750,8 @@ def main():
         return
     adj = run_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
     adj_err, cpu_grads, cpu_el = adjoint_cpu_check(adj["case"], adj["g_gpu"], args.adj_check)
+    gadj = run_ground_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
+    g_err, g_cpu_rate, g_cpu_el, g_entries = ground_cpu_check(gadj["case"], gadj["g_gpu"], min(args.adj_check, 2))
     single, _, _, kind = cpu_ticks_per_second(1, args.cpu_seconds)
     allc, n, el, _ = cpu_ticks_per_second(threads, args.cpu_seconds)
     line = {
@@ -629,6 +782,20 @@ def main():
             "cpu_baseline": {"value": cpu_grads, "unit": "grads/s", "cores": 1, "kind": "port",
                              "sample": f"FP64 central differences of the numpy restatement, "
                                        f"{args.adj_check} instances x 240 inputs x 2 rollouts ({cpu_el:.1f} s)"}},
+        "ground_adjoint": {
+            "metric": "adjoint grads/s", "value": gadj["value"], "unit": "grads/s (120-tick ground rollouts)",
+            "workload": GROUND_WORKLOAD, "rel_err_max_vs_fp64_fd": g_err,
+            "rel_err_sample": f"{min(args.adj_check, 2)} instances x {g_entries} control entries",
+            "ms_per_step": gadj["ms_per_step"], "step": "eager: forward + loss + backward",
+            "ms_forward_with_checkpoints": gadj["ms_forward_ckpt"], "ms_forward_plain": gadj["ms_forward_plain"],
+            "ms_backward": gadj["ms_backward"], "backward_over_forward": gadj["backward_over_forward"],
+            "c_abi_ms_forward_with_checkpoints": gadj["kernel_ms_forward_ckpt"],
+            "c_abi_ms_backward": gadj["kernel_ms_backward"], "workspace_bytes": gadj["workspace_bytes"],
+            "flagged_instances": gadj["flagged_instances"], "gpu_launches_per_step": 3,
+            "cpu_baseline": {"value": g_cpu_rate, "unit": "gradient entries/s", "cores": 1, "kind": "port",
+                             "sample": f"FP64 central differences of the numpy restatement, "
+                                       f"{min(args.adj_check, 2)} instances x {g_entries} entries x 2 rollouts "
+                                       f"({g_cpu_el:.1f} s)"}},
     }
     print(json.dumps(line))
 

@@ -332,6 +332,40 @@ int rsg_air_backward_noalloc(const rsg_car_config* car, float tick_rate, int n, 
                              const float* d_ckpt, int ckpt_every, const float* d_grad_final, float* d_grad_controls,
                              float* d_grad_state0, void* stream);
 
+/* ---- differentiable ground-driving rollouts -------------------------------- */
+
+/* Rollouts of one car driving on the arena floor (z = 0) and the ball per
+ * instance, and their adjoint.  No counterpart in the reference: they restate
+ * the ground path of Arena::Step for a car with four wheels on the floor and a
+ * chassis that touches nothing (btVehicleRL::rayCast, calcFrictionImpulses,
+ * updateSuspension, applyFrictionImpulses, btVehicleRL.cpp:66-395;
+ * Car::_UpdateWheels, Car.cpp:339-484, without handbrake; the ground boost
+ * force of Car::_UpdateBoost, Car.cpp:486-533, with the boost input relaxed to
+ * [0, 1] and its full throttle to throttle + boost (1 - throttle); gravity,
+ * integrateTransform and the clamps of Car::_FinishPhysicsTick) for
+ * gradient-based control.  For boost inputs of exactly 0 or 1 held over the
+ * rollout the forward follows rsg_step on a car driving on the floor.
+ *
+ * All pointers are device pointers.  State: [n][39] floats per instance, Bullet
+ * units: car position, velocity, angular velocity, basis rows (9), front steer
+ * angle, engine force, brake force, lateral friction factor per wheel (4),
+ * longitudinal friction factor per wheel (4), extra push-back per wheel (4),
+ * ball position, ball velocity.  Controls: [ticks][n][4] = throttle and steer
+ * in [-1, 1], boost in [0, 1], one unused float.  d_flags (may be NULL)
+ * receives per instance the OR over the ticks of bit 0 (a wheel's ray missed
+ * the floor) and bit 1 (the car tilted past the suspension's contact limit),
+ * the ticks that left the model.  Checkpoints, gradients and workspace as for
+ * the air rollouts, with 39 floats per state: the workspace is
+ * rsg_ground_backward_workspace_size bytes (156 bytes per instance and tick).
+ * The gradient at boost 1 is the one-sided derivative from inside [0, 1]. */
+int rsg_ground_forward(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_state0,
+                       const float* d_controls, float* d_final, float* d_ckpt, int ckpt_every, int* d_flags,
+                       void* stream);
+int rsg_ground_backward_workspace_size(int n, int ticks, size_t* bytes);
+int rsg_ground_backward(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_controls,
+                        const float* d_ckpt, int ckpt_every, const float* d_grad_final, float* d_grad_controls,
+                        float* d_grad_state0, void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* Device flags of every arena after the last step ([n_arenas] words).  Bits 0-7
  * are capacity overflows (the step also returns RSG_ERR_DEVICE); bit 8 marks a
  * box contact deeper than GJK resolves and bit 9 overlapping car boxes, two

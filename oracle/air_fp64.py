@@ -153,8 +153,16 @@ def car_tick(x: np.ndarray, u: np.ndarray, iinv: np.ndarray, dt: float) -> np.nd
     total_force = total_force + np.array([0.0, 0.0, GRAVITY_Z * UU_TO_BT]) * CAR_MASS_BT
     v1 = v + total_force / CAR_MASS_BT * dt
     w1 = w + np.einsum("nij,nj->ni", iw, total_torque) * dt
+    out = x.copy()
+    out[:, 0:3], out[:, 3:6], out[:, 6:9], B1 = integrate(p, B, v1, w1, dt)
+    out[:, 9:18] = B1.reshape(-1, 9)
+    return out
+
+
+def integrate(p, B, v1, w1, dt):
+    """btTransformUtil::integrateTransform of position and basis with the velocities after the
+    solver, then the speed clamps of Car::_FinishPhysicsTick; returns p, v, w, B after the tick."""
     p1 = p + v1 * dt
-    # integrateTransform, angular part
     ang = np.sqrt(np.einsum("ni,ni->n", w1, w1))
     ang = np.where(ang * ang > FLT_EPSILON, ang, 0.0)
     ang = np.minimum(ang, ANGULAR_MOTION_THRESHOLD / dt)
@@ -165,12 +173,7 @@ def car_tick(x: np.ndarray, u: np.ndarray, iinv: np.ndarray, dt: float) -> np.nd
     dorn = np.concatenate([w1 * s[:, None], np.cos(ang * dt * 0.5)[:, None]], axis=1)
     q = _q_mul(dorn, _q_from_m(B))
     q = q / np.sqrt(np.einsum("ni,ni->n", q, q))[:, None]
-    out = x.copy()
-    out[:, 0:3] = p1
-    out[:, 3:6] = _clamp_len(v1, CAR_MAX_SPEED * UU_TO_BT)
-    out[:, 6:9] = _clamp_len(w1, CAR_MAX_ANG_SPEED)
-    out[:, 9:18] = _m_from_q(q).reshape(-1, 9)
-    return out
+    return (p1, _clamp_len(v1, CAR_MAX_SPEED * UU_TO_BT), _clamp_len(w1, CAR_MAX_ANG_SPEED), _m_from_q(q))
 
 
 def ball_tick(x: np.ndarray, dt: float) -> np.ndarray:

@@ -271,6 +271,15 @@ class SimArena:
         self.lib[self.p + "wheel_debug"](self.h, car_id, buf)
         return [list(buf[i * 16:(i + 1) * 16]) for i in range(4)]
 
+    def vehicle_state(self, car_id: int) -> list[float]:
+        """Front steer angle, engine force, brake, lateral (4), longitudinal (4) friction
+        factors and extra push-back (4) of a car (reference library only)."""
+        buf = (C.c_float * 15)()
+        fn = self.lib[self.p + "get_vehicle_state"]
+        fn.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_float)]
+        assert fn(self.h, car_id, buf) == 0
+        return list(buf)
+
     def wheel_internals(self, car_id: int) -> list[float]:
         buf = (C.c_float * 8)()
         self.lib[self.p + "get_wheel_internals"](self.h, car_id, buf)

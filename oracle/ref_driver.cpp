@@ -343,6 +343,24 @@ int rsref_get_wheel_internals(void* h, uint32_t id, float* out8) {
     return 0;
 }
 
+// The vehicle state the next tick starts from that CarState leaves out (btVehicleRL.h:9-27,
+// btWheelInfo.h:73-101): front steer angle, engine force, brake, then per wheel the lateral and
+// longitudinal friction factors and the extra push-back (15 floats).
+int rsref_get_vehicle_state(void* h, uint32_t id, float* out15) {
+    Car* car = FindCar((RefArena*)h, id);
+    if (!car) return -1;
+    auto& wi = car->_bulletVehicle.m_wheelInfo;
+    out15[0] = wi[0].m_steerAngle;
+    out15[1] = wi[0].m_engineForce;
+    out15[2] = wi[0].m_brake;
+    for (int i = 0; i < 4; i++) {
+        out15[3 + i] = wi[i].m_latFriction;
+        out15[7 + i] = wi[i].m_longFriction;
+        out15[11 + i] = wi[i].m_extraPushback;
+    }
+    return 0;
+}
+
 }  // extern "C"
 
 extern "C" {

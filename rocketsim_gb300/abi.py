@@ -140,6 +140,9 @@ PROTOTYPES = {
     "rsg_air_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
     "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),
     "rsg_air_backward_noalloc": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
+    "rsg_ground_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp, vp]),
+    "rsg_ground_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
+    "rsg_ground_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),
 }
 
 _LIB = None

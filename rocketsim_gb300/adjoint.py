@@ -1,4 +1,5 @@
-"""Differentiable contact-free air rollouts: torch.autograd over rsg_air_forward / rsg_air_backward.
+"""Differentiable rollouts: torch.autograd over rsg_air_* (contact-free air phase) and
+rsg_ground_* (driving on the floor).
 
 A rollout advances, per instance, one airborne car and the ball through `ticks` arena ticks
 under pitch/yaw/roll/boost controls, with nothing to touch (the air path of Arena::Step,
@@ -20,6 +21,11 @@ Example::
     u = torch.zeros(60, n, 4, device="cuda", requires_grad=True)     # pitch, yaw, roll, boost
     final = adjoint.air_rollout(s0, u)
     adjoint.aim_loss(final, target_basis).sum().backward()           # u.grad: [60, n, 4]
+
+Ground rollouts work the same way on a 39-float state (``ground_state_vector``: the kinematics,
+the vehicle state of btVehicleRL's wheels, the ball) with throttle, steer and boost controls
+(``ground_rollout``, ``drive_loss``); the boost input is relaxed the same way and its full
+throttle becomes throttle + boost * (1 - throttle).
 """
 from __future__ import annotations
 
@@ -32,6 +38,7 @@ from . import abi
 from .abi import BallState, CarConfig, CarState, check
 
 STATE = 24
+GROUND_STATE = 39
 UU_TO_BT = np.float32(1.0 / 50.0)  # RLConst::UU_TO_BT, a float
 BT_TO_UU = np.float32(50.0)
 
@@ -115,6 +122,84 @@ def air_rollout(state0: torch.Tensor, controls: torch.Tensor, car: CarConfig | i
     return AirRollout.apply(state0, controls, car, tick_rate, ckpt_every)
 
 
+class GroundRollout(torch.autograd.Function):
+    """(final_state, flags) = ground rollout(state0, controls); final_state is differentiable in
+    both inputs, flags ([n] int32, the ticks that left the ground model) is not."""
+
+    @staticmethod
+    def forward(ctx, state0: torch.Tensor, controls: torch.Tensor, car: CarConfig, tick_rate: float,
+                ckpt_every: int):
+        lib = abi.load(build_if_missing=False)
+        n = state0.shape[0]
+        ticks = controls.shape[0]
+        state0 = state0.contiguous()
+        controls = controls.contiguous()
+        _check_tensor(state0, "state0", (n, GROUND_STATE))
+        _check_tensor(controls, "controls", (ticks, n, 4))
+        if state0.device != controls.device:
+            raise ValueError("state0 and controls must be on the same device")
+        if ckpt_every < 1:
+            raise ValueError("ckpt_every must be >= 1")
+        final = torch.empty_like(state0)
+        flags = torch.empty((n,), dtype=torch.int32, device=state0.device)
+        need_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        ckpt = None
+        if need_grad:
+            nseg = (ticks + ckpt_every - 1) // ckpt_every
+            ckpt = torch.empty((max(nseg, 1), n, GROUND_STATE), device=state0.device, dtype=torch.float32)
+        with torch.cuda.device(state0.device):
+            check(lib.rsg_ground_forward(C.byref(car), float(tick_rate), n, ticks, _ptr(state0), _ptr(controls),
+                                         _ptr(final), _ptr(ckpt), ckpt_every, _ptr(flags), _stream()),
+                  "rsg_ground_forward")
+        if need_grad:
+            ctx.save_for_backward(controls, ckpt)
+        ctx.car = car
+        ctx.tick_rate = float(tick_rate)
+        ctx.ckpt_every = ckpt_every
+        ctx.n = n
+        ctx.mark_non_differentiable(flags)
+        return final, flags
+
+    @staticmethod
+    @torch.autograd.function.once_differentiable
+    def backward(ctx, grad_final: torch.Tensor, grad_flags):
+        lib = abi.load(build_if_missing=False)
+        controls, ckpt = ctx.saved_tensors
+        ticks, n = controls.shape[0], ctx.n
+        grad_final = grad_final.contiguous().to(torch.float32)
+        grad_controls = torch.empty_like(controls)
+        grad_state0 = torch.empty_like(grad_final) if ctx.needs_input_grad[0] else None
+        nbytes = C.c_size_t()
+        check(lib.rsg_ground_backward_workspace_size(n, ticks, C.byref(nbytes)), "rsg_ground_backward_workspace_size")
+        work = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, device=controls.device)
+        with torch.cuda.device(controls.device):
+            check(lib.rsg_ground_backward(C.byref(ctx.car), ctx.tick_rate, n, ticks, _ptr(controls), _ptr(ckpt),
+                                          ctx.ckpt_every, _ptr(grad_final), _ptr(grad_controls), _ptr(grad_state0),
+                                          _ptr(work), nbytes.value, _stream()), "rsg_ground_backward")
+        return grad_state0, (grad_controls if ctx.needs_input_grad[1] else None), None, None, None
+
+
+def ground_rollout(state0: torch.Tensor, controls: torch.Tensor, car: CarConfig | int = abi.CAR_OCTANE,
+                   tick_rate: float = 120.0, ckpt_every: int = 16, return_flags: bool = False):
+    """Final state [n, 39] after controls.shape[0] ticks of driving on the floor from state0
+    [n, 39]; controls [ticks, n, 4] = throttle, steer, boost, unused.  With `return_flags` also
+    the [n] int32 flags: bit 0 where a wheel's ray missed the floor, bit 1 where the car tilted
+    past the suspension's contact limit (ticks outside the model)."""
+    if not isinstance(car, CarConfig):
+        from .arena import car_config
+        car = car_config(car)
+    final, flags = GroundRollout.apply(state0, controls, car, tick_rate, ckpt_every)
+    return (final, flags) if return_flags else final
+
+
+def drive_loss(final: torch.Tensor, target_xy: torch.Tensor, target_dir: torch.Tensor) -> torch.Tensor:
+    """Per-instance loss of a ground rollout: squared distance of the final car position to
+    `target_xy` ([n, 2]) plus that of its forward axis to the unit vector `target_dir` ([n, 3])."""
+    d = final[:, 0:2] - target_xy
+    f = final[:, 9:18].reshape(-1, 3, 3)[:, :, 0] - target_dir
+    return (d * d).sum(dim=1) + (f * f).sum(dim=1)
+
+
 def aim_loss(final: torch.Tensor, target_basis: torch.Tensor, dist_scale: float = 1e-2) -> torch.Tensor:
     """Per-instance loss: squared Frobenius distance of the final basis to `target_basis`
     ([n, 3, 3]) plus dist_scale * |car position + forward - ball position|^2."""
@@ -140,6 +225,22 @@ def state_vector(cars, balls) -> torch.Tensor:
         rows[i, 18:21] = np.array([b.pos.x, b.pos.y, b.pos.z], f32) * UU_TO_BT
         rows[i, 21:24] = np.array([b.vel.x, b.vel.y, b.vel.z], f32) * UU_TO_BT
     return torch.from_numpy(rows)
+
+
+def ground_state_vector(cars, balls, vehicle=None) -> torch.Tensor:
+    """[n, 39] float32 CPU tensor for ground rollouts: the kinematics of `state_vector`, then the
+    vehicle state the next tick starts from (front steer angle, engine force, brake, lateral
+    friction factor per wheel, longitudinal friction factor per wheel, extra push-back per wheel:
+    15 floats per car, the btWheelInfoRL fields of src/Sim/btVehicleRL/btVehicleRL.h:9-27), then
+    the ball.  Without `vehicle` ([n, 15]) the vehicle state is that of a car that has not run a
+    tick yet: all zero."""
+    kin = state_vector(cars, balls).numpy()
+    out = np.zeros((kin.shape[0], GROUND_STATE), np.float32)
+    out[:, 0:18] = kin[:, 0:18]
+    if vehicle is not None:
+        out[:, 18:33] = np.asarray(vehicle, np.float32).reshape(-1, 15)
+    out[:, 33:39] = kin[:, 18:24]
+    return torch.from_numpy(out)
 
 
 def car_state_from_vector(v, template: CarState | None = None) -> CarState:

@@ -1,6 +1,6 @@
 """Builds the in-tree shared library ``rocketsim_gb300/_lib/librsg_gb300.so``.
 
-nvcc compiles the three translation units in parallel for sm_103a only and
+nvcc compiles the translation units in parallel for sm_103a only and
 links them into one library exporting the C ABI of include/rocketsim_gb300.h.
 Floating-point contraction is off on both sides (``-fmad=false`` for device
 code, ``-ffp-contract=off`` for host code) so that every multiply and add
@@ -20,7 +20,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "librsg_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-SOURCES = ["rsg_kernels.cu", "rsg_air.cu", "rsg_air_noalloc.cu", "rsg_capi.cpp", "rsg_mesh.cpp"]
+SOURCES = ["rsg_kernels.cu", "rsg_air.cu", "rsg_air_noalloc.cu", "rsg_ground.cu", "rsg_capi.cpp", "rsg_mesh.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 

@@ -361,6 +361,7 @@ cudaError_t launch_remove_car(const BatchBuffers& b, uint32_t arena, uint32_t sl
                               cudaStream_t st);
 cudaError_t launch_init_arenas(const BatchBuffers& b, uint32_t ball_cell, cudaStream_t st);
 cudaError_t launch_demolish(const BatchBuffers& b, uint32_t arena, uint32_t slot, float delay, cudaStream_t st);
+CarCfgDev car_config_derived(const rsg_car_config& c) { return derive_config(c); }
 }  // namespace rsg
 
 extern "C" {

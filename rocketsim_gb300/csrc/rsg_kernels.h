@@ -50,6 +50,9 @@ int tick_smem_per_arena(int max_cars);
 // Allocates the current device's pool of EPA work slots (once per device; about 14 MB).
 cudaError_t ensure_epa_pool();
 
+// The constants Car::_BulletSetup derives from a car configuration (src/Sim/Car/Car.cpp:195-292).
+CarCfgDev car_config_derived(const rsg_car_config& c);
+
 // Records `msg` as the calling thread's last error (rsg_get_last_error) and returns `code`.
 int report_error(int code, const char* msg);
 
