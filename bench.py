@@ -20,7 +20,8 @@ loss, hand-written adjoint backward) of 60-tick air-control rollouts over
 8192 instances, replayed as one captured CUDA graph (and eagerly), their
 relative error against FP64 central finite differences on a few instances,
 and the backward / forward cost ratio of the C-ABI calls; and ``ground_adjoint``:
-the same for 120-tick ground-driving rollouts (eager steps).
+the same for 120-tick ground-driving rollouts over 65536 instances (eager
+steps), checked on 256 of them.
 
 ``--impl reference`` times the CPU implementation of the same tick on the
 host cores instead: the reference library built from its sources when it is
@@ -552,8 +553,9 @@ def adjoint_cpu_check(case, g_gpu: np.ndarray, k: int):
 # ---------------------------------------------------------------- adjoint (ground driving)
 GROUND_TICKS = 120
 GROUND_SETTLE = 24
-GROUND_WORKLOAD = ("ground-driving adjoint: 8192 instances x (1 Octane on the floor + ball), 120 ticks, controls "
-                   "throttle/steer in [-1, 1] and relaxed boost in [0, 1], checkpoints every 16 ticks")
+GROUND_WORKLOAD = ("ground-driving adjoint: 65536 instances x (1 Octane on the procedural mesh floor + ball), 120 "
+                   "ticks, throttle/steer in [-1, 1] and relaxed boost in [0, 1], loss on the car's nose point and "
+                   "velocity at tick 120, checkpoints every 16 ticks")
 
 
 def _smooth_controls(rng, ticks: int, n: int, lo: float, hi: float, knots: int = 4) -> np.ndarray:
@@ -567,9 +569,10 @@ def _smooth_controls(rng, ticks: int, n: int, lo: float, hi: float, knots: int =
 
 def ground_adjoint_case(n: int, seed: int, dev: str):
     """Ground-driving workload: an Octane on the floor within 800 uu of the centre, random heading,
-    forward speed 0..1200 uu/s, settled for 24 ticks at throttle 0.5 by the rollout itself; smooth
-    random controls inside the ranges; a drive_loss target 50..150 uu from where an uncontrolled
-    rollout would end and a random target heading.  Bullet units."""
+    forward speed 0..1200 uu/s, settled for 24 ticks at throttle 0.5 by the rollout itself; the ball
+    in the air far away; smooth random controls inside the ranges; a nose-point target 50..150 uu
+    from where the car would be after 1 s at its start velocity, at nose height, and a random
+    horizontal target velocity of up to 1500 uu/s.  Bullet units."""
     import torch
     from rocketsim_gb300 import adjoint
     rng = np.random.default_rng(seed)
@@ -592,11 +595,14 @@ def ground_adjoint_case(n: int, seed: int, dev: str):
     u[..., 1] = _smooth_controls(rng, GROUND_TICKS, n, -0.6, 0.6)
     u[..., 2] = _smooth_controls(rng, GROUND_TICKS, n, 0.2, 0.8)
     ang = rng.uniform(0, 2 * np.pi, n)
-    target_xy = s[:, 0:2] + s[:, 3:5] * (GROUND_TICKS / 120.0) + \
+    tp = np.zeros((n, 3), np.float32)
+    tp[:, 0:2] = s[:, 0:2] + s[:, 3:5] * (GROUND_TICKS / 120.0) + \
         np.stack([np.cos(ang), np.sin(ang)], 1) * rng.uniform(1, 3, (n, 1))
+    tp[:, 2] = (17.0 + 20.755) / 50.0
     ang = rng.uniform(0, 2 * np.pi, n)
-    target_dir = np.stack([np.cos(ang), np.sin(ang), np.zeros(n)], 1)
-    return s, u, target_xy.astype(np.float32), target_dir.astype(np.float32)
+    tv = np.zeros((n, 3), np.float32)
+    tv[:, 0:2] = np.stack([np.cos(ang), np.sin(ang)], 1) * rng.uniform(0, 1500, (n, 1)) / 50.0
+    return s, u, tp, tv
 
 
 def run_ground_adjoint(args, dev: int):
@@ -605,21 +611,17 @@ def run_ground_adjoint(args, dev: int):
     import torch
     from rocketsim_gb300 import abi, adjoint
     from rocketsim_gb300.arena import car_config
-    n = args.adj_instances
+    n = args.ground_instances
     d = f"cuda:{dev}"
-    s, u, txy, tdir = ground_adjoint_case(n, 2468, d)
+    s, u, tp, tv = ground_adjoint_case(n, 2468, d)
     ds = torch.from_numpy(s).to(d)
     du = torch.from_numpy(u).to(d).requires_grad_(True)
-    t_xy, t_dir = torch.from_numpy(txy).to(d), torch.from_numpy(tdir).to(d)
-
-    def grad_step():
-        du.grad = None
-        fin, flags = adjoint.ground_rollout(ds, du, ckpt_every=16, return_flags=True)
-        adjoint.drive_loss(fin, t_xy, t_dir).sum().backward()
-        return flags
+    t_p, t_v = torch.from_numpy(tp).to(d), torch.from_numpy(tv).to(d)
 
     for _ in range(args.warmup):
-        flags = grad_step()
+        du.grad = None
+        fin, flags = adjoint.ground_rollout(ds, du, ckpt_every=16, return_flags=True)
+        adjoint.contact_loss(fin, t_p, t_v).sum().backward()
     torch.cuda.synchronize()
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     for k in range(args.steps):
@@ -627,13 +629,13 @@ def run_ground_adjoint(args, dev: int):
         ev[k][0].record()
         fin = adjoint.ground_rollout(ds, du, ckpt_every=16)
         ev[k][1].record()
-        adjoint.drive_loss(fin, t_xy, t_dir).sum().backward()
+        adjoint.contact_loss(fin, t_p, t_v).sum().backward()
         ev[k][2].record()
     torch.cuda.synchronize()
     fwd = [a.elapsed_time(b) for a, b, _ in ev]
     bwd = [b.elapsed_time(c) for _, b, c in ev]
     total_ms = sum(a.elapsed_time(c) for a, _, c in ev)
-    g_gpu = du.grad[:, :args.adj_check].detach().cpu().numpy().astype(np.float64)
+    g_gpu = du.grad[:, :args.ground_check].detach().cpu().numpy().astype(np.float64)
     with torch.no_grad():
         adjoint.ground_rollout(ds, du.detach())
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -674,29 +676,37 @@ def run_ground_adjoint(args, dev: int):
             "ms_backward": statistics.median(bwd), "backward_over_forward": statistics.median(bwd) / plain_fwd_ms,
             "kernel_ms_forward_ckpt": statistics.median(kf), "kernel_ms_backward": statistics.median(kb),
             "workspace_bytes": nb.value, "flagged_instances": int((flags != 0).sum()),
-            "case": (s, u, txy, tdir), "g_gpu": g_gpu}
+            "case": (s, u, tp, tv), "g_gpu": g_gpu}
 
 
 GROUND_FD_TICKS = (0, 30, 60, 90, 110, 119)
 
 
-def ground_cpu_check(case, g_gpu: np.ndarray, k: int):
-    """FP64 central finite differences (step 1e-4) of the ground restatement for the first k
-    instances at six ticks x three controls: the relative error of the GPU adjoint and the CPU's
-    rate of such gradient entries."""
+def ground_cpu_check(case, g_gpu: np.ndarray):
+    """FP64 central finite differences (step 1e-4) of the ground restatement for the instances of
+    g_gpu at six ticks x three controls: the relative error of the GPU adjoint per instance (the
+    maximum over them) and the CPU's rate of such gradient entries."""
     from oracle import ground_fp64 as Gr
-    s, u, txy, tdir = case
+    s, u, tp, tv = case
+    k = g_gpu.shape[1]
     s64, u64 = s[:k].astype(np.float64), u[:, :k].astype(np.float64)
     which = [(t, c) for t in GROUND_FD_TICKS for c in range(3)]
+    loss = lambda f: Gr.contact_loss(f, tp[:k].astype(np.float64), tv[:k].astype(np.float64))  # noqa: E731
     t0 = time.perf_counter()
-    gfd = Gr.fd_grad(s64, u64, Gr.car_geometry(), 1.0 / 120.0,
-                     lambda f: Gr.drive_loss(f, txy[:k].astype(np.float64), tdir[:k].astype(np.float64)),
-                     h=1e-4, which=which)
+    gfd = Gr.fd_grad(s64, u64, Gr.car_geometry(), 1.0 / 120.0, loss, h=1e-4, which=which)
     el = time.perf_counter() - t0
-    a = np.stack([g_gpu[t, :k, c] for t, c in which], 1)
+    gfd2 = Gr.fd_grad(s64, u64, Gr.car_geometry(), 1.0 / 120.0, loss, h=5e-5, which=which)
+    a = np.stack([g_gpu[t, :, c] for t, c in which], 1)
     b = np.stack([gfd[t, :, c] for t, c in which], 1)
+    b2 = np.stack([gfd2[t, :, c] for t, c in which], 1)
     rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
-    return float(rel.max()), k * len(which) / el, el, len(which)
+    # instances whose two central differences disagree have a jump of the tick inside the
+    # stencil (the lateral-friction input switching on at 5 uu/s of side slip, a push-back
+    # starting): the difference quotient is no derivative there
+    smooth = np.linalg.norm(b - b2, axis=1) <= 1e-5 * np.linalg.norm(b, axis=1)
+    return {"max": float(rel[smooth].max()), "median": float(np.median(rel[smooth])),
+            "nonsmooth": int((~smooth).sum()), "max_all": float(rel.max()),
+            "rate": k * len(which) / el, "seconds": el, "entries": len(which)}
 
 
 def main():
@@ -709,6 +719,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=1.5)
     ap.add_argument("--adj-instances", type=int, default=8192)
     ap.add_argument("--adj-check", type=int, default=4, help="instances checked against FP64 finite differences")
+    ap.add_argument("--ground-instances", type=int, default=65536)
+    ap.add_argument("--ground-check", type=int, default=256,
+                    help="ground instances checked against FP64 finite differences")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -751,7 +764,7 @@ def main():
     adj = run_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
     adj_err, cpu_grads, cpu_el = adjoint_cpu_check(adj["case"], adj["g_gpu"], args.adj_check)
     gadj = run_ground_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
-    g_err, g_cpu_rate, g_cpu_el, g_entries = ground_cpu_check(gadj["case"], gadj["g_gpu"], min(args.adj_check, 2))
+    gchk = ground_cpu_check(gadj["case"], gadj["g_gpu"])
     single, _, _, kind = cpu_ticks_per_second(1, args.cpu_seconds)
     allc, n, el, _ = cpu_ticks_per_second(threads, args.cpu_seconds)
     line = {
@@ -784,18 +797,20 @@ def main():
                                        f"{args.adj_check} instances x 240 inputs x 2 rollouts ({cpu_el:.1f} s)"}},
         "ground_adjoint": {
             "metric": "adjoint grads/s", "value": gadj["value"], "unit": "grads/s (120-tick ground rollouts)",
-            "workload": GROUND_WORKLOAD, "rel_err_max_vs_fp64_fd": g_err,
-            "rel_err_sample": f"{min(args.adj_check, 2)} instances x {g_entries} control entries",
+            "workload": GROUND_WORKLOAD, "rel_err_max_vs_fp64_fd": gchk["max"], "rel_err_median": gchk["median"],
+            "rel_err_sample": f"{args.ground_check} instances x {gchk['entries']} control entries; "
+                              f"{gchk['nonsmooth']} instances left out whose central differences at steps 1e-4 "
+                              f"and 5e-5 disagree (a jump inside the stencil; max over all {gchk['max_all']:.2e})",
             "ms_per_step": gadj["ms_per_step"], "step": "eager: forward + loss + backward",
             "ms_forward_with_checkpoints": gadj["ms_forward_ckpt"], "ms_forward_plain": gadj["ms_forward_plain"],
             "ms_backward": gadj["ms_backward"], "backward_over_forward": gadj["backward_over_forward"],
             "c_abi_ms_forward_with_checkpoints": gadj["kernel_ms_forward_ckpt"],
             "c_abi_ms_backward": gadj["kernel_ms_backward"], "workspace_bytes": gadj["workspace_bytes"],
             "flagged_instances": gadj["flagged_instances"], "gpu_launches_per_step": 3,
-            "cpu_baseline": {"value": g_cpu_rate, "unit": "gradient entries/s", "cores": 1, "kind": "port",
+            "cpu_baseline": {"value": gchk["rate"], "unit": "gradient entries/s", "cores": 1, "kind": "port",
                              "sample": f"FP64 central differences of the numpy restatement, "
-                                       f"{min(args.adj_check, 2)} instances x {g_entries} entries x 2 rollouts "
-                                       f"({g_cpu_el:.1f} s)"}},
+                                       f"{args.ground_check} instances x {gchk['entries']} entries x 2 rollouts "
+                                       f"({gchk['seconds']:.1f} s)"}},
     }
     print(json.dumps(line))
 

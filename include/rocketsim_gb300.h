@@ -356,7 +356,7 @@ int rsg_air_backward_noalloc(const rsg_car_config* car, float tick_rate, int n, 
  * the floor) and bit 1 (the car tilted past the suspension's contact limit),
  * the ticks that left the model.  Checkpoints, gradients and workspace as for
  * the air rollouts, with 39 floats per state: the workspace is
- * rsg_ground_backward_workspace_size bytes (156 bytes per instance and tick).
+ * rsg_ground_backward_workspace_size bytes (180 bytes per instance and tick).
  * The gradient at boost 1 is the one-sided derivative from inside [0, 1]. */
 int rsg_ground_forward(const rsg_car_config* car, float tick_rate, int n, int ticks, const float* d_state0,
                        const float* d_controls, float* d_final, float* d_ckpt, int ckpt_every, int* d_flags,

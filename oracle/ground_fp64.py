@@ -289,6 +289,33 @@ def drive_loss_grad(final: np.ndarray, target_xy: np.ndarray, target_dir: np.nda
     return g
 
 
+# front centre of the Octane hitbox in car space, Bullet units: the hitbox offset plus half its
+# length along forward, the offset along up (CarConfig.cpp:20-27)
+NOSE = np.array([(13.8757 + 120.507 / 2) * UU, 0.0, 20.755 * UU])
+
+
+def contact_loss(final: np.ndarray, target_point: np.ndarray, target_vel: np.ndarray,
+                 vel_scale: float = 1e-2) -> np.ndarray:
+    """Per-instance loss at the end of the horizon: squared distance of the car's nose (the front
+    centre of its hitbox, where it would meet a ball) to `target_point` ([n, 3]) plus vel_scale
+    times the squared distance of its velocity to `target_vel` ([n, 3])."""
+    B = final[:, 9:18].reshape(-1, 3, 3)
+    d = final[:, 0:3] + np.einsum("nij,j->ni", B, NOSE) - target_point
+    e = final[:, 3:6] - target_vel
+    return (d * d).sum(axis=1) + vel_scale * (e * e).sum(axis=1)
+
+
+def contact_loss_grad(final, target_point, target_vel, vel_scale: float = 1e-2) -> np.ndarray:
+    """d contact_loss / d final state, [n, 39]."""
+    B = final[:, 9:18].reshape(-1, 3, 3)
+    d = final[:, 0:3] + np.einsum("nij,j->ni", B, NOSE) - target_point
+    g = np.zeros_like(final)
+    g[:, 0:3] = 2.0 * d
+    g[:, 3:6] = 2.0 * vel_scale * (final[:, 3:6] - target_vel)
+    g[:, 9:18] = (2.0 * d[:, :, None] * NOSE[None, None, :]).reshape(-1, 9)
+    return g
+
+
 def fd_grad(state0, controls, geo, dt, loss_fn, h: float = 1e-4, which=None) -> np.ndarray:
     """Central finite differences of sum(loss_fn(final)) with respect to the controls, in FP64.
 

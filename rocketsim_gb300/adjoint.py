@@ -209,6 +209,22 @@ def aim_loss(final: torch.Tensor, target_basis: torch.Tensor, dist_scale: float 
     return orient + dist_scale * (d * d).sum(dim=1)
 
 
+# front centre of the Octane hitbox in car space, Bullet units (hitbox offset plus half length
+# along forward, offset along up; src/Sim/Car/CarConfig/CarConfig.cpp:20-27)
+OCTANE_NOSE = (float(np.float32((13.8757 + 120.507 / 2) / 50.0)), 0.0, float(np.float32(20.755 / 50.0)))
+
+
+def contact_loss(final: torch.Tensor, target_point: torch.Tensor, target_vel: torch.Tensor,
+                 vel_scale: float = 1e-2, nose=OCTANE_NOSE) -> torch.Tensor:
+    """Per-instance loss of a ground rollout at the end of the horizon: squared distance of the
+    car's nose (`nose`, car space) to `target_point` ([n, 3]) plus vel_scale times the squared
+    distance of its velocity to `target_vel` ([n, 3])."""
+    B = final[:, 9:18].reshape(-1, 3, 3)
+    d = final[:, 0:3] + B @ torch.tensor(nose, dtype=final.dtype, device=final.device) - target_point
+    e = final[:, 3:6] - target_vel
+    return (d * d).sum(dim=1) + vel_scale * (e * e).sum(dim=1)
+
+
 # ---------------------------------------------------------------- state conversion
 def state_vector(cars, balls) -> torch.Tensor:
     """[n, 24] float32 CPU tensor from sequences of CarState and BallState (uu units), converted

@@ -150,7 +150,7 @@ def test_ground_flags_and_c_abi_errors(torch_cuda):
     gu = torch.empty_like(du)
     nb = C.c_size_t()
     assert lib.rsg_ground_backward_workspace_size(5, 9, C.byref(nb)) == abi.OK
-    assert nb.value == 156 * 5 * 9
+    assert nb.value == 180 * 5 * 9
     work = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
     assert lib.rsg_ground_backward(C.byref(cfg), 120.0, 5, 9, P(du), P(ck), 4, P(gfin), P(gu), None, P(work),
                                    nb.value, None) == abi.OK
