@@ -20,7 +20,11 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "librsg_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-SOURCES = ["rsg_kernels.cu", "rsg_air.cu", "rsg_air_noalloc.cu", "rsg_ground.cu", "rsg_capi.cpp", "rsg_mesh.cpp"]
+SOURCES = ["rsg_kernels.cu", "rsg_air.cu", "rsg_air_noalloc.cu", "rsg_ground.cu", "rsg_ground_sweep.cu", "rsg_capi.cpp",
+           "rsg_mesh.cpp"]
+# The ground adjoint's reverse sweep only linearises around recomputed intermediates: division and
+# square root correct to about 2 ulp are enough there (see rsg_ground_sweep.cu).
+EXTRA = {"rsg_ground_sweep.cu": ["-prec-div=false", "-prec-sqrt=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 
@@ -42,6 +46,7 @@ def _digest() -> str:
                     h.update(name.encode())
                     h.update(f.read())
     h.update(" ".join(ARCH + COMMON).encode())
+    h.update(repr(sorted(EXTRA.items())).encode())
     return h.hexdigest()
 
 
@@ -60,7 +65,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src: str) -> str:
         out = os.path.join(obj_dir, src + ".o")
-        cmd = [nvcc, *ARCH, *COMMON, "-c", os.path.join(CSRC, src), "-o", out]
+        cmd = [nvcc, *ARCH, *COMMON, *EXTRA.get(src, []), "-c", os.path.join(CSRC, src), "-o", out]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

@@ -946,6 +946,37 @@ RSG_D void apply_friction_impulses(Car& c, float dt) {  // btVehicleRL.cpp:383-3
     }
 }
 
+// The chassis velocity changes of wheel i's suspension impulse (apply_suspension) and friction
+// impulse (apply_friction_impulses), each computed as Body::apply_impulse computes it.
+struct ImpulseDeltas {
+    V3 dvs, dws, dvf, dwf;
+    bool son, fon;
+};
+RSG_D ImpulseDeltas wheel_impulse_deltas(const Car& c, int i, float dt) {
+    ImpulseDeltas d;
+    const WheelRT& w = c.w[i];
+    const V3 off = w.contact_point - c.rb.xf.o;
+    d.son = w.susp_force != 0;
+    d.dvs = d.dws = d.dvf = d.dwf = V3(0, 0, 0);
+    if (d.son) {
+        const V3 imp = w.contact_normal * ((w.susp_force * dt) + c.pushback[i]);
+        d.dvs = imp * c.rb.inv_mass;
+        d.dws = c.rb.inv_inertia_world * cross(off, imp);
+    }
+    d.fon = !is_zero(w.impulse);
+    if (d.fon) {
+        const V3 up = c.rb.xf.b.col(2);
+        const float dd = dot(up, off);
+        const V3 imp = w.impulse * dt, rel = off - up * dd;
+        d.dvf = imp * c.rb.inv_mass;
+        d.dwf = c.rb.inv_inertia_world * cross(rel, imp);
+    }
+    return d;
+}
+RSG_D V3 shfl_v3(unsigned mask, V3 v, int src) {
+    return V3(__shfl_sync(mask, v.x, src), __shfl_sync(mask, v.y, src), __shfl_sync(mask, v.z, src));
+}
+
 // ---------------------------------------------------------------- car logic (Car.cpp)
 RSG_D float rs_maxf(float a, float b) { return (a > b) ? a : b; }
 RSG_D float rs_minf(float a, float b) { return (a < b) ? a : b; }
@@ -1301,10 +1332,38 @@ RSG_DN void car_pre_after_rays_grp(const BatchView& bv, Ctx& a, Car& c, int wl, 
     for (int i = wl; i < 4; i += gsize) suspension_force(c, i);
     __syncwarp(gmask);
     RSG_FT(43);
-    if (wl == 0) {
+    // btVehicleRL's suspension impulses (wheels 0-3), then its friction impulses (wheels 0-3): each
+    // wheel's velocity changes are computed on the wheel's thread, the first thread of the group
+    // adds them to the chassis in that order (the same sums as applying the impulses one by one).
+    if (gsize == 4) {
+        ImpulseDeltas d = wheel_impulse_deltas(c, wl, dt);
+        const int base = (threadIdx.x & 31) & ~3;
+        V3 dv[4], dw[4];
+        bool on[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            dv[j] = shfl_v3(gmask, d.dvs, base + j);
+            dw[j] = shfl_v3(gmask, d.dws, base + j);
+            on[j] = __shfl_sync(gmask, (int)d.son, base + j) != 0;
+        }
+        if (wl == 0)
+            for (int j = 0; j < 4; j++)
+                if (on[j]) { c.rb.lin_vel += dv[j]; c.rb.ang_vel += dw[j]; }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            dv[j] = shfl_v3(gmask, d.dvf, base + j);
+            dw[j] = shfl_v3(gmask, d.dwf, base + j);
+            on[j] = __shfl_sync(gmask, (int)d.fon, base + j) != 0;
+        }
+        if (wl == 0)
+            for (int j = 0; j < 4; j++)
+                if (on[j]) { c.rb.lin_vel += dv[j]; c.rb.ang_vel += dw[j]; }
+    } else {
         apply_suspension(c, dt);
         apply_friction_impulses(c, dt);
-        RSG_FT(44);
+    }
+    RSG_FT(44);
+    if (wl == 0) {
         update_boost(c, dt);
         RSG_FT(45);
     }
@@ -1315,12 +1374,16 @@ RSG_D void car_pre_after_rays(const BatchView& bv, Ctx& a, Car& c) {
 }
 
 // Start of Car::_PreTickUpdate for a car that is not demolished and was not at the last
-// pre-tick: control clamping, activation and the wheel transforms.
-RSG_D void car_pre_before_rays(Car& c) {
-    for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
-    c.rb.act = ACTIVE_TAG;
-    c.rb.no_contact_response = false;
-    for (int i = 0; i < 4; i++) update_wheel_transform(c, i);
+// pre-tick, the part of wheel `wh`: wheel 0 clamps the controls and sets the activation (nothing
+// before the vehicle update reads them, and no other car's ray sees a change: the car is not and
+// was not demolished), every wheel its own transform.
+RSG_D void car_pre_before_rays_wheel(Car& c, int wh) {
+    if (wh == 0) {
+        for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
+        c.rb.act = ACTIVE_TAG;
+        c.rb.no_contact_response = false;
+    }
+    update_wheel_transform(c, wh);
 }
 
 RSG_DN void car_pre_tick(const BatchView& bv, Ctx& a, Car& c) {  // Car::_PreTickUpdate (Car.cpp:58-131)
@@ -3862,29 +3925,19 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
     }
     __syncthreads();
     RSG_SUB(8);
-    {  // units spread over the block's warps (a few per warp): less divergence, more warps at work
-        const int u = spread_unit(tid, nthreads);
-        Ctx& a = B(u / MC);
-        int k = u % MC;
-        if (u < B.nact * MC && k < a.ncars) {
-        if (a.serial) {
-            if (k == 0)
-                for (int kk = 0; kk < a.ncars; kk++) car_pre_tick(bv, a, a.cars[a.order[kk]]);
-        } else {
-            car_pre_before_rays(a.cars[k]);
-        }
-        }
-    }
-    __syncthreads();
     RSG_SUB(9);
-    {
+    {  // one unit per wheel, spread over the block's warps: the wheel's transform and ray (an arena
+       // in the reference's order runs its whole pre-tick on its first wheel's unit)
         const int u = spread_unit(tid, nthreads);
         Ctx& a = B(u / (MC * 4));
         int r = u % (MC * 4), k = r >> 2, wh = r & 3;
+        if (u < B.nact * MC * 4 && a.serial && r == 0)
+            for (int kk = 0; kk < a.ncars; kk++) car_pre_tick(bv, a, a.cars[a.order[kk]]);
         if (u < B.nact * MC * 4 && !a.serial && k < a.ncars) {
 #if defined(RSG_PHASE_TIMERS)
         long long rt0_ = clock64();
 #endif
+        car_pre_before_rays_wheel(a.cars[k], wh);
         ray_cast_wheel(bv, a, a.cars[k], wh);
 #if defined(RSG_PHASE_TIMERS)
         {
@@ -3964,9 +4017,30 @@ RSG_DN void body_post(Body& b, float dt) {
     b.total_torque = V3(0, 0, 0);
 }
 
+// Pad positions for per-thread reads: threads of a warp test different pads, and constant memory
+// serialises a warp's loads of different addresses.
+__device__ const float g_pad_locs[NUM_PADS][3] = RSG_PAD_LOCS_INIT;
+
+// A pad's position (Bullet units), size and cell of BoostPadGrid (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25)
+struct PadGeo {
+    V3 pos_bt;
+    int px, py;
+    bool big;
+};
+RSG_D PadGeo pad_geo(int pi) {
+    const int CX = 8, CY = 10, SX = (int)(4096.f / (CX / 2)), SY = (int)(5120.f / (CY / 2));
+    const float x = __ldg(&g_pad_locs[pi][0]), y = __ldg(&g_pad_locs[pi][1]), z = __ldg(&g_pad_locs[pi][2]);
+    PadGeo g;
+    g.px = (int)(x / SX + (CX / 2));
+    g.py = (int)(y / SY + (CY / 2));
+    g.pos_bt = V3(x, y, z) * RL::UU_TO_BT;
+    g.big = pi < 6;
+    return g;
+}
+
 // The pad grid test of one (pad, car): BoostPadGrid::CheckCollision's cell neighbourhood
 // (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25) and BoostPad::_CheckCollide (BoostPad.cpp:62-86).
-RSG_D bool pad_touches(Ctx& a, const Pad& p, int pi, int ci) {
+RSG_D bool pad_touches(Ctx& a, const Pad& p, const PadGeo& g, int ci) {
     Car& c = a.cars[ci];
     if (c.f(F_DEMOED) || c.boost >= RL::BOOST_MAX) return false;
     V3 cpu = c.rb.xf.o * RL::BT_TO_UU;
@@ -3975,25 +4049,22 @@ RSG_D bool pad_touches(Ctx& a, const Pad& p, int pi, int ci) {
     const int CX = 8, CY = 10, SX = (int)(4096.f / (CX / 2)), SY = (int)(5120.f / (CY / 2));
     int ix = (int)(cpu.x / SX + (CX / 2));
     int iy = (int)(cpu.y / SY + (CY / 2));
-    int px = (int)(c_pad_locs[pi][0] / SX + (CX / 2));
-    int py = (int)(c_pad_locs[pi][1] / SY + (CY / 2));
     int i0 = ix - 1 > 0 ? ix - 1 : 0, i1 = ix + 1 < CX - 1 ? ix + 1 : CX - 1;
     int j0 = iy - 1 > 0 ? iy - 1 : 0, j1 = iy + 1 < CY - 1 ? iy + 1 : CY - 1;
-    if (px < i0 || px > i1 || py < j0 || py > j1) return false;
+    if (g.px < i0 || g.px > i1 || g.py < j0 || g.py > j1) return false;
     V3 cp = c.rb.xf.o;
-    bool big = pi < 6;
-    V3 pos_bt = V3(c_pad_locs[pi][0], c_pad_locs[pi][1], c_pad_locs[pi][2]) * RL::UU_TO_BT;
+    const V3 pos_bt = g.pos_bt;
     if (p.prev_locked == c.id) {
         V3 mn, mx;
         car_compound_aabb(c, c.rb.xf, mn, mx);
-        float br = (big ? RL::PAD_BOX_RAD_BIG : RL::PAD_BOX_RAD_SMALL) * RL::UU_TO_BT;
+        float br = (g.big ? RL::PAD_BOX_RAD_BIG : RL::PAD_BOX_RAD_SMALL) * RL::UU_TO_BT;
         V3 bmin = pos_bt - V3(br, br, 0);
         V3 bmax = pos_bt + V3(br, br, RL::PAD_BOX_HEIGHT * RL::UU_TO_BT);
         bool gt = (bmax.x > mn.x) && (bmax.y > mn.y) && (bmax.z > mn.z);
         bool lt = (bmin.x < mx.x) && (bmin.y < mx.y) && (bmin.z < mx.z);
         return gt && lt;
     }
-    float rad = (big ? RL::PAD_CYL_RAD_BIG : RL::PAD_CYL_RAD_SMALL) * RL::UU_TO_BT;
+    float rad = (g.big ? RL::PAD_CYL_RAD_BIG : RL::PAD_CYL_RAD_SMALL) * RL::UU_TO_BT;
     float dx = cp.x - pos_bt.x, dy = cp.y - pos_bt.y;
     if (dx * dx + dy * dy < rad * rad) return fabsf(cp.z - pos_bt.z) < (RL::PAD_CYL_HEIGHT * RL::UU_TO_BT);
     return false;
@@ -4053,8 +4124,9 @@ RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, 
             Ctx& a = B(u / NUM_PADS);
             int pi = u % NUM_PADS;
             Pad& p = a.pads[pi];
+            const PadGeo g = pad_geo(pi);
             for (int kk = 0; kk < a.ncars; kk++)
-                if (pad_touches(a, p, pi, a.order[kk])) p.cur_locked = a.order[kk];
+                if (pad_touches(a, p, g, a.order[kk])) p.cur_locked = a.order[kk];
         }
         __syncthreads();
         for (int u = tid; u < B.nact * MC; u += nthreads) {  // BoostPad::_PostTickUpdate boost, in pad order
