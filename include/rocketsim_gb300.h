@@ -162,6 +162,43 @@ typedef struct rsg_car_config {
     float dodge_deadzone;
 } rsg_car_config;
 
+/* MutatorConfig (src/Sim/MutatorConfig/MutatorConfig.h:16-79), field for field,
+ * uu units like the reference.  demo_mode: 0 normal, 1 on contact, 2 disabled. */
+typedef struct rsg_mutator_config {
+    rsg_vec3 gravity;
+    float car_mass;
+    float car_world_friction;
+    float car_world_restitution;
+    float ball_mass;
+    float ball_max_speed;
+    float ball_drag;
+    float ball_world_friction;
+    float ball_world_restitution;
+    float jump_accel;
+    float jump_immediate_force;
+    float boost_accel_ground;
+    float boost_accel_air;
+    float boost_used_per_second;
+    float respawn_delay;
+    float bump_cooldown_time;
+    float boost_pad_cooldown_big;
+    float boost_pad_cooldown_small;
+    float car_spawn_boost_amount;
+    float ball_hit_extra_force_scale;
+    float bump_force_scale;
+    float ball_radius;
+    uint8_t unlimited_flips;
+    uint8_t unlimited_double_jumps;
+    uint8_t recharge_boost_enabled;
+    uint8_t _pad0;
+    float recharge_boost_per_second;
+    float recharge_boost_delay;
+    uint8_t demo_mode;
+    uint8_t enable_team_demos;
+    uint8_t _pad1[2];
+    float goal_base_threshold_y;
+} rsg_mutator_config;
+
 /* Event kinds delivered to the callbacks after a step completes. */
 #define RSG_EVENT_GOAL 1      /* a = scoring team (Arena.cpp:748-752) */
 #define RSG_EVENT_BUMP 2      /* a = bumper id, b = victim id, flag = is_demo (Arena.cpp:399-400) */
@@ -208,6 +245,18 @@ int rsg_get_car_config_preset(int preset, rsg_car_config* out);
 rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate);
 void rsg_batch_destroy(rsg_batch* batch);
 int rsg_batch_num_arenas(const rsg_batch* batch, uint32_t* out);
+
+/* MutatorConfig(GameMode) (MutatorConfig.cpp:5-40): the defaults of a game mode. */
+int rsg_get_default_mutator_config(int game_mode, rsg_mutator_config* out);
+/* Arena::SetMutatorConfig / GetMutatorConfig (Arena.cpp:17-48, Arena.h:52-53),
+ * for every arena of the batch.  Cars added afterwards respawn with
+ * car_spawn_boost_amount (Arena.cpp:58-59).  car_mass must stay at its default
+ * (CAR_MASS_BT = 180): the reference applies a changed car mass
+ * only to the cars that exist at the call, with the ball's mass
+ * (Arena.cpp:35-41), and not to cars added later (Car.cpp:206-209); any other
+ * value returns RSG_ERR_ARG.  Flows between ticks (synchronous). */
+int rsg_set_mutator_config(rsg_batch* batch, const rsg_mutator_config* config);
+int rsg_get_mutator_config(const rsg_batch* batch, rsg_mutator_config* out);
 
 /* ---- cars ----------------------------------------------------------------- */
 

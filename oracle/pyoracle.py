@@ -271,6 +271,13 @@ class SimArena:
         self.lib[self.p + "wheel_debug"](self.h, car_id, buf)
         return [list(buf[i * 16:(i + 1) * 16]) for i in range(4)]
 
+    def set_mutator_config(self, config) -> None:
+        """Arena::SetMutatorConfig from an rsg_mutator_config mirror (reference library only)."""
+        fn = self.lib[self.p + "set_mutator_config"]
+        fn.argtypes = [C.c_void_p, C.c_void_p]
+        buf = C.create_string_buffer(bytes(config), len(bytes(config)))
+        assert fn(self.h, buf) == 0
+
     def vehicle_state(self, car_id: int) -> list[float]:
         """Front steer angle, engine force, brake, lateral (4), longitudinal (4) friction
         factors and extra push-back (4) of a car (reference library only)."""

@@ -343,6 +343,81 @@ int rsref_get_wheel_internals(void* h, uint32_t id, float* out8) {
     return 0;
 }
 
+// Arena::SetMutatorConfig / MutatorConfig(GameMode) through the POD mirror
+// (src/Sim/MutatorConfig/MutatorConfig.h:16-79, field for field).
+int rsref_set_mutator_config(void* h, const rsg_mutator_config* c) {
+    RefArena* ra = (RefArena*)h;
+    MutatorConfig m = ra->arena->GetMutatorConfig();
+    m.gravity = V(c->gravity);
+    m.carMass = c->car_mass;
+    m.carWorldFriction = c->car_world_friction;
+    m.carWorldRestitution = c->car_world_restitution;
+    m.ballMass = c->ball_mass;
+    m.ballMaxSpeed = c->ball_max_speed;
+    m.ballDrag = c->ball_drag;
+    m.ballWorldFriction = c->ball_world_friction;
+    m.ballWorldRestitution = c->ball_world_restitution;
+    m.jumpAccel = c->jump_accel;
+    m.jumpImmediateForce = c->jump_immediate_force;
+    m.boostAccelGround = c->boost_accel_ground;
+    m.boostAccelAir = c->boost_accel_air;
+    m.boostUsedPerSecond = c->boost_used_per_second;
+    m.respawnDelay = c->respawn_delay;
+    m.bumpCooldownTime = c->bump_cooldown_time;
+    m.boostPadCooldown_Big = c->boost_pad_cooldown_big;
+    m.boostPadCooldown_Small = c->boost_pad_cooldown_small;
+    m.carSpawnBoostAmount = c->car_spawn_boost_amount;
+    m.ballHitExtraForceScale = c->ball_hit_extra_force_scale;
+    m.bumpForceScale = c->bump_force_scale;
+    m.ballRadius = c->ball_radius;
+    m.unlimitedFlips = c->unlimited_flips != 0;
+    m.unlimitedDoubleJumps = c->unlimited_double_jumps != 0;
+    m.rechargeBoostEnabled = c->recharge_boost_enabled != 0;
+    m.rechargeBoostPerSecond = c->recharge_boost_per_second;
+    m.rechargeBoostDelay = c->recharge_boost_delay;
+    m.demoMode = (DemoMode)c->demo_mode;
+    m.enableTeamDemos = c->enable_team_demos != 0;
+    m.goalBaseThresholdY = c->goal_base_threshold_y;
+    ra->arena->SetMutatorConfig(m);
+    return 0;
+}
+
+int rsref_default_mutator_config(int game_mode, rsg_mutator_config* o) {
+    MutatorConfig m((GameMode)game_mode);
+    std::memset(o, 0, sizeof(*o));
+    o->gravity = rsg_vec3{m.gravity.x, m.gravity.y, m.gravity.z};
+    o->car_mass = m.carMass;
+    o->car_world_friction = m.carWorldFriction;
+    o->car_world_restitution = m.carWorldRestitution;
+    o->ball_mass = m.ballMass;
+    o->ball_max_speed = m.ballMaxSpeed;
+    o->ball_drag = m.ballDrag;
+    o->ball_world_friction = m.ballWorldFriction;
+    o->ball_world_restitution = m.ballWorldRestitution;
+    o->jump_accel = m.jumpAccel;
+    o->jump_immediate_force = m.jumpImmediateForce;
+    o->boost_accel_ground = m.boostAccelGround;
+    o->boost_accel_air = m.boostAccelAir;
+    o->boost_used_per_second = m.boostUsedPerSecond;
+    o->respawn_delay = m.respawnDelay;
+    o->bump_cooldown_time = m.bumpCooldownTime;
+    o->boost_pad_cooldown_big = m.boostPadCooldown_Big;
+    o->boost_pad_cooldown_small = m.boostPadCooldown_Small;
+    o->car_spawn_boost_amount = m.carSpawnBoostAmount;
+    o->ball_hit_extra_force_scale = m.ballHitExtraForceScale;
+    o->bump_force_scale = m.bumpForceScale;
+    o->ball_radius = m.ballRadius;
+    o->unlimited_flips = m.unlimitedFlips;
+    o->unlimited_double_jumps = m.unlimitedDoubleJumps;
+    o->recharge_boost_enabled = m.rechargeBoostEnabled;
+    o->recharge_boost_per_second = m.rechargeBoostPerSecond;
+    o->recharge_boost_delay = m.rechargeBoostDelay;
+    o->demo_mode = (uint8_t)m.demoMode;
+    o->enable_team_demos = m.enableTeamDemos;
+    o->goal_base_threshold_y = m.goalBaseThresholdY;
+    return 0;
+}
+
 // The vehicle state the next tick starts from that CarState leaves out (btVehicleRL.h:9-27,
 // btWheelInfo.h:73-101): front steer angle, engine force, brake, then per wheel the lateral and
 // longitudinal friction factors and the extra push-back (15 floats).

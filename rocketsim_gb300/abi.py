@@ -88,6 +88,22 @@ class CarConfig(C.Structure):
                 ("dodge_deadzone", C.c_float)]
 
 
+class MutatorConfig(C.Structure):
+    _fields_ = [("gravity", Vec3)] + [(n, C.c_float) for n in (
+        "car_mass", "car_world_friction", "car_world_restitution", "ball_mass", "ball_max_speed", "ball_drag",
+        "ball_world_friction", "ball_world_restitution", "jump_accel", "jump_immediate_force", "boost_accel_ground",
+        "boost_accel_air", "boost_used_per_second", "respawn_delay", "bump_cooldown_time", "boost_pad_cooldown_big",
+        "boost_pad_cooldown_small", "car_spawn_boost_amount", "ball_hit_extra_force_scale", "bump_force_scale",
+        "ball_radius")] + [
+        ("unlimited_flips", C.c_uint8), ("unlimited_double_jumps", C.c_uint8), ("recharge_boost_enabled", C.c_uint8),
+        ("_pad0", C.c_uint8), ("recharge_boost_per_second", C.c_float), ("recharge_boost_delay", C.c_float),
+        ("demo_mode", C.c_uint8), ("enable_team_demos", C.c_uint8), ("_pad1", C.c_uint8 * 2),
+        ("goal_base_threshold_y", C.c_float)]
+
+
+DEMO_NORMAL, DEMO_ON_CONTACT, DEMO_DISABLED = 0, 1, 2
+
+assert C.sizeof(MutatorConfig) == 116
 assert C.sizeof(CarState) == 272
 assert C.sizeof(BallState) == 80
 assert C.sizeof(PadState) == 16
@@ -140,6 +156,9 @@ PROTOTYPES = {
     "rsg_air_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
     "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),
     "rsg_air_backward_noalloc": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
+    "rsg_get_default_mutator_config": (i32, [i32, P(MutatorConfig)]),
+    "rsg_set_mutator_config": (i32, [vp, P(MutatorConfig)]),
+    "rsg_get_mutator_config": (i32, [vp, P(MutatorConfig)]),
     "rsg_ground_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp, vp]),
     "rsg_ground_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
     "rsg_ground_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),

@@ -41,6 +41,13 @@ def init(path: str, game_mode: int = abi.GAMEMODE_SOCCAR) -> None:
     init_from_mem(blobs, game_mode)
 
 
+def default_mutator_config(game_mode: int = abi.GAMEMODE_SOCCAR) -> "abi.MutatorConfig":
+    """MutatorConfig(GameMode): the game mode's default mutators."""
+    m = abi.MutatorConfig()
+    check(abi.load().rsg_get_default_mutator_config(game_mode, C.byref(m)), "rsg_get_default_mutator_config")
+    return m
+
+
 def car_config(preset: int = abi.CAR_OCTANE) -> CarConfig:
     c = CarConfig()
     check(abi.load().rsg_get_car_config_preset(preset, C.byref(c)), "rsg_get_car_config_preset")
@@ -127,6 +134,15 @@ class ArenaBatch:
         check(self.lib.rsg_demolish_car(self.h, arena, car_id, respawn_delay), "rsg_demolish_car")
 
     # ---- ball, pads, arena
+    # ---- mutators (Arena::SetMutatorConfig / GetMutatorConfig, for every arena of the batch)
+    def get_mutator_config(self) -> "abi.MutatorConfig":
+        m = abi.MutatorConfig()
+        check(self.lib.rsg_get_mutator_config(self.h, C.byref(m)), "rsg_get_mutator_config")
+        return m
+
+    def set_mutator_config(self, config: "abi.MutatorConfig") -> None:
+        check(self.lib.rsg_set_mutator_config(self.h, C.byref(config)), "rsg_set_mutator_config")
+
     def get_ball_state(self, arena: int) -> BallState:
         s = BallState()
         check(self.lib.rsg_get_ball_state(self.h, arena, C.byref(s)), "rsg_get_ball_state")
@@ -296,6 +312,12 @@ class Arena:
 
     def is_ball_scored(self) -> bool:
         return self.batch.is_ball_scored(0)
+
+    def get_mutator_config(self) -> "abi.MutatorConfig":
+        return self.batch.get_mutator_config()
+
+    def set_mutator_config(self, config: "abi.MutatorConfig") -> None:
+        self.batch.set_mutator_config(config)
 
     def set_goal_score_callback(self, fn) -> None:
         self.batch.set_goal_score_callback((lambda a, team: fn(self, team)) if fn else None)

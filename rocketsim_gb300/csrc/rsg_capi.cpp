@@ -222,6 +222,7 @@ struct rsg_batch {
     void* bump_user = nullptr;
     rsg_ball_hit_fn hit_fn = nullptr;
     void* hit_user = nullptr;
+    rsg_mutator_config mutators{};
 };
 
 namespace {
@@ -362,6 +363,80 @@ cudaError_t launch_remove_car(const BatchBuffers& b, uint32_t arena, uint32_t sl
 cudaError_t launch_init_arenas(const BatchBuffers& b, uint32_t ball_cell, cudaStream_t st);
 cudaError_t launch_demolish(const BatchBuffers& b, uint32_t arena, uint32_t slot, float delay, cudaStream_t st);
 CarCfgDev car_config_derived(const rsg_car_config& c) { return derive_config(c); }
+
+// MutatorConfig(GameMode) (src/Sim/MutatorConfig/MutatorConfig.cpp:5-40, defaults in MutatorConfig.h:16-79)
+// for the game modes the batch supports (soccar and THE_VOID share them).
+rsg_mutator_config default_mutators(int /*game_mode*/) {
+    rsg_mutator_config m;
+    std::memset(&m, 0, sizeof(m));
+    m.gravity = rsg_vec3{0, 0, RL::GRAVITY_Z};
+    m.car_mass = RL::CAR_MASS_BT;
+    m.car_world_friction = RL::CARWORLD_COLLISION_FRICTION;
+    m.car_world_restitution = RL::CARWORLD_COLLISION_RESTITUTION;
+    m.ball_mass = RL::BALL_MASS_BT;
+    m.ball_max_speed = RL::BALL_MAX_SPEED;
+    m.ball_drag = RL::BALL_DRAG;
+    m.ball_world_friction = RL::BALL_FRICTION;
+    m.ball_world_restitution = RL::BALL_RESTITUTION;
+    m.jump_accel = RL::JUMP_ACCEL;
+    m.jump_immediate_force = RL::JUMP_IMMEDIATE_FORCE;
+    m.boost_accel_ground = RL::BOOST_ACCEL_GROUND;
+    m.boost_accel_air = RL::BOOST_ACCEL_AIR;
+    m.boost_used_per_second = RL::BOOST_USED_PER_SECOND;
+    m.respawn_delay = RL::DEMO_RESPAWN_TIME;
+    m.bump_cooldown_time = RL::BUMP_COOLDOWN_TIME;
+    m.boost_pad_cooldown_big = RL::PAD_COOLDOWN_BIG;
+    m.boost_pad_cooldown_small = RL::PAD_COOLDOWN_SMALL;
+    m.car_spawn_boost_amount = RL::BOOST_SPAWN_AMOUNT;
+    m.ball_hit_extra_force_scale = 1;
+    m.bump_force_scale = 1;
+    m.ball_radius = RL::BALL_COLLISION_RADIUS_SOCCAR;
+    m.recharge_boost_per_second = RL::RECHARGE_BOOST_PER_SECOND;
+    m.recharge_boost_delay = RL::RECHARGE_BOOST_DELAY;
+    m.demo_mode = 0;
+    m.goal_base_threshold_y = RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y;
+    return m;
+}
+
+// The device copy the tick reads: gravity as btDiscreteDynamicsWorld::setGravity receives it
+// (gravity * UU_TO_BT, Arena.cpp:26), the ball radius as Ball::_BulletSetup sizes the sphere
+// (ballRadius * UU_TO_BT, Ball.cpp:79).
+MutatorsDev mutators_dev(const rsg_mutator_config& m) {
+    MutatorsDev d;
+    d.grav_bt[0] = m.gravity.x * RL::UU_TO_BT;
+    d.grav_bt[1] = m.gravity.y * RL::UU_TO_BT;
+    d.grav_bt[2] = m.gravity.z * RL::UU_TO_BT;
+    d.car_world_friction = m.car_world_friction;
+    d.car_world_restitution = m.car_world_restitution;
+    d.ball_mass = m.ball_mass;
+    d.ball_max_speed = m.ball_max_speed;
+    d.ball_drag = m.ball_drag;
+    d.ball_world_friction = m.ball_world_friction;
+    d.ball_world_restitution = m.ball_world_restitution;
+    d.jump_accel = m.jump_accel;
+    d.jump_immediate_force = m.jump_immediate_force;
+    d.boost_accel_ground = m.boost_accel_ground;
+    d.boost_accel_air = m.boost_accel_air;
+    d.boost_used_per_second = m.boost_used_per_second;
+    d.respawn_delay = m.respawn_delay;
+    d.bump_cooldown_time = m.bump_cooldown_time;
+    d.pad_cooldown_big = m.boost_pad_cooldown_big;
+    d.pad_cooldown_small = m.boost_pad_cooldown_small;
+    d.car_spawn_boost = m.car_spawn_boost_amount;
+    d.ball_hit_scale = m.ball_hit_extra_force_scale;
+    d.bump_force_scale = m.bump_force_scale;
+    d.ball_radius_uu = m.ball_radius;
+    d.ball_radius_bt = m.ball_radius * RL::UU_TO_BT;
+    d.unlimited_flips = m.unlimited_flips != 0;
+    d.unlimited_double_jumps = m.unlimited_double_jumps != 0;
+    d.recharge_boost = m.recharge_boost_enabled != 0;
+    d.recharge_per_second = m.recharge_boost_per_second;
+    d.recharge_delay = m.recharge_boost_delay;
+    d.demo_mode = m.demo_mode;
+    d.team_demos = m.enable_team_demos != 0;
+    d.goal_threshold_y = m.goal_base_threshold_y;
+    return d;
+}
 }  // namespace rsg
 
 extern "C" {
@@ -535,6 +610,8 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
     B.MC = (int)max_cars_per_arena;
     B.has_arena = arena ? 1 : 0;
     B.dt = 1.f / tick_rate;
+    b->mutators = default_mutators(game_mode);
+    B.mut = mutators_dev(b->mutators);
     B.mesh = mesh_ptrs(g_soccar);
     B.grid = default_grid();
     size_t A = n_arenas, MC = max_cars_per_arena;
@@ -608,6 +685,66 @@ int rsg_batch_num_arenas(const rsg_batch* b, uint32_t* out) {
     return RSG_OK;
 }
 
+static_assert(sizeof(rsg_mutator_config) == 116, "rsg_mutator_config layout");
+
+int rsg_get_default_mutator_config(int game_mode, rsg_mutator_config* out) {
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_THE_VOID)
+        return fail(RSG_ERR_ARG, "game mode not supported (soccar and THE_VOID are)");
+    *out = default_mutators(game_mode);
+    return RSG_OK;
+}
+
+int rsg_get_mutator_config(const rsg_batch* b, rsg_mutator_config* out) {
+    if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
+    *out = b->mutators;
+    return RSG_OK;
+}
+
+// Arena::SetMutatorConfig (src/Sim/Arena/Arena.cpp:17-48) for every arena of the batch.
+int rsg_set_mutator_config(rsg_batch* b, const rsg_mutator_config* c) {
+    if (!b || !c) return fail(RSG_ERR_ARG, "null argument");
+    if (c->car_mass != RL::CAR_MASS_BT)
+        return fail(RSG_ERR_ARG, "car_mass other than CAR_MASS_BT is not supported (RocketSim applies it only to "
+                                 "existing cars, with the ball's mass: Arena.cpp:35-41)");
+    if (!(c->ball_radius > 0) || !(c->ball_mass > 0) || c->demo_mode > 2)
+        return fail(RSG_ERR_ARG, "ball_radius and ball_mass must be > 0 and demo_mode 0..2");
+    {  // btRSBroadphase::createProxy rejects a dynamic AABB whose diagonal exceeds the cell size
+       // (libsrc/bullet3-3.24/BulletCollision/BroadphaseCollision/btRSBroadphase.cpp:228-229)
+        const float side = 2.f * (c->ball_radius * RL::UU_TO_BT + 0.08f);
+        if (3.f * side * side > b->buf.grid.cell * b->buf.grid.cell)
+            return fail(RSG_ERR_ARG, "ball_radius too large: the ball's bounding box must fit a broadphase cell");
+    }
+    const bool ball_changed = c->ball_radius != b->mutators.ball_radius || c->ball_mass != b->mutators.ball_mass;
+    if (ball_changed)
+        for (uint32_t n : b->ncars)
+            if (n) return fail(RSG_ERR_STATE, "ball_radius / ball_mass can change only while the batch holds no car "
+                                              "(RocketSim re-creates its ball, after the cars in Bullet's object "
+                                              "order: Arena.cpp:28-33)");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    b->mutators = *c;
+    b->buf.mut = mutators_dev(*c);
+    if (ball_changed) {  // the new ball starts at rest at (0, 0, radius) (Ball::_BulletSetup, Ball.cpp:85-115)
+        const size_t A = (size_t)b->buf.A;
+        std::vector<rsg_ball_state> balls(A);
+        rsg_ball_state s;
+        std::memset(&s, 0, sizeof(s));
+        s.pos = rsg_vec3{0, 0, c->ball_radius};
+        s.rot_mat.forward = rsg_vec3{1, 0, 0};
+        s.rot_mat.right = rsg_vec3{0, 1, 0};
+        s.rot_mat.up = rsg_vec3{0, 0, 1};
+        for (auto& x : balls) x = s;
+        if ((rc = ensure_stage(b, sizeof(rsg_ball_state) * A))) return rc;
+        RSG_CUDA(cudaMemcpyAsync(b->d_stage, balls.data(), sizeof(rsg_ball_state) * A, cudaMemcpyHostToDevice,
+                                 b->stream));
+        RSG_CUDA(launch_set_balls(b->buf, nullptr, (int)A, (const rsg_ball_state*)b->d_stage, b->stream));
+        RSG_CUDA(cudaStreamSynchronize(b->stream));
+    }
+    return RSG_OK;
+}
+
 int rsg_add_car(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* config, int respawn_index,
                 uint32_t* out_car_id) {
     int rc = check_arena(b, arena);
@@ -638,7 +775,7 @@ int rsg_add_car(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* co
     uint32_t cell = (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16);
     uint32_t flags = F_PRESENT | (team == RSG_TEAM_ORANGE ? F_TEAM_ORANGE : 0u);
     RSG_CUDA(launch_add_car(b->buf, arena, slot, id, (uint32_t)ci, flags, cell, slot + 1, pack_order(b, arena), b->stream));
-    rsg_car_state s = respawn_state(team, respawn_index < 0 ? 0 : respawn_index, RL::BOOST_SPAWN_AMOUNT);
+    rsg_car_state s = respawn_state(team, respawn_index < 0 ? 0 : respawn_index, b->mutators.car_spawn_boost_amount);
     if ((rc = ensure_stage(b, sizeof(rsg_car_state) + 8))) return rc;
     uint32_t idx[2] = {arena, slot};
     char* st = (char*)b->d_stage;
@@ -883,7 +1020,7 @@ int rsg_is_ball_scored(rsg_batch* b, uint32_t arena, int* out) {
     rsg_ball_state s;
     if ((rc = rsg_get_ball_state(b, arena, &s))) return rc;
     // Arena::IsBallScored, soccar (Arena.cpp:893-901), on the state in uu
-    *out = std::fabs(s.pos.y) > (RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y + RL::BALL_COLLISION_RADIUS_SOCCAR) ? 1 : 0;
+    *out = std::fabs(s.pos.y) > (b->mutators.goal_base_threshold_y + b->mutators.ball_radius) ? 1 : 0;
     return RSG_OK;
 }
 

@@ -22,6 +22,7 @@ constexpr float BALL_REST_Z = 93.15f, BALL_MAX_ANG_SPEED = 6.f, BALL_DRAG = 0.03
 constexpr float BALL_FRICTION = 0.35f, BALL_RESTITUTION = 0.6f;
 constexpr float CAR_MAX_SPEED = 2300.f, BALL_MAX_SPEED = 6000.f;
 constexpr float BOOST_MAX = 100.f, BOOST_USED_PER_SECOND = BOOST_MAX / 3, BOOST_MIN_TIME = 0.1f;
+constexpr float RECHARGE_BOOST_PER_SECOND = 10, RECHARGE_BOOST_DELAY = 0.25f;
 constexpr float BOOST_ACCEL_GROUND = 2975 / 3.f, BOOST_ACCEL_AIR = 3175 / 3.f, BOOST_SPAWN_AMOUNT = BOOST_MAX / 3;
 constexpr float CAR_MAX_ANG_SPEED = 5.5f;
 constexpr float SUPERSONIC_START_SPEED = 2200.f, SUPERSONIC_MAINTAIN_MIN_SPEED = SUPERSONIC_START_SPEED - 100.f;

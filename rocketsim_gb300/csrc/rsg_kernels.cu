@@ -19,6 +19,7 @@ static BatchView make_view(const BatchBuffers& b) {
     v.MC = b.MC;
     v.has_arena = b.has_arena;
     v.dt = b.dt;
+    v.mut = b.mut;
     v.rec = b.rec;
     v.rec_words = rec_words(b.MC);
     v.au = b.au;
@@ -431,7 +432,7 @@ __global__ void rsg_is_scored_kernel(BatchView bv, int* __restrict__ out) {
     if (ar >= bv.A) return;
     SoA s{bv, ar};
     float y = s.bf(BF_POS + 1) * RL::BT_TO_UU;
-    out[ar] = fabsf(y) > (RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y + RL::BALL_COLLISION_RADIUS_SOCCAR) ? 1 : 0;
+    out[ar] = fabsf(y) > (bv.mut.goal_threshold_y + bv.mut.ball_radius_uu) ? 1 : 0;
 }
 
 static int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }

@@ -28,6 +28,7 @@ struct DevMeshPtrs {
 struct BatchBuffers {
     int A, MC, has_arena;
     float dt;
+    MutatorsDev mut;
     uint32_t* rec;  // A records of rec_words(MC) 32-bit words
     uint32_t* au;   // [AU_COUNT][A]
     const CarCfgDev* cfgs;

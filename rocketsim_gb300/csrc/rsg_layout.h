@@ -148,6 +148,26 @@ RSG_LAYOUT_FN int rec_pad_u(int f, int pad) { return REC_PADS + pad * PAD_WORDS 
 RSG_LAYOUT_FN int rec_car_f(int f, int slot) { return REC_CARS + slot * CAR_WORDS + f; }
 RSG_LAYOUT_FN int rec_car_u(int f, int slot) { return REC_CARS + slot * CAR_WORDS + CF_COUNT + f; }
 
+// The mutator values the tick reads (MutatorConfig, src/Sim/MutatorConfig/MutatorConfig.h:16-79),
+// in the units the tick uses: gravity multiplied by UU_TO_BT as btDiscreteDynamicsWorld::setGravity
+// receives it (Arena.cpp:26), the ball radius in both units.
+struct MutatorsDev {
+    float grav_bt[3];
+    float car_world_friction, car_world_restitution;
+    float ball_mass, ball_max_speed, ball_drag, ball_world_friction, ball_world_restitution;
+    float jump_accel, jump_immediate_force;
+    float boost_accel_ground, boost_accel_air, boost_used_per_second;
+    float respawn_delay, bump_cooldown_time;
+    float pad_cooldown_big, pad_cooldown_small;
+    float car_spawn_boost;
+    float ball_hit_scale, bump_force_scale;
+    float ball_radius_uu, ball_radius_bt;
+    int unlimited_flips, unlimited_double_jumps, recharge_boost;
+    float recharge_per_second, recharge_delay;
+    int demo_mode, team_demos;
+    float goal_threshold_y;
+};
+
 // Per-car-config constants uploaded once (derived like Car::_BulletSetup, Car.cpp:195-292)
 struct CarCfgDev {
     float he[3];          // box implicit half extents (without margin)

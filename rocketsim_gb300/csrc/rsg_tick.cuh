@@ -101,6 +101,7 @@ struct BatchView {
     int A, MC;  // arenas, car slots per arena
     int has_arena;
     float dt;
+    MutatorsDev mut;
     uint32_t* rec;  // A records of rec_words(MC) words
     int rec_words;
     uint32_t* au;   // [AU_COUNT][A]
@@ -237,6 +238,7 @@ struct Ctx {
     uint32_t err;
     int nevents;
     float solver_dt;
+    float ball_r, ball_breaking;  // ball radius (Bullet units) and its contact breaking threshold
     int serial;  // the pre-tick of this tick runs car by car in update order
     const Subtree* sub;  // BVH subtree headers (the block's shared-memory copy when there is one)
     int on_car;  // a wheel rests on another car: the car logic after the rays runs in update order
@@ -711,7 +713,7 @@ RSG_DN RayHit cast_ray(const BatchView& bv, Ctx& a, V3 from, V3 to, int self_obj
         if (frac == 0.f) break;
         V3 n;
         if (o == OBJ_BALL) {
-            if (ray_sphere(from, to, a.ball.xf.o, RL::BALL_COLLISION_RADIUS_SOCCAR * RL::UU_TO_BT, frac, n)) { obj = o; nrm = n; }
+            if (ray_sphere(from, to, a.ball.xf.o, a.ball_r, frac, n)) { obj = o; nrm = n; }
         } else {
             Car& c = a.cars[o - OBJ_CAR0];
             Xf bx = c.rb.xf;
@@ -1079,7 +1081,7 @@ RSG_D void update_wheels_sticky(Car& c, const WheelsCommon& wc) {
     }
 }
 
-RSG_D void update_boost(Car& c, float dt) {  // Car::_UpdateBoost (Car.cpp:486-533)
+RSG_D void update_boost(Car& c, float dt, const MutatorsDev& m) {  // Car::_UpdateBoost (Car.cpp:486-533)
     bool has = c.boost > 0;
     bool boosting = c.f(F_BOOSTING);
     if (has) {
@@ -1092,17 +1094,19 @@ RSG_D void update_boost(Car& c, float dt) {  // Car::_UpdateBoost (Car.cpp:486-5
     if (boosting) c.boosting_time += dt;
     else c.boosting_time = 0;
     if (boosting) {
-        c.boost = rs_maxf(c.boost - RL::BOOST_USED_PER_SECOND * dt, 0);
-        c.rb.total_force += (c.f(F_ON_GROUND) ? RL::BOOST_ACCEL_GROUND : RL::BOOST_ACCEL_AIR) * RL::UU_TO_BT * c.fwd() *
+        c.boost = rs_maxf(c.boost - m.boost_used_per_second * dt, 0);
+        c.rb.total_force += (c.f(F_ON_GROUND) ? m.boost_accel_ground : m.boost_accel_air) * RL::UU_TO_BT * c.fwd() *
                             RL::CAR_MASS_BT;
         c.time_since_boost = 0;
     } else {
         c.time_since_boost += dt;
+        if (m.recharge_boost)
+            if (c.time_since_boost >= m.recharge_delay) c.boost += m.recharge_per_second * dt;
     }
     c.boost = rs_minf(c.boost, RL::BOOST_MAX);
 }
 
-RSG_D void update_jump(Car& c, float dt, bool pressed) {  // Car::_UpdateJump (Car.cpp:535-582)
+RSG_D void update_jump(Car& c, float dt, bool pressed, const MutatorsDev& m) {  // Car::_UpdateJump (Car.cpp:535-582)
     if (c.f(F_ON_GROUND) && !c.f(F_JUMPING)) {
         if (c.f(F_HAS_JUMPED) && c.jump_time < RL::JUMP_MIN_TIME + RL::JUMP_RESET_TIME_PAD) {
         } else {
@@ -1115,11 +1119,11 @@ RSG_D void update_jump(Car& c, float dt, bool pressed) {  // Car::_UpdateJump (C
     } else if (c.f(F_ON_GROUND) && pressed) {
         c.setf(F_JUMPING, true);
         c.jump_time = 0;
-        c.rb.apply_central_impulse(c.up() * RL::JUMP_IMMEDIATE_FORCE * RL::UU_TO_BT * RL::CAR_MASS_BT);
+        c.rb.apply_central_impulse(c.up() * m.jump_immediate_force * RL::UU_TO_BT * RL::CAR_MASS_BT);
     }
     if (c.f(F_JUMPING)) {
         c.setf(F_HAS_JUMPED, true);
-        V3 tf = c.up() * RL::JUMP_ACCEL;
+        V3 tf = c.up() * m.jump_accel;
         if (c.jump_time < RL::JUMP_MIN_TIME) tf *= 0.62f;
         c.rb.total_force += tf * RL::UU_TO_BT * RL::CAR_MASS_BT;
     }
@@ -1175,7 +1179,8 @@ RSG_D void update_air_torque(Car& c, bool update_air_control) {  // Car::_Update
     if (c.ctrl[0] != 0) c.rb.total_force += c.fwd() * c.ctrl[0] * RL::THROTTLE_AIR_ACCEL * RL::UU_TO_BT * RL::CAR_MASS_BT;
 }
 
-RSG_D void update_double_jump_or_flip(Car& c, float dt, bool pressed, float fwd_speed) {  // Car.cpp:671-781
+RSG_D void update_double_jump_or_flip(Car& c, float dt, bool pressed, float fwd_speed,
+                                      const MutatorsDev& m) {  // Car.cpp:671-781
     if (c.f(F_ON_GROUND)) {
         c.setf(F_HAS_DJ, false);
         c.setf(F_HAS_FLIPPED, false);
@@ -1190,7 +1195,7 @@ RSG_D void update_double_jump_or_flip(Car& c, float dt, bool pressed, float fwd_
             float pitch = c.ctrl[2], yaw = c.ctrl[3], roll = c.ctrl[4];
             float mag = fabsf(yaw) + fabsf(pitch) + fabsf(roll);
             bool flip_input = mag >= c.cfg->dodge_deadzone;
-            bool can = (!c.f(F_HAS_DJ) && !c.f(F_HAS_FLIPPED));
+            bool can = (!c.f(F_HAS_DJ) && !c.f(F_HAS_FLIPPED)) || (flip_input ? m.unlimited_flips : m.unlimited_double_jumps);
             if (c.f(F_AUTOFLIPPING)) can = false;
             if (can) {
                 if (flip_input) {
@@ -1322,9 +1327,9 @@ RSG_DN void car_pre_after_rays_grp(const BatchView& bv, Ctx& a, Car& c, int wl, 
         update_wheels_sticky(c, wc);
         if (nwc < 3) update_air_torque(c, nwc == 0);
         else c.setf(F_FLIPPING, false);
-        update_jump(c, dt, pressed);
+        update_jump(c, dt, pressed, bv.mut);
         update_auto_flip(c, dt, pressed);
-        update_double_jump_or_flip(c, dt, pressed, fwd_speed);
+        update_double_jump_or_flip(c, dt, pressed, fwd_speed, bv.mut);
         if (c.ctrl[0] && ((nwc > 0 && nwc < 4) || c.f(F_WC_CONTACT))) update_auto_roll(c, nwc);
         c.setf(F_WC_CONTACT, false);
     }
@@ -1364,7 +1369,7 @@ RSG_DN void car_pre_after_rays_grp(const BatchView& bv, Ctx& a, Car& c, int wl, 
     }
     RSG_FT(44);
     if (wl == 0) {
-        update_boost(c, dt);
+        update_boost(c, dt, bv.mut);
         RSG_FT(45);
     }
     __syncwarp(gmask);
@@ -1391,7 +1396,7 @@ RSG_DN void car_pre_tick(const BatchView& bv, Ctx& a, Car& c) {  // Car::_PreTic
     for (int k = 0; k < 5; k++) c.ctrl[k] = rs_clampf(c.ctrl[k], -1, 1);
     if (c.f(F_DEMOED)) {
         c.demo_timer = rs_maxf(c.demo_timer - dt, 0);
-        if (c.demo_timer == 0) car_set_respawn(c, 0, RL::BOOST_SPAWN_AMOUNT);
+        if (c.demo_timer == 0) car_set_respawn(c, 0, bv.mut.car_spawn_boost);
         c.rb.act = DISABLE_SIMULATION;
         c.rb.no_contact_response = true;
     } else {
@@ -1482,9 +1487,8 @@ RSG_D void car_compound_aabb(const Car& c, const Xf& t, V3& mn, V3& mx) {  // bt
     mn = center - ext;
     mx = center + ext;
 }
-constexpr float BALL_RADIUS_BT = RL::BALL_COLLISION_RADIUS_SOCCAR * RL::UU_TO_BT;
-RSG_D void ball_aabb(const Xf& t, V3& mn, V3& mx) {
-    float m = BALL_RADIUS_BT + 0.08f;
+RSG_D void ball_aabb(const Xf& t, float radius, V3& mn, V3& mx) {
+    float m = radius + 0.08f;
     mn = t.o - V3(m, m, m);
     mx = t.o + V3(m, m, m);
 }
@@ -2488,7 +2492,7 @@ RSG_DN void contact_added(const BatchView& bv, Ctx& a, Manifold& m, int idx, int
                     V3 hit = rs_normalized(rel_pos * V3(1, 1, RL::BALL_CAR_EXTRA_IMPULSE_Z_SCALE));
                     V3 adj = cf * dot(hit, cf) * (1 - RL::BALL_CAR_EXTRA_IMPULSE_FORWARD_SCALE);
                     hit = rs_normalized(hit - adj);
-                    V3 added = (hit * rs) * curve_eval(c_curves[CV_BALL_EXTRA], rs) * 1.f;
+                    V3 added = (hit * rs) * curve_eval(c_curves[CV_BALL_EXTRA], rs) * bv.mut.ball_hit_scale;
                     car.bhi_extra = added;
                     a.ball_cache += added * RL::UU_TO_BT;
                 }
@@ -2518,20 +2522,20 @@ RSG_DN void contact_added(const BatchView& bv, Ctx& a, Manifold& m, int idx, int
                         V3 lp = sw ? cp.local_b : cp.local_a;
                         bool bumper = (lp.x * RL::BT_TO_UU) > RL::BUMP_MIN_FORWARD_DIST;
                         if (bumper) {
-                            bool demo = s.f(F_SUPERSONIC);
-                            if (demo) demo = s.f(F_TEAM_ORANGE) != o.f(F_TEAM_ORANGE);
+                            bool demo = bv.mut.demo_mode == 1 ? true : (bv.mut.demo_mode == 2 ? false : s.f(F_SUPERSONIC));
+                            if (demo && !bv.mut.team_demos) demo = s.f(F_TEAM_ORANGE) != o.f(F_TEAM_ORANGE);
                             if (demo) {
                                 o.setf(F_DEMOED, true);
-                                o.demo_timer = RL::DEMO_RESPAWN_TIME;
+                                o.demo_timer = bv.mut.respawn_delay;
                             } else {
                                 bool gh = o.f(F_ON_GROUND);
                                 float bs = curve_eval(c_curves[gh ? CV_BUMP_GROUND : CV_BUMP_AIR], sto);
                                 V3 hu = gh ? o.up() : V3(0, 0, 1);
-                                V3 bi = vd * bs + hu * curve_eval(c_curves[CV_BUMP_UP], sto) * 1.f;
+                                V3 bi = vd * bs + hu * curve_eval(c_curves[CV_BUMP_UP], sto) * bv.mut.bump_force_scale;
                                 o.vel_cache += bi * RL::UU_TO_BT;
                             }
                             s.cc_other = o.id;
-                            s.cc_cooldown = RL::BUMP_COOLDOWN_TIME;
+                            s.cc_cooldown = bv.mut.bump_cooldown_time;
                             push_event(a, RSG_EVENT_BUMP, s.id, o.id, demo ? 1u : 0u);
                         }
                     }
@@ -2541,8 +2545,8 @@ RSG_DN void contact_added(const BatchView& bv, Ctx& a, Manifold& m, int idx, int
             // car-world (src/Sim/Arena/Arena.cpp:407-414)
             car.setf(F_WC_CONTACT, true);
             car.wc_normal = cp.normal;
-            cp.friction = RL::CARWORLD_COLLISION_FRICTION;
-            cp.restitution = RL::CARWORLD_COLLISION_RESTITUTION;
+            cp.friction = bv.mut.car_world_friction;
+            cp.restitution = bv.mut.car_world_restitution;
         }
     } else if (ua == 2 && ub == -1) {
         cp.special = true;  // ball-world (src/Sim/Arena/Arena.cpp:298-306)
@@ -3095,7 +3099,7 @@ RSG_D void step_bodies_pre(const BatchView& bv, Ctx& a, int lane) {
     if (lane < nd) {
         Body& b = a.body(OBJ_BALL + lane);
         // applyGravity (btDiscreteDynamicsWorld.cpp:265-277)
-        if (b.is_active()) b.total_force += V3(0, 0, RL::GRAVITY_Z * RL::UU_TO_BT) * (1.f / b.inv_mass);
+        if (b.is_active()) b.total_force += V3(bv.mut.grav_bt[0], bv.mut.grav_bt[1], bv.mut.grav_bt[2]) * (1.f / b.inv_mass);
         // predictUnconstraintMotion (btDiscreteDynamicsWorld.cpp:1029-1044)
         b.lin_vel *= powf(1.f - b.lin_damping, dt);
         b.ang_vel *= powf(1.f - 0.f, dt);
@@ -3103,8 +3107,8 @@ RSG_D void step_bodies_pre(const BatchView& bv, Ctx& a, int lane) {
         // updateSingleAabb + btRSBroadphase::setAabb
         V3 mn, mx, mn2, mx2;
         if (lane == 0) {
-            ball_aabb(b.xf, mn, mx);
-            ball_aabb(b.interp, mn2, mx2);
+            ball_aabb(b.xf, a.ball_r, mn, mx);
+            ball_aabb(b.interp, a.ball_r, mn2, mx2);
         } else {
             Car& c = a.cars[lane - 1];
             car_compound_aabb(c, b.xf, mn, mx);
@@ -3137,7 +3141,6 @@ RSG_D void step_bodies_pre(const BatchView& bv, Ctx& a, int lane) {
 // lanes, results committed in pair order by lane 0), islands and the solver (lane 0).
 enum PairKind : int8_t { PK_SKIP = 0, PK_BALL_MESH, PK_BALL_PLANE, PK_CAR_MESH, PK_CAR_PLANE, PK_CAR_BALL, PK_CAR_CAR };
 
-constexpr float BALL_BREAKING = (BALL_RADIUS_BT + 0.08f) * 0.02f;  // getAngularMotionDisc * gContactBreakingThreshold
 
 // calculateOverlappingPairs (btRSBroadphase.cpp:392-468) and the dispatcher's choice of algorithm
 RSG_DN void build_pairs(const BatchView& bv, Ctx& a) {
@@ -3204,7 +3207,7 @@ RSG_DN void build_pairs(const BatchView& bv, Ctx& a) {
                 car_child_xf(c, cx);
                 V3 bmn, bmx, smn, smx;
                 car_box_aabb(c, cx, bmn, bmx);
-                ball_aabb(a.ball.xf, smn, smx);
+                ball_aabb(a.ball.xf, a.ball_r, smn, smx);
                 if (aabb_overlap(bmn, bmx, smn, smx)) k = PK_CAR_BALL;
             } else {
                 k = PK_CAR_CAR;
@@ -3246,7 +3249,7 @@ RSG_D int8_t classify_pair(const BatchView& bv, Ctx& a, int o0, int o1) {
             car_child_xf(c, cx);
             V3 bmn, bmx, smn, smx;
             car_box_aabb(c, cx, bmn, bmx);
-            ball_aabb(a.ball.xf, smn, smx);
+            ball_aabb(a.ball.xf, a.ball_r, smn, smx);
             if (aabb_overlap(bmn, bmx, smn, smx)) k = PK_CAR_BALL;
         } else {
             k = PK_CAR_CAR;
@@ -3327,8 +3330,8 @@ RSG_D void dyn_shape(Ctx& a, int o, Xf& xf, Convex& sh, float& breaking) {
     if (o == OBJ_BALL) {
         xf = a.ball.xf;
         sh.type = 1;
-        sh.margin = BALL_RADIUS_BT;
-        breaking = BALL_BREAKING;
+        sh.margin = a.ball_r;
+        breaking = a.ball_breaking;
     } else {
         Car& c = a.cars[o - OBJ_CAR0];
         car_child_xf(c, xf);
@@ -3350,9 +3353,9 @@ RSG_D CandRes car_ball_test(Ctx& a, int car_obj, uint32_t& warn) {
     box.margin = c.cfg->margin;
     Convex sph;
     sph.type = 1;
-    sph.margin = BALL_RADIUS_BT;
+    sph.margin = a.ball_r;
     sph.he = V3(0, 0, 0);
-    float br = c.cfg->breaking < BALL_BREAKING ? c.cfg->breaking : BALL_BREAKING;
+    float br = c.cfg->breaking < a.ball_breaking ? c.cfg->breaking : a.ball_breaking;
     float md = box.margin + sph.margin + br;
     GjkOut g = gjk(box, cx, sph, a.ball.xf, md * md);
     if (g.epa_needed) warn |= WARN_EPA_SKIPPED;
@@ -3447,7 +3450,7 @@ RSG_DN void commit_sweep(const BatchView& bv, Ctx& a, CommitState& cs, int base,
             if (k == PK_CAR_BALL) {
                 float cb = a.cars[o1 - OBJ_CAR0].cfg->breaking;
                 cs.mi = a.nman;
-                new_manifold(a, o1, OBJ_BALL, cb < BALL_BREAKING ? cb : BALL_BREAKING);
+                new_manifold(a, o1, OBJ_BALL, cb < a.ball_breaking ? cb : a.ball_breaking);
                 cs.x0 = a.body(o1).xf;
                 cs.x1 = a.ball.xf;
                 cs.fr = combined_friction(a, OBJ_BALL, o1);
@@ -3828,9 +3831,9 @@ RSG_D void step_bodies_post(const BatchView& bv, Ctx& a, int lane) {
 }
 
 // ---------------------------------------------------------------- boost pads and goal
-RSG_D bool ball_scored(const Ctx& a) {  // Arena::IsBallScored, soccar (src/Sim/Arena/Arena.cpp:893-901)
+RSG_D bool ball_scored(const Ctx& a, const MutatorsDev& m) {  // Arena::IsBallScored, soccar (src/Sim/Arena/Arena.cpp:893-901)
     float y = a.ball.xf.o.y * RL::BT_TO_UU;
-    return fabsf(y) > (RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y + RL::BALL_COLLISION_RADIUS_SOCCAR);
+    return fabsf(y) > (m.goal_threshold_y + m.ball_radius_uu);
 }
 
 RSG_D void pad_check(Ctx& a, Pad& p, int pi, int ci) {  // BoostPad::_CheckCollide (src/Sim/BoostPad/BoostPad.cpp:62-86)
@@ -4084,14 +4087,14 @@ RSG_D void arena_post(const BatchView& bv, Ctx& a) {
             a.ball_cache = V3(0, 0, 0);
         }
         V3 v = ball.lin_vel, wv = ball.ang_vel;
-        const float ms = RL::BALL_MAX_SPEED * RL::UU_TO_BT;
+        const float ms = bv.mut.ball_max_speed * RL::UU_TO_BT;
         if (len2(v) > ms * ms) v = normalized(v) * ms;
         if (len2(wv) > (RL::BALL_MAX_ANG_SPEED * RL::BALL_MAX_ANG_SPEED)) wv = normalized(wv) * RL::BALL_MAX_ANG_SPEED;
         ball.lin_vel = v;
         ball.ang_vel = wv;
         a.ball_ticks++;
     }
-    if (bv.has_arena && ball_scored(a)) {
+    if (bv.has_arena && ball_scored(a, bv.mut)) {
         uint32_t team = (-(a.ball.xf.o.y) < 0) ? 0u : 1u;  // RS_TEAM_FROM_Y(-y)
         push_event(a, RSG_EVENT_GOAL, team, 0, 0);
     }
@@ -4151,7 +4154,7 @@ RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, 
                 locked = a.cars[p.cur_locked].id;
                 if (p.active) {
                     p.active = false;
-                    p.cooldown = i < 6 ? RL::PAD_COOLDOWN_BIG : RL::PAD_COOLDOWN_SMALL;
+                    p.cooldown = i < 6 ? bv.mut.pad_cooldown_big : bv.mut.pad_cooldown_small;
                 }
             }
             p.prev_locked = locked;
@@ -4230,18 +4233,20 @@ RSG_DN void load_arena(const BatchView& bv, int ar, Ctx& a) {  // scalars and ba
     for (int r = 0; r < 3; r++) b.xf.b.r[r] = V3(s.bf(BF_BASIS + 3 * r), s.bf(BF_BASIS + 3 * r + 1), s.bf(BF_BASIS + 3 * r + 2));
     b.lin_vel = V3(s.bf(BF_VEL), s.bf(BF_VEL + 1), s.bf(BF_VEL + 2));
     b.ang_vel = V3(s.bf(BF_ANG), s.bf(BF_ANG + 1), s.bf(BF_ANG + 2));
+    a.ball_r = bv.mut.ball_radius_bt;
+    a.ball_breaking = (a.ball_r + 0.08f) * 0.02f;  // getAngularMotionDisc * gContactBreakingThreshold
     {
-        const float r = BALL_RADIUS_BT, mass = RL::BALL_MASS_BT;
+        const float r = a.ball_r, mass = bv.mut.ball_mass;
         float elem = 0.4f * mass * r * r;
         b.inv_mass = 1.f / mass;
         b.inv_inertia_local = V3(1.f / elem, 1.f / elem, 1.f / elem);
     }
-    b.lin_damping = RL::BALL_DRAG;
+    b.lin_damping = bv.mut.ball_drag;
     b.act = ACTIVE_TAG;
     b.no_rot = true;
     b.no_contact_response = false;
-    b.friction = RL::BALL_FRICTION;
-    b.restitution = RL::BALL_RESTITUTION;
+    b.friction = bv.mut.ball_world_friction;
+    b.restitution = bv.mut.ball_world_restitution;
     body_cell_load(bv.grid, b, s.bu(BU_CELL));
     b.cell_seq = s.bu(BU_CELL_SEQ);
     body_common(b);

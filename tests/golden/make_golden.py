@@ -39,11 +39,12 @@ def scenario_list():
     return out
 
 
-def main():
+def record(scs, mutators=None, epa=True):
+    """Plays the scenarios through the reference (and, with `epa`, the restatement to find the
+    first EPA tick) and returns the arrays of the golden file."""
     from oracle.pyoracle import build_ref
     if build_ref() is None:
         raise SystemExit("reference sources not found")
-    scs = scenario_list()
     S, MC = len(scs), max(len(s.cars) for s in scs)
     car_dt, ball_dt = np.dtype(abi.CarState), np.dtype(abi.BallState)
     ncars = np.array([len(s.cars) for s in scs], np.int32)
@@ -77,22 +78,24 @@ def main():
             disc_pads[si, t] = discrete_pads(pads)
             for e in a.pop_events():
                 events.append((si,) + e)
-
-        a, ids = run_cpu("ref", sc, TICKS, rec)  # fixes sc.order to the reference's iteration order
+        a, ids = run_cpu("ref", sc, TICKS, rec, mutators)  # fixes sc.order to the reference's iteration order
         a.close()
         order[si, :n] = sc.order
-
-        def rec_oracle(t, a, ids):
-            if epa_tick[si] < 0 and a.counters()[3] > 0:
-                epa_tick[si] = t
-        o, _ = run_cpu("oracle", sc, TICKS, rec_oracle)
-        o.close()
+        if epa:
+            def rec_oracle(t, a, ids):
+                if epa_tick[si] < 0 and a.counters()[3] > 0:
+                    epa_tick[si] = t
+            o, _ = run_cpu("oracle", sc, TICKS, rec_oracle)
+            o.close()
         print(f"scenario {si}: seed {sc.seed} cars {n} epa_tick {epa_tick[si]}")
-    np.savez_compressed(
-        OUT, seeds=np.array([s.seed for s in scs]), ncars=ncars, presets=presets, teams=teams, order=order,
-        init_cars=init_cars, init_ball=init_ball, controls=controls, cars_t1=cars_t[1], ball_t1=ball_t[1],
-        cars_t8=cars_t[8], ball_t8=ball_t[8], disc_cars=disc_cars, disc_pads=disc_pads,
-        events=np.array(events, np.uint64).reshape(-1, 6), epa_tick=epa_tick, mesh_seed=np.int32(0))
+    return dict(seeds=np.array([s.seed for s in scs]), ncars=ncars, presets=presets, teams=teams, order=order,
+                init_cars=init_cars, init_ball=init_ball, controls=controls, cars_t1=cars_t[1], ball_t1=ball_t[1],
+                cars_t8=cars_t[8], ball_t8=ball_t[8], disc_cars=disc_cars, disc_pads=disc_pads,
+                events=np.array(events, np.uint64).reshape(-1, 6), epa_tick=epa_tick, mesh_seed=np.int32(0))
+
+
+def main():
+    np.savez_compressed(OUT, **record(scenario_list()))
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
 

@@ -161,10 +161,13 @@ def _controls_struct(row) -> abi.CarControls:
 
 
 # ---------------------------------------------------------------- CPU checkers
-def setup_cpu(kind: str, sc: Scenario):
-    """Builds the scenario on a SimArena of `kind` ('ref', 'oracle', 'oracle_sse')."""
+def setup_cpu(kind: str, sc: Scenario, mutators=None):
+    """Builds the scenario on a SimArena of `kind` ('ref', 'oracle', 'oracle_sse'); `mutators` (an
+    abi.MutatorConfig, reference only) is set before the cars are added."""
     from oracle.pyoracle import SimArena, CarState as OCarState, BallState as OBallState, CarControls as OCtl
     a = SimArena(kind, mesh_bytes())
+    if mutators is not None:
+        a.set_mutator_config(mutators)
     ids = [a.add_car(t, p) for t, p in zip(sc.teams, sc.presets)]
     for cid, s in zip(ids, sc.cars):
         a.set_car(cid, OCarState.from_buffer_copy(bytes(s)))
@@ -179,12 +182,12 @@ def setup_cpu(kind: str, sc: Scenario):
     return a, ids
 
 
-def run_cpu(kind: str, sc: Scenario, ticks: int, record=None):
+def run_cpu(kind: str, sc: Scenario, ticks: int, record=None, mutators=None):
     """Steps a fresh checker arena through `ticks` ticks of the scenario.
 
     `record(t, arena, ids)` is called after each tick."""
     from oracle.pyoracle import CarControls as OCtl
-    a, ids = setup_cpu(kind, sc)
+    a, ids = setup_cpu(kind, sc, mutators)
     for t in range(ticks):
         for i, cid in enumerate(ids):
             a.set_controls(cid, OCtl.from_buffer_copy(bytes(_controls_struct(sc.controls[t, i]))))
@@ -202,12 +205,14 @@ def cpu_snapshot(a, ids):
 
 
 # ---------------------------------------------------------------- GPU
-def setup_gpu(scs: list[Scenario], max_cars: int | None = None):
-    """One ArenaBatch holding one arena per scenario."""
+def setup_gpu(scs: list[Scenario], max_cars: int | None = None, mutators=None):
+    """One ArenaBatch holding one arena per scenario (`mutators` set before the cars are added)."""
     import rocketsim_gb300 as rsg
     rsg.init_from_mem([mesh_bytes()])
     mc = max_cars or max(len(s.cars) for s in scs)
     batch = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, len(scs), mc, 120.0)
+    if mutators is not None:
+        batch.set_mutator_config(mutators)
     all_ids = []
     for ai, sc in enumerate(scs):
         ids = [batch.add_car(ai, t, p, 0) for t, p in zip(sc.teams, sc.presets)]
