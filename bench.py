@@ -313,7 +313,7 @@ def run_gpu(args, rank: int, world: int):
     ctl_np = h_ctl.numpy().view(rsg.CONTROLS_DTYPE)
     out_cars = np.zeros(A * CARS, rsg.CAR_STATE_DTYPE)
     out_balls = np.zeros(A, rsg.BALL_STATE_DTYPE)
-    out_pads = np.zeros(A * abi.NUM_BOOST_PADS, rsg.PAD_STATE_DTYPE)
+    out_pads = np.zeros(A * batch.num_pads, rsg.PAD_STATE_DTYPE)
     e2e_steps = max(3, min(args.steps, 20))
     for s in range(2):
         ctl_np[:] = seq[s, 0]

@@ -162,6 +162,32 @@ typedef struct rsg_car_config {
     float dodge_deadzone;
 } rsg_car_config;
 
+/* BoostPadConfig (src/Sim/BoostPad/BoostPad.h:14-18) */
+typedef struct rsg_boost_pad_config {
+    rsg_vec3 pos;
+    uint8_t is_big;
+    uint8_t _pad0[3];
+} rsg_boost_pad_config;
+
+/* ArenaConfig (src/Sim/Arena/ArenaConfig/ArenaConfig.h:19-50), field for field.
+ * custom_boost_pads is a host array of num_custom_boost_pads entries, read at
+ * batch creation.  The batch holds up to 34 pads per arena, keeps the broadphase
+ * of the default min_pos / max_pos / max_aabb_len / use_custom_broadphase
+ * (other values return RSG_ERR_ARG), and sizes its memory by the batch
+ * (mem_weight_mode and max_objects are accepted and have no effect). */
+typedef struct rsg_arena_config {
+    uint8_t mem_weight_mode;
+    uint8_t no_ball_rot;
+    uint8_t use_custom_broadphase;
+    uint8_t use_custom_boost_pads;
+    rsg_vec3 min_pos;
+    rsg_vec3 max_pos;
+    float max_aabb_len;
+    int32_t max_objects;
+    uint32_t num_custom_boost_pads;
+    const rsg_boost_pad_config* custom_boost_pads;
+} rsg_arena_config;
+
 /* MutatorConfig (src/Sim/MutatorConfig/MutatorConfig.h:16-79), field for field,
  * uu units like the reference.  demo_mode: 0 normal, 1 on contact, 2 disabled. */
 typedef struct rsg_mutator_config {
@@ -243,8 +269,18 @@ int rsg_get_car_config_preset(int preset, rsg_car_config* out);
  * max_cars_per_arena cars.  tick_rate must be 15..120 (Arena.cpp:419).
  * Allocates all device memory of the batch. */
 rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate);
+/* rsg_batch_create with an ArenaConfig (Arena::Create's second argument,
+ * Arena.h:111): custom boost pads (checked against every car without
+ * BoostPadGrid, Arena.cpp:501-506, 724-728) and noBallRot. */
+rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate,
+                               const rsg_arena_config* config);
+/* ArenaConfig's defaults */
+int rsg_get_default_arena_config(rsg_arena_config* out);
 void rsg_batch_destroy(rsg_batch* batch);
 int rsg_batch_num_arenas(const rsg_batch* batch, uint32_t* out);
+/* Boost pads per arena (Arena::GetBoostPads().size()): the pad arrays of the
+ * state calls hold this many pads per arena. */
+int rsg_batch_num_pads(const rsg_batch* batch, uint32_t* out);
 
 /* MutatorConfig(GameMode) (MutatorConfig.cpp:5-40): the defaults of a game mode. */
 int rsg_get_default_mutator_config(int game_mode, rsg_mutator_config* out);

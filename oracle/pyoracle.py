@@ -167,7 +167,8 @@ def load(kind: str) -> _Lib:
 class SimArena:
     """One arena of the reference (kind='ref') or of the restatement (kind='oracle')."""
 
-    def __init__(self, kind: str, cmf: bytes | None, game_mode: int = 0, tick_rate: float = 120.0):
+    def __init__(self, kind: str, cmf: bytes | None, game_mode: int = 0, tick_rate: float = 120.0,
+                 config=None):
         self.kind = kind
         self.lib = load(kind)
         p = self.lib.prefix
@@ -183,7 +184,13 @@ class SimArena:
                 _INIT[kind] = cmf
             elif prev != cmf:
                 raise RuntimeError("a different mesh was already loaded in this process")
-        self.h = self.lib[p + "arena_create"](game_mode, tick_rate)
+        if config is None:
+            self.h = self.lib[p + "arena_create"](game_mode, tick_rate)
+        else:  # an rsg_arena_config mirror (reference library only)
+            fn = self.lib[p + "arena_create_ex"]
+            fn.restype = C.c_void_p
+            fn.argtypes = [C.c_int, C.c_float, C.c_void_p]
+            self.h = fn(game_mode, tick_rate, C.addressof(config))
         if not self.h:
             raise RuntimeError("arena_create failed")
 

@@ -161,6 +161,35 @@ void* rsref_arena_create(int game_mode, float tick_rate) {
     return ra;
 }
 
+// Arena::Create with an ArenaConfig from its POD mirror (ArenaConfig.h:19-50)
+void* rsref_arena_create_ex(int game_mode, float tick_rate, const rsg_arena_config* c) {
+    ArenaConfig cfg;
+    cfg.memWeightMode = (ArenaMemWeightMode)c->mem_weight_mode;
+    cfg.minPos = V(c->min_pos);
+    cfg.maxPos = V(c->max_pos);
+    cfg.maxAABBLen = c->max_aabb_len;
+    cfg.noBallRot = c->no_ball_rot != 0;
+    cfg.useCustomBroadphase = c->use_custom_broadphase != 0;
+    cfg.maxObjects = c->max_objects;
+    cfg.useCustomBoostPads = c->use_custom_boost_pads != 0;
+    for (uint32_t i = 0; i < c->num_custom_boost_pads; i++) {
+        BoostPadConfig pc;
+        pc.pos = V(c->custom_boost_pads[i].pos);
+        pc.isBig = c->custom_boost_pads[i].is_big != 0;
+        cfg.customBoostPads.push_back(pc);
+    }
+    RefArena* ra = new RefArena();
+    try {
+        ra->arena = Arena::Create((GameMode)game_mode, cfg, tick_rate);
+    } catch (...) {
+        delete ra;
+        return nullptr;
+    }
+    ra->arena->SetCarBumpCallback(OnBump, ra);
+    if ((GameMode)game_mode != GameMode::THE_VOID) ra->arena->SetGoalScoreCallback(OnGoal, ra);
+    return ra;
+}
+
 void rsref_arena_destroy(void* h) {
     RefArena* ra = (RefArena*)h;
     delete ra->arena;

@@ -5,10 +5,11 @@ The simulation runs in the CUDA library built from ``rocketsim_gb300/csrc``
 ``include/rocketsim_gb300.h``; this package is the Python host side over that
 ABI.  Importing it does not touch the GPU; creating an ``ArenaBatch`` does.
 """
-from .abi import (BallState, CarConfig, CarControls, CarState, MutatorConfig, PadState, RSGError, Vec3,  # noqa: F401
-                  RotMat,
+from .abi import (ArenaConfig, BallState, BoostPadConfig, CarConfig, CarControls, CarState, MutatorConfig,  # noqa: F401
+                  PadState, RSGError, Vec3, RotMat,
                   GAMEMODE_SOCCAR, GAMEMODE_THE_VOID, TEAM_BLUE, TEAM_ORANGE, CAR_OCTANE, CAR_DOMINUS,
                   CAR_PLANK, CAR_BREAKOUT, CAR_HYBRID, CAR_MERC)
-from .arena import (Arena, ArenaBatch, Ball, Car, car_config, default_mutator_config, init, init_from_mem,  # noqa: F401
+from .arena import (Arena, ArenaBatch, Ball, Car, arena_config, car_config, default_mutator_config, init,  # noqa: F401
+                    init_from_mem,
                     CAR_STATE_DTYPE, BALL_STATE_DTYPE, PAD_STATE_DTYPE, CONTROLS_DTYPE)
 from .arena_mesh import arena_cmf, build_arena_mesh  # noqa: F401

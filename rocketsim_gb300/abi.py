@@ -103,6 +103,17 @@ class MutatorConfig(C.Structure):
 
 DEMO_NORMAL, DEMO_ON_CONTACT, DEMO_DISABLED = 0, 1, 2
 
+
+class BoostPadConfig(C.Structure):
+    _fields_ = [("pos", Vec3), ("is_big", C.c_uint8), ("_pad0", C.c_uint8 * 3)]
+
+
+class ArenaConfig(C.Structure):
+    _fields_ = [("mem_weight_mode", C.c_uint8), ("no_ball_rot", C.c_uint8), ("use_custom_broadphase", C.c_uint8),
+                ("use_custom_boost_pads", C.c_uint8), ("min_pos", Vec3), ("max_pos", Vec3),
+                ("max_aabb_len", C.c_float), ("max_objects", C.c_int32), ("num_custom_boost_pads", C.c_uint32),
+                ("custom_boost_pads", C.POINTER(BoostPadConfig))]
+
 assert C.sizeof(MutatorConfig) == 116
 assert C.sizeof(CarState) == 272
 assert C.sizeof(BallState) == 80
@@ -156,6 +167,9 @@ PROTOTYPES = {
     "rsg_air_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
     "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),
     "rsg_air_backward_noalloc": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
+    "rsg_batch_create_ex": (vp, [i32, u32, u32, f32, P(ArenaConfig)]),
+    "rsg_get_default_arena_config": (i32, [P(ArenaConfig)]),
+    "rsg_batch_num_pads": (i32, [vp, P(u32)]),
     "rsg_get_default_mutator_config": (i32, [i32, P(MutatorConfig)]),
     "rsg_set_mutator_config": (i32, [vp, P(MutatorConfig)]),
     "rsg_get_mutator_config": (i32, [vp, P(MutatorConfig)]),

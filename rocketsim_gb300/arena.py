@@ -41,6 +41,24 @@ def init(path: str, game_mode: int = abi.GAMEMODE_SOCCAR) -> None:
     init_from_mem(blobs, game_mode)
 
 
+def arena_config(custom_boost_pads=None, no_ball_rot: bool = True) -> "abi.ArenaConfig":
+    """ArenaConfig with its defaults; `custom_boost_pads` (a list of (x, y, z, is_big), uu) switches
+    to custom pads.  The returned struct keeps the pad array alive."""
+    c = abi.ArenaConfig()
+    check(abi.load().rsg_get_default_arena_config(C.byref(c)), "rsg_get_default_arena_config")
+    c.no_ball_rot = 1 if no_ball_rot else 0
+    if custom_boost_pads is not None:
+        arr = (abi.BoostPadConfig * max(len(custom_boost_pads), 1))()
+        for i, (x, y, z, big) in enumerate(custom_boost_pads):
+            arr[i].pos = abi.Vec3(float(x), float(y), float(z))
+            arr[i].is_big = 1 if big else 0
+        c.use_custom_boost_pads = 1
+        c.num_custom_boost_pads = len(custom_boost_pads)
+        c.custom_boost_pads = C.cast(arr, C.POINTER(abi.BoostPadConfig))
+        c._pads_keepalive = arr
+    return c
+
+
 def default_mutator_config(game_mode: int = abi.GAMEMODE_SOCCAR) -> "abi.MutatorConfig":
     """MutatorConfig(GameMode): the game mode's default mutators."""
     m = abi.MutatorConfig()
@@ -64,12 +82,18 @@ class ArenaBatch:
     """``n_arenas`` independent arenas of one game mode on the current CUDA device."""
 
     def __init__(self, game_mode: int = abi.GAMEMODE_SOCCAR, n_arenas: int = 1, max_cars: int = 4,
-                 tick_rate: float = 120.0):
+                 tick_rate: float = 120.0, config: "abi.ArenaConfig | None" = None):
         self.lib = abi.load()
-        h = self.lib.rsg_batch_create(game_mode, n_arenas, max_cars, tick_rate)
+        if config is None:
+            h = self.lib.rsg_batch_create(game_mode, n_arenas, max_cars, tick_rate)
+        else:
+            h = self.lib.rsg_batch_create_ex(game_mode, n_arenas, max_cars, tick_rate, C.byref(config))
         if not h:
             raise abi.RSGError(abi.ERR_STATE, "rsg_batch_create")
         self.h = C.c_void_p(h)
+        n = C.c_uint32()
+        check(self.lib.rsg_batch_num_pads(self.h, C.byref(n)), "rsg_batch_num_pads")
+        self.num_pads = n.value
         self.game_mode = game_mode
         self.n_arenas = n_arenas
         self.max_cars = max_cars
@@ -186,7 +210,7 @@ class ArenaBatch:
         balls = np.zeros(A, BALL_STATE_DTYPE) if balls is None else balls
         has_pads = self.game_mode != abi.GAMEMODE_THE_VOID
         if pads is None and has_pads:
-            pads = np.zeros(A * abi.NUM_BOOST_PADS, PAD_STATE_DTYPE)
+            pads = np.zeros(A * self.num_pads, PAD_STATE_DTYPE)
         check(self.lib.rsg_get_all_states(self.h, cars.ctypes.data, balls.ctypes.data,
                                           pads.ctypes.data if pads is not None else None), "rsg_get_all_states")
         return cars, balls, pads
@@ -271,16 +295,18 @@ class Ball:
 class Arena:
     """One arena with RocketSim's method names (Arena::Create, AddCar, Step, ...)."""
 
-    def __init__(self, game_mode: int = abi.GAMEMODE_SOCCAR, tick_rate: float = 120.0, max_cars: int = 8):
-        self.batch = ArenaBatch(game_mode, 1, max_cars, tick_rate)
+    def __init__(self, game_mode: int = abi.GAMEMODE_SOCCAR, tick_rate: float = 120.0, max_cars: int = 8,
+                 config: "abi.ArenaConfig | None" = None):
+        self.batch = ArenaBatch(game_mode, 1, max_cars, tick_rate, config)
         self.game_mode = game_mode
         self.tick_time = 1.0 / tick_rate
         self.ball = Ball(self)
         self._cars: dict[int, Car] = {}
 
     @classmethod
-    def create(cls, game_mode: int = abi.GAMEMODE_SOCCAR, tick_rate: float = 120.0) -> "Arena":
-        return cls(game_mode, tick_rate)
+    def create(cls, game_mode: int = abi.GAMEMODE_SOCCAR, tick_rate: float = 120.0,
+               config: "abi.ArenaConfig | None" = None) -> "Arena":
+        return cls(game_mode, tick_rate, config=config)
 
     def add_car(self, team: int, config: CarConfig | int = abi.CAR_OCTANE, respawn_index: int = -1) -> Car:
         cfg = car_config(config) if isinstance(config, int) else config

@@ -223,6 +223,8 @@ struct rsg_batch {
     rsg_ball_hit_fn hit_fn = nullptr;
     void* hit_user = nullptr;
     rsg_mutator_config mutators{};
+    std::vector<float4> pads;  // per pad: position (uu), is_big
+    float4* d_pads = nullptr;
 };
 
 namespace {
@@ -567,7 +569,43 @@ cudaError_t tuned_launch(rsg_batch* b, const rsg_car_controls* controls, int tic
 
 }  // namespace
 
+int rsg_get_default_arena_config(rsg_arena_config* out) {
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    std::memset(out, 0, sizeof(*out));
+    out->mem_weight_mode = 0;  // HEAVY
+    out->no_ball_rot = 1;
+    out->use_custom_broadphase = 1;
+    out->use_custom_boost_pads = 0;
+    out->min_pos = rsg_vec3{-5600, -6000, 0};
+    out->max_pos = rsg_vec3{5600, 6000, 2200};
+    out->max_aabb_len = 370;
+    out->max_objects = 512;
+    return RSG_OK;
+}
+
 rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate) {
+    return rsg_batch_create_ex(game_mode, n_arenas, max_cars_per_arena, tick_rate, nullptr);
+}
+
+rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_cars_per_arena, float tick_rate,
+                               const rsg_arena_config* config) {
+    rsg_arena_config cfg;
+    rsg_get_default_arena_config(&cfg);
+    if (config) {
+        const rsg_arena_config& c = *config;
+        if (c.min_pos.x != cfg.min_pos.x || c.min_pos.y != cfg.min_pos.y || c.min_pos.z != cfg.min_pos.z ||
+            c.max_pos.x != cfg.max_pos.x || c.max_pos.y != cfg.max_pos.y || c.max_pos.z != cfg.max_pos.z ||
+            c.max_aabb_len != cfg.max_aabb_len || !c.use_custom_broadphase) {
+            fail(RSG_ERR_ARG, "only the default broadphase bounds, cell size and custom broadphase are supported");
+            return nullptr;
+        }
+        if (c.use_custom_boost_pads && (c.num_custom_boost_pads > (uint32_t)NUM_PADS ||
+                                        (c.num_custom_boost_pads && !c.custom_boost_pads))) {
+            fail(RSG_ERR_ARG, "custom boost pads: at most 34, given as a host array");
+            return nullptr;
+        }
+        cfg = c;
+    }
     if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_THE_VOID) {
         fail(RSG_ERR_ARG, "game mode not supported (soccar and the void only)");
         return nullptr;
@@ -612,6 +650,20 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
     B.dt = 1.f / tick_rate;
     b->mutators = default_mutators(game_mode);
     B.mut = mutators_dev(b->mutators);
+    // boost pads: ArenaConfig's custom list or the soccar pads (Arena.cpp:498-533)
+    b->pads.clear();
+    if (cfg.use_custom_boost_pads) {
+        for (uint32_t i = 0; i < cfg.num_custom_boost_pads; i++) {
+            const rsg_boost_pad_config& pc = cfg.custom_boost_pads[i];
+            b->pads.push_back(float4{pc.pos.x, pc.pos.y, pc.pos.z, pc.is_big ? 1.f : 0.f});
+        }
+    } else {
+        for (int i = 0; i < NUM_PADS; i++)
+            b->pads.push_back(float4{PAD_LOCS[i][0], PAD_LOCS[i][1], PAD_LOCS[i][2], i < 6 ? 1.f : 0.f});
+    }
+    B.npads = (int)b->pads.size();
+    B.custom_pads = cfg.use_custom_boost_pads ? 1 : 0;
+    B.no_ball_rot = cfg.no_ball_rot ? 1 : 0;
     B.mesh = mesh_ptrs(g_soccar);
     B.grid = default_grid();
     size_t A = n_arenas, MC = max_cars_per_arena;
@@ -633,7 +685,12 @@ rsg_batch* rsg_batch_create(int game_mode, uint32_t n_arenas, uint32_t max_cars_
         rsg_batch_destroy(b);
         return nullptr;
     }
-    bool ok = alloc((void**)&B.rec, sizeof(uint32_t) * (size_t)rec_words((int)MC) * A);
+    bool ok = alloc((void**)&b->d_pads, sizeof(float4) * NUM_PADS);
+    if (ok && !b->pads.empty())
+        ok = cudaMemcpy(b->d_pads, b->pads.data(), sizeof(float4) * b->pads.size(), cudaMemcpyHostToDevice) ==
+             cudaSuccess;
+    B.pad_cfg = b->d_pads;
+    ok = ok && alloc((void**)&B.rec, sizeof(uint32_t) * (size_t)rec_words((int)MC) * A);
     ok = ok && alloc((void**)&B.au, sizeof(uint32_t) * AU_COUNT * A);
     ok = ok && alloc(&B.events, (size_t)DEV_EVENT_BYTES * MAX_EVENTS_PER_ARENA * A);
     if (!ok) {
@@ -670,7 +727,7 @@ void rsg_batch_destroy(rsg_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     BatchBuffers& B = b->buf;
-    void* ptrs[] = {B.rec, B.au, B.events, b->d_cfgs, b->d_stage};
+    void* ptrs[] = {B.rec, B.au, B.events, b->d_cfgs, b->d_stage, b->d_pads};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -682,6 +739,12 @@ void rsg_batch_destroy(rsg_batch* b) {
 int rsg_batch_num_arenas(const rsg_batch* b, uint32_t* out) {
     if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
     *out = (uint32_t)b->buf.A;
+    return RSG_OK;
+}
+
+int rsg_batch_num_pads(const rsg_batch* b, uint32_t* out) {
+    if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
+    *out = b->buf.has_arena ? (uint32_t)b->buf.npads : 0u;
     return RSG_OK;
 }
 
@@ -951,10 +1014,10 @@ int rsg_set_ball_state(rsg_batch* b, uint32_t arena, const rsg_ball_state* in) {
 int rsg_get_pad_state(rsg_batch* b, uint32_t arena, uint32_t pad, rsg_pad_state* out) {
     int rc = check_arena(b, arena);
     if (rc) return rc;
-    if (!out || pad >= (uint32_t)NUM_PADS) return fail(RSG_ERR_ARG, "pad index out of range");
+    if (!out || pad >= (uint32_t)b->buf.npads) return fail(RSG_ERR_ARG, "pad index out of range");
     if (!b->buf.has_arena) return fail(RSG_ERR_STATE, "this game mode has no boost pads");
     if ((rc = set_device(b))) return rc;
-    size_t bytes = sizeof(rsg_pad_state) * NUM_PADS;
+    size_t bytes = sizeof(rsg_pad_state) * b->buf.npads;
     if ((rc = ensure_stage(b, bytes + 8))) return rc;
     char* st = (char*)b->d_stage;
     RSG_CUDA(cudaMemcpyAsync(st + bytes, &arena, 4, cudaMemcpyHostToDevice, b->stream));
@@ -967,7 +1030,7 @@ int rsg_get_pad_state(rsg_batch* b, uint32_t arena, uint32_t pad, rsg_pad_state*
 int rsg_set_pad_state(rsg_batch* b, uint32_t arena, uint32_t pad, const rsg_pad_state* in) {
     int rc = check_arena(b, arena);
     if (rc) return rc;
-    if (!in || pad >= (uint32_t)NUM_PADS) return fail(RSG_ERR_ARG, "pad index out of range");
+    if (!in || pad >= (uint32_t)b->buf.npads) return fail(RSG_ERR_ARG, "pad index out of range");
     if (!b->buf.has_arena) return fail(RSG_ERR_STATE, "this game mode has no boost pads");
     if ((rc = set_device(b))) return rc;
     // one pad block of the arena record: cooldown, active, previous and current locked car
@@ -983,12 +1046,13 @@ int rsg_set_pad_state(rsg_batch* b, uint32_t arena, uint32_t pad, const rsg_pad_
 }
 
 int rsg_get_pad_config(const rsg_batch* b, uint32_t pad, rsg_vec3* pos, int* is_big) {
-    if (!b || pad >= (uint32_t)NUM_PADS || !pos || !is_big) return fail(RSG_ERR_ARG, "bad argument");
+    if (!b || !pos || !is_big) return fail(RSG_ERR_ARG, "bad argument");
     if (!b->buf.has_arena) return fail(RSG_ERR_STATE, "this game mode has no boost pads");
-    pos->x = PAD_LOCS[pad][0];
-    pos->y = PAD_LOCS[pad][1];
-    pos->z = PAD_LOCS[pad][2];
-    *is_big = pad < 6 ? 1 : 0;
+    if (pad >= (uint32_t)b->buf.npads) return fail(RSG_ERR_ARG, "pad index out of range");
+    pos->x = b->pads[pad].x;
+    pos->y = b->pads[pad].y;
+    pos->z = b->pads[pad].z;
+    *is_big = b->pads[pad].w != 0.f ? 1 : 0;
     return RSG_OK;
 }
 
@@ -1030,7 +1094,7 @@ int rsg_get_all_states(rsg_batch* b, rsg_car_state* cars, rsg_ball_state* balls,
     if ((rc = set_device(b))) return rc;
     size_t A = b->buf.A, MC = b->buf.MC;
     size_t cb = cars ? sizeof(rsg_car_state) * A * MC : 0, bb = balls ? sizeof(rsg_ball_state) * A : 0;
-    size_t pb = (pads && b->buf.has_arena) ? sizeof(rsg_pad_state) * A * NUM_PADS : 0;
+    size_t pb = (pads && b->buf.has_arena) ? sizeof(rsg_pad_state) * A * b->buf.npads : 0;
     if ((rc = ensure_stage(b, cb + bb + pb + 16))) return rc;
     char* st = (char*)b->d_stage;
     if (cars) {
@@ -1057,7 +1121,7 @@ int rsg_set_all_states(rsg_batch* b, const rsg_car_state* cars, const rsg_ball_s
     if ((rc = set_device(b))) return rc;
     size_t A = b->buf.A, MC = b->buf.MC;
     size_t cb = cars ? sizeof(rsg_car_state) * A * MC : 0, bb = balls ? sizeof(rsg_ball_state) * A : 0;
-    size_t pb = (pads && b->buf.has_arena) ? sizeof(rsg_pad_state) * A * NUM_PADS : 0;
+    size_t pb = (pads && b->buf.has_arena) ? sizeof(rsg_pad_state) * A * b->buf.npads : 0;
     if ((rc = ensure_stage(b, cb + bb + pb + 16))) return rc;
     char* st = (char*)b->d_stage;
     if (cars) {

@@ -20,6 +20,10 @@ static BatchView make_view(const BatchBuffers& b) {
     v.has_arena = b.has_arena;
     v.dt = b.dt;
     v.mut = b.mut;
+    v.pad_cfg = b.pad_cfg;
+    v.npads = b.npads;
+    v.custom_pads = b.custom_pads;
+    v.no_ball_rot = b.no_ball_rot;
     v.rec = b.rec;
     v.rec_words = rec_words(b.MC);
     v.au = b.au;
@@ -381,8 +385,8 @@ __global__ void rsg_set_balls_kernel(BatchView bv, const uint32_t* __restrict__ 
 // BoostPad::GetState / SetState (src/Sim/BoostPad/BoostPad.h:44-45)
 __global__ void rsg_get_pads_kernel(BatchView bv, const uint32_t* __restrict__ arenas, int n, rsg_pad_state* __restrict__ out) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n * NUM_PADS) return;
-    int q = k / NUM_PADS, p = k % NUM_PADS;
+    if (k >= n * bv.npads) return;
+    int q = k / bv.npads, p = k % bv.npads;
     int ar = arenas ? (int)arenas[q] : q;
     if (ar < 0 || ar >= bv.A) return;
     SoA s{bv, ar};
@@ -397,8 +401,8 @@ __global__ void rsg_get_pads_kernel(BatchView bv, const uint32_t* __restrict__ a
 }
 __global__ void rsg_set_pads_kernel(BatchView bv, const uint32_t* __restrict__ arenas, int n, const rsg_pad_state* __restrict__ in) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n * NUM_PADS) return;
-    int q = k / NUM_PADS, p = k % NUM_PADS;
+    if (k >= n * bv.npads) return;
+    int q = k / bv.npads, p = k % bv.npads;
     int ar = arenas ? (int)arenas[q] : q;
     if (ar < 0 || ar >= bv.A) return;
     SoA s{bv, ar};
@@ -458,13 +462,13 @@ cudaError_t launch_set_balls(const BatchBuffers& b, const uint32_t* arenas, int 
     return cudaGetLastError();
 }
 cudaError_t launch_get_pads(const BatchBuffers& b, const uint32_t* arenas, int n, rsg_pad_state* out, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    rsg_get_pads_kernel<<<blocks_for(n * NUM_PADS, 128), 128, 0, st>>>(make_view(b), arenas, n, out);
+    if (n <= 0 || b.npads <= 0) return cudaSuccess;
+    rsg_get_pads_kernel<<<blocks_for(n * b.npads, 128), 128, 0, st>>>(make_view(b), arenas, n, out);
     return cudaGetLastError();
 }
 cudaError_t launch_set_pads(const BatchBuffers& b, const uint32_t* arenas, int n, const rsg_pad_state* in, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    rsg_set_pads_kernel<<<blocks_for(n * NUM_PADS, 128), 128, 0, st>>>(make_view(b), arenas, n, in);
+    if (n <= 0 || b.npads <= 0) return cudaSuccess;
+    rsg_set_pads_kernel<<<blocks_for(n * b.npads, 128), 128, 0, st>>>(make_view(b), arenas, n, in);
     return cudaGetLastError();
 }
 cudaError_t launch_set_controls(const BatchBuffers& b, const rsg_car_controls* in, cudaStream_t st) {

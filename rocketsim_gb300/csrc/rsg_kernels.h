@@ -29,6 +29,8 @@ struct BatchBuffers {
     int A, MC, has_arena;
     float dt;
     MutatorsDev mut;
+    const float4* pad_cfg;  // [npads] position (uu), is_big
+    int npads, custom_pads, no_ball_rot;
     uint32_t* rec;  // A records of rec_words(MC) 32-bit words
     uint32_t* au;   // [AU_COUNT][A]
     const CarCfgDev* cfgs;

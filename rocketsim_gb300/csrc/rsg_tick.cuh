@@ -65,7 +65,6 @@ __device__ unsigned long long g_phase_cycles[64];
 #define RSG_L0_BEGIN
 #define RSG_L0(i)
 #endif
-__constant__ float c_pad_locs[NUM_PADS][3] = RSG_PAD_LOCS_INIT;
 __constant__ float c_respawn_locs[4][2] = {{-2304, -4608}, {-2688, -4608}, {2304, -4608}, {2688, -4608}};
 
 struct DevMesh {
@@ -102,6 +101,9 @@ struct BatchView {
     int has_arena;
     float dt;
     MutatorsDev mut;
+    const float4* pad_cfg;  // per pad: position (uu) and is_big (ArenaConfig's pads or the soccar ones)
+    int npads, custom_pads;  // pad count; custom pads skip BoostPadGrid (Arena.cpp:724-731)
+    int no_ball_rot;         // ArenaConfig::noBallRot
     uint32_t* rec;  // A records of rec_words(MC) words
     int rec_words;
     uint32_t* au;   // [AU_COUNT][A]
@@ -3836,49 +3838,6 @@ RSG_D bool ball_scored(const Ctx& a, const MutatorsDev& m) {  // Arena::IsBallSc
     return fabsf(y) > (m.goal_threshold_y + m.ball_radius_uu);
 }
 
-RSG_D void pad_check(Ctx& a, Pad& p, int pi, int ci) {  // BoostPad::_CheckCollide (src/Sim/BoostPad/BoostPad.cpp:62-86)
-    Car& c = a.cars[ci];
-    V3 cp = c.rb.xf.o;
-    bool big = pi < 6;
-    V3 pos_bt = V3(c_pad_locs[pi][0], c_pad_locs[pi][1], c_pad_locs[pi][2]) * RL::UU_TO_BT;
-    bool col = false;
-    if (p.prev_locked == c.id) {
-        V3 mn, mx;
-        car_compound_aabb(c, c.rb.xf, mn, mx);
-        float br = (big ? RL::PAD_BOX_RAD_BIG : RL::PAD_BOX_RAD_SMALL) * RL::UU_TO_BT;
-        V3 bmin = pos_bt - V3(br, br, 0);
-        V3 bmax = pos_bt + V3(br, br, RL::PAD_BOX_HEIGHT * RL::UU_TO_BT);
-        bool gt = (bmax.x > mn.x) && (bmax.y > mn.y) && (bmax.z > mn.z);
-        bool lt = (bmin.x < mx.x) && (bmin.y < mx.y) && (bmin.z < mx.z);
-        col = gt && lt;
-    } else {
-        float rad = (big ? RL::PAD_CYL_RAD_BIG : RL::PAD_CYL_RAD_SMALL) * RL::UU_TO_BT;
-        float dx = cp.x - pos_bt.x, dy = cp.y - pos_bt.y;
-        if (dx * dx + dy * dy < rad * rad) col = fabsf(cp.z - pos_bt.z) < (RL::PAD_CYL_HEIGHT * RL::UU_TO_BT);
-    }
-    if (col) p.cur_locked = ci;
-}
-
-RSG_D void grid_check(Ctx& a, int ci) {  // BoostPadGrid::CheckCollision (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25)
-    Car& c = a.cars[ci];
-    if (c.f(F_DEMOED) || c.boost >= RL::BOOST_MAX) return;
-    V3 cp = c.rb.xf.o * RL::BT_TO_UU;
-    const float EXT_Z = RL::PAD_CYL_HEIGHT + 250.f;
-    if (cp.z > EXT_Z) return;
-    const int CX = 8, CY = 10, SX = (int)(4096.f / (CX / 2)), SY = (int)(5120.f / (CY / 2));
-    int ix = (int)(cp.x / SX + (CX / 2));
-    int iy = (int)(cp.y / SY + (CY / 2));
-    int i0 = ix - 1 > 0 ? ix - 1 : 0, i1 = ix + 1 < CX - 1 ? ix + 1 : CX - 1;
-    int j0 = iy - 1 > 0 ? iy - 1 : 0, j1 = iy + 1 < CY - 1 ? iy + 1 : CY - 1;
-    // Every pad lies in exactly one grid cell and a check only touches that pad, so visiting the
-    // pads of the 3x3 neighbourhood in pad order equals the reference's cell-by-cell visit.
-    for (int k = 0; k < NUM_PADS; k++) {
-        int px = (int)(c_pad_locs[k][0] / SX + (CX / 2));
-        int py = (int)(c_pad_locs[k][1] / SY + (CY / 2));
-        if (px >= i0 && px <= i1 && py >= j0 && py <= j1) pad_check(a, a.pads[k], k, ci);
-    }
-}
-
 // Arena::Step, one tick (src/Sim/Arena/Arena.cpp:689-756), run by the 32 lanes of one warp in four
 // parts (tick_pre, step_bodies_pre, step_collide_warp, tick_post); the kernel puts a block-wide
 // barrier between the parts so that the warps of a block run the same code at the same time.
@@ -3982,10 +3941,10 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
         }
     }
     if (bv.has_arena)
-        for (int u = tid; u < B.nact * NUM_PADS; u += nthreads) {  // BoostPad::_PreTickUpdate (BoostPad.cpp:51-60)
-            Ctx& a = B(u / NUM_PADS);
+        for (int u = tid; u < B.nact * bv.npads; u += nthreads) {  // BoostPad::_PreTickUpdate (BoostPad.cpp:51-60)
+            Ctx& a = B(u / bv.npads);
             if (a.ncars == 0) continue;
-            Pad& p = a.pads[u % NUM_PADS];
+            Pad& p = a.pads[u % bv.npads];
             if (p.cooldown > 0) p.cooldown = rs_maxf(p.cooldown - bv.dt, 0);
             p.active = (p.cooldown == 0);
             p.cur_locked = -1;
@@ -4020,31 +3979,26 @@ RSG_DN void body_post(Body& b, float dt) {
     b.total_torque = V3(0, 0, 0);
 }
 
-// Pad positions for per-thread reads: threads of a warp test different pads, and constant memory
-// serialises a warp's loads of different addresses.
-__device__ const float g_pad_locs[NUM_PADS][3] = RSG_PAD_LOCS_INIT;
-
-// A pad's position (Bullet units), size and cell of BoostPadGrid (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25)
+// A pad's position (Bullet units), size and cell of BoostPadGrid (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25),
+// read from the batch's pad table (global memory: threads of a warp test different pads).
 struct PadGeo {
     V3 pos_bt;
     int px, py;
     bool big;
 };
-RSG_D PadGeo pad_geo(int pi) {
+RSG_D PadGeo pad_geo(const BatchView& bv, int pi) {
     const int CX = 8, CY = 10, SX = (int)(4096.f / (CX / 2)), SY = (int)(5120.f / (CY / 2));
-    const float x = __ldg(&g_pad_locs[pi][0]), y = __ldg(&g_pad_locs[pi][1]), z = __ldg(&g_pad_locs[pi][2]);
+    const float4 c = __ldg(bv.pad_cfg + pi);
     PadGeo g;
-    g.px = (int)(x / SX + (CX / 2));
-    g.py = (int)(y / SY + (CY / 2));
-    g.pos_bt = V3(x, y, z) * RL::UU_TO_BT;
-    g.big = pi < 6;
+    g.px = (int)(c.x / SX + (CX / 2));
+    g.py = (int)(c.y / SY + (CY / 2));
+    g.pos_bt = V3(c.x, c.y, c.z) * RL::UU_TO_BT;
+    g.big = c.w != 0.f;
     return g;
 }
 
-// The pad grid test of one (pad, car): BoostPadGrid::CheckCollision's cell neighbourhood
-// (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25) and BoostPad::_CheckCollide (BoostPad.cpp:62-86).
-RSG_D bool pad_touches(Ctx& a, const Pad& p, const PadGeo& g, int ci) {
-    Car& c = a.cars[ci];
+// BoostPadGrid::CheckCollision's early outs and the 3x3 cell neighbourhood of the car
+RSG_D bool pad_grid_near(const Car& c, const PadGeo& g) {
     if (c.f(F_DEMOED) || c.boost >= RL::BOOST_MAX) return false;
     V3 cpu = c.rb.xf.o * RL::BT_TO_UU;
     const float EXT_Z = RL::PAD_CYL_HEIGHT + 250.f;
@@ -4054,8 +4008,16 @@ RSG_D bool pad_touches(Ctx& a, const Pad& p, const PadGeo& g, int ci) {
     int iy = (int)(cpu.y / SY + (CY / 2));
     int i0 = ix - 1 > 0 ? ix - 1 : 0, i1 = ix + 1 < CX - 1 ? ix + 1 : CX - 1;
     int j0 = iy - 1 > 0 ? iy - 1 : 0, j1 = iy + 1 < CY - 1 ? iy + 1 : CY - 1;
-    if (g.px < i0 || g.px > i1 || g.py < j0 || g.py > j1) return false;
-    V3 cp = c.rb.xf.o;
+    return !(g.px < i0 || g.px > i1 || g.py < j0 || g.py > j1);
+}
+
+// The pad test of one (pad, car): BoostPadGrid::CheckCollision's early outs and cell neighbourhood
+// (src/Sim/BoostPadGrid/BoostPadGrid.cpp:5-25), then BoostPad::_CheckCollide (BoostPad.cpp:62-86).
+// Custom pads skip the grid and its early outs (Arena.cpp:724-728).
+RSG_D bool pad_touches(Ctx& a, const Pad& p, const PadGeo& g, int ci, bool custom) {
+    Car& c = a.cars[ci];
+    if (!custom && !pad_grid_near(c, g)) return false;
+    const V3 cp = c.rb.xf.o;
     const V3 pos_bt = g.pos_bt;
     if (p.prev_locked == c.id) {
         V3 mn, mx;
@@ -4123,13 +4085,13 @@ RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, 
     __syncthreads();
     RSG_SUB(13);
     if (bv.has_arena) {
-        for (int u = tid; u < B.nact * NUM_PADS; u += nthreads) {  // which car each pad is locked to
-            Ctx& a = B(u / NUM_PADS);
-            int pi = u % NUM_PADS;
+        for (int u = tid; u < B.nact * bv.npads; u += nthreads) {  // which car each pad is locked to
+            Ctx& a = B(u / bv.npads);
+            int pi = u % bv.npads;
             Pad& p = a.pads[pi];
-            const PadGeo g = pad_geo(pi);
+            const PadGeo g = pad_geo(bv, pi);
             for (int kk = 0; kk < a.ncars; kk++)
-                if (pad_touches(a, p, g, a.order[kk])) p.cur_locked = a.order[kk];
+                if (pad_touches(a, p, g, a.order[kk], bv.custom_pads)) p.cur_locked = a.order[kk];
         }
         __syncthreads();
         for (int u = tid; u < B.nact * MC; u += nthreads) {  // BoostPad::_PostTickUpdate boost, in pad order
@@ -4137,24 +4099,25 @@ RSG_DN void block_tick_post(const BatchView& bv, const BlockArenas& B, int tid, 
             int k = u % MC;
             if (k >= a.ncars) continue;
             Car& c = a.cars[k];
-            for (int i = 0; i < NUM_PADS; i++) {
+            for (int i = 0; i < bv.npads; i++) {
                 const Pad& p = a.pads[i];
                 if (p.cur_locked == k && p.active)
-                    c.boost = rs_minf(c.boost + (i < 6 ? RL::PAD_BOOST_BIG : RL::PAD_BOOST_SMALL), RL::BOOST_MAX);
+                    c.boost = rs_minf(c.boost + (__ldg(&bv.pad_cfg[i].w) != 0.f ? RL::PAD_BOOST_BIG : RL::PAD_BOOST_SMALL),
+                                      RL::BOOST_MAX);
             }
         }
         __syncthreads();
-        for (int u = tid; u < B.nact * NUM_PADS; u += nthreads) {  // BoostPad::_PostTickUpdate (BoostPad.cpp:88-105)
-            Ctx& a = B(u / NUM_PADS);
+        for (int u = tid; u < B.nact * bv.npads; u += nthreads) {  // BoostPad::_PostTickUpdate (BoostPad.cpp:88-105)
+            Ctx& a = B(u / bv.npads);
             if (a.ncars == 0) continue;
-            int i = u % NUM_PADS;
+            int i = u % bv.npads;
             Pad& p = a.pads[i];
             uint32_t locked = 0;
             if (p.cur_locked >= 0) {
                 locked = a.cars[p.cur_locked].id;
                 if (p.active) {
                     p.active = false;
-                    p.cooldown = i < 6 ? bv.mut.pad_cooldown_big : bv.mut.pad_cooldown_small;
+                    p.cooldown = __ldg(&bv.pad_cfg[i].w) != 0.f ? bv.mut.pad_cooldown_big : bv.mut.pad_cooldown_small;
                 }
             }
             p.prev_locked = locked;
@@ -4243,7 +4206,7 @@ RSG_DN void load_arena(const BatchView& bv, int ar, Ctx& a) {  // scalars and ba
     }
     b.lin_damping = bv.mut.ball_drag;
     b.act = ACTIVE_TAG;
-    b.no_rot = true;
+    b.no_rot = bv.no_ball_rot != 0;
     b.no_contact_response = false;
     b.friction = bv.mut.ball_world_friction;
     b.restitution = bv.mut.ball_world_restitution;

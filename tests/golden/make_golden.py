@@ -39,7 +39,7 @@ def scenario_list():
     return out
 
 
-def record(scs, mutators=None, epa=True):
+def record(scs, mutators=None, epa=True, config=None):
     """Plays the scenarios through the reference (and, with `epa`, the restatement to find the
     first EPA tick) and returns the arrays of the golden file."""
     from oracle.pyoracle import build_ref
@@ -57,7 +57,8 @@ def record(scs, mutators=None, epa=True):
     cars_t = {1: np.zeros((S, MC), car_dt), 8: np.zeros((S, MC), car_dt)}
     ball_t = {1: np.zeros(S, ball_dt), 8: np.zeros(S, ball_dt)}
     disc_cars = np.zeros((S, TICKS, MC, 28), np.float32)
-    disc_pads = np.zeros((S, TICKS, 34, 3), np.float32)
+    npads = int(config.num_custom_boost_pads) if config is not None and config.use_custom_boost_pads else 34
+    disc_pads = np.zeros((S, TICKS, npads, 3), np.float32)
     events = []
     epa_tick = np.full(S, -1, np.int32)
     for si, sc in enumerate(scs):
@@ -78,7 +79,7 @@ def record(scs, mutators=None, epa=True):
             disc_pads[si, t] = discrete_pads(pads)
             for e in a.pop_events():
                 events.append((si,) + e)
-        a, ids = run_cpu("ref", sc, TICKS, rec, mutators)  # fixes sc.order to the reference's iteration order
+        a, ids = run_cpu("ref", sc, TICKS, rec, mutators, config)  # fixes sc.order to the reference's order
         a.close()
         order[si, :n] = sc.order
         if epa:

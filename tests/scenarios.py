@@ -161,11 +161,12 @@ def _controls_struct(row) -> abi.CarControls:
 
 
 # ---------------------------------------------------------------- CPU checkers
-def setup_cpu(kind: str, sc: Scenario, mutators=None):
+def setup_cpu(kind: str, sc: Scenario, mutators=None, config=None):
     """Builds the scenario on a SimArena of `kind` ('ref', 'oracle', 'oracle_sse'); `mutators` (an
-    abi.MutatorConfig, reference only) is set before the cars are added."""
+    abi.MutatorConfig) is set before the cars are added and `config` (an abi.ArenaConfig) passed
+    to Arena::Create, both for the reference only."""
     from oracle.pyoracle import SimArena, CarState as OCarState, BallState as OBallState, CarControls as OCtl
-    a = SimArena(kind, mesh_bytes())
+    a = SimArena(kind, mesh_bytes(), config=config)
     if mutators is not None:
         a.set_mutator_config(mutators)
     ids = [a.add_car(t, p) for t, p in zip(sc.teams, sc.presets)]
@@ -182,12 +183,12 @@ def setup_cpu(kind: str, sc: Scenario, mutators=None):
     return a, ids
 
 
-def run_cpu(kind: str, sc: Scenario, ticks: int, record=None, mutators=None):
+def run_cpu(kind: str, sc: Scenario, ticks: int, record=None, mutators=None, config=None):
     """Steps a fresh checker arena through `ticks` ticks of the scenario.
 
     `record(t, arena, ids)` is called after each tick."""
     from oracle.pyoracle import CarControls as OCtl
-    a, ids = setup_cpu(kind, sc, mutators)
+    a, ids = setup_cpu(kind, sc, mutators, config)
     for t in range(ticks):
         for i, cid in enumerate(ids):
             a.set_controls(cid, OCtl.from_buffer_copy(bytes(_controls_struct(sc.controls[t, i]))))
@@ -205,12 +206,13 @@ def cpu_snapshot(a, ids):
 
 
 # ---------------------------------------------------------------- GPU
-def setup_gpu(scs: list[Scenario], max_cars: int | None = None, mutators=None):
-    """One ArenaBatch holding one arena per scenario (`mutators` set before the cars are added)."""
+def setup_gpu(scs: list[Scenario], max_cars: int | None = None, mutators=None, config=None):
+    """One ArenaBatch holding one arena per scenario (`mutators` set before the cars are added,
+    `config` an abi.ArenaConfig for the batch)."""
     import rocketsim_gb300 as rsg
     rsg.init_from_mem([mesh_bytes()])
     mc = max_cars or max(len(s.cars) for s in scs)
-    batch = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, len(scs), mc, 120.0)
+    batch = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, len(scs), mc, 120.0, config)
     if mutators is not None:
         batch.set_mutator_config(mutators)
     all_ids = []
@@ -239,7 +241,7 @@ def gpu_snapshot(batch, scs: list[Scenario]):
     for ai, sc in enumerate(scs):
         n = len(sc.cars)
         out.append((cars[ai * mc:ai * mc + n].copy(), balls[ai:ai + 1].copy(),
-                    pads[ai * 34:(ai + 1) * 34].copy()))
+                    pads[ai * batch.num_pads:(ai + 1) * batch.num_pads].copy()))
     return out
 
 
