@@ -451,6 +451,28 @@ int rsg_ground_backward(const rsg_car_config* car, float tick_rate, int n, int t
                         const float* d_ckpt, int ckpt_every, const float* d_grad_final, float* d_grad_controls,
                         float* d_grad_state0, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* ---- serialisation -------------------------------------------------------- */
+
+/* Arena::Serialize (src/Sim/Arena/Arena.cpp:546-574) of arena `arena`, in
+ * RocketSim's byte format (DataStreamOut, without the file's version word):
+ * the reference's DeserializeNew reads it and rsg_deserialize_arena reads the
+ * reference's output.  Cars are written by ascending id (the reference's
+ * DeserializeNew keeps every car only then, Arena.cpp:590-606).  With
+ * `out` NULL only *len is set; with `cap` < *len, RSG_ERR_ARG. */
+int rsg_serialize_arena(rsg_batch* batch, uint32_t arena, uint8_t* out, uint64_t cap, uint64_t* len);
+/* Arena::DeserializeNew (Arena.cpp:576-643) into arena `arena`: its cars are
+ * replaced by the serialized ones (ids, teams, configurations, controls,
+ * states), then the pads, the ball, the tick count and the last car id.  The
+ * game mode, tick rate and arena config must be the batch's; mutators that
+ * differ from the batch's are applied when the batch holds one arena.  As in
+ * the reference, every car's boost comes back as the game mode's default spawn
+ * amount (DeserializeNewCar sets up the car body after reading its state,
+ * Arena.cpp:676-687 and Car.cpp:291); rsg_clone_arena keeps the boost. */
+int rsg_deserialize_arena(rsg_batch* batch, uint32_t arena, const uint8_t* data, uint64_t len);
+/* Arena::Clone (Arena.cpp:646-674): arena `src_arena` of `src` into arena
+ * `dst_arena` of `dst` (callbacks stay with each batch). */
+int rsg_clone_arena(rsg_batch* dst, uint32_t dst_arena, rsg_batch* src, uint32_t src_arena);
+
 /* Device flags of every arena after the last step ([n_arenas] words).  Bits 0-7
  * are capacity overflows (the step also returns RSG_ERR_DEVICE); bit 8 marks a
  * box contact deeper than GJK resolves and bit 9 overlapping car boxes, two

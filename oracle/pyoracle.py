@@ -278,6 +278,41 @@ class SimArena:
         self.lib[self.p + "wheel_debug"](self.h, car_id, buf)
         return [list(buf[i * 16:(i + 1) * 16]) for i in range(4)]
 
+    def serialize(self) -> bytes:
+        """Arena::Serialize (reference library only)."""
+        fn = self.lib[self.p + "serialize"]
+        fn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
+        n = C.c_uint64()
+        fn(self.h, None, 0, C.byref(n))
+        buf = (C.c_uint8 * n.value)()
+        fn(self.h, buf, n.value, C.byref(n))
+        return bytes(buf)
+
+    @classmethod
+    def deserialize_new(cls, data: bytes) -> "SimArena":
+        """Arena::DeserializeNew (reference library only)."""
+        self = cls.__new__(cls)
+        self.kind, self.lib = "ref", load("ref")
+        self.p = self.lib.prefix
+        fn = self.lib[self.p + "deserialize_new"]
+        fn.restype = C.c_void_p
+        fn.argtypes = [C.c_void_p, C.c_uint64]
+        buf = (C.c_uint8 * len(data)).from_buffer_copy(data)
+        self.h = fn(buf, len(data))
+        if not self.h:
+            raise RuntimeError("DeserializeNew failed")
+        return self
+
+    def clone(self) -> "SimArena":
+        """Arena::Clone (reference library only)."""
+        other = type(self).__new__(type(self))
+        other.kind, other.lib, other.p = self.kind, self.lib, self.p
+        fn = self.lib[self.p + "clone"]
+        fn.restype = C.c_void_p
+        fn.argtypes = [C.c_void_p]
+        other.h = fn(self.h)
+        return other
+
     def set_mutator_config(self, config) -> None:
         """Arena::SetMutatorConfig from an rsg_mutator_config mirror (reference library only)."""
         fn = self.lib[self.p + "set_mutator_config"]

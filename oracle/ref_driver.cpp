@@ -372,6 +372,40 @@ int rsref_get_wheel_internals(void* h, uint32_t id, float* out8) {
     return 0;
 }
 
+// Arena::Serialize into `out` (DataStreamOut's bytes, no version word); *len receives the size.
+int rsref_serialize(void* h, uint8_t* out, uint64_t cap, uint64_t* len) {
+    DataStreamOut o;
+    ((RefArena*)h)->arena->Serialize(o);
+    *len = o.data.size();
+    if (out && cap >= o.data.size()) std::memcpy(out, o.data.data(), o.data.size());
+    return 0;
+}
+
+// Arena::DeserializeNew from bytes; a new arena handle (NULL on failure).
+void* rsref_deserialize_new(const uint8_t* data, uint64_t len) {
+    DataStreamIn in;
+    in.data.assign(data, data + len);
+    RefArena* ra = new RefArena();
+    try {
+        ra->arena = Arena::DeserializeNew(in);
+    } catch (...) {
+        delete ra;
+        return nullptr;
+    }
+    ra->arena->SetCarBumpCallback(OnBump, ra);
+    if (ra->arena->gameMode != GameMode::THE_VOID) ra->arena->SetGoalScoreCallback(OnGoal, ra);
+    return ra;
+}
+
+// Arena::Clone (without the callbacks, which are set to this driver's own); a new arena handle.
+void* rsref_clone(void* h) {
+    RefArena* ra = new RefArena();
+    ra->arena = ((RefArena*)h)->arena->Clone(false);
+    ra->arena->SetCarBumpCallback(OnBump, ra);
+    if (ra->arena->gameMode != GameMode::THE_VOID) ra->arena->SetGoalScoreCallback(OnGoal, ra);
+    return ra;
+}
+
 // Arena::SetMutatorConfig / MutatorConfig(GameMode) through the POD mirror
 // (src/Sim/MutatorConfig/MutatorConfig.h:16-79, field for field).
 int rsref_set_mutator_config(void* h, const rsg_mutator_config* c) {

@@ -171,6 +171,9 @@ PROTOTYPES = {
     "rsg_get_default_arena_config": (i32, [P(ArenaConfig)]),
     "rsg_batch_num_pads": (i32, [vp, P(u32)]),
     "rsg_get_default_mutator_config": (i32, [i32, P(MutatorConfig)]),
+    "rsg_serialize_arena": (i32, [vp, u32, vp, C.c_uint64, P(C.c_uint64)]),
+    "rsg_deserialize_arena": (i32, [vp, u32, vp, C.c_uint64]),
+    "rsg_clone_arena": (i32, [vp, u32, vp, u32]),
     "rsg_set_mutator_config": (i32, [vp, P(MutatorConfig)]),
     "rsg_get_mutator_config": (i32, [vp, P(MutatorConfig)]),
     "rsg_ground_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp, vp]),

@@ -158,6 +158,21 @@ class ArenaBatch:
         check(self.lib.rsg_demolish_car(self.h, arena, car_id, respawn_delay), "rsg_demolish_car")
 
     # ---- ball, pads, arena
+    # ---- serialisation (Arena::Serialize / DeserializeNew / Clone, RocketSim's byte format)
+    def serialize(self, arena: int) -> bytes:
+        n = C.c_uint64()
+        check(self.lib.rsg_serialize_arena(self.h, arena, None, 0, C.byref(n)), "rsg_serialize_arena")
+        buf = (C.c_uint8 * n.value)()
+        check(self.lib.rsg_serialize_arena(self.h, arena, buf, n.value, C.byref(n)), "rsg_serialize_arena")
+        return bytes(buf)
+
+    def deserialize(self, arena: int, data: bytes) -> None:
+        buf = (C.c_uint8 * len(data)).from_buffer_copy(data)
+        check(self.lib.rsg_deserialize_arena(self.h, arena, buf, len(data)), "rsg_deserialize_arena")
+
+    def clone_arena_from(self, arena: int, src: "ArenaBatch", src_arena: int) -> None:
+        check(self.lib.rsg_clone_arena(self.h, arena, src.h, src_arena), "rsg_clone_arena")
+
     # ---- mutators (Arena::SetMutatorConfig / GetMutatorConfig, for every arena of the batch)
     def get_mutator_config(self) -> "abi.MutatorConfig":
         m = abi.MutatorConfig()

@@ -211,6 +211,8 @@ struct rsg_batch {
     std::vector<uint32_t> ncars, last_id;
     std::vector<uint32_t> ids;     // [A][MC] car id by slot
     std::vector<uint8_t> order;    // [A][MC] slot by update position
+    std::vector<rsg_car_config> car_cfg;  // [A][MC] configuration by slot (for Arena::Serialize)
+    std::vector<uint8_t> car_team;        // [A][MC] team by slot
     // staging
     void* d_stage = nullptr;
     size_t stage_bytes = 0;
@@ -224,6 +226,8 @@ struct rsg_batch {
     void* hit_user = nullptr;
     rsg_mutator_config mutators{};
     std::vector<float4> pads;  // per pad: position (uu), is_big
+    rsg_arena_config arena_cfg{};                  // as given at creation (custom pads copied below)
+    std::vector<rsg_boost_pad_config> custom_pads;
     float4* d_pads = nullptr;
 };
 
@@ -662,6 +666,9 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
             b->pads.push_back(float4{PAD_LOCS[i][0], PAD_LOCS[i][1], PAD_LOCS[i][2], i < 6 ? 1.f : 0.f});
     }
     B.npads = (int)b->pads.size();
+    b->arena_cfg = cfg;
+    b->custom_pads.assign(cfg.custom_boost_pads, cfg.custom_boost_pads + (cfg.use_custom_boost_pads ? cfg.num_custom_boost_pads : 0));
+    b->arena_cfg.custom_boost_pads = b->custom_pads.empty() ? nullptr : b->custom_pads.data();
     B.custom_pads = cfg.use_custom_boost_pads ? 1 : 0;
     B.no_ball_rot = cfg.no_ball_rot ? 1 : 0;
     B.mesh = mesh_ptrs(g_soccar);
@@ -701,6 +708,8 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
     b->last_id.assign(A, 0);
     b->ids.assign(A * MC, 0);
     b->order.assign(A * MC, 0);
+    b->car_cfg.assign(A * MC, rsg_car_config{});
+    b->car_team.assign(A * MC, 0);
     // ball at rest (Arena.cpp:491-496) and its broadphase proxy created before any car
     {
         V3 p(0, 0, RL::BALL_REST_Z * RL::UU_TO_BT);
@@ -808,8 +817,9 @@ int rsg_set_mutator_config(rsg_batch* b, const rsg_mutator_config* c) {
     return RSG_OK;
 }
 
-int rsg_add_car(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* config, int respawn_index,
-                uint32_t* out_car_id) {
+// Arena::AddCar with the next car id, or with `forced_id` (Arena::DeserializeNew keeps ids)
+static int add_car_impl(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* config, int respawn_index,
+                        uint32_t forced_id, uint32_t* out_car_id) {
     int rc = check_arena(b, arena);
     if (rc) return rc;
     if (!config) return fail(RSG_ERR_ARG, "null car config");
@@ -821,9 +831,11 @@ int rsg_add_car(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* co
     int ci = cfg_index(b, d);
     if (ci < 0) return ci;
     uint32_t slot = b->ncars[arena];
-    uint32_t id = ++b->last_id[arena];
+    uint32_t id = forced_id ? forced_id : ++b->last_id[arena];
     size_t MC = b->buf.MC;
     b->ids[arena * MC + slot] = id;
+    b->car_cfg[arena * MC + slot] = *config;
+    b->car_team[arena * MC + slot] = (uint8_t)team;
     b->order[arena * MC + slot] = (uint8_t)slot;
     b->ncars[arena] = slot + 1;
     // broadphase proxy at the AddCar-time transform (identity): cell of the compound AABB minimum
@@ -850,6 +862,11 @@ int rsg_add_car(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* co
     return RSG_OK;
 }
 
+int rsg_add_car(rsg_batch* b, uint32_t arena, int team, const rsg_car_config* config, int respawn_index,
+                uint32_t* out_car_id) {
+    return add_car_impl(b, arena, team, config, respawn_index, 0, out_car_id);
+}
+
 int rsg_remove_car(rsg_batch* b, uint32_t arena, uint32_t car_id) {
     int rc = check_arena(b, arena);
     if (rc) return rc;
@@ -858,7 +875,11 @@ int rsg_remove_car(rsg_batch* b, uint32_t arena, uint32_t car_id) {
     if ((rc = set_device(b))) return rc;
     size_t MC = b->buf.MC;
     uint32_t n = b->ncars[arena];
-    for (uint32_t s = (uint32_t)slot; s + 1 < n; s++) b->ids[arena * MC + s] = b->ids[arena * MC + s + 1];
+    for (uint32_t s = (uint32_t)slot; s + 1 < n; s++) {
+        b->ids[arena * MC + s] = b->ids[arena * MC + s + 1];
+        b->car_cfg[arena * MC + s] = b->car_cfg[arena * MC + s + 1];
+        b->car_team[arena * MC + s] = b->car_team[arena * MC + s + 1];
+    }
     // drop the slot from the update order and renumber the slots behind it
     std::vector<uint8_t> ord;
     for (uint32_t k = 0; k < n; k++) {
@@ -1210,6 +1231,371 @@ int rsg_get_device_flags(rsg_batch* b, uint32_t* out) {
     RSG_CUDA(cudaMemcpyAsync(out, b->buf.au + au_index(b, AU_ERR, 0), 4 * (size_t)b->buf.A, cudaMemcpyDeviceToHost, b->stream));
     RSG_CUDA(cudaStreamSynchronize(b->stream));
     return RSG_OK;
+}
+
+// ---------------------------------------------------------------- Arena::Serialize / DeserializeNew / Clone
+// RocketSim's byte format (src/DataStream/DataStreamOut.h, DataStreamIn.h): fields little-endian and
+// raw; every WriteMultiple group starts with its field count (uint32); Vec is four floats (the
+// fourth written 0), RotMat three Vec, bool one byte, enums one byte, CarControls its 24-byte struct.
+}  // extern "C"
+
+namespace {
+
+struct StreamOut {
+    std::vector<uint8_t> d;
+    template <class T>
+    void w(T v) {
+        const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
+        d.insert(d.end(), p, p + sizeof(T));
+    }
+    void u8(uint32_t v) { w<uint8_t>((uint8_t)v); }
+    void vec(rsg_vec3 v) { w(v.x); w(v.y); w(v.z); w(0.f); }
+    void rot(const rsg_rotmat& m) { vec(m.forward); vec(m.right); vec(m.up); }
+    void group(uint32_t n) { w<uint32_t>(n); }
+};
+
+struct StreamIn {
+    const uint8_t* p;
+    size_t n, pos = 0;
+    bool ok = true;
+    template <class T>
+    T r() {
+        T v{};
+        if (pos + sizeof(T) > n) { ok = false; pos = n; return v; }
+        std::memcpy(&v, p + pos, sizeof(T));
+        pos += sizeof(T);
+        return v;
+    }
+    uint8_t u8() { return r<uint8_t>(); }
+    rsg_vec3 vec() { rsg_vec3 v{r<float>(), r<float>(), r<float>()}; r<float>(); return v; }
+    rsg_rotmat rot() { rsg_rotmat m; m.forward = vec(); m.right = vec(); m.up = vec(); return m; }
+    bool group(uint32_t expect) { uint32_t g = r<uint32_t>(); ok = ok && g == expect; return ok; }
+};
+
+void put_controls_raw(StreamOut& o, const rsg_car_controls& c) {  // the CarControls struct, 24 bytes
+    o.w(c.throttle); o.w(c.steer); o.w(c.pitch); o.w(c.yaw); o.w(c.roll);
+    o.u8(c.jump); o.u8(c.boost); o.u8(c.handbrake); o.u8(0);
+}
+rsg_car_controls get_controls_raw(StreamIn& in) {
+    rsg_car_controls c{};
+    c.throttle = in.r<float>(); c.steer = in.r<float>(); c.pitch = in.r<float>(); c.yaw = in.r<float>();
+    c.roll = in.r<float>();
+    c.jump = in.u8(); c.boost = in.u8(); c.handbrake = in.u8(); in.u8();
+    return c;
+}
+
+// The current controls of slot `slot` (what Car::controls holds), read from the arena record.
+rsg_car_controls record_controls(const std::vector<uint32_t>& rec, int slot) {
+    rsg_car_controls c{};
+    auto f = [&](int k) { float v; std::memcpy(&v, &rec[rec_car_f(CF_CTRL + k, slot)], 4); return v; };
+    c.throttle = f(0); c.steer = f(1); c.pitch = f(2); c.yaw = f(3); c.roll = f(4);
+    const uint32_t fl = rec[rec_car_u(CU_FLAGS, slot)];
+    c.jump = (fl & F_CTRL_JUMP) ? 1 : 0;
+    c.boost = (fl & F_CTRL_BOOST) ? 1 : 0;
+    c.handbrake = (fl & F_CTRL_HB) ? 1 : 0;
+    return c;
+}
+
+void put_mutators(StreamOut& o, const rsg_mutator_config& m) {  // MutatorConfig::Serialize (MutatorConfig.cpp:42-45)
+    o.w<uint16_t>(30);
+    o.group(30);
+    o.vec(m.gravity);
+    o.w(m.car_mass); o.w(m.car_world_friction); o.w(m.car_world_restitution); o.w(m.ball_mass);
+    o.w(m.ball_max_speed); o.w(m.ball_drag); o.w(m.ball_world_friction); o.w(m.ball_world_restitution);
+    o.w(m.jump_accel); o.w(m.jump_immediate_force); o.w(m.boost_accel_ground); o.w(m.boost_accel_air);
+    o.w(m.boost_used_per_second); o.w(m.respawn_delay); o.w(m.car_spawn_boost_amount); o.w(m.bump_cooldown_time);
+    o.w(m.boost_pad_cooldown_big); o.w(m.boost_pad_cooldown_small); o.w(m.ball_hit_extra_force_scale);
+    o.w(m.bump_force_scale); o.w(m.ball_radius);
+    o.u8(m.unlimited_flips); o.u8(m.unlimited_double_jumps); o.u8(m.recharge_boost_enabled);
+    o.w(m.recharge_boost_per_second); o.w(m.recharge_boost_delay);
+    o.u8(m.demo_mode); o.u8(m.enable_team_demos);
+    o.w(m.goal_base_threshold_y);
+}
+bool get_mutators(StreamIn& in, rsg_mutator_config& m) {
+    std::memset(&m, 0, sizeof(m));
+    if (in.r<uint16_t>() != 30 || !in.group(30)) return false;
+    m.gravity = in.vec();
+    m.car_mass = in.r<float>(); m.car_world_friction = in.r<float>(); m.car_world_restitution = in.r<float>();
+    m.ball_mass = in.r<float>(); m.ball_max_speed = in.r<float>(); m.ball_drag = in.r<float>();
+    m.ball_world_friction = in.r<float>(); m.ball_world_restitution = in.r<float>(); m.jump_accel = in.r<float>();
+    m.jump_immediate_force = in.r<float>(); m.boost_accel_ground = in.r<float>(); m.boost_accel_air = in.r<float>();
+    m.boost_used_per_second = in.r<float>(); m.respawn_delay = in.r<float>(); m.car_spawn_boost_amount = in.r<float>();
+    m.bump_cooldown_time = in.r<float>(); m.boost_pad_cooldown_big = in.r<float>();
+    m.boost_pad_cooldown_small = in.r<float>(); m.ball_hit_extra_force_scale = in.r<float>();
+    m.bump_force_scale = in.r<float>(); m.ball_radius = in.r<float>();
+    m.unlimited_flips = in.u8(); m.unlimited_double_jumps = in.u8(); m.recharge_boost_enabled = in.u8();
+    m.recharge_boost_per_second = in.r<float>(); m.recharge_boost_delay = in.r<float>();
+    m.demo_mode = in.u8(); m.enable_team_demos = in.u8();
+    m.goal_base_threshold_y = in.r<float>();
+    return in.ok;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Arena::Serialize (src/Sim/Arena/Arena.cpp:546-574) of one arena.  With `out` NULL or `cap` too
+// small, only *len is set (and RSG_OK returned when out is NULL).
+int rsg_serialize_arena(rsg_batch* b, uint32_t arena, uint8_t* out, uint64_t cap, uint64_t* len) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!len) return fail(RSG_ERR_ARG, "null length");
+    if ((rc = set_device(b))) return rc;
+    const size_t MC = b->buf.MC;
+    const size_t words = rec_words((int)MC);
+    std::vector<uint32_t> rec(words);
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    RSG_CUDA(cudaMemcpy(rec.data(), b->buf.rec + words * arena, 4 * words, cudaMemcpyDeviceToHost));
+    uint64_t tick = 0;
+    if ((rc = rsg_get_tick_count(b, arena, &tick))) return rc;
+    StreamOut o;
+    o.group(4);  // gameMode, tickTime, tickCount, _lastCarID
+    o.u8((uint32_t)b->game_mode);
+    o.w(b->buf.dt);
+    o.w<uint64_t>(tick);
+    o.w<uint32_t>(b->last_id[arena]);
+    const rsg_arena_config& ac = b->arena_cfg;  // ArenaConfig::Serialize (ArenaConfig.cpp:5-14)
+    o.group(5);
+    o.vec(ac.min_pos); o.vec(ac.max_pos); o.w(ac.max_aabb_len); o.u8(ac.no_ball_rot); o.u8(ac.use_custom_broadphase);
+    o.u8(ac.use_custom_boost_pads);
+    if (ac.use_custom_boost_pads) {
+        o.w<uint32_t>((uint32_t)b->custom_pads.size());
+        for (const auto& pc : b->custom_pads) {  // BoostPadConfig::Serialize
+            o.group(2);
+            o.vec(pc.pos);
+            o.u8(pc.is_big);
+        }
+    }
+    const uint32_t n = b->ncars[arena];
+    o.w<uint32_t>(n);
+    // cars by ascending id: Arena::DeserializeNew gives each car read the next id before forcing
+    // the written one (Arena.cpp:590-606), and loses cars whose written ids collide with those
+    std::vector<int> slots(n);
+    for (uint32_t k = 0; k < n; k++) slots[k] = (int)k;
+    std::sort(slots.begin(), slots.end(), [&](int x, int y) { return b->ids[arena * MC + x] < b->ids[arena * MC + y]; });
+    for (uint32_t k = 0; k < n; k++) {
+        const int slot = slots[k];
+        const uint32_t id = b->ids[arena * MC + slot];
+        const rsg_car_config& cc = b->car_cfg[arena * MC + slot];
+        rsg_car_state st;
+        if ((rc = rsg_get_car_state(b, arena, id, &st))) return rc;
+        o.u8(b->car_team[arena * MC + slot]);
+        o.w<uint32_t>(id);
+        const rsg_car_controls c = record_controls(rec, slot);  // Car::Serialize (Car.cpp:325-329)
+        o.group(8);
+        o.w(c.throttle); o.w(c.steer); o.w(c.pitch); o.w(c.yaw); o.w(c.roll);
+        o.u8(c.boost); o.u8(c.jump); o.u8(c.handbrake);
+        o.group(9);
+        o.w(cc.dodge_deadzone); o.vec(cc.hitbox_pos_offset); o.vec(cc.hitbox_size);
+        o.vec(cc.front_wheels.connection_point_offset); o.w(cc.front_wheels.suspension_rest_length);
+        o.w(cc.front_wheels.wheel_radius);
+        o.vec(cc.back_wheels.connection_point_offset); o.w(cc.back_wheels.suspension_rest_length);
+        o.w(cc.back_wheels.wheel_radius);
+        const rsg_ball_hit_info& h = st.ball_hit_info;  // CarState::Serialize (Car.cpp:308-314)
+        o.u8(h.is_valid);
+        if (h.is_valid) {
+            o.group(5);
+            o.vec(h.relative_pos_on_ball); o.vec(h.ball_pos); o.vec(h.extra_hit_vel);
+            o.w(h.tick_count_when_hit); o.w(h.tick_count_when_extra_impulse_applied);
+        }
+        o.group(30);
+        o.vec(st.pos); o.rot(st.rot_mat); o.vec(st.vel); o.vec(st.ang_vel);
+        o.u8(st.is_on_ground); o.u8(st.has_jumped); o.u8(st.has_double_jumped); o.u8(st.has_flipped);
+        o.vec(st.flip_rel_torque); o.w(st.jump_time); o.u8(st.is_flipping); o.w(st.flip_time); o.u8(st.is_jumping);
+        o.w(st.air_time_since_jump); o.w(st.boost); o.u8(st.is_boosting); o.w(st.boosting_time);
+        o.w(st.time_since_boosted); o.w(st.supersonic_time); o.w(st.handbrake_val); o.u8(st.is_auto_flipping);
+        o.w(st.auto_flip_timer); o.w(st.auto_flip_torque_scale); o.u8(st.is_demoed); o.w(st.demo_respawn_timer);
+        put_controls_raw(o, st.last_controls);
+        o.u8(st.world_contact_has_contact); o.vec(st.world_contact_normal);
+        o.w(st.car_contact_other_car_id); o.w(st.car_contact_cooldown_timer);
+    }
+    if (b->buf.has_arena && b->buf.npads > 0) {
+        o.w<uint32_t>((uint32_t)b->buf.npads);
+        for (int i = 0; i < b->buf.npads; i++) {  // BoostPadState::Serialize
+            rsg_pad_state ps;
+            if ((rc = rsg_get_pad_state(b, arena, (uint32_t)i, &ps))) return rc;
+            o.group(3);
+            o.u8(ps.is_active); o.w(ps.cooldown); o.w(ps.prev_locked_car_id);
+        }
+    }
+    rsg_ball_state bs;
+    if ((rc = rsg_get_ball_state(b, arena, &bs))) return rc;
+    o.group(12);  // BallState::Serialize (Ball.cpp:19-21): soccar has no heatseeker / dropshot state
+    o.vec(bs.pos); o.rot(bs.rot_mat); o.vec(bs.vel); o.vec(bs.ang_vel);
+    o.w(0.f); o.w(2900.f); o.w(0.f);        // hsInfo: yTargetDir, curTargetSpeed (INITIAL_TARGET_SPEED), timeSinceHit
+    o.w<int32_t>(1); o.w(0.f); o.w(0.f);    // dsInfo: chargeLevel, accumulatedHitForce, yTargetDir
+    o.u8(0); o.w<uint64_t>(0);              // dsInfo: hasDamaged, lastDamageTick
+    put_mutators(o, b->mutators);
+    *len = o.d.size();
+    if (!out) return RSG_OK;
+    if (cap < o.d.size()) return fail(RSG_ERR_ARG, "output buffer smaller than the serialized arena");
+    std::memcpy(out, o.d.data(), o.d.size());
+    return RSG_OK;
+}
+
+// Arena::DeserializeNew (Arena.cpp:576-643) into arena `arena` of the batch: its cars are replaced by
+// the serialized ones (ids, teams, configurations, controls and states), then the pads, the ball, the
+// tick count and the last car id.  The game mode, tick time, arena config and pad count must be the
+// batch's; different mutators are applied when the batch holds this one arena only.
+// `spawn_boost`: DeserializeNewCar (Arena.cpp:676-687) runs Car::_BulletSetup after reading the state,
+// which sets the boost to the spawn amount of the new arena's mutators (Car.cpp:291); those are still
+// the game mode's defaults then, the serialized mutators being read after the cars.
+static int deserialize_impl(rsg_batch* b, uint32_t arena, const uint8_t* data, uint64_t len, bool spawn_boost) {
+    int rc = check_arena(b, arena);
+    if (rc) return rc;
+    if (!data) return fail(RSG_ERR_ARG, "null data");
+    StreamIn in{data, (size_t)len};
+    if (!in.group(4)) return fail(RSG_ERR_ARG, "not a serialized arena (header)");
+    const int mode = in.u8();
+    const float tick_time = in.r<float>();
+    const uint64_t tick = in.r<uint64_t>();
+    const uint32_t last_id = in.r<uint32_t>();
+    if (mode != b->game_mode || tick_time != b->buf.dt)
+        return fail(RSG_ERR_ARG, "serialized arena has another game mode or tick rate than the batch");
+    if (!in.group(5)) return fail(RSG_ERR_ARG, "not a serialized arena (arena config)");
+    rsg_arena_config ac{};
+    ac.min_pos = in.vec(); ac.max_pos = in.vec(); ac.max_aabb_len = in.r<float>();
+    ac.no_ball_rot = in.u8(); ac.use_custom_broadphase = in.u8(); ac.use_custom_boost_pads = in.u8();
+    std::vector<rsg_boost_pad_config> pads;
+    if (ac.use_custom_boost_pads) {
+        const uint32_t np = in.r<uint32_t>();
+        for (uint32_t i = 0; i < np && in.ok; i++) {
+            rsg_boost_pad_config pc{};
+            if (!in.group(2)) break;
+            pc.pos = in.vec();
+            pc.is_big = in.u8();
+            pads.push_back(pc);
+        }
+    }
+    const rsg_arena_config& mine = b->arena_cfg;
+    bool same = in.ok && (ac.no_ball_rot != 0) == (mine.no_ball_rot != 0) &&
+                (ac.use_custom_boost_pads != 0) == (mine.use_custom_boost_pads != 0) &&
+                pads.size() == b->custom_pads.size();
+    for (size_t i = 0; same && i < pads.size(); i++)
+        same = std::memcmp(&pads[i].pos, &b->custom_pads[i].pos, sizeof(rsg_vec3)) == 0 &&
+               (pads[i].is_big != 0) == (b->custom_pads[i].is_big != 0);
+    if (!same) return fail(RSG_ERR_ARG, "serialized arena config differs from the batch's");
+    struct CarRec {
+        uint8_t team;
+        uint32_t id;
+        rsg_car_controls ctl;
+        rsg_car_config cfg;
+        rsg_car_state st;
+    };
+    std::vector<CarRec> cars;
+    const float spawn_boost_amount = default_mutators(mode).car_spawn_boost_amount;
+    const uint32_t ncars = in.r<uint32_t>();
+    if (!in.ok || ncars > (uint32_t)b->buf.MC) return fail(RSG_ERR_ARG, "serialized arena has more cars than the batch holds");
+    for (uint32_t k = 0; k < ncars && in.ok; k++) {
+        CarRec c{};
+        c.team = in.u8();
+        c.id = in.r<uint32_t>();
+        if (!in.group(8)) break;
+        c.ctl.throttle = in.r<float>(); c.ctl.steer = in.r<float>(); c.ctl.pitch = in.r<float>();
+        c.ctl.yaw = in.r<float>(); c.ctl.roll = in.r<float>();
+        c.ctl.boost = in.u8(); c.ctl.jump = in.u8(); c.ctl.handbrake = in.u8();
+        if (!in.group(9)) break;
+        rsg_get_car_config_preset(RSG_CAR_OCTANE, &c.cfg);  // three_wheels is not serialized
+        c.cfg.dodge_deadzone = in.r<float>(); c.cfg.hitbox_pos_offset = in.vec(); c.cfg.hitbox_size = in.vec();
+        c.cfg.front_wheels.connection_point_offset = in.vec(); c.cfg.front_wheels.suspension_rest_length = in.r<float>();
+        c.cfg.front_wheels.wheel_radius = in.r<float>();
+        c.cfg.back_wheels.connection_point_offset = in.vec(); c.cfg.back_wheels.suspension_rest_length = in.r<float>();
+        c.cfg.back_wheels.wheel_radius = in.r<float>();
+        c.cfg.three_wheels = 0;
+        rsg_car_state& st = c.st;
+        std::memset(&st, 0, sizeof(st));
+        st.ball_hit_info.is_valid = in.u8();
+        st.ball_hit_info.tick_count_when_hit = ~0ull;
+        st.ball_hit_info.tick_count_when_extra_impulse_applied = ~0ull;
+        if (st.ball_hit_info.is_valid) {
+            if (!in.group(5)) break;
+            st.ball_hit_info.relative_pos_on_ball = in.vec(); st.ball_hit_info.ball_pos = in.vec();
+            st.ball_hit_info.extra_hit_vel = in.vec();
+            st.ball_hit_info.tick_count_when_hit = in.r<uint64_t>();
+            st.ball_hit_info.tick_count_when_extra_impulse_applied = in.r<uint64_t>();
+        }
+        if (!in.group(30)) break;
+        st.pos = in.vec(); st.rot_mat = in.rot(); st.vel = in.vec(); st.ang_vel = in.vec();
+        st.is_on_ground = in.u8(); st.has_jumped = in.u8(); st.has_double_jumped = in.u8(); st.has_flipped = in.u8();
+        st.flip_rel_torque = in.vec(); st.jump_time = in.r<float>(); st.is_flipping = in.u8(); st.flip_time = in.r<float>();
+        st.is_jumping = in.u8(); st.air_time_since_jump = in.r<float>(); st.boost = in.r<float>();
+        st.is_boosting = in.u8(); st.boosting_time = in.r<float>(); st.time_since_boosted = in.r<float>();
+        st.supersonic_time = in.r<float>(); st.handbrake_val = in.r<float>(); st.is_auto_flipping = in.u8();
+        st.auto_flip_timer = in.r<float>(); st.auto_flip_torque_scale = in.r<float>(); st.is_demoed = in.u8();
+        st.demo_respawn_timer = in.r<float>();
+        st.last_controls = get_controls_raw(in);
+        st.world_contact_has_contact = in.u8(); st.world_contact_normal = in.vec();
+        st.car_contact_other_car_id = in.r<uint32_t>(); st.car_contact_cooldown_timer = in.r<float>();
+        if (spawn_boost) st.boost = spawn_boost_amount;
+        cars.push_back(c);
+    }
+    if (!in.ok) return fail(RSG_ERR_ARG, "serialized arena is truncated or malformed (cars)");
+    std::vector<rsg_pad_state> pad_states;
+    if (b->buf.has_arena && b->buf.npads > 0) {
+        const uint32_t np = in.r<uint32_t>();
+        if (np != (uint32_t)b->buf.npads) return fail(RSG_ERR_ARG, "serialized arena has another boost pad count");
+        for (uint32_t i = 0; i < np && in.ok; i++) {
+            rsg_pad_state ps{};
+            if (!in.group(3)) break;
+            ps.is_active = in.u8(); ps.cooldown = in.r<float>(); ps.prev_locked_car_id = in.r<uint32_t>();
+            pad_states.push_back(ps);
+        }
+    }
+    rsg_ball_state bs{};
+    if (in.group(12)) {
+        bs.pos = in.vec(); bs.rot_mat = in.rot(); bs.vel = in.vec(); bs.ang_vel = in.vec();
+        in.r<float>(); in.r<float>(); in.r<float>(); in.r<int32_t>(); in.r<float>(); in.r<float>(); in.u8();
+        in.r<uint64_t>();
+    }
+    rsg_mutator_config mut;
+    if (!in.ok || !get_mutators(in, mut)) return fail(RSG_ERR_ARG, "serialized arena is truncated or malformed");
+    if (std::memcmp(&mut, &b->mutators, sizeof(mut)) != 0) {
+        if (b->buf.A != 1) return fail(RSG_ERR_ARG, "serialized mutators differ from the batch's (a batch shares them)");
+    }
+    // replace the cars
+    while (b->ncars[arena] > 0) {
+        if ((rc = rsg_remove_car(b, arena, b->ids[arena * b->buf.MC]))) return rc;
+    }
+    if (std::memcmp(&mut, &b->mutators, sizeof(mut)) != 0)
+        if ((rc = rsg_set_mutator_config(b, &mut))) return rc;
+    for (const CarRec& c : cars) {
+        uint32_t id;
+        if ((rc = add_car_impl(b, arena, c.team, &c.cfg, 0, c.id, &id))) return rc;
+        if ((rc = rsg_set_car_state(b, arena, id, &c.st))) return rc;
+        if ((rc = rsg_set_car_controls(b, arena, id, &c.ctl))) return rc;
+    }
+    b->last_id[arena] = last_id;
+    for (size_t i = 0; i < pad_states.size(); i++)
+        if ((rc = rsg_set_pad_state(b, arena, (uint32_t)i, &pad_states[i]))) return rc;
+    if ((rc = rsg_set_ball_state(b, arena, &bs))) return rc;
+    return rsg_set_tick_count(b, arena, tick);
+}
+
+int rsg_deserialize_arena(rsg_batch* b, uint32_t arena, const uint8_t* data, uint64_t len) {
+    return deserialize_impl(b, arena, data, len, true);
+}
+
+// Arena::Clone (Arena.cpp:646-674) from one batch arena into another: the cars, pads, tick count and
+// last car id through the serialized form, then every car state and the ball state whole, as Clone
+// copies them with Car::SetState / Ball::SetState (the fields the byte format leaves out, such as
+// the air time, included).
+int rsg_clone_arena(rsg_batch* dst, uint32_t dst_arena, rsg_batch* src, uint32_t src_arena) {
+    uint64_t n = 0;
+    int rc = rsg_serialize_arena(src, src_arena, nullptr, 0, &n);
+    if (rc) return rc;
+    std::vector<uint8_t> buf(n);
+    if ((rc = rsg_serialize_arena(src, src_arena, buf.data(), n, &n))) return rc;
+    const std::vector<uint32_t> ids(src->ids.begin() + (size_t)src_arena * src->buf.MC,
+                                    src->ids.begin() + (size_t)src_arena * src->buf.MC + src->ncars[src_arena]);
+    std::vector<rsg_car_state> states(ids.size());
+    for (size_t k = 0; k < ids.size(); k++)
+        if ((rc = rsg_get_car_state(src, src_arena, ids[k], &states[k]))) return rc;
+    rsg_ball_state bs;
+    if ((rc = rsg_get_ball_state(src, src_arena, &bs))) return rc;
+    if ((rc = deserialize_impl(dst, dst_arena, buf.data(), n, false))) return rc;
+    for (size_t k = 0; k < ids.size(); k++)
+        if ((rc = rsg_set_car_state(dst, dst_arena, ids[k], &states[k]))) return rc;
+    return rsg_set_ball_state(dst, dst_arena, &bs);
 }
 
 }  // extern "C"
