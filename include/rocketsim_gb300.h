@@ -473,6 +473,46 @@ int rsg_deserialize_arena(rsg_batch* batch, uint32_t arena, const uint8_t* data,
  * `dst_arena` of `dst` (callbacks stay with each batch). */
 int rsg_clone_arena(rsg_batch* dst, uint32_t dst_arena, rsg_batch* src, uint32_t src_arena);
 
+/* ---- ball prediction ------------------------------------------------------ */
+
+/* BallPredTracker (src/Sim/BallPredTracker/BallPredTracker.h:7-35) for every
+ * arena of a batch.  Each arena gets a ball-only shadow arena (the source's
+ * game mode, arena config and tick rate; default mutators; no cars) and
+ * `num_pred_ticks` predicted ball states (predData) in device memory.
+ * Creation runs the constructor's UpdatePredFromArena (a full prediction from
+ * the arenas' balls).  Update calls return when the predictions are written. */
+typedef struct rsg_ball_pred rsg_ball_pred;
+rsg_ball_pred* rsg_ball_pred_create(rsg_batch* batch, uint32_t num_pred_ticks);
+void rsg_ball_pred_destroy(rsg_ball_pred* tracker);
+/* UpdatePredFromArena (BallPredTracker.cpp:18-24) for every arena with
+ * mask[a] != 0 (mask NULL: all): the batch's ball states and tick counts.
+ * `batch` has the tracker's arena count; work queued on its stream comes
+ * first. */
+int rsg_ball_pred_update_from_batch(rsg_ball_pred* tracker, rsg_batch* batch, const uint8_t* mask);
+/* UpdatePredManual (BallPredTracker.cpp:26-62): host arrays [n_arenas] of
+ * current ball states and ticks since the last update.  With 0 <= k <
+ * num_pred_ticks and predData[k] matching the current state (BallState::
+ * Matches, Ball.cpp:12-17) the prediction is shifted by k and extended by k
+ * ticks; otherwise everything is predicted again. */
+int rsg_ball_pred_update_manual(rsg_ball_pred* tracker, const rsg_ball_state* cur,
+                                const int32_t* ticks_since_last_update, const uint8_t* mask);
+/* ForceUpdateAllPred (BallPredTracker.cpp:64-72) from initial[n_arenas]. */
+int rsg_ball_pred_force_update_all(rsg_ball_pred* tracker, const rsg_ball_state* initial, const uint8_t* mask);
+uint32_t rsg_ball_pred_num_pred_ticks(const rsg_ball_pred* tracker);
+/* predData of one arena, front first: out[num_pred_ticks]. */
+int rsg_ball_pred_get_pred(rsg_ball_pred* tracker, uint32_t arena, rsg_ball_state* out);
+/* predData of every arena: out[n_arenas][num_pred_ticks], front first. */
+int rsg_ball_pred_get_all(rsg_ball_pred* tracker, rsg_ball_state* out);
+/* GetBallStateForTime (BallPredTracker.cpp:74-79). */
+int rsg_ball_pred_get_state_for_time(rsg_ball_pred* tracker, uint32_t arena, float pred_time, rsg_ball_state* out);
+/* lastUpdateTickCount (BallPredTracker.h:12) of one arena. */
+int rsg_ball_pred_get_last_update_tick(rsg_ball_pred* tracker, uint32_t arena, int32_t* out);
+/* The device ring: d_pred[a * num_pred_ticks + (d_head[a] + i) % num_pred_ticks]
+ * is predData[i] of arena a (valid between update calls). */
+int rsg_ball_pred_device_buffers(rsg_ball_pred* tracker, const rsg_ball_state** d_pred, const uint32_t** d_head);
+/* Device error flags of the shadow arenas ([n_arenas] words, as rsg_get_device_flags). */
+int rsg_ball_pred_device_flags(rsg_ball_pred* tracker, uint32_t* out);
+
 /* Device flags of every arena after the last step ([n_arenas] words).  Bits 0-7
  * are capacity overflows (the step also returns RSG_ERR_DEVICE); bit 8 marks a
  * box contact deeper than GJK resolves and bit 9 overlapping car boxes, two

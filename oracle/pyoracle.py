@@ -232,6 +232,10 @@ class SimArena:
     def set_ball(self, s: BallState):
         self.lib[self.p + "set_ball"](self.h, C.byref(s))
 
+    def ball_pred_tracker(self, num_pred_ticks: int) -> "RefBallPredTracker":
+        """BallPredTracker(arena, numPredTicks) (reference library only)."""
+        return RefBallPredTracker(self, num_pred_ticks)
+
     def num_pads(self) -> int:
         return int(self.lib[self.p + "num_pads"](self.h))
 
@@ -340,3 +344,47 @@ def preset(kind: str, idx: int) -> CarConfig:
     c = CarConfig()
     assert lib[lib.prefix + "preset"](idx, C.byref(c)) == 0
     return c
+
+
+class RefBallPredTracker:
+    """The reference's BallPredTracker (src/Sim/BallPredTracker/BallPredTracker.cpp) over a SimArena."""
+
+    def __init__(self, arena: SimArena, num_pred_ticks: int):
+        self.lib, self.p, self.T = arena.lib, arena.p, num_pred_ticks
+        fn = self.lib[self.p + "ballpred_create"]
+        fn.restype, fn.argtypes = C.c_void_p, [C.c_void_p, C.c_uint32]
+        self.h = fn(arena.h, num_pred_ticks)
+        for name, args in (("ballpred_destroy", [C.c_void_p]), ("ballpred_update_from_arena", [C.c_void_p, C.c_void_p]),
+                           ("ballpred_update_manual", [C.c_void_p, C.c_void_p, C.c_int]),
+                           ("ballpred_force_update_all", [C.c_void_p, C.c_void_p]),
+                           ("ballpred_get", [C.c_void_p, C.c_void_p, C.c_int]),
+                           ("ballpred_state_for_time", [C.c_void_p, C.c_float, C.c_void_p]),
+                           ("ballpred_last_update_tick", [C.c_void_p])):
+            self.lib[self.p + name].argtypes = args
+
+    def update_from_arena(self, arena: SimArena) -> None:
+        self.lib[self.p + "ballpred_update_from_arena"](self.h, arena.h)
+
+    def update_manual(self, state: BallState, ticks: int) -> None:
+        self.lib[self.p + "ballpred_update_manual"](self.h, C.byref(state), ticks)
+
+    def force_update_all(self, state: BallState) -> None:
+        self.lib[self.p + "ballpred_force_update_all"](self.h, C.byref(state))
+
+    def pred_data(self) -> list:
+        buf = (BallState * self.T)()
+        n = self.lib[self.p + "ballpred_get"](self.h, buf, self.T)
+        return [buf[i] for i in range(n)]
+
+    def state_for_time(self, t: float) -> BallState:
+        s = BallState()
+        self.lib[self.p + "ballpred_state_for_time"](self.h, t, C.byref(s))
+        return s
+
+    def last_update_tick(self) -> int:
+        return int(self.lib[self.p + "ballpred_last_update_tick"](self.h))
+
+    def close(self) -> None:
+        if self.h:
+            self.lib[self.p + "ballpred_destroy"](self.h)
+            self.h = None

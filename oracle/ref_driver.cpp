@@ -11,6 +11,7 @@
 // src/Sim/Ball/Ball.h:18-57, src/Sim/BoostPad/BoostPad.h:23-35).
 
 #include "RocketSim.h"
+#include "Sim/BallPredTracker/BallPredTracker.h"
 #include "../include/rocketsim_gb300.h"
 
 #include <cstring>
@@ -266,6 +267,40 @@ int rsref_set_ball(void* h, const rsg_ball_state* in) {
     ra->arena->ball->SetState(s);
     return 0;
 }
+
+// BallPredTracker over an arena of this driver (the tracker makes its own ball-only arena).
+static BallState PodToBall(const rsg_ball_state* in) {
+    BallState s;
+    s.pos = V(in->pos); s.rotMat = RM(in->rot_mat); s.vel = V(in->vel); s.angVel = V(in->ang_vel);
+    s.tickCountSinceUpdate = in->tick_count_since_update;
+    return s;
+}
+static void BallToPod(const BallState& s, rsg_ball_state* out) {
+    std::memset(out, 0, sizeof(*out));
+    out->pos = P(s.pos); out->rot_mat = PM(s.rotMat); out->vel = P(s.vel); out->ang_vel = P(s.angVel);
+    out->tick_count_since_update = s.tickCountSinceUpdate;
+}
+void* rsref_ballpred_create(void* h, uint32_t num_pred_ticks) {
+    return new BallPredTracker(((RefArena*)h)->arena, num_pred_ticks);
+}
+void rsref_ballpred_destroy(void* t) { delete (BallPredTracker*)t; }
+void rsref_ballpred_update_from_arena(void* t, void* h) { ((BallPredTracker*)t)->UpdatePredFromArena(((RefArena*)h)->arena); }
+void rsref_ballpred_update_manual(void* t, const rsg_ball_state* cur, int ticks) {
+    ((BallPredTracker*)t)->UpdatePredManual(PodToBall(cur), ticks);
+}
+void rsref_ballpred_force_update_all(void* t, const rsg_ball_state* initial) {
+    ((BallPredTracker*)t)->ForceUpdateAllPred(PodToBall(initial));
+}
+// predData (out[cap]); returns its size
+int rsref_ballpred_get(void* t, rsg_ball_state* out, int cap) {
+    auto& d = ((BallPredTracker*)t)->predData;
+    for (int i = 0; i < (int)d.size() && i < cap; i++) BallToPod(d[i], out + i);
+    return (int)d.size();
+}
+void rsref_ballpred_state_for_time(void* t, float pred_time, rsg_ball_state* out) {
+    BallToPod(((BallPredTracker*)t)->GetBallStateForTime(pred_time), out);
+}
+int rsref_ballpred_last_update_tick(void* t) { return ((BallPredTracker*)t)->lastUpdateTickCount; }
 
 int rsref_num_pads(void* h) { return (int)((RefArena*)h)->arena->GetBoostPads().size(); }
 

@@ -174,6 +174,18 @@ PROTOTYPES = {
     "rsg_serialize_arena": (i32, [vp, u32, vp, C.c_uint64, P(C.c_uint64)]),
     "rsg_deserialize_arena": (i32, [vp, u32, vp, C.c_uint64]),
     "rsg_clone_arena": (i32, [vp, u32, vp, u32]),
+    "rsg_ball_pred_create": (vp, [vp, u32]),
+    "rsg_ball_pred_destroy": (None, [vp]),
+    "rsg_ball_pred_update_from_batch": (i32, [vp, vp, vp]),
+    "rsg_ball_pred_update_manual": (i32, [vp, P(BallState), P(C.c_int32), vp]),
+    "rsg_ball_pred_force_update_all": (i32, [vp, P(BallState), vp]),
+    "rsg_ball_pred_num_pred_ticks": (u32, [vp]),
+    "rsg_ball_pred_get_pred": (i32, [vp, u32, P(BallState)]),
+    "rsg_ball_pred_get_all": (i32, [vp, P(BallState)]),
+    "rsg_ball_pred_get_state_for_time": (i32, [vp, u32, f32, P(BallState)]),
+    "rsg_ball_pred_get_last_update_tick": (i32, [vp, u32, P(C.c_int32)]),
+    "rsg_ball_pred_device_buffers": (i32, [vp, P(vp), P(vp)]),
+    "rsg_ball_pred_device_flags": (i32, [vp, P(u32)]),
     "rsg_set_mutator_config": (i32, [vp, P(MutatorConfig)]),
     "rsg_get_mutator_config": (i32, [vp, P(MutatorConfig)]),
     "rsg_ground_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp, vp]),

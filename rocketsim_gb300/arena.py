@@ -270,6 +270,92 @@ class ArenaBatch:
         check(self.lib.rsg_set_ball_hit_callback(self.h, cb, None), "rsg_set_ball_hit_callback")
 
 
+class BallPredTracker:
+    """BallPredTracker (src/Sim/BallPredTracker/BallPredTracker.h:7-35) for every arena of a batch:
+    each arena gets a ball-only shadow arena and `num_pred_ticks` predicted ball states on the device.
+    Creation predicts from the batch's balls, as the reference's constructor does."""
+
+    def __init__(self, batch: ArenaBatch, num_pred_ticks: int):
+        self.lib, self.n_arenas, self.num_pred_ticks = batch.lib, batch.n_arenas, num_pred_ticks
+        self.h = self.lib.rsg_ball_pred_create(batch.h, num_pred_ticks)
+        if not self.h:
+            raise RuntimeError(abi.last_error())
+
+    @staticmethod
+    def _mask(mask):
+        if mask is None:
+            return None
+        m = np.ascontiguousarray(mask, np.uint8)
+        return m, m.ctypes.data_as(C.c_void_p)
+
+    def update_from_batch(self, batch: ArenaBatch, mask=None) -> None:
+        """UpdatePredFromArena for every arena (mask[a] != 0)."""
+        m = self._mask(mask)
+        check(self.lib.rsg_ball_pred_update_from_batch(self.h, batch.h, m and m[1]), "rsg_ball_pred_update_from_batch")
+
+    def update_manual(self, states, ticks_since_last_update, mask=None) -> None:
+        """UpdatePredManual for every arena: `states` n_arenas BallStates (a ctypes array or numpy
+        records of the same layout), `ticks_since_last_update` n_arenas ints."""
+        st = _ball_array(states, self.n_arenas)
+        k = np.ascontiguousarray(ticks_since_last_update, np.int32)
+        assert k.shape == (self.n_arenas,)
+        m = self._mask(mask)
+        check(self.lib.rsg_ball_pred_update_manual(self.h, st, k.ctypes.data_as(C.POINTER(C.c_int32)), m and m[1]),
+              "rsg_ball_pred_update_manual")
+
+    def force_update_all(self, states, mask=None) -> None:
+        st = _ball_array(states, self.n_arenas)
+        m = self._mask(mask)
+        check(self.lib.rsg_ball_pred_force_update_all(self.h, st, m and m[1]), "rsg_ball_pred_force_update_all")
+
+    def pred_data(self, arena: int) -> list[BallState]:
+        out = (BallState * self.num_pred_ticks)()
+        check(self.lib.rsg_ball_pred_get_pred(self.h, arena, out), "rsg_ball_pred_get_pred")
+        return list(out)
+
+    def pred_all(self) -> np.ndarray:
+        """predData of every arena as [n_arenas, num_pred_ticks] BallState records."""
+        out = np.zeros((self.n_arenas, self.num_pred_ticks), BALL_STATE_DTYPE)
+        check(self.lib.rsg_ball_pred_get_all(self.h, out.ctypes.data_as(C.POINTER(BallState))), "rsg_ball_pred_get_all")
+        return out
+
+    def get_ball_state_for_time(self, arena: int, pred_time: float) -> BallState:
+        s = BallState()
+        check(self.lib.rsg_ball_pred_get_state_for_time(self.h, arena, pred_time, C.byref(s)),
+              "rsg_ball_pred_get_state_for_time")
+        return s
+
+    def last_update_tick(self, arena: int) -> int:
+        v = C.c_int32()
+        check(self.lib.rsg_ball_pred_get_last_update_tick(self.h, arena, C.byref(v)), "rsg_ball_pred_get_last_update_tick")
+        return v.value
+
+    def device_flags(self) -> np.ndarray:
+        out = np.zeros(self.n_arenas, np.uint32)
+        check(self.lib.rsg_ball_pred_device_flags(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32))),
+              "rsg_ball_pred_device_flags")
+        return out
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.rsg_ball_pred_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ball_array(states, n: int):
+    if isinstance(states, np.ndarray):
+        assert states.nbytes == n * C.sizeof(BallState)
+        return np.ascontiguousarray(states).ctypes.data_as(C.POINTER(BallState))
+    arr = (BallState * n)(*states)
+    return arr
+
+
 class Car:
     """Car handle of a one-arena view (src/Sim/Car/Car.h:140-160)."""
 

@@ -20,7 +20,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "librsg_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-SOURCES = ["rsg_kernels.cu", "rsg_air.cu", "rsg_air_noalloc.cu", "rsg_ground.cu", "rsg_ground_sweep.cu", "rsg_capi.cpp",
+SOURCES = ["rsg_kernels.cu", "rsg_ballpred.cu", "rsg_air.cu", "rsg_air_noalloc.cu", "rsg_ground.cu", "rsg_ground_sweep.cu", "rsg_capi.cpp",
            "rsg_mesh.cpp"]
 # The ground adjoint's reverse sweep only linearises around recomputed intermediates: division and
 # square root correct to about 2 ulp are enough there (see rsg_ground_sweep.cu).

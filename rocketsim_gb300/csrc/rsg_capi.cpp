@@ -1599,3 +1599,211 @@ int rsg_clone_arena(rsg_batch* dst, uint32_t dst_arena, rsg_batch* src, uint32_t
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- ball prediction
+// BallPredTracker (src/Sim/BallPredTracker/BallPredTracker.cpp) for every arena of a batch: the
+// tracker batch holds one ball-only arena per source arena (Arena::Create with the source's game
+// mode, arena config and tick rate, BallPredTracker.cpp:5-12: default mutators, no cars) and the
+// device side (BallPredDev) the predictions and the run list of an update.
+struct rsg_ball_pred {
+    rsg_batch* arena = nullptr;
+    int A = 0, T = 0;
+    float tick_time = 0;
+    BallPredDev d{};
+    void* d_in = nullptr;  // staging: cur [A] states, ticks [A], mask [A]
+    cudaEvent_t src_done = nullptr;
+};
+
+namespace {
+
+void ball_pred_free(rsg_ball_pred* p) {
+    if (!p) return;
+    cudaFree(p->d.pred); cudaFree(p->d.head); cudaFree(p->d.last_update); cudaFree(p->d.valid);
+    cudaFree(p->d.list); cudaFree(p->d.count); cudaFree(p->d.steps); cudaFree(p->d.base); cudaFree(p->d_in);
+    if (p->src_done) cudaEventDestroy(p->src_done);
+    if (p->arena) rsg_batch_destroy(p->arena);
+    delete p;
+}
+
+size_t in_bytes(int A) { return (size_t)A * (sizeof(rsg_ball_state) + sizeof(int32_t) + 1); }
+
+// Stages the host inputs of an update (any may be null) and runs it on the tracker's stream.
+int ball_pred_update(rsg_ball_pred* p, rsg_batch* src, int mode, const rsg_ball_state* cur, const int32_t* ticks,
+                     const uint8_t* mask) {
+    if (!p) return fail(RSG_ERR_ARG, "null tracker");
+    rsg_batch* b = p->arena;
+    int rc = set_device(b);
+    if (rc) return rc;
+    const size_t A = (size_t)p->A;
+    char* in = (char*)p->d_in;
+    rsg_ball_state* d_cur = (rsg_ball_state*)in;
+    int32_t* d_ticks = (int32_t*)(in + A * sizeof(rsg_ball_state));
+    uint8_t* d_mask = (uint8_t*)(in + A * (sizeof(rsg_ball_state) + sizeof(int32_t)));
+    if (cur) RSG_CUDA(cudaMemcpyAsync(d_cur, cur, A * sizeof(rsg_ball_state), cudaMemcpyHostToDevice, b->stream));
+    if (ticks) RSG_CUDA(cudaMemcpyAsync(d_ticks, ticks, A * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
+    if (mask) RSG_CUDA(cudaMemcpyAsync(d_mask, mask, A, cudaMemcpyHostToDevice, b->stream));
+    if (src) {  // the source batch's queued ticks come first
+        RSG_CUDA(cudaEventRecord(p->src_done, src->stream));
+        RSG_CUDA(cudaStreamWaitEvent(b->stream, p->src_done, 0));
+    }
+    RSG_CUDA(launch_ball_pred(b->buf, p->d, src ? &src->buf : nullptr, mode, d_cur, d_ticks, mask ? d_mask : nullptr,
+                              b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rsg_ball_pred* rsg_ball_pred_create(rsg_batch* src, uint32_t num_pred_ticks) {
+    if (!src) { fail(RSG_ERR_ARG, "null batch"); return nullptr; }
+    if (num_pred_ticks == 0 || num_pred_ticks > (1u << 20)) {
+        fail(RSG_ERR_ARG, "num_pred_ticks must be 1..1048576");
+        return nullptr;
+    }
+    if (set_device(src)) return nullptr;
+    const size_t A = (size_t)src->buf.A, T = num_pred_ticks;
+    rsg_ball_pred* p = new rsg_ball_pred();
+    p->A = (int)A;
+    p->T = (int)T;
+    // Arena::Create(arena->gameMode, arena->GetArenaConfig(), arena->GetTickRate())
+    p->arena = rsg_batch_create_ex(src->game_mode, (uint32_t)A, 1, 1.f / src->buf.dt, &src->arena_cfg);
+    if (!p->arena) { ball_pred_free(p); return nullptr; }
+    p->tick_time = p->arena->buf.dt;
+    p->d.T = (int)T;
+    bool ok = true;
+    auto alloc = [&](void** q, size_t bytes) {
+        if (!ok) return;
+        cudaError_t e = cudaMalloc(q, bytes);
+        if (e == cudaSuccess) e = cudaMemset(*q, 0, bytes);
+        if (e != cudaSuccess) { cuda_fail(e, "cudaMalloc(ball prediction)"); ok = false; }
+    };
+    alloc((void**)&p->d.pred, sizeof(rsg_ball_state) * A * T);
+    alloc((void**)&p->d.head, sizeof(uint32_t) * A);
+    alloc((void**)&p->d.last_update, sizeof(int32_t) * A);
+    alloc((void**)&p->d.valid, A);
+    alloc((void**)&p->d.list, sizeof(int) * A);
+    alloc((void**)&p->d.count, sizeof(int));
+    alloc((void**)&p->d.steps, sizeof(int) * A);
+    alloc((void**)&p->d.base, sizeof(uint32_t) * A);
+    alloc(&p->d_in, in_bytes((int)A));
+    if (ok && cudaEventCreateWithFlags(&p->src_done, cudaEventDisableTiming) != cudaSuccess) {
+        fail(RSG_ERR_CUDA, "cudaEventCreate");
+        ok = false;
+    }
+    // the constructor's UpdatePredFromArena (BallPredTracker.cpp:11)
+    if (!ok || ball_pred_update(p, src, 0, nullptr, nullptr, nullptr) != RSG_OK) {
+        ball_pred_free(p);
+        return nullptr;
+    }
+    return p;
+}
+
+void rsg_ball_pred_destroy(rsg_ball_pred* p) {
+    if (p && p->arena) set_device(p->arena);
+    ball_pred_free(p);
+}
+
+int rsg_ball_pred_update_from_batch(rsg_ball_pred* p, rsg_batch* src, const uint8_t* mask) {
+    if (!p || !src) return fail(RSG_ERR_ARG, "null tracker or batch");
+    if (src->buf.A != p->A) return fail(RSG_ERR_ARG, "the batch has another arena count than the tracker");
+    if (src->device != p->arena->device) return fail(RSG_ERR_ARG, "the batch is on another device");
+    return ball_pred_update(p, src, 0, nullptr, nullptr, mask);
+}
+
+int rsg_ball_pred_update_manual(rsg_ball_pred* p, const rsg_ball_state* cur, const int32_t* ticks_since_last_update,
+                                const uint8_t* mask) {
+    if (!p || !cur || !ticks_since_last_update) return fail(RSG_ERR_ARG, "null tracker or input");
+    return ball_pred_update(p, nullptr, 1, cur, ticks_since_last_update, mask);
+}
+
+int rsg_ball_pred_force_update_all(rsg_ball_pred* p, const rsg_ball_state* initial, const uint8_t* mask) {
+    if (!p || !initial) return fail(RSG_ERR_ARG, "null tracker or input");
+    return ball_pred_update(p, nullptr, 2, initial, nullptr, mask);
+}
+
+uint32_t rsg_ball_pred_num_pred_ticks(const rsg_ball_pred* p) { return p ? (uint32_t)p->T : 0; }
+
+int rsg_ball_pred_get_pred(rsg_ball_pred* p, uint32_t arena, rsg_ball_state* out) {
+    if (!p || !out) return fail(RSG_ERR_ARG, "null tracker or output");
+    if (arena >= (uint32_t)p->A) return fail(RSG_ERR_ARG, "arena index out of range");
+    int rc = set_device(p->arena);
+    if (rc) return rc;
+    uint32_t head = 0;
+    cudaStream_t st = p->arena->stream;
+    RSG_CUDA(cudaMemcpyAsync(&head, p->d.head + arena, sizeof(head), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    const size_t T = (size_t)p->T;
+    const rsg_ball_state* ring = p->d.pred + (size_t)arena * T;
+    RSG_CUDA(cudaMemcpyAsync(out, ring + head, (T - head) * sizeof(rsg_ball_state), cudaMemcpyDeviceToHost, st));
+    if (head) RSG_CUDA(cudaMemcpyAsync(out + (T - head), ring, head * sizeof(rsg_ball_state), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    return RSG_OK;
+}
+
+int rsg_ball_pred_get_all(rsg_ball_pred* p, rsg_ball_state* out) {
+    if (!p || !out) return fail(RSG_ERR_ARG, "null tracker or output");
+    int rc = set_device(p->arena);
+    if (rc) return rc;
+    const size_t A = (size_t)p->A, T = (size_t)p->T;
+    std::vector<uint32_t> head(A);
+    std::vector<rsg_ball_state> ring(A * T);
+    cudaStream_t st = p->arena->stream;
+    RSG_CUDA(cudaMemcpyAsync(head.data(), p->d.head, A * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaMemcpyAsync(ring.data(), p->d.pred, A * T * sizeof(rsg_ball_state), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    for (size_t a = 0; a < A; a++) {
+        const rsg_ball_state* r = ring.data() + a * T;
+        rsg_ball_state* o = out + a * T;
+        std::memcpy(o, r + head[a], (T - head[a]) * sizeof(rsg_ball_state));
+        std::memcpy(o + (T - head[a]), r, head[a] * sizeof(rsg_ball_state));
+    }
+    return RSG_OK;
+}
+
+// GetBallStateForTime (BallPredTracker.cpp:74-79): predData[(int)RS_CLAMP(predTime / tickTime, 0, size - 1)],
+// the clamp in float as the macro's conditional expressions give it.
+int rsg_ball_pred_get_state_for_time(rsg_ball_pred* p, uint32_t arena, float pred_time, rsg_ball_state* out) {
+    if (!p || !out) return fail(RSG_ERR_ARG, "null tracker or output");
+    if (arena >= (uint32_t)p->A) return fail(RSG_ERR_ARG, "arena index out of range");
+    int rc = set_device(p->arena);
+    if (rc) return rc;
+    float x = pred_time / p->tick_time;
+    x = x > 0 ? x : 0.f;
+    const float hi = (float)(p->T - 1);
+    x = x < hi ? x : hi;
+    const uint32_t idx = (uint32_t)(int)x;
+    uint32_t head = 0;
+    cudaStream_t st = p->arena->stream;
+    RSG_CUDA(cudaMemcpyAsync(&head, p->d.head + arena, sizeof(head), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    const size_t slot = (size_t)arena * p->T + (head + idx) % (uint32_t)p->T;
+    RSG_CUDA(cudaMemcpyAsync(out, p->d.pred + slot, sizeof(rsg_ball_state), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    return RSG_OK;
+}
+
+int rsg_ball_pred_get_last_update_tick(rsg_ball_pred* p, uint32_t arena, int32_t* out) {
+    if (!p || !out) return fail(RSG_ERR_ARG, "null tracker or output");
+    if (arena >= (uint32_t)p->A) return fail(RSG_ERR_ARG, "arena index out of range");
+    int rc = set_device(p->arena);
+    if (rc) return rc;
+    RSG_CUDA(cudaMemcpyAsync(out, p->d.last_update + arena, sizeof(int32_t), cudaMemcpyDeviceToHost, p->arena->stream));
+    RSG_CUDA(cudaStreamSynchronize(p->arena->stream));
+    return RSG_OK;
+}
+
+int rsg_ball_pred_device_buffers(rsg_ball_pred* p, const rsg_ball_state** d_pred, const uint32_t** d_head) {
+    if (!p || !d_pred || !d_head) return fail(RSG_ERR_ARG, "null tracker or output");
+    *d_pred = p->d.pred;
+    *d_head = p->d.head;
+    return RSG_OK;
+}
+
+int rsg_ball_pred_device_flags(rsg_ball_pred* p, uint32_t* out) {
+    if (!p) return fail(RSG_ERR_ARG, "null tracker");
+    return rsg_get_device_flags(p->arena, out);
+}
+
+}  // extern "C"

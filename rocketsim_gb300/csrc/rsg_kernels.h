@@ -73,4 +73,25 @@ cudaError_t launch_set_controls(const BatchBuffers& b, const rsg_car_controls* i
 // Ball-scored test of every arena into out[A] (0/1).
 cudaError_t launch_is_scored(const BatchBuffers& b, int* out, cudaStream_t st);
 
+// Device side of a ball prediction tracker (rsg_ballpred.cu): per arena a ring of T ball states
+// ([A][T], head = predData[0]), lastUpdateTickCount and whether predData is filled; the run list
+// of one update (arena, step count, first ring slot) and its length.
+struct BallPredDev {
+    int T;
+    rsg_ball_state* pred;
+    uint32_t* head;
+    int32_t* last_update;
+    uint8_t* valid;
+    int* list;
+    int* count;
+    int* steps;
+    uint32_t* base;
+};
+
+// One BallPredTracker update of every arena (mask[a] != 0, or all with mask null) of the tracker
+// batch `pred`: mode 0 UpdatePredFromArena from `src`, 1 UpdatePredManual (cur, ticks: device
+// arrays [A]), 2 ForceUpdateAllPred (cur).
+cudaError_t launch_ball_pred(const BatchBuffers& pred, const BallPredDev& d, const BatchBuffers* src, int mode,
+                             const rsg_ball_state* cur, const int32_t* ticks, const uint8_t* mask, cudaStream_t st);
+
 }  // namespace rsg

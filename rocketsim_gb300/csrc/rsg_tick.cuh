@@ -23,7 +23,7 @@ namespace rsg {
 #error "rsg_tick.cuh is device code"
 #endif
 #define RSG_D __device__ __forceinline__
-#define RSG_DN __device__ __noinline__
+#define RSG_DN static __device__ __noinline__
 
 __constant__ Curve c_curves[CV_COUNT] = RSG_CURVES_INIT;
 
