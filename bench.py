@@ -709,6 +709,83 @@ def ground_cpu_check(case, g_gpu: np.ndarray):
             "rate": k * len(which) / el, "seconds": el, "entries": len(which)}
 
 
+def _pred_balls(n: int, seed: int, dt) -> np.ndarray:
+    """Balls in flight anywhere over the field: position, speed up to 3000 uu/s, spin up to 3 rad/s."""
+    rng = np.random.default_rng(seed)
+    b = np.zeros(n, dt)
+    for f, (lo, hi) in zip("xyz", ((-3000, 3000), (-4000, 4000), (100, 1800))):
+        b["pos"][f] = rng.uniform(lo, hi, n)
+    d = rng.normal(size=(n, 3))
+    d *= (rng.uniform(0, 3000, n) / np.linalg.norm(d, axis=1))[:, None]
+    for i, f in enumerate("xyz"):
+        b["vel"][f] = d[:, i]
+        b["ang_vel"][f] = rng.uniform(-3, 3, n)
+    b["rot_mat"]["forward"]["x"] = b["rot_mat"]["right"]["y"] = b["rot_mat"]["up"]["z"] = 1
+    return b
+
+
+def run_ball_pred(args):
+    """Batched BallPredTracker: full predictions (ForceUpdateAllPred of every arena from host states)
+    and the incremental update after one tick of the source batch (UpdatePredFromArena: one new
+    tick per arena), both through the C ABI, timed on the host around the synchronous calls."""
+    import rocketsim_gb300 as rsg
+    from rocketsim_gb300 import BALL_STATE_DTYPE, abi
+    A, T = args.pred_arenas, args.pred_ticks
+    b = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, A, 1, 120.0)
+    balls = _pred_balls(A, 4321, BALL_STATE_DTYPE)
+    b.set_all_states(None, balls)
+    tr = rsg.BallPredTracker(b, T)
+    for _ in range(args.warmup):
+        tr.force_update_all(balls)
+    full = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        tr.force_update_all(balls)
+        full.append(time.perf_counter() - t0)
+    tr.update_from_batch(b)
+    inc = []
+    for k in range(args.warmup + args.steps):
+        b.step(1)
+        t0 = time.perf_counter()
+        tr.update_from_batch(b)
+        if k >= args.warmup:
+            inc.append(time.perf_counter() - t0)
+    flags = int(np.count_nonzero(tr.device_flags()))
+    tr.close()
+    b.close()
+    ms_full = statistics.median(full) * 1e3
+    return {"value": A * (T - 1) / (ms_full / 1e3), "ms_full_prediction": ms_full,
+            "ms_incremental_update": statistics.median(inc) * 1e3, "flagged_arenas": flags,
+            "h2d_bytes_per_full_prediction": A * BALL_STATE_DTYPE.itemsize}
+
+
+def ball_pred_cpu(seconds: float, T: int):
+    """Ball-ticks/s of one CPU thread predicting: the reference's own BallPredTracker::ForceUpdateAllPred
+    when the reference library is built here, else the CPU restatement stepping a ball-only arena
+    T - 1 ticks per prediction in one native call (the per-tick state copy left out)."""
+    from oracle.pyoracle import SimArena, BallState as OBallState
+    from rocketsim_gb300.arena_mesh import arena_cmf
+    kind = cpu_kind()
+    a = SimArena(kind, arena_cmf(0))
+    balls = [OBallState.from_buffer_copy(x.tobytes()) for x in _pred_balls(64, 4321, np.dtype(OBallState))]
+    tr = a.ball_pred_tracker(T) if kind == "ref" else None
+    n, i = 0, 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        if tr is not None:
+            tr.force_update_all(balls[i % len(balls)])
+        else:
+            a.set_ball(balls[i % len(balls)])
+            a.step(T - 1)
+        n += T - 1
+        i += 1
+    el = time.perf_counter() - t0
+    if tr is not None:
+        tr.close()
+    a.close()
+    return n / el, n, el, kind
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -722,6 +799,8 @@ def main():
     ap.add_argument("--ground-instances", type=int, default=65536)
     ap.add_argument("--ground-check", type=int, default=256,
                     help="ground instances checked against FP64 finite differences")
+    ap.add_argument("--pred-arenas", type=int, default=4096, help="arenas of the ball-prediction leg")
+    ap.add_argument("--pred-ticks", type=int, default=360, help="predicted ticks per arena (BallPredTracker numPredTicks)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -765,6 +844,8 @@ def main():
     adj_err, cpu_grads, cpu_el = adjoint_cpu_check(adj["case"], adj["g_gpu"], args.adj_check)
     gadj = run_ground_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
     gchk = ground_cpu_check(gadj["case"], gadj["g_gpu"])
+    bp = run_ball_pred(args)
+    bp_cpu, bp_n, bp_el, bp_kind = ball_pred_cpu(args.cpu_seconds, args.pred_ticks)
     single, _, _, kind = cpu_ticks_per_second(1, args.cpu_seconds)
     allc, n, el, _ = cpu_ticks_per_second(threads, args.cpu_seconds)
     line = {
@@ -811,6 +892,21 @@ def main():
                              "sample": f"FP64 central differences of the numpy restatement, "
                                        f"{args.ground_check} instances x {gchk['entries']} entries x 2 rollouts "
                                        f"({gchk['seconds']:.1f} s)"}},
+        "ball_pred": {
+            "metric": "predicted ball-ticks/s", "value": bp["value"], "unit": "ball-ticks/s",
+            "workload": f"BallPredTracker over {args.pred_arenas} arenas x {args.pred_ticks} ticks, balls in flight "
+                        f"(procedural soccar mesh seed 0); full prediction = ForceUpdateAllPred of every arena from "
+                        f"host states",
+            "ms_full_prediction": bp["ms_full_prediction"], "ms_incremental_update": bp["ms_incremental_update"],
+            "h2d_bytes_per_full_prediction": bp["h2d_bytes_per_full_prediction"],
+            "flagged_arenas": bp["flagged_arenas"], "gpu_launches_per_update": 2,
+            "cpu_baseline": {"value": bp_cpu, "unit": "ball-ticks/s", "cores": 1,
+                             "kind": "reference" if bp_kind == "ref" else "port",
+                             "sample": f"one thread, {bp_n} predicted ticks in {bp_el:.1f} s: "
+                                       + ("BallPredTracker::ForceUpdateAllPred of the reference built from its "
+                                          "own sources (oracle/_ref)" if bp_kind == "ref" else
+                                          "the CPU restatement (oracle/) stepping a ball-only arena, the per-tick "
+                                          "state copy left out")}},
     }
     print(json.dumps(line))
 
