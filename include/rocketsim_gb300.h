@@ -473,6 +473,22 @@ int rsg_deserialize_arena(rsg_batch* batch, uint32_t arena, const uint8_t* data,
  * `dst_arena` of `dst` (callbacks stay with each batch). */
 int rsg_clone_arena(rsg_batch* dst, uint32_t dst_arena, rsg_batch* src, uint32_t src_arena);
 
+/* ---- kickoffs and goal prediction -------------------------------------------- */
+
+/* Arena::ResetToRandomKickoff(seed) (src/Sim/Arena/Arena.cpp:113-222), soccar:
+ * the kickoff spots shuffled by std::default_random_engine(seed) as libstdc++'s
+ * std::shuffle does (seed -1: one engine for the process, seeded from the
+ * clock), cars placed in update order, the ball at rest at the centre, every
+ * pad reset.  The _many form resets arenas[k] with seeds[k] (seeds NULL: all
+ * -1) in one transfer. */
+int rsg_reset_to_random_kickoff(rsg_batch* batch, uint32_t arena, int32_t seed);
+int rsg_reset_to_random_kickoff_many(rsg_batch* batch, const uint32_t* arenas, const int32_t* seeds, uint32_t n);
+/* Arena::IsBallProbablyGoingIn(maxTime, extraMargin, &team) (Arena.cpp:770-806,
+ * soccar) of every arena: out[n_arenas] 0/1, goal_team[n_arenas] (may be NULL)
+ * the team whose goal line the ball crosses (RSG_TEAM_*; -1 where out is 0).
+ * RSG_ERR_STATE for other game modes (the reference refuses them). */
+int rsg_is_ball_probably_going_in(rsg_batch* batch, float max_time, float extra_margin, int* out, int* goal_team);
+
 /* ---- ball prediction ------------------------------------------------------ */
 
 /* BallPredTracker (src/Sim/BallPredTracker/BallPredTracker.h:7-35) for every

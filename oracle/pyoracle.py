@@ -232,6 +232,20 @@ class SimArena:
     def set_ball(self, s: BallState):
         self.lib[self.p + "set_ball"](self.h, C.byref(s))
 
+    def reset_to_random_kickoff(self, seed: int) -> None:
+        """Arena::ResetToRandomKickoff (reference library only)."""
+        fn = self.lib[self.p + "reset_to_random_kickoff"]
+        fn.argtypes = [C.c_void_p, C.c_int]
+        fn(self.h, seed)
+
+    def is_ball_probably_going_in(self, max_time: float, extra_margin: float) -> tuple[bool, int]:
+        """Arena::IsBallProbablyGoingIn (reference library only): (going in, goal team or -1)."""
+        fn = self.lib[self.p + "is_ball_probably_going_in"]
+        fn.argtypes = [C.c_void_p, C.c_float, C.c_float, C.POINTER(C.c_int)]
+        t = C.c_int()
+        r = fn(self.h, max_time, extra_margin, C.byref(t))
+        return bool(r), t.value
+
     def ball_pred_tracker(self, num_pred_ticks: int) -> "RefBallPredTracker":
         """BallPredTracker(arena, numPredTicks) (reference library only)."""
         return RefBallPredTracker(self, num_pred_ticks)

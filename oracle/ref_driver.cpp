@@ -302,6 +302,15 @@ void rsref_ballpred_state_for_time(void* t, float pred_time, rsg_ball_state* out
 }
 int rsref_ballpred_last_update_tick(void* t) { return ((BallPredTracker*)t)->lastUpdateTickCount; }
 
+void rsref_reset_to_random_kickoff(void* h, int seed) { ((RefArena*)h)->arena->ResetToRandomKickoff(seed); }
+// Arena::IsBallProbablyGoingIn; *team = the goal's team, or -1
+int rsref_is_ball_probably_going_in(void* h, float max_time, float extra_margin, int* team) {
+    Team t = Team::BLUE;
+    bool in = ((RefArena*)h)->arena->IsBallProbablyGoingIn(max_time, extra_margin, &t);
+    *team = in ? (int)t : -1;
+    return in ? 1 : 0;
+}
+
 int rsref_num_pads(void* h) { return (int)((RefArena*)h)->arena->GetBoostPads().size(); }
 
 int rsref_get_pad(void* h, int i, rsg_pad_state* out) {

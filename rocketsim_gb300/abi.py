@@ -174,6 +174,9 @@ PROTOTYPES = {
     "rsg_serialize_arena": (i32, [vp, u32, vp, C.c_uint64, P(C.c_uint64)]),
     "rsg_deserialize_arena": (i32, [vp, u32, vp, C.c_uint64]),
     "rsg_clone_arena": (i32, [vp, u32, vp, u32]),
+    "rsg_reset_to_random_kickoff": (i32, [vp, u32, C.c_int32]),
+    "rsg_reset_to_random_kickoff_many": (i32, [vp, P(u32), P(C.c_int32), u32]),
+    "rsg_is_ball_probably_going_in": (i32, [vp, f32, f32, P(i32), P(i32)]),
     "rsg_ball_pred_create": (vp, [vp, u32]),
     "rsg_ball_pred_destroy": (None, [vp]),
     "rsg_ball_pred_update_from_batch": (i32, [vp, vp, vp]),

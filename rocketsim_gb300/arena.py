@@ -158,6 +158,29 @@ class ArenaBatch:
         check(self.lib.rsg_demolish_car(self.h, arena, car_id, respawn_delay), "rsg_demolish_car")
 
     # ---- ball, pads, arena
+    # ---- kickoffs and goal prediction
+    def reset_to_random_kickoff(self, arena: int, seed: int = -1) -> None:
+        """Arena::ResetToRandomKickoff(seed)."""
+        check(self.lib.rsg_reset_to_random_kickoff(self.h, arena, seed), "rsg_reset_to_random_kickoff")
+
+    def reset_to_random_kickoff_many(self, arenas, seeds=None) -> None:
+        """ResetToRandomKickoff of arenas[k] with seeds[k] (None: -1 for all) in one transfer."""
+        ar = np.ascontiguousarray(arenas, np.uint32)
+        sd = None if seeds is None else np.ascontiguousarray(seeds, np.int32)
+        check(self.lib.rsg_reset_to_random_kickoff_many(
+            self.h, ar.ctypes.data_as(C.POINTER(C.c_uint32)),
+            None if sd is None else sd.ctypes.data_as(C.POINTER(C.c_int32)), len(ar)), "rsg_reset_to_random_kickoff_many")
+
+    def is_ball_probably_going_in(self, max_time: float = 2.0, extra_margin: float = 0.0):
+        """Arena::IsBallProbablyGoingIn of every arena: (going_in [n_arenas] bool, goal team [n_arenas], -1 if none)."""
+        out = np.zeros(self.n_arenas, np.int32)
+        team = np.zeros(self.n_arenas, np.int32)
+        check(self.lib.rsg_is_ball_probably_going_in(self.h, max_time, extra_margin,
+                                                     out.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                     team.ctypes.data_as(C.POINTER(C.c_int32))),
+              "rsg_is_ball_probably_going_in")
+        return out.astype(bool), team
+
     # ---- serialisation (Arena::Serialize / DeserializeNew / Clone, RocketSim's byte format)
     def serialize(self, arena: int) -> bytes:
         n = C.c_uint64()

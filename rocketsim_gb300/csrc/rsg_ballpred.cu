@@ -99,7 +99,7 @@ RSG_D rsg_ball_state ball_from_ctx(const Ctx& a) {
 }
 
 // The arena tick of rsg_tick_kernel (rsg_kernels.cu) over the run list, recording the ball.
-__global__ void __launch_bounds__(256, 1) rsg_ball_pred_run_kernel(BatchView bv, BallPredDev d, int hdr_cache) {
+__global__ void __launch_bounds__(256, 2) rsg_ball_pred_run_kernel(BatchView bv, BallPredDev d, int hdr_cache) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const int count = *d.count;
@@ -171,7 +171,8 @@ cudaError_t launch_ball_pred(const BatchBuffers& pred, const BallPredDev& d, con
     const int per_arena = smem_layout(pred.MC).bytes;
     int smem = per_arena * wpb;
     const int hdr_bytes = pred.mesh.sub ? pred.mesh.nsub * (int)sizeof(Subtree) : 0;
-    const int hdr_cache = (hdr_bytes > 0 && smem + hdr_bytes <= 227 * 1024) ? 1 : 0;
+    // two blocks per SM (128 registers a thread): the header copy only where both still fit
+    const int hdr_cache = (hdr_bytes > 0 && 2 * (smem + hdr_bytes + 1024) <= 228 * 1024) ? 1 : 0;
     if (hdr_cache) smem += hdr_bytes;
     if ((e = cudaFuncSetAttribute(rsg_ball_pred_run_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
         cudaSuccess)

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1109,6 +1110,23 @@ int rsg_is_ball_scored(rsg_batch* b, uint32_t arena, int* out) {
     return RSG_OK;
 }
 
+int rsg_is_ball_probably_going_in(rsg_batch* b, float max_time, float extra_margin, int* out, int* goal_team) {
+    if (!b || !out) return fail(RSG_ERR_ARG, "null batch or output");
+    if (b->game_mode != RSG_GAMEMODE_SOCCAR)
+        return fail(RSG_ERR_STATE, "IsBallProbablyGoingIn is not supported for this game mode");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    const size_t A = b->buf.A;
+    if ((rc = ensure_stage(b, 2 * sizeof(int) * A))) return rc;
+    int* d = (int*)b->d_stage;
+    RSG_CUDA(launch_going_in(b->buf, max_time, extra_margin, b->mutators.gravity.x, b->mutators.gravity.z, d, d + A,
+                             b->stream));
+    RSG_CUDA(cudaMemcpyAsync(out, d, sizeof(int) * A, cudaMemcpyDeviceToHost, b->stream));
+    if (goal_team) RSG_CUDA(cudaMemcpyAsync(goal_team, d + A, sizeof(int) * A, cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
 int rsg_get_all_states(rsg_batch* b, rsg_car_state* cars, rsg_ball_state* balls, rsg_pad_state* pads) {
     if (!b) return fail(RSG_ERR_ARG, "null batch");
     int rc;
@@ -1596,6 +1614,156 @@ int rsg_clone_arena(rsg_batch* dst, uint32_t dst_arena, rsg_batch* src, uint32_t
     for (size_t k = 0; k < ids.size(); k++)
         if ((rc = rsg_set_car_state(dst, dst_arena, ids[k], &states[k]))) return rc;
     return rsg_set_ball_state(dst, dst_arena, &bs);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- kickoff
+namespace {
+
+// std::default_random_engine of libstdc++ (minstd_rand0: x <- 16807 x mod 2^31 - 1, seed 0 -> 1)
+struct MinStd0 {  // the engine's word is 64 bits wide on LP64 (uint_fast32_t): a negative seed wraps there
+    uint32_t x;
+    explicit MinStd0(int64_t seed) { x = (uint32_t)((uint64_t)seed % 2147483647u); if (x == 0) x = 1; }
+    uint32_t operator()() { x = (uint32_t)(((uint64_t)x * 16807u) % 2147483647u); return x; }
+};
+
+// std::uniform_int_distribution<size_t>{0, hi} over it (libstdc++'s down-scaling with rejection: the
+// engine's range [1, 2^31 - 2] is cut into hi + 1 equal buckets, draws past the last one are redrawn)
+uint32_t uniform_upto(MinStd0& g, uint32_t hi) {
+    const uint32_t range = 2147483646u - 1u, buckets = hi + 1;
+    const uint32_t scaling = range / buckets, past = buckets * scaling;
+    uint32_t r;
+    do r = g() - 1u; while (r >= past);
+    return r / scaling;
+}
+
+// std::shuffle of libstdc++ for an engine whose range exceeds n^2: after an up-front swap when n is
+// even, positions are drawn two at a time, (i, i + 1) from one uniform draw over (i + 1)(i + 2).
+void shuffle5(int* v, int n, MinStd0& g) {
+    if (n < 2) return;
+    int i = 1;
+    if (n % 2 == 0) std::swap(v[i++], v[uniform_upto(g, 1)]);
+    while (i != n) {
+        const uint32_t r0 = (uint32_t)i + 1, r1 = r0 + 1;
+        const uint32_t x = uniform_upto(g, r0 * r1 - 1);
+        std::swap(v[i++], v[x / r1]);
+        std::swap(v[i++], v[x % r1]);
+    }
+}
+
+MinStd0& process_engine() {  // Math::GetRandEngine: one engine for the process, seeded from the clock
+    static MinStd0 g((int64_t)(std::chrono::steady_clock::now().time_since_epoch().count() & 0x7fffffff));
+    return g;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Arena::ResetToRandomKickoff (src/Sim/Arena/Arena.cpp:113-222) for arenas[k] with seeds[k] (-1:
+// the process-wide engine): the five soccar kickoff spots shuffled, blue cars placed in update
+// order on them (then on the respawn spots, 250 uu further back for each car already there),
+// orange cars mirrored; the ball at rest at the centre and every pad reset.
+int rsg_reset_to_random_kickoff_many(rsg_batch* b, const uint32_t* arenas, const int32_t* seeds, uint32_t n) {
+    if (!b || (n && !arenas)) return fail(RSG_ERR_ARG, "null batch or arena list");
+    if (b->game_mode != RSG_GAMEMODE_SOCCAR) return fail(RSG_ERR_STATE, "kickoffs need the soccar arena");
+    static const float SPAWN[5][3] = {{-2048, -2560, (float)(M_PI_4 * 1)}, {2048, -2560, (float)(M_PI_4 * 3)},
+                                      {-256, -3840, (float)(M_PI_4 * 2)}, {256, -3840, (float)(M_PI_4 * 2)},
+                                      {0, -4608, (float)(M_PI_4 * 2)}};
+    static const float RESPAWN[4][3] = {{-2304, -4608, (float)(M_PI / 2)}, {-2688, -4608, (float)(M_PI / 2)},
+                                        {2304, -4608, (float)(M_PI / 2)}, {2688, -4608, (float)(M_PI / 2)}};
+    const int MC = b->buf.MC;
+    std::vector<uint32_t> idx;
+    std::vector<rsg_car_state> cars;
+    for (uint32_t k = 0; k < n; k++) {
+        const uint32_t ar = arenas[k];
+        int rc = check_arena(b, ar);
+        if (rc) return rc;
+        int order[5] = {0, 1, 2, 3, 4};
+        const int32_t seed = seeds ? seeds[k] : -1;
+        if (seed == -1) {
+            shuffle5(order, 5, process_engine());
+        } else {
+            MinStd0 g((int64_t)seed);
+            shuffle5(order, 5, g);
+        }
+        std::vector<int> team_slots[2];
+        for (uint32_t p = 0; p < b->ncars[ar]; p++) {
+            const int slot = b->order[(size_t)ar * MC + p];
+            team_slots[b->car_team[(size_t)ar * MC + slot] == RSG_TEAM_BLUE ? 0 : 1].push_back(slot);
+        }
+        int at_respawn[4] = {};
+        const int npos = (int)std::max(team_slots[0].size(), team_slots[1].size());
+        for (int i = 0; i < npos; i++) {
+            float x, y, yaw;
+            if (i < 5) {
+                const float* sp = SPAWN[std::min(order[i], 4)];
+                x = sp[0]; y = sp[1]; yaw = sp[2];
+            } else {
+                const int r = (i - 5) % 5;
+                const float* sp = RESPAWN[r < 4 ? r : 3];
+                x = sp[0]; y = sp[1]; yaw = sp[2];
+                if (r < 4) y += 250.f * at_respawn[r]++;
+            }
+            for (int t = 0; t < 2; t++) {
+                if (i >= (int)team_slots[t].size()) continue;
+                rsg_car_state st = respawn_state(RSG_TEAM_BLUE, 0, b->mutators.car_spawn_boost_amount);
+                float yy = yaw;
+                st.pos = rsg_vec3{x, y, RL::CAR_SPAWN_REST_Z};
+                if (t == 1) {
+                    st.pos.x *= -1; st.pos.y *= -1;
+                    yy = (float)((double)yaw + M_PI);
+                }
+                const M3 m = m_euler_ypr(yy, -0.f, -0.f);
+                const V3 f = m.col(0), r = m.col(1), u = m.col(2);
+                st.rot_mat.forward = {f.x, f.y, f.z};
+                st.rot_mat.right = {r.x, r.y, r.z};
+                st.rot_mat.up = {u.x, u.y, u.z};
+                idx.push_back(ar);
+                idx.push_back((uint32_t)team_slots[t][i]);
+                cars.push_back(st);
+            }
+        }
+    }
+    if (!n) return RSG_OK;
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    std::vector<rsg_ball_state> balls(n);
+    for (auto& bs : balls) {
+        std::memset(&bs, 0, sizeof(bs));
+        bs.pos.z = RL::BALL_REST_Z;
+        bs.rot_mat.forward.x = bs.rot_mat.right.y = bs.rot_mat.up.z = 1;
+    }
+    std::vector<rsg_pad_state> pads((size_t)n * b->buf.npads);
+    for (auto& ps : pads) {
+        std::memset(&ps, 0, sizeof(ps));
+        ps.is_active = 1;
+    }
+    const size_t ib = idx.size() * 4, cb = cars.size() * sizeof(rsg_car_state), ab = (size_t)n * 4;
+    const size_t bb = balls.size() * sizeof(rsg_ball_state), pb = pads.size() * sizeof(rsg_pad_state);
+    auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    if ((rc = ensure_stage(b, al(ib) + al(cb) + al(ab) + al(bb) + al(pb) + 16))) return rc;
+    char* st = (char*)b->d_stage;
+    char *d_idx = st, *d_cars = d_idx + al(ib), *d_ar = d_cars + al(cb), *d_balls = d_ar + al(ab), *d_pads = d_balls + al(bb);
+    if (!cars.empty()) {
+        RSG_CUDA(cudaMemcpyAsync(d_idx, idx.data(), ib, cudaMemcpyHostToDevice, b->stream));
+        RSG_CUDA(cudaMemcpyAsync(d_cars, cars.data(), cb, cudaMemcpyHostToDevice, b->stream));
+        RSG_CUDA(launch_set_cars(b->buf, (const uint32_t*)d_idx, (int)cars.size(), (const rsg_car_state*)d_cars, b->stream));
+    }
+    RSG_CUDA(cudaMemcpyAsync(d_ar, arenas, ab, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(cudaMemcpyAsync(d_balls, balls.data(), bb, cudaMemcpyHostToDevice, b->stream));
+    RSG_CUDA(launch_set_balls(b->buf, (const uint32_t*)d_ar, (int)n, (const rsg_ball_state*)d_balls, b->stream));
+    if (pb) {
+        RSG_CUDA(cudaMemcpyAsync(d_pads, pads.data(), pb, cudaMemcpyHostToDevice, b->stream));
+        RSG_CUDA(launch_set_pads(b->buf, (const uint32_t*)d_ar, (int)n, (const rsg_pad_state*)d_pads, b->stream));
+    }
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_reset_to_random_kickoff(rsg_batch* b, uint32_t arena, int32_t seed) {
+    return rsg_reset_to_random_kickoff_many(b, &arena, &seed, 1);
 }
 
 }  // extern "C"

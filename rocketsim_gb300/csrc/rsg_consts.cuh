@@ -48,7 +48,7 @@ constexpr float CAR_AUTOFLIP_NORMZ_THRESH = 0.70710678118654752440, CAR_AUTOFLIP
 constexpr float CAR_AUTOROLL_FORCE = 100, CAR_AUTOROLL_TORQUE = 80;
 constexpr float BALL_CAR_EXTRA_IMPULSE_Z_SCALE = 0.35f, BALL_CAR_EXTRA_IMPULSE_FORWARD_SCALE = 0.65f;
 constexpr float BALL_CAR_EXTRA_IMPULSE_MAXDELTAVEL_UU = 4600.f;
-constexpr float CAR_RESPAWN_Z = 36.f;
+constexpr float CAR_RESPAWN_Z = 36.f, CAR_SPAWN_REST_Z = 17.f;
 constexpr float BUMP_COOLDOWN_TIME = 0.25f, BUMP_MIN_FORWARD_DIST = 64.5f, DEMO_RESPAWN_TIME = 3.f;
 constexpr float AIR_TORQUE_X = 130, AIR_TORQUE_Y = 95, AIR_TORQUE_Z = 400;
 constexpr float AIR_DAMP_X = 30, AIR_DAMP_Y = 20, AIR_DAMP_Z = 50;

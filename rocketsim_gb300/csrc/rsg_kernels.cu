@@ -358,7 +358,44 @@ __global__ void rsg_is_scored_kernel(BatchView bv, int* __restrict__ out) {
     out[ar] = fabsf(y) > (bv.mut.goal_threshold_y + bv.mut.ball_radius_uu) ? 1 : 0;
 }
 
+// Arena::IsBallProbablyGoingIn (src/Sim/Arena/Arena.cpp:770-806), the soccar branch: the ball's
+// time to the goal line along y, the point it would cross at under gravity, and the approximate
+// goal mouth (half width 892.755, height 642.775) widened by a tenth of the ball radius plus the
+// caller's margin.  gravity in uu/s^2 as the mutator config holds it.
+__global__ void rsg_going_in_kernel(BatchView bv, float max_time, float extra_margin, float gx, float gz,
+                                    int* __restrict__ out, int* __restrict__ team) {
+    int ar = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ar >= bv.A) return;
+    SoA s{bv, ar};
+    const float px = s.bf(BF_POS) * RL::BT_TO_UU, py = s.bf(BF_POS + 1) * RL::BT_TO_UU, pz = s.bf(BF_POS + 2) * RL::BT_TO_UU;
+    const float vx = s.bf(BF_VEL) * RL::BT_TO_UU, vy = s.bf(BF_VEL + 1) * RL::BT_TO_UU, vz = s.bf(BF_VEL + 2) * RL::BT_TO_UU;
+    int in = 0, tm = -1;
+    if (!(fabsf(vy) < 1.1920928955078125e-7f)) {  // FLT_EPSILON
+        const float sgn = (float)((vy > 0) - (vy < 0));
+        const float goal_y = bv.mut.goal_threshold_y * sgn;
+        const float t = fabsf(py - goal_y) / fabsf(vy);
+        if (!(t > max_time)) {
+            const float ex = (px + vx * t) + ((gx * t) * t) / 2.f;
+            const float ez = (pz + vz * t) + ((gz * t) * t) / 2.f;
+            const float margin = bv.mut.ball_radius_uu * 0.1f + extra_margin;
+            if (!(ez > 642.775f + margin) && !(fabsf(ex) > 892.755f + margin)) {
+                in = 1;
+                tm = sgn < 0 ? RSG_TEAM_BLUE : RSG_TEAM_ORANGE;
+            }
+        }
+    }
+    out[ar] = in;
+    if (team) team[ar] = tm;
+}
+
 static int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }
+
+cudaError_t launch_going_in(const BatchBuffers& b, float max_time, float extra_margin, float gx, float gz, int* out,
+                            int* team, cudaStream_t st) {
+    if (b.A <= 0) return cudaSuccess;
+    rsg_going_in_kernel<<<blocks_for(b.A, 128), 128, 0, st>>>(make_view(b), max_time, extra_margin, gx, gz, out, team);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_get_cars(const BatchBuffers& b, const uint32_t* idx, int n, rsg_car_state* out, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;

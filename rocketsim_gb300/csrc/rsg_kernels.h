@@ -70,6 +70,10 @@ cudaError_t launch_get_pads(const BatchBuffers& b, const uint32_t* arenas, int n
 cudaError_t launch_set_pads(const BatchBuffers& b, const uint32_t* arenas, int n, const rsg_pad_state* in, cudaStream_t st);
 // Writes controls [A][MC] into the per-car control fields.
 cudaError_t launch_set_controls(const BatchBuffers& b, const rsg_car_controls* in, cudaStream_t st);
+// Arena::IsBallProbablyGoingIn (soccar) of every arena into out[A] (0/1) and team[A] (may be null;
+// the scoring goal's team, -1 where no goal is coming); gravity components in uu/s^2.
+cudaError_t launch_going_in(const BatchBuffers& b, float max_time, float extra_margin, float gx, float gz, int* out,
+                            int* team, cudaStream_t st);
 // Ball-scored test of every arena into out[A] (0/1).
 cudaError_t launch_is_scored(const BatchBuffers& b, int* out, cudaStream_t st);
 
