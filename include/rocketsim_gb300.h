@@ -489,6 +489,47 @@ int rsg_reset_to_random_kickoff_many(rsg_batch* batch, const uint32_t* arenas, c
  * RSG_ERR_STATE for other game modes (the reference refuses them). */
 int rsg_is_ball_probably_going_in(rsg_batch* batch, float max_time, float extra_margin, int* out, int* goal_team);
 
+/* ---- game events ------------------------------------------------------------ */
+
+/* GameEventTrackerConfig (src/Sim/GameEventTracker/GameEventTracker.h:10-40) and
+ * its autoStateSetDetection flag (GameEventTracker.h:93). */
+typedef struct rsg_game_event_tracker_config {
+    float shot_min_speed;
+    float shot_touch_min_delay;
+    float pred_score_extra_margin;
+    float shot_event_cooldown;
+    float shot_min_score_time;
+    float goal_max_touch_time;
+    float pass_max_touch_time;
+    uint8_t auto_state_set_detection;
+    uint8_t _pad0[3];
+} rsg_game_event_tracker_config;
+
+#define RSG_GAME_EVENT_NONE 0
+#define RSG_GAME_EVENT_SHOT 1 /* car_id: shooter, other_car_id: passer (0: none) */
+#define RSG_GAME_EVENT_GOAL 2 /* car_id: scorer, other_car_id: passer (0: none) */
+#define RSG_GAME_EVENT_SAVE 3 /* car_id: saver */
+typedef struct rsg_game_event {
+    int32_t kind;
+    uint32_t car_id;
+    uint32_t other_car_id;
+} rsg_game_event;
+
+/* GameEventTracker for every arena of a batch (soccar): Update() of all arenas
+ * at once reports at most one event per arena (the reference's callbacks fire
+ * at most once per Update). */
+typedef struct rsg_game_event_tracker rsg_game_event_tracker;
+int rsg_get_default_game_event_tracker_config(rsg_game_event_tracker_config* out);
+rsg_game_event_tracker* rsg_game_event_tracker_create(rsg_batch* batch, const rsg_game_event_tracker_config* config);
+void rsg_game_event_tracker_destroy(rsg_game_event_tracker* tracker);
+/* GameEventTracker::Update (GameEventTracker.cpp:48-158) of every arena:
+ * events[n_arenas] (host) receives each arena's event (kind RSG_GAME_EVENT_NONE if
+ * none). */
+int rsg_game_event_tracker_update(rsg_game_event_tracker* tracker, rsg_batch* batch, rsg_game_event* events);
+/* ResetPersistentInfo (GameEventTracker.cpp:160-166) of one arena, or of all
+ * with arena = -1. */
+int rsg_game_event_tracker_reset_persistent_info(rsg_game_event_tracker* tracker, int32_t arena);
+
 /* ---- ball prediction ------------------------------------------------------ */
 
 /* BallPredTracker (src/Sim/BallPredTracker/BallPredTracker.h:7-35) for every

@@ -12,6 +12,7 @@
 
 #include "RocketSim.h"
 #include "Sim/BallPredTracker/BallPredTracker.h"
+#include "Sim/GameEventTracker/GameEventTracker.h"
 #include "../include/rocketsim_gb300.h"
 
 #include <cstring>
@@ -310,6 +311,33 @@ int rsref_is_ball_probably_going_in(void* h, float max_time, float extra_margin,
     *team = in ? (int)t : -1;
     return in ? 1 : 0;
 }
+
+// GameEventTracker with callbacks that record the event of the last Update (kind 1 shot, 2 goal,
+// 3 save; ids of the cars, 0 for none).
+struct RefEventTracker {
+    GameEventTracker t;
+    int ev[3] = {0, 0, 0};
+};
+void* rsref_gevt_create(const float* cfg7, int auto_detect) {
+    RefEventTracker* r = new RefEventTracker();
+    GameEventTrackerConfig& c = r->t.config;
+    c.shotMinSpeed = cfg7[0]; c.shotTouchMinDelay = cfg7[1]; c.predScoreExtraMargin = cfg7[2];
+    c.shotEventCooldown = cfg7[3]; c.shotMinScoreTime = cfg7[4]; c.goalMaxTouchTime = cfg7[5]; c.passMaxTouchTime = cfg7[6];
+    r->t.autoStateSetDetection = auto_detect != 0;
+    auto id = [](Car* c) { return c ? (int)c->id : 0; };
+    r->t.SetShotCallback([id](Arena*, Car* s, Car* p, void* u) { int* e = (int*)u; e[0] = 1; e[1] = id(s); e[2] = id(p); }, r->ev);
+    r->t.SetGoalCallback([id](Arena*, Car* s, Car* p, void* u) { int* e = (int*)u; e[0] = 2; e[1] = id(s); e[2] = id(p); }, r->ev);
+    r->t.SetSaveCallback([id](Arena*, Car* s, void* u) { int* e = (int*)u; e[0] = 3; e[1] = id(s); e[2] = 0; }, r->ev);
+    return r;
+}
+void rsref_gevt_update(void* t, void* h, int* out3) {
+    RefEventTracker* r = (RefEventTracker*)t;
+    r->ev[0] = r->ev[1] = r->ev[2] = 0;
+    r->t.Update(((RefArena*)h)->arena);
+    out3[0] = r->ev[0]; out3[1] = r->ev[1]; out3[2] = r->ev[2];
+}
+void rsref_gevt_reset(void* t) { ((RefEventTracker*)t)->t.ResetPersistentInfo(); }
+void rsref_gevt_destroy(void* t) { delete (RefEventTracker*)t; }
 
 int rsref_num_pads(void* h) { return (int)((RefArena*)h)->arena->GetBoostPads().size(); }
 

@@ -9,7 +9,7 @@ from .abi import (ArenaConfig, BallState, BoostPadConfig, CarConfig, CarControls
                   PadState, RSGError, Vec3, RotMat,
                   GAMEMODE_SOCCAR, GAMEMODE_THE_VOID, TEAM_BLUE, TEAM_ORANGE, CAR_OCTANE, CAR_DOMINUS,
                   CAR_PLANK, CAR_BREAKOUT, CAR_HYBRID, CAR_MERC)
-from .arena import (Arena, ArenaBatch, Ball, BallPredTracker, Car, arena_config, car_config, default_mutator_config, init,  # noqa: F401
+from .arena import (Arena, ArenaBatch, Ball, BallPredTracker, Car, GameEventTracker, arena_config, car_config, default_mutator_config, init,  # noqa: F401
                     init_from_mem,
                     CAR_STATE_DTYPE, BALL_STATE_DTYPE, PAD_STATE_DTYPE, CONTROLS_DTYPE)
 from .arena_mesh import arena_cmf, build_arena_mesh  # noqa: F401

@@ -126,6 +126,20 @@ BUMP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_
 BALL_HIT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_void_p)
 
 P = C.POINTER
+class GameEventTrackerConfig(C.Structure):
+    """rsg_game_event_tracker_config (GameEventTrackerConfig, GameEventTracker.h:10-40)."""
+    _fields_ = [("shot_min_speed", C.c_float), ("shot_touch_min_delay", C.c_float),
+                ("pred_score_extra_margin", C.c_float), ("shot_event_cooldown", C.c_float),
+                ("shot_min_score_time", C.c_float), ("goal_max_touch_time", C.c_float),
+                ("pass_max_touch_time", C.c_float), ("auto_state_set_detection", C.c_uint8), ("_pad0", C.c_uint8 * 3)]
+
+
+class GameEvent(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("car_id", C.c_uint32), ("other_car_id", C.c_uint32)]
+
+
+GAME_EVENT_NONE, GAME_EVENT_SHOT, GAME_EVENT_GOAL, GAME_EVENT_SAVE = 0, 1, 2, 3
+
 u32, u64, i32, f32, vp = C.c_uint32, C.c_uint64, C.c_int, C.c_float, C.c_void_p
 
 # name -> (restype, argtypes), in the order of include/rocketsim_gb300.h
@@ -177,6 +191,11 @@ PROTOTYPES = {
     "rsg_reset_to_random_kickoff": (i32, [vp, u32, C.c_int32]),
     "rsg_reset_to_random_kickoff_many": (i32, [vp, P(u32), P(C.c_int32), u32]),
     "rsg_is_ball_probably_going_in": (i32, [vp, f32, f32, P(i32), P(i32)]),
+    "rsg_get_default_game_event_tracker_config": (i32, [P(GameEventTrackerConfig)]),
+    "rsg_game_event_tracker_create": (vp, [vp, P(GameEventTrackerConfig)]),
+    "rsg_game_event_tracker_destroy": (None, [vp]),
+    "rsg_game_event_tracker_update": (i32, [vp, vp, P(GameEvent)]),
+    "rsg_game_event_tracker_reset_persistent_info": (i32, [vp, C.c_int32]),
     "rsg_ball_pred_create": (vp, [vp, u32]),
     "rsg_ball_pred_destroy": (None, [vp]),
     "rsg_ball_pred_update_from_batch": (i32, [vp, vp, vp]),

@@ -371,6 +371,44 @@ class BallPredTracker:
             pass
 
 
+class GameEventTracker:
+    """GameEventTracker (src/Sim/GameEventTracker/GameEventTracker.h) for every arena of a batch:
+    update() returns each arena's event of this update as records (kind, car_id, other_car_id)."""
+
+    def __init__(self, batch: ArenaBatch, config: "abi.GameEventTrackerConfig | None" = None):
+        self.lib, self.n_arenas = batch.lib, batch.n_arenas
+        self.h = self.lib.rsg_game_event_tracker_create(batch.h, C.byref(config) if config is not None else None)
+        if not self.h:
+            raise RuntimeError(abi.last_error())
+
+    @staticmethod
+    def default_config() -> "abi.GameEventTrackerConfig":
+        c = abi.GameEventTrackerConfig()
+        check(abi.load().rsg_get_default_game_event_tracker_config(C.byref(c)), "rsg_get_default_game_event_tracker_config")
+        return c
+
+    def update(self, batch: ArenaBatch) -> np.ndarray:
+        out = np.zeros(self.n_arenas, np.dtype(abi.GameEvent))
+        check(self.lib.rsg_game_event_tracker_update(self.h, batch.h, out.ctypes.data_as(C.POINTER(abi.GameEvent))),
+              "rsg_game_event_tracker_update")
+        return out
+
+    def reset_persistent_info(self, arena: int = -1) -> None:
+        check(self.lib.rsg_game_event_tracker_reset_persistent_info(self.h, arena),
+              "rsg_game_event_tracker_reset_persistent_info")
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.rsg_game_event_tracker_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _ball_array(states, n: int):
     if isinstance(states, np.ndarray):
         assert states.nbytes == n * C.sizeof(BallState)

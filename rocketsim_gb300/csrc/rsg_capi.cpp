@@ -1768,6 +1768,112 @@ int rsg_reset_to_random_kickoff(rsg_batch* b, uint32_t arena, int32_t seed) {
 
 }  // extern "C"
 
+// ---------------------------------------------------------------- game events
+struct rsg_game_event_tracker {
+    int A = 0, device = 0;
+    GameEventCfgDev cfg{};
+    GameEventDev d{};
+    rsg_game_event* d_ev = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t src_done = nullptr;
+};
+
+namespace {
+void event_tracker_free(rsg_game_event_tracker* t) {
+    if (!t) return;
+    cudaFree(t->d.shot_cooldown); cudaFree(t->d.ball_shot); cudaFree(t->d.shot_goal_team); cudaFree(t->d.scored_last);
+    cudaFree(t->d.last_update); cudaFree(t->d_ev);
+    if (t->src_done) cudaEventDestroy(t->src_done);
+    if (t->stream) cudaStreamDestroy(t->stream);
+    delete t;
+}
+}  // namespace
+
+extern "C" {
+
+// GameEventTrackerConfig's defaults (GameEventTracker.h:10-40), autoStateSetDetection on
+int rsg_get_default_game_event_tracker_config(rsg_game_event_tracker_config* out) {
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    std::memset(out, 0, sizeof(*out));
+    out->shot_min_speed = 1750;
+    out->shot_touch_min_delay = 0.3f;
+    out->pred_score_extra_margin = 0;
+    out->shot_event_cooldown = 1.0f;
+    out->shot_min_score_time = 2.0f;
+    out->goal_max_touch_time = 4.0f;
+    out->pass_max_touch_time = 2.0f;
+    out->auto_state_set_detection = 1;
+    return RSG_OK;
+}
+
+rsg_game_event_tracker* rsg_game_event_tracker_create(rsg_batch* b, const rsg_game_event_tracker_config* config) {
+    if (!b) { fail(RSG_ERR_ARG, "null batch"); return nullptr; }
+    if (b->game_mode != RSG_GAMEMODE_SOCCAR) { fail(RSG_ERR_STATE, "game events need the soccar arena"); return nullptr; }
+    if (set_device(b)) return nullptr;
+    rsg_game_event_tracker_config c;
+    if (config) c = *config; else rsg_get_default_game_event_tracker_config(&c);
+    rsg_game_event_tracker* t = new rsg_game_event_tracker();
+    t->A = b->buf.A;
+    t->device = b->device;
+    t->cfg = GameEventCfgDev{c.shot_min_speed, c.shot_touch_min_delay, c.pred_score_extra_margin, c.shot_event_cooldown,
+                             c.shot_min_score_time, c.goal_max_touch_time, c.pass_max_touch_time,
+                             c.auto_state_set_detection ? 1 : 0};
+    const size_t A = (size_t)t->A;
+    bool ok = true;
+    auto alloc = [&](void** q, size_t bytes) {
+        if (!ok) return;
+        cudaError_t e = cudaMalloc(q, bytes);
+        if (e == cudaSuccess) e = cudaMemset(*q, 0, bytes);
+        if (e != cudaSuccess) { cuda_fail(e, "cudaMalloc(game events)"); ok = false; }
+    };
+    alloc((void**)&t->d.shot_cooldown, 4 * A);
+    alloc((void**)&t->d.ball_shot, 4 * A);
+    alloc((void**)&t->d.shot_goal_team, 4 * A);
+    alloc((void**)&t->d.scored_last, 4 * A);
+    alloc((void**)&t->d.last_update, 8 * A);
+    alloc((void**)&t->d_ev, sizeof(rsg_game_event) * A);
+    if (ok && cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) ok = false;
+    if (ok && cudaEventCreateWithFlags(&t->src_done, cudaEventDisableTiming) != cudaSuccess) ok = false;
+    if (!ok) {
+        fail(RSG_ERR_CUDA, "game event tracker allocation");
+        event_tracker_free(t);
+        return nullptr;
+    }
+    return t;
+}
+
+void rsg_game_event_tracker_destroy(rsg_game_event_tracker* t) {
+    if (t) cudaSetDevice(t->device);
+    event_tracker_free(t);
+}
+
+int rsg_game_event_tracker_update(rsg_game_event_tracker* t, rsg_batch* b, rsg_game_event* events) {
+    if (!t || !b || !events) return fail(RSG_ERR_ARG, "null tracker, batch or output");
+    if (b->buf.A != t->A || b->device != t->device) return fail(RSG_ERR_ARG, "the batch is not the tracker's shape or device");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    RSG_CUDA(cudaEventRecord(t->src_done, b->stream));
+    RSG_CUDA(cudaStreamWaitEvent(t->stream, t->src_done, 0));
+    RSG_CUDA(launch_game_events(b->buf, t->d, t->cfg, b->mutators.gravity.x, b->mutators.gravity.z, t->d_ev, t->stream));
+    RSG_CUDA(cudaMemcpyAsync(events, t->d_ev, sizeof(rsg_game_event) * (size_t)t->A, cudaMemcpyDeviceToHost, t->stream));
+    RSG_CUDA(cudaStreamSynchronize(t->stream));
+    return RSG_OK;
+}
+
+int rsg_game_event_tracker_reset_persistent_info(rsg_game_event_tracker* t, int32_t arena) {
+    if (!t) return fail(RSG_ERR_ARG, "null tracker");
+    if (arena < -1 || arena >= t->A) return fail(RSG_ERR_ARG, "arena index out of range");
+    RSG_CUDA(cudaSetDevice(t->device));
+    const size_t off = arena < 0 ? 0 : (size_t)arena, n = arena < 0 ? (size_t)t->A : 1;
+    RSG_CUDA(cudaMemsetAsync(t->d.scored_last + off, 0, 4 * n, t->stream));
+    RSG_CUDA(cudaMemsetAsync(t->d.ball_shot + off, 0, 4 * n, t->stream));
+    RSG_CUDA(cudaMemsetAsync(t->d.shot_cooldown + off, 0, 4 * n, t->stream));
+    RSG_CUDA(cudaStreamSynchronize(t->stream));
+    return RSG_OK;
+}
+
+}  // extern "C"
+
 // ---------------------------------------------------------------- ball prediction
 // BallPredTracker (src/Sim/BallPredTracker/BallPredTracker.cpp) for every arena of a batch: the
 // tracker batch holds one ball-only arena per source arena (Arena::Create with the source's game

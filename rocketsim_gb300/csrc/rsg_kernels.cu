@@ -362,33 +362,145 @@ __global__ void rsg_is_scored_kernel(BatchView bv, int* __restrict__ out) {
 // time to the goal line along y, the point it would cross at under gravity, and the approximate
 // goal mouth (half width 892.755, height 642.775) widened by a tenth of the ball radius plus the
 // caller's margin.  gravity in uu/s^2 as the mutator config holds it.
+RSG_D bool going_in(const SoA& s, const BatchView& bv, float max_time, float extra_margin, float gx, float gz,
+                    int& team) {
+    const float px = s.bf(BF_POS) * RL::BT_TO_UU, py = s.bf(BF_POS + 1) * RL::BT_TO_UU, pz = s.bf(BF_POS + 2) * RL::BT_TO_UU;
+    const float vx = s.bf(BF_VEL) * RL::BT_TO_UU, vy = s.bf(BF_VEL + 1) * RL::BT_TO_UU, vz = s.bf(BF_VEL + 2) * RL::BT_TO_UU;
+    team = -1;
+    if (fabsf(vy) < 1.1920928955078125e-7f) return false;  // FLT_EPSILON
+    const float sgn = (float)((vy > 0) - (vy < 0));
+    const float goal_y = bv.mut.goal_threshold_y * sgn;
+    const float t = fabsf(py - goal_y) / fabsf(vy);
+    if (t > max_time) return false;
+    const float ex = (px + vx * t) + ((gx * t) * t) / 2.f;
+    const float ez = (pz + vz * t) + ((gz * t) * t) / 2.f;
+    const float margin = bv.mut.ball_radius_uu * 0.1f + extra_margin;
+    if (ez > 642.775f + margin || fabsf(ex) > 892.755f + margin) return false;
+    team = sgn < 0 ? RSG_TEAM_BLUE : RSG_TEAM_ORANGE;
+    return true;
+}
+
 __global__ void rsg_going_in_kernel(BatchView bv, float max_time, float extra_margin, float gx, float gz,
                                     int* __restrict__ out, int* __restrict__ team) {
     int ar = blockIdx.x * blockDim.x + threadIdx.x;
     if (ar >= bv.A) return;
-    SoA s{bv, ar};
-    const float px = s.bf(BF_POS) * RL::BT_TO_UU, py = s.bf(BF_POS + 1) * RL::BT_TO_UU, pz = s.bf(BF_POS + 2) * RL::BT_TO_UU;
-    const float vx = s.bf(BF_VEL) * RL::BT_TO_UU, vy = s.bf(BF_VEL + 1) * RL::BT_TO_UU, vz = s.bf(BF_VEL + 2) * RL::BT_TO_UU;
-    int in = 0, tm = -1;
-    if (!(fabsf(vy) < 1.1920928955078125e-7f)) {  // FLT_EPSILON
-        const float sgn = (float)((vy > 0) - (vy < 0));
-        const float goal_y = bv.mut.goal_threshold_y * sgn;
-        const float t = fabsf(py - goal_y) / fabsf(vy);
-        if (!(t > max_time)) {
-            const float ex = (px + vx * t) + ((gx * t) * t) / 2.f;
-            const float ez = (pz + vz * t) + ((gz * t) * t) / 2.f;
-            const float margin = bv.mut.ball_radius_uu * 0.1f + extra_margin;
-            if (!(ez > 642.775f + margin) && !(fabsf(ex) > 892.755f + margin)) {
-                in = 1;
-                tm = sgn < 0 ? RSG_TEAM_BLUE : RSG_TEAM_ORANGE;
-            }
-        }
-    }
-    out[ar] = in;
+    int tm = -1;
+    out[ar] = going_in(SoA{bv, ar}, bv, max_time, extra_margin, gx, gz, tm) ? 1 : 0;
     if (team) team[ar] = tm;
 }
 
+// GetShooterPasser (src/Sim/GameEventTracker/GameEventTracker.cpp:5-46): the car of `team` (cars in
+// update order) that touched the ball last within max_shooter ticks, and the teammate that touched it
+// last within max_passer ticks before that; ids, 0 for none.
+RSG_D bool shooter_passer(const SoA& s, uint64_t tick, int team, bool find_passer, uint64_t max_shooter,
+                          uint64_t max_passer, uint32_t& shooter, uint32_t& passer) {
+    const int n = (int)s.au(AU_NCARS);
+    const uint32_t ord = s.au(AU_ORDER);
+    int sh = -1, pa = -1;
+    uint64_t sh_tick = 0, pa_tick = 0;
+    for (int k = 0; k < n; k++) {
+        const int slot = (int)((ord >> (4 * k)) & 0xf);
+        const uint32_t fl = s.cu(CU_FLAGS, slot);
+        if (((fl & F_TEAM_ORANGE) ? 1 : 0) != team || !(fl & F_BHI_VALID)) continue;
+        const uint64_t hit = u64(s.cu(CU_BHI_HIT_LO, slot), s.cu(CU_BHI_HIT_HI, slot));
+        if (hit + max_shooter >= tick && (sh < 0 || hit > sh_tick)) { sh = slot; sh_tick = hit; }
+    }
+    if (sh >= 0 && find_passer) {
+        for (int k = 0; k < n; k++) {
+            const int slot = (int)((ord >> (4 * k)) & 0xf);
+            const uint32_t fl = s.cu(CU_FLAGS, slot);
+            if (((fl & F_TEAM_ORANGE) ? 1 : 0) != team || !(fl & F_BHI_VALID) || slot == sh) continue;
+            const uint64_t hit = u64(s.cu(CU_BHI_HIT_LO, slot), s.cu(CU_BHI_HIT_HI, slot));
+            if (hit + max_passer >= sh_tick && (pa < 0 || hit > pa_tick)) { pa = slot; pa_tick = hit; }
+        }
+    }
+    shooter = sh >= 0 ? s.cu(CU_ID, sh) : 0;
+    passer = pa >= 0 ? s.cu(CU_ID, pa) : 0;
+    return sh >= 0;
+}
+
+// GameEventTracker::Update (GameEventTracker.cpp:48-158) of every arena, one thread each; the
+// tracker's persistent fields live in `st`, the event of this update (if any) goes to ev[ar].
+__global__ void rsg_game_events_kernel(BatchView bv, GameEventDev st, GameEventCfgDev c, float gx, float gz,
+                                       rsg_game_event* __restrict__ ev) {
+    const int ar = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ar >= bv.A) return;
+    SoA s{bv, ar};
+    rsg_game_event e{0, 0, 0};
+    const float py = s.bf(BF_POS + 1) * RL::BT_TO_UU;
+    const bool scored = fabsf(py) > (bv.mut.goal_threshold_y + bv.mut.ball_radius_uu);
+    const float tick_time = bv.dt, tickrate = 1.f / bv.dt;
+    const uint64_t tick = u64(s.au(AU_TICK_LO), s.au(AU_TICK_HI));
+    const uint64_t upd = u64(s.bu(BU_TICKS_LO), s.bu(BU_TICKS_HI));
+    const uint64_t last = st.last_update[ar];
+    if (upd > last || !c.auto_state_set_detection) {
+        const uint64_t dticks = upd - last;
+        const float dt = (float)dticks * tick_time;
+        if (scored && !st.scored_last[ar]) {
+            uint32_t a = 0, b = 0;
+            const int team = -py < 0 ? RSG_TEAM_BLUE : RSG_TEAM_ORANGE;
+            if (shooter_passer(s, tick, team, true, (uint64_t)(c.goal_max_touch_time * tickrate),
+                               (uint64_t)(c.pass_max_touch_time * tickrate), a, b))
+                e = rsg_game_event{RSG_GAME_EVENT_GOAL, a, b};
+        } else if (!st.ball_shot[ar]) {
+            if (st.shot_cooldown[ar] > 0) {
+                const float v = st.shot_cooldown[ar] - dt;
+                st.shot_cooldown[ar] = v > 0 ? v : 0.f;
+            } else {
+                const float vx = s.bf(BF_VEL) * RL::BT_TO_UU, vy = s.bf(BF_VEL + 1) * RL::BT_TO_UU,
+                            vz = s.bf(BF_VEL + 2) * RL::BT_TO_UU;
+                const float speed_sq = (vx * vx + vy * vy) + vz * vz;
+                int goal_team = -1;
+                if (speed_sq >= c.shot_min_speed * c.shot_min_speed &&
+                    going_in(s, bv, c.shot_min_score_time, c.pred_score_extra_margin, gx, gz, goal_team)) {
+                    const int shooter_team = 1 - goal_team;
+                    const uint64_t min_delay = (uint64_t)(c.shot_touch_min_delay * tickrate);
+                    uint32_t a = 0, b = 0;
+                    if (shooter_passer(s, tick, shooter_team, true, dticks + min_delay,
+                                       (uint64_t)(c.pass_max_touch_time * tickrate), a, b)) {
+                        int slot = -1;
+                        for (int k = 0; k < (int)s.au(AU_NCARS); k++)
+                            if (s.cu(CU_ID, k) == a) slot = k;
+                        const uint64_t since = tick - u64(s.cu(CU_BHI_HIT_LO, slot), s.cu(CU_BHI_HIT_HI, slot));
+                        if (since >= min_delay) {
+                            st.ball_shot[ar] = 1;
+                            st.shot_goal_team[ar] = goal_team;
+                            st.shot_cooldown[ar] = c.shot_event_cooldown;
+                            e = rsg_game_event{RSG_GAME_EVENT_SHOT, a, b};
+                        }
+                    }
+                }
+            }
+        } else {
+            int t_unused = -1;
+            if (!going_in(s, bv, c.shot_min_score_time, c.pred_score_extra_margin, gx, gz, t_unused)) {
+                uint32_t a = 0, b = 0;
+                if (shooter_passer(s, tick, st.shot_goal_team[ar], false, dticks, 0, a, b))
+                    e = rsg_game_event{RSG_GAME_EVENT_SAVE, a, 0};
+                st.ball_shot[ar] = 0;
+            }
+        }
+    } else if (upd == last) {
+        ev[ar] = e;
+        return;
+    } else {  // ResetPersistentInfo
+        st.scored_last[ar] = 0;
+        st.ball_shot[ar] = 0;
+        st.shot_cooldown[ar] = 0;
+    }
+    st.scored_last[ar] = scored ? 1 : 0;
+    st.last_update[ar] = upd;
+    ev[ar] = e;
+}
+
 static int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }
+
+cudaError_t launch_game_events(const BatchBuffers& b, const GameEventDev& st, const GameEventCfgDev& c, float gx,
+                               float gz, rsg_game_event* ev, cudaStream_t s) {
+    if (b.A <= 0) return cudaSuccess;
+    rsg_game_events_kernel<<<blocks_for(b.A, 128), 128, 0, s>>>(make_view(b), st, c, gx, gz, ev);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_going_in(const BatchBuffers& b, float max_time, float extra_margin, float gx, float gz, int* out,
                             int* team, cudaStream_t st) {

@@ -74,6 +74,22 @@ cudaError_t launch_set_controls(const BatchBuffers& b, const rsg_car_controls* i
 // the scoring goal's team, -1 where no goal is coming); gravity components in uu/s^2.
 cudaError_t launch_going_in(const BatchBuffers& b, float max_time, float extra_margin, float gx, float gz, int* out,
                             int* team, cudaStream_t st);
+// GameEventTracker's persistent fields for every arena (device arrays [A]) and its config.
+struct GameEventDev {
+    float* shot_cooldown;
+    int* ball_shot;
+    int* shot_goal_team;
+    int* scored_last;
+    uint64_t* last_update;
+};
+struct GameEventCfgDev {
+    float shot_min_speed, shot_touch_min_delay, pred_score_extra_margin, shot_event_cooldown, shot_min_score_time,
+        goal_max_touch_time, pass_max_touch_time;
+    int auto_state_set_detection;
+};
+// GameEventTracker::Update of every arena; ev[A] (device) receives each arena's event.
+cudaError_t launch_game_events(const BatchBuffers& b, const GameEventDev& st, const GameEventCfgDev& c, float gx,
+                               float gz, rsg_game_event* ev, cudaStream_t s);
 // Ball-scored test of every arena into out[A] (0/1).
 cudaError_t launch_is_scored(const BatchBuffers& b, int* out, cudaStream_t st);
 
