@@ -461,8 +461,9 @@ __global__ void rsg_game_events_kernel(BatchView bv, GameEventDev st, GameEventC
                         int slot = -1;
                         for (int k = 0; k < (int)s.au(AU_NCARS); k++)
                             if (s.cu(CU_ID, k) == a) slot = k;
-                        const uint64_t since = tick - u64(s.cu(CU_BHI_HIT_LO, slot), s.cu(CU_BHI_HIT_HI, slot));
-                        if (since >= min_delay) {
+                        const uint64_t since =
+                            slot < 0 ? 0 : tick - u64(s.cu(CU_BHI_HIT_LO, slot), s.cu(CU_BHI_HIT_HI, slot));
+                        if (slot >= 0 && since >= min_delay) {
                             st.ball_shot[ar] = 1;
                             st.shot_goal_team[ar] = goal_team;
                             st.shot_cooldown[ar] = c.shot_event_cooldown;
