@@ -6,7 +6,7 @@ import os
 
 import numpy as np
 
-from serial_format import parse_arena
+from serial_format import parse_arena, reorder_cars_ascending
 
 PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "serial_arenas.npz")
 
@@ -25,3 +25,17 @@ def test_reference_bytes_parse_completely():
             assert c["state"]["boost"] == ref["boost"] and c["state"]["is_on_ground"] == ref["is_on_ground"]
         b = z["ball_t0"][i]
         assert d["ball"]["vel"] == (b["vel"]["x"], b["vel"]["y"], b["vel"]["z"])
+
+
+def test_car_reordering_keeps_every_field():
+    """The fixture's blobs hold their cars by ascending id; reordering them again is the identity, and
+    reordering a blob with its cars reversed gives the same bytes back."""
+    z = np.load(PATH)
+    for i in range(len(z["offsets"]) - 1):
+        blob = z["blob"][z["offsets"][i]:z["offsets"][i + 1]].tobytes()
+        d = parse_arena(blob)
+        assert [c["id"] for c in d["cars"]] == sorted(c["id"] for c in d["cars"])
+        assert reorder_cars_ascending(blob) == blob
+        first, last = d["cars"][0]["span"][0], d["cars"][-1]["span"][1]
+        rev = blob[:first] + b"".join(blob[c["span"][0]:c["span"][1]] for c in reversed(d["cars"])) + blob[last:]
+        assert reorder_cars_ascending(rev) == blob
