@@ -50,11 +50,11 @@ WORKLOAD = "batched uniform 2v2: 4096 arenas x (4 Octane + ball), procedural soc
 
 
 # ---------------------------------------------------------------- workload
-def initial_states(n_arenas: int, seed: int, car_dt, ball_dt):
+def initial_states(n_arenas: int, seed: int, car_dt, ball_dt, cars_per_arena: int = CARS):
     rng = np.random.default_rng(seed)
     A = n_arenas
-    cars = np.zeros(A * CARS, car_dt)
-    n = A * CARS
+    cars = np.zeros(A * cars_per_arena, car_dt)
+    n = A * cars_per_arena
     air = rng.random(n) < 0.25
     x, y = rng.uniform(-3500, 3500, n), rng.uniform(-4500, 4500, n)
     z = np.where(air, rng.uniform(200, 1800, n), 17.0)
@@ -238,6 +238,25 @@ def cpu_ticks_per_second(threads: int, seconds: float, seed: int = 7, kind: str 
     return sum(counts) / el, sum(counts), el, kind
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform string)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
 def reference_kind_note(kind: str) -> str:
     if kind == "ref":
         return "the reference RocketSim built from its own sources (oracle/_ref)"
@@ -246,101 +265,203 @@ def reference_kind_note(kind: str) -> str:
 
 
 # ---------------------------------------------------------------- GPU arm
-def run_gpu(args, rank: int, world: int):
+HITBOXES = 6  # Octane, Dominus, Plank, Breakout, Hybrid, Merc
+
+
+def uneven_layout(n_arenas: int, seed: int):
+    """Car counts 2, 4 or 6 drawn 1:1:1 per arena and a hitbox preset drawn uniformly per car."""
+    rng = np.random.default_rng(seed)
+    counts = rng.choice([2, 4, 6], n_arenas)
+    presets = [rng.integers(0, HITBOXES, int(c)) for c in counts]
+    return counts, presets
+
+
+def make_batch(rsg, abi, A: int, mc: int, counts=None, presets=None):
+    batch = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, A, mc, 120.0)
+    for a in range(A):
+        n = mc if counts is None else int(counts[a])
+        for i in range(n):
+            batch.add_car(a, i % 2, abi.CAR_OCTANE if presets is None else int(presets[a][i]), 0)
+    return batch
+
+
+def place_states(batch, rsg, A: int, mc: int, seed: int):
+    """Seeded starting states of the batched workloads (slots without a car are ignored on set)."""
+    cars, balls = initial_states(A, seed, rsg.CAR_STATE_DTYPE, rsg.BALL_STATE_DTYPE, cars_per_arena=mc)
+    batch.set_all_states(cars, balls, None)
+
+
+def run_arena_leg(args, dev: int, A: int, mc: int, steps: int, warmup: int, settle: int, counts=None,
+                  presets=None, reset_every: int = 0, reset_frac: float = 0.0, rank: int = 0, world: int = 1,
+                  e2e: bool = True, flush_l2: bool = True, curve: bool = True, tps: int = TICKS_PER_STEP):
+    """One batched workload: `settle` ticks to leave the start transient, `warmup` untimed steps,
+    then `steps` timed steps of `tps` ticks, each one rsg_step_async launch with its
+    controls already in device memory (L2 flushed before each).  Optionally the end-to-end leg
+    through the synchronous host API with pinned host buffers."""
     import torch
     import rocketsim_gb300 as rsg
     from rocketsim_gb300 import abi
-    from rocketsim_gb300.arena_mesh import arena_cmf
 
-    dev = int(os.environ.get("LOCAL_RANK", 0))
-    torch.cuda.set_device(dev)
-    rsg.init_from_mem([arena_cmf(0)])
-    A = args.arenas
-    batch = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, A, CARS, 120.0)
-    for a in range(A):
-        for i in range(CARS):
-            batch.add_car(a, i % 2, abi.CAR_OCTANE, 0)
-    cars, balls = initial_states(A, 1234 + rank, rsg.CAR_STATE_DTYPE, rsg.BALL_STATE_DTYPE)
-    batch.set_all_states(cars, balls, None)
+    batch = make_batch(rsg, abi, A, mc, counts, presets)
+    place_states(batch, rsg, A, mc, 1234 + rank)
+    n_ctl = A * mc
+    proc = ControlProcess(n_ctl, 99 + rank, rsg.CONTROLS_DTYPE)
+    rng = np.random.default_rng(555 + rank)
+    d = f"cuda:{dev}"
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=d) if flush_l2 else None
+    stream = torch.cuda.ExternalStream(batch.stream(), device=d)
+    ticks_done = 0
+    resets = 0
 
-    nsteps = args.warmup + args.steps
-    proc = ControlProcess(A * CARS, 99 + rank, rsg.CONTROLS_DTYPE)
-    seq = np.stack([np.stack([proc.tick() for _ in range(TICKS_PER_STEP)]) for _ in range(nsteps)])
-    d_seq = torch.from_numpy(seq.view(np.uint8).reshape(nsteps, -1).copy()).to(f"cuda:{dev}")
-    step_bytes = d_seq.shape[1]
-    stream = torch.cuda.ExternalStream(batch.stream(), device=f"cuda:{dev}")
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")
+    def maybe_reset(t0: int, t1: int):
+        # a goal or reset re-randomises reset_frac of the arenas once per reset_every ticks
+        nonlocal resets
+        if not reset_every or t1 // reset_every == t0 // reset_every:
+            return
+        k = max(1, int(round(A * reset_frac)))
+        which = rng.choice(A, k, replace=False).astype(np.uint32)
+        batch.reset_to_random_kickoff_many(which, rng.integers(0, 2 ** 31 - 1, k).astype(np.int32))
+        resets += k
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    def chunk(nticks: int) -> torch.Tensor:
+        seq = np.stack([proc.tick() for _ in range(nticks)])
+        t = torch.from_numpy(seq.view(np.uint8).reshape(-1).copy()).to(d)
+        torch.cuda.current_stream().synchronize()  # the batch's stream reads it next
+        return t
 
-    # ---- value: device-resident inputs, one launch per step.  The warm-up steps also let the
-    # batch's block-shape tuner finish its trials (each trial is read after its launch completes).
-    for s in range(args.warmup):
-        batch.step_async(d_seq[s].data_ptr(), TICKS_PER_STEP)
+    # ---- settle: leave the start transient (cars land, drive on walls, collide); ticks/s against
+    # game time on the way
+    settle_curve = []
+    win = 120
+    while ticks_done < settle:
+        n = min(win, settle - ticks_done)
+        dc = chunk(n)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for k in range(0, n, tps):
+                m = min(tps, n - k)
+                batch.step_async(dc[k * n_ctl * 24:(k + m) * n_ctl * 24].data_ptr(), m)
+            e1.record(stream)
         batch.sync()
+        maybe_reset(ticks_done, ticks_done + n)
+        ticks_done += n
+        if curve:
+            settle_curve.append([ticks_done, A * n / (e0.elapsed_time(e1) / 1e3)])
+    # ---- warm-up and timed steps
+    nsteps = warmup + steps
+    d_seq = chunk(nsteps * tps).view(nsteps, -1)
+    for s in range(warmup):
+        batch.step_async(d_seq[s].data_ptr(), tps)
+        batch.sync()
+        maybe_reset(ticks_done, ticks_done + tps)
+        ticks_done += tps
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     clocks = ClockSampler(dev)
     clocks.start()
-    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     torch.cuda.synchronize()
+    first_tick = ticks_done
     with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.fill_(k & 0xff)
+        for k in range(steps):
+            if flush is not None:
+                flush.fill_(k & 0xff)
             ev[k][0].record(stream)
-            batch.step_async(d_seq[args.warmup + k].data_ptr(), TICKS_PER_STEP)
+            batch.step_async(d_seq[warmup + k].data_ptr(), tps)
             ev[k][1].record(stream)
+            if reset_every and (ticks_done + tps) // reset_every != ticks_done // reset_every:
+                batch.sync()  # the reset is a host call between launches; it stays outside the events
+                maybe_reset(ticks_done, ticks_done + tps)
+            ticks_done += tps
     batch.sync()
     torch.cuda.synchronize()
-    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     clk = clocks.stop()
     times_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(times_ms)
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        t = torch.tensor([total_ms], device=d)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    arena_ticks = A * TICKS_PER_STEP * args.steps * world
-    value = arena_ticks / (total_ms / 1e3)
+    value = A * tps * steps * world / (total_ms / 1e3)
     flags = batch.device_flags()
-
-    # ---- e2e: host buffers through the synchronous API
-    h_ctl = torch.empty(A * CARS * rsg.CONTROLS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
-    ctl_np = h_ctl.numpy().view(rsg.CONTROLS_DTYPE)
-    out_cars = np.zeros(A * CARS, rsg.CAR_STATE_DTYPE)
-    out_balls = np.zeros(A, rsg.BALL_STATE_DTYPE)
-    out_pads = np.zeros(A * batch.num_pads, rsg.PAD_STATE_DTYPE)
-    e2e_steps = max(3, min(args.steps, 20))
-    for s in range(2):
-        ctl_np[:] = seq[s, 0]
-        batch.set_controls_all(ctl_np)
-        batch.step(TICKS_PER_STEP)
-        batch.get_all_states(out_cars, out_balls, out_pads)
-    barrier()
-    e2e_time = 0.0
-    for s in range(e2e_steps):
-        ctl_np[:] = seq[(s + 2) % nsteps, 0]
-        flush.fill_(s & 0xff)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        batch.set_controls_all(ctl_np)
-        batch.step(TICKS_PER_STEP)
-        batch.get_all_states(out_cars, out_balls, out_pads)
-        e2e_time += time.perf_counter() - t0
-    e2e_value = A * TICKS_PER_STEP * e2e_steps * world / e2e_time
-    h2d = ctl_np.nbytes
-    d2h = out_cars.nbytes + out_balls.nbytes + out_pads.nbytes
+    out = {"value": value, "ms_per_step": total_ms / steps, "times_ms": times_ms, "clocks": clk,
+           "game_tick_first_timed": first_tick, "game_tick_last_timed": ticks_done,
+           "ticks_per_s_vs_game_tick": [[t, round(v)] for t, v in settle_curve],
+           "warn_flags_any": int(np.bitwise_or.reduce(flags)) if flags.size else 0, "arenas_reset": resets,
+           "gpu_launches": steps}
+    if e2e:
+        # ---- e2e: host buffers (pinned) through the synchronous API: controls in, every car, ball and
+        # pad state out, each step
+        ctl_h = torch.empty(n_ctl * rsg.CONTROLS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+        ctl_np = ctl_h.numpy().view(rsg.CONTROLS_DTYPE)
+        pin = lambda dt, n: torch.empty(n * dt.itemsize, dtype=torch.uint8).pin_memory().numpy().view(dt)  # noqa
+        out_cars = pin(rsg.CAR_STATE_DTYPE, A * mc)
+        out_balls = pin(rsg.BALL_STATE_DTYPE, A)
+        out_pads = pin(rsg.PAD_STATE_DTYPE, A * batch.num_pads)
+        e2e_steps = max(3, min(steps, 20))
+        seq_h = np.stack([proc.tick() for _ in range(e2e_steps + 2)])
+        for s in range(2):
+            ctl_np[:] = seq_h[s]
+            batch.set_controls_all(ctl_np)
+            batch.step(tps)
+            batch.get_all_states(out_cars, out_balls, out_pads)
+        e2e_time = 0.0
+        for s in range(e2e_steps):
+            ctl_np[:] = seq_h[s + 2]
+            if flush is not None:
+                flush.fill_(s & 0xff)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            batch.set_controls_all(ctl_np)
+            batch.step(tps)
+            batch.get_all_states(out_cars, out_balls, out_pads)
+            e2e_time += time.perf_counter() - t0
+        out["e2e"] = {"value": A * tps * e2e_steps * world / e2e_time, "unit": "arena-ticks/s",
+                      "h2d_bytes_per_step": int(ctl_np.nbytes),
+                      "d2h_bytes_per_step": int(out_cars.nbytes + out_balls.nbytes + out_pads.nbytes),
+                      "host_buffers": "pinned", "controls": "the same control for all 8 ticks of a step"}
     batch.close()
+    return out
 
-    # roofline of the tick kernel: algorithmic bytes per launch
-    state_rt = 1548  # minimal 2v2 arena state read + written once per launch (bytes)
+
+def load_counters() -> dict:
+    """Per-launch figures of the tick kernels from the committed ncu summary (profiles/)."""
+    p = os.path.join(REPO, "profiles", "tick_counters.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def sm_count(dev: int) -> int:
+    import torch
+    return torch.cuda.get_device_properties(dev).multi_processor_count
+
+
+def run_gpu(args, rank: int, world: int):
+    """The headline workload (4096 uniform 2v2 arenas) with its roofline and issue-slot figures."""
+    import rocketsim_gb300 as rsg
+    from rocketsim_gb300.arena_mesh import arena_cmf
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    import torch
+    torch.cuda.set_device(dev)
+    rsg.init_from_mem([arena_cmf(0)])
+    A = args.arenas
+    r = run_arena_leg(args, dev, A, CARS, args.steps, args.warmup, args.settle_ticks, rank=rank, world=world)
+    # roofline of the tick: algorithmic bytes per launch (minimal 2v2 state read + written once per
+    # launch, controls read every tick)
+    state_rt = 1548
     ctl_per_tick = CARS * 24
     alg_bytes = A * (state_rt + ctl_per_tick * TICKS_PER_STEP)
-    avg_launch_s = (sum(times_ms) / len(times_ms)) / 1e3
+    avg_launch_s = (sum(r["times_ms"]) / len(r["times_ms"])) / 1e3
     peaks = {}
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -349,22 +470,42 @@ def run_gpu(args, rank: int, world: int):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / avg_launch_s / 1e9
+    cnt = load_counters()
     traffic = None
-    tp = os.path.join(REPO, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            tj = json.load(f)
-        per_arena = tj.get("rsg_tick_kernel_bytes_per_arena_launch")
-        if per_arena:
-            traffic = per_arena * A
-    return {
-        "value": value, "ms_per_step": total_ms / args.steps, "e2e": {
-            "value": e2e_value, "unit": "arena-ticks/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
-        "clocks": clk, "gpu_launches": args.steps, "step_bytes_controls": step_bytes,
-        "warn_flags_any": int(np.bitwise_or.reduce(flags)) if flags.size else 0,
-    }
+    if cnt.get("dram_bytes_per_arena_launch") is not None:
+        traffic = {"per_launch": cnt["dram_bytes_per_arena_launch"] * A + cnt.get("dram_bytes_fixed_per_launch", 0),
+                   "per_arena_records": cnt["dram_bytes_per_arena_launch"],
+                   "fixed_mesh_per_launch": cnt.get("dram_bytes_fixed_per_launch", 0),
+                   "source": cnt.get("source", "")}
+    issue = None
+    wi = cnt.get("warp_instructions_per_arena_tick")
+    clk_mhz = r["clocks"].get("sm_mhz") or 2070.0
+    if wi:
+        slots = sm_count(dev) * 4 * clk_mhz * 1e6
+        issue = {"warp_instructions_per_arena_tick": wi, "issue_slots_per_s": slots,
+                 "frac": wi * r["value"] / world / slots,
+                 "note": "warp instructions per arena-tick (ncu) x arena-ticks/s / (SMs x 4 schedulers x SM clock)"}
+    r["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic["per_launch"] if traffic else None, "traffic_split": traffic,
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "issue_slots": issue}
+    return r
+
+
+def run_config0(args, dev: int):
+    """One arena, 2v2 Octane: the reference's own benchmark shape, a bounded sample of its 1M ticks."""
+    return run_arena_leg(args, dev, 1, CARS, args.c0_steps, 3, 240, e2e=False, flush_l2=False, curve=False,
+                         tps=120)
+
+
+def run_config2(args, dev: int):
+    """16384 arenas with 2, 4 or 6 cars (1:1:1) of all six hitboxes, 34 pads, 1 % of the arenas reset
+    to a random kickoff every 300 ticks."""
+    import rocketsim_gb300 as rsg  # noqa: F401
+    counts, presets = uneven_layout(args.c2_arenas, 77)
+    r = run_arena_leg(args, dev, args.c2_arenas, 6, args.c2_steps, args.warmup, args.settle_ticks, counts=counts,
+                      presets=presets, reset_every=300, reset_frac=0.01, e2e=False)
+    r["cars"] = int(np.sum(counts))
+    return r
 
 
 # ---------------------------------------------------------------- adjoint (air phase)
@@ -801,6 +942,12 @@ def main():
                     help="ground instances checked against FP64 finite differences")
     ap.add_argument("--pred-arenas", type=int, default=4096, help="arenas of the ball-prediction leg")
     ap.add_argument("--pred-ticks", type=int, default=360, help="predicted ticks per arena (BallPredTracker numPredTicks)")
+    ap.add_argument("--settle-ticks", type=int, default=1200,
+                    help="game ticks run before the warm-up steps, to time the steady state rather than the start")
+    ap.add_argument("--c0-steps", type=int, default=10, help="timed 120-tick launches of the one-arena workload")
+    ap.add_argument("--c2-arenas", type=int, default=16384, help="arenas of the uneven workload")
+    ap.add_argument("--c2-steps", type=int, default=40, help="timed 8-tick steps of the uneven workload")
+    ap.add_argument("--legs", default="all", help="comma list of extra legs: c0,c2,adjoint,ground,pred (or all / none)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -808,25 +955,28 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     threads = os.cpu_count() or 1
     config = {"workload": WORKLOAD, "arenas": args.arenas, "cars_per_arena": CARS, "ticks_per_step": TICKS_PER_STEP,
-              "tick_rate": 120, "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{world}"}
+              "tick_rate": 120, "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{world}",
+              "settle_ticks": args.settle_ticks}
 
     if args.impl == "reference":
         if rank != 0:
             return
         # each step: every host thread steps its own 2v2 arena for a bounded time
-        vals = []
+        vals, els = [], []
         kind = cpu_kind()
         for s in range(args.warmup + args.steps):
             v, n, el, kind = cpu_ticks_per_second(threads, 0.25 if s < args.warmup else 0.5, kind=kind)
             if s >= args.warmup:
                 vals.append(v)
+                els.append(el)
         value = statistics.mean(vals)
         line = {"impl": "reference", "metric": "2v2 arena-ticks/s", "value": value, "unit": "arena-ticks/s",
-                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 500.0,
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": statistics.mean(els) * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": value, "unit": "arena-ticks/s", "cores": threads,
-                                 "kind": "reference" if kind == "ref" else "port",
+                                 "cpu_model": cpu_model(), "kind": "reference" if kind == "ref" else "port",
                                  "sample": f"{threads} threads x one 2v2 arena each, 0.5 s per step; "
                                            + reference_kind_note(kind)},
                 "e2e": {"value": value, "unit": "arena-ticks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -840,12 +990,9 @@ def main():
     r = run_gpu(args, rank, world)
     if rank != 0:
         return
-    adj = run_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
-    adj_err, cpu_grads, cpu_el = adjoint_cpu_check(adj["case"], adj["g_gpu"], args.adj_check)
-    gadj = run_ground_adjoint(args, int(os.environ.get("LOCAL_RANK", 0)))
-    gchk = ground_cpu_check(gadj["case"], gadj["g_gpu"])
-    bp = run_ball_pred(args)
-    bp_cpu, bp_n, bp_el, bp_kind = ball_pred_cpu(args.cpu_seconds, args.pred_ticks)
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    legs = set(["c0", "c2", "adjoint", "ground", "pred"] if args.legs == "all" else
+               ([] if args.legs == "none" else args.legs.split(",")))
     single, _, _, kind = cpu_ticks_per_second(1, args.cpu_seconds)
     allc, n, el, _ = cpu_ticks_per_second(threads, args.cpu_seconds)
     line = {
@@ -853,14 +1000,40 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
         "e2e": r["e2e"], "roofline": r["roofline"],
-        "cpu_baseline": {"value": allc, "unit": "arena-ticks/s", "cores": threads,
+        "cpu_baseline": {"value": allc, "unit": "arena-ticks/s", "cores": threads, "cpu_model": cpu_model(),
                          "kind": "reference" if kind == "ref" else "port", "single_thread": single,
                          "sample": f"{threads} threads x one 2v2 arena each for {args.cpu_seconds:.1f} s "
                                    f"({n} arena-ticks) plus 1 thread for {args.cpu_seconds:.1f} s; "
                                    + reference_kind_note(kind)},
         "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "device_warn_flags": r["warn_flags_any"],
         "host": platform.machine(),
-        "adjoint": {
+        "steady_state": {"game_tick_first_timed": r["game_tick_first_timed"],
+                         "game_tick_last_timed": r["game_tick_last_timed"],
+                         "ticks_per_s_vs_game_tick": r["ticks_per_s_vs_game_tick"]},
+    }
+    if "c0" in legs:
+        c0 = run_config0(args, dev)
+        line["config0_one_arena"] = {
+            "metric": "2v2 ticks/s of one arena", "value": c0["value"], "unit": "ticks/s",
+            "workload": "1 arena x (4 Octane + ball), procedural soccar mesh, the same input process; "
+                        f"{args.c0_steps} timed launches of 120 ticks after 240 + 360 ticks (a bounded sample of "
+                        "the 1M-tick run)",
+            "ms_per_launch": c0["ms_per_step"], "cpu_single_thread": single}
+    if "c2" in legs:
+        c2 = run_config2(args, dev)
+        line["config2_uneven"] = {
+            "metric": "arena-ticks/s", "value": c2["value"], "unit": "arena-ticks/s",
+            "workload": f"{args.c2_arenas} arenas with 2/4/6 cars drawn 1:1:1 ({c2['cars']} cars), hitboxes drawn "
+                        "uniformly from the six presets, 34 pads, 1% of the arenas reset to a random kickoff "
+                        "every 300 ticks; 8 ticks per launch, L2 flushed between timed steps",
+            "ms_per_step": c2["ms_per_step"], "steps": args.c2_steps,
+            "game_tick_first_timed": c2["game_tick_first_timed"], "arenas_reset": c2["arenas_reset"],
+            "ticks_per_s_vs_game_tick": c2["ticks_per_s_vs_game_tick"], "device_warn_flags": c2["warn_flags_any"],
+            "clocks": c2["clocks"]}
+    if "adjoint" in legs:
+        adj = run_adjoint(args, dev)
+        adj_err, cpu_grads, cpu_el = adjoint_cpu_check(adj["case"], adj["g_gpu"], args.adj_check)
+        line["adjoint"] = {
             "metric": "adjoint grads/s", "value": adj["value"], "unit": "grads/s (60-tick air rollouts)",
             "workload": ADJ_WORKLOAD, "rel_err_max_vs_fp64_fd": adj_err, "rel_err_instances": args.adj_check,
             "ms_per_step": adj["ms_per_step"], "step": adj["step_kind"],
@@ -875,8 +1048,11 @@ def main():
             "gpu_launches_per_step": 3,
             "cpu_baseline": {"value": cpu_grads, "unit": "grads/s", "cores": 1, "kind": "port",
                              "sample": f"FP64 central differences of the numpy restatement, "
-                                       f"{args.adj_check} instances x 240 inputs x 2 rollouts ({cpu_el:.1f} s)"}},
-        "ground_adjoint": {
+                                       f"{args.adj_check} instances x 240 inputs x 2 rollouts ({cpu_el:.1f} s)"}}
+    if "ground" in legs:
+        gadj = run_ground_adjoint(args, dev)
+        gchk = ground_cpu_check(gadj["case"], gadj["g_gpu"])
+        line["ground_adjoint"] = {
             "metric": "adjoint grads/s", "value": gadj["value"], "unit": "grads/s (120-tick ground rollouts)",
             "workload": GROUND_WORKLOAD, "rel_err_max_vs_fp64_fd": gchk["max"], "rel_err_median": gchk["median"],
             "rel_err_sample": f"{args.ground_check} instances x {gchk['entries']} control entries; "
@@ -887,12 +1063,16 @@ def main():
             "ms_backward": gadj["ms_backward"], "backward_over_forward": gadj["backward_over_forward"],
             "c_abi_ms_forward_with_checkpoints": gadj["kernel_ms_forward_ckpt"],
             "c_abi_ms_backward": gadj["kernel_ms_backward"], "workspace_bytes": gadj["workspace_bytes"],
+            "c_abi_backward_over_forward": gadj["kernel_ms_backward"] / gadj["ms_forward_plain"],
             "flagged_instances": gadj["flagged_instances"], "gpu_launches_per_step": 3,
             "cpu_baseline": {"value": gchk["rate"], "unit": "gradient entries/s", "cores": 1, "kind": "port",
                              "sample": f"FP64 central differences of the numpy restatement, "
                                        f"{args.ground_check} instances x {gchk['entries']} entries x 2 rollouts "
-                                       f"({gchk['seconds']:.1f} s)"}},
-        "ball_pred": {
+                                       f"({gchk['seconds']:.1f} s)"}}
+    if "pred" in legs:
+        bp = run_ball_pred(args)
+        bp_cpu, bp_n, bp_el, bp_kind = ball_pred_cpu(args.cpu_seconds, args.pred_ticks)
+        line["ball_pred"] = {
             "metric": "predicted ball-ticks/s", "value": bp["value"], "unit": "ball-ticks/s",
             "workload": f"BallPredTracker over {args.pred_arenas} arenas x {args.pred_ticks} ticks, balls in flight "
                         f"(procedural soccar mesh seed 0); full prediction = ForceUpdateAllPred of every arena from "
@@ -906,8 +1086,7 @@ def main():
                                        + ("BallPredTracker::ForceUpdateAllPred of the reference built from its "
                                           "own sources (oracle/_ref)" if bp_kind == "ref" else
                                           "the CPU restatement (oracle/) stepping a ball-only arena, the per-tick "
-                                          "state copy left out")}},
-    }
+                                          "state copy left out")}}
     print(json.dumps(line))
 
 

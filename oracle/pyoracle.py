@@ -90,9 +90,14 @@ def build_oracle() -> str:
     return ORACLE_SO
 
 
+def reference_dir() -> str:
+    """The reference source tree: $RSG_REFERENCE_DIR, else a checkout named `reference` beside the repository."""
+    return os.environ.get("RSG_REFERENCE_DIR", os.path.abspath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
+
+
 def build_ref() -> str | None:
     """Compile the reference from its sources when they are present here."""
-    ref = os.environ.get("RSG_REFERENCE_DIR", "/root/reference")
+    ref = reference_dir()
     if not os.path.isdir(os.path.join(ref, "src")):
         return REF_SO if os.path.exists(REF_SO) else None
     subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", "ref", f"REF={ref}"], check=True)

@@ -217,6 +217,8 @@ struct rsg_batch {
     // staging
     void* d_stage = nullptr;
     size_t stage_bytes = 0;
+    void* h_bounce = nullptr;  // pinned host buffer of the bulk getter (batches with empty car slots)
+    size_t bounce_bytes = 0;
     std::vector<uint32_t> h_counts;
     std::vector<DevEventHost> h_events;
     rsg_goal_fn goal_fn = nullptr;
@@ -241,6 +243,16 @@ int ensure_stage(rsg_batch* b, size_t bytes) {
     b->stage_bytes = 0;
     RSG_CUDA(cudaMalloc(&b->d_stage, bytes));
     b->stage_bytes = bytes;
+    return RSG_OK;
+}
+
+int ensure_host_bounce(rsg_batch* b, size_t bytes) {
+    if (b->bounce_bytes >= bytes) return RSG_OK;
+    if (b->h_bounce) cudaFreeHost(b->h_bounce);
+    b->h_bounce = nullptr;
+    b->bounce_bytes = 0;
+    RSG_CUDA(cudaMallocHost(&b->h_bounce, bytes));
+    b->bounce_bytes = bytes;
     return RSG_OK;
 }
 
@@ -740,6 +752,7 @@ void rsg_batch_destroy(rsg_batch* b) {
     void* ptrs[] = {B.rec, B.au, B.events, b->d_cfgs, b->d_stage, b->d_pads};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (b->h_bounce) cudaFreeHost(b->h_bounce);
     if (b->stream) cudaStreamDestroy(b->stream);
     for (cudaEvent_t e : b->tune_ev)
         if (e) cudaEventDestroy(e);
@@ -1136,11 +1149,20 @@ int rsg_get_all_states(rsg_batch* b, rsg_car_state* cars, rsg_ball_state* balls,
     size_t pb = (pads && b->buf.has_arena) ? sizeof(rsg_pad_state) * A * b->buf.npads : 0;
     if ((rc = ensure_stage(b, cb + bb + pb + 16))) return rc;
     char* st = (char*)b->d_stage;
+    // Occupied car slots are a prefix of each arena's slots.  When every slot of the batch holds a
+    // car the gathered array goes straight to the caller; otherwise it lands in a host bounce
+    // buffer and only each arena's occupied prefix is copied out, so empty slots keep the caller's
+    // contents without any host-to-device traffic.
+    bool full = true;
+    for (size_t a = 0; a < A && full; a++) full = b->ncars[a] == MC;
     if (cars) {
-        // slots without a car keep the caller's contents: stage them first
-        RSG_CUDA(cudaMemcpyAsync(st, cars, cb, cudaMemcpyHostToDevice, b->stream));
         RSG_CUDA(launch_get_cars(b->buf, nullptr, (int)(A * MC), (rsg_car_state*)st, b->stream));
-        RSG_CUDA(cudaMemcpyAsync(cars, st, cb, cudaMemcpyDeviceToHost, b->stream));
+        if (full) {
+            RSG_CUDA(cudaMemcpyAsync(cars, st, cb, cudaMemcpyDeviceToHost, b->stream));
+        } else {
+            if ((rc = ensure_host_bounce(b, cb))) return rc;
+            RSG_CUDA(cudaMemcpyAsync(b->h_bounce, st, cb, cudaMemcpyDeviceToHost, b->stream));
+        }
     }
     if (balls) {
         RSG_CUDA(launch_get_balls(b->buf, nullptr, (int)A, (rsg_ball_state*)(st + cb), b->stream));
@@ -1151,6 +1173,11 @@ int rsg_get_all_states(rsg_batch* b, rsg_car_state* cars, rsg_ball_state* balls,
         RSG_CUDA(cudaMemcpyAsync(pads, st + cb + bb, pb, cudaMemcpyDeviceToHost, b->stream));
     }
     RSG_CUDA(cudaStreamSynchronize(b->stream));
+    if (cars && !full) {
+        const rsg_car_state* src = (const rsg_car_state*)b->h_bounce;
+        for (size_t a = 0; a < A; a++)
+            if (b->ncars[a]) std::memcpy(cars + a * MC, src + a * MC, sizeof(rsg_car_state) * b->ncars[a]);
+    }
     return RSG_OK;
 }
 

@@ -1,9 +1,10 @@
 // rsg_kernels.cu -- kernels of the batched arena tick and the state gather /
 // scatter kernels behind the C ABI.
 //
-// rsg_tick_kernel: one thread advances one arena by `ticks` ticks (load the
-// arena's SoA state, run the ticks in registers / local memory, store it back).
-// Arenas are independent, so the grid is simply ceil(A / block) blocks.
+// rsg_tick_kernel: one warp advances one arena by `ticks` ticks (its record is
+// loaded into the warp's shared-memory region, the ticks run there in block-wide
+// parts, and the record is stored back).  Arenas are independent, so the grid is
+// simply ceil(A / arenas per block) blocks.
 #include <mutex>
 
 #include "rsg_kernels.h"

@@ -1,7 +1,9 @@
 // rsg_tick.cuh -- device implementation of one RocketSim Arena::Step tick.
 //
-// One arena is advanced by one CUDA thread (arena-per-thread); all arenas of a
-// batch advance in parallel.  The per-arena algorithm restates RocketSim v2.2's
+// One warp advances one arena; the warps of a block step through the parts of a
+// tick together, and work that is independent within an arena (wheels, cars,
+// bodies, pads, narrow-phase candidates) is spread over lanes and warps.  The
+// per-arena algorithm restates RocketSim v2.2's
 // tick (src/Sim/Arena/Arena.cpp:689-756) including the parts of Bullet 3.24
 // that decide its results: the voxel broadphase pair order, manifold creation
 // order, the island quicksort that orders solver rows, 4-point manifolds, the
