@@ -13,6 +13,7 @@
 #include "RocketSim.h"
 #include "Sim/BallPredTracker/BallPredTracker.h"
 #include "Sim/GameEventTracker/GameEventTracker.h"
+#include "../libsrc/bullet3-3.24/BulletCollision/NarrowPhaseCollision/btSubSimplexConvexCast.h"
 #include "../include/rocketsim_gb300.h"
 
 #include <cstring>
@@ -608,5 +609,90 @@ int rsref_body_debug(void* h, uint32_t id, float* out) {
     btVector3 he = car->_childHitboxShape.getHalfExtentsWithoutMargin();
     out[13] = he.x(); out[14] = he.y(); out[15] = he.z(); out[16] = car->_childHitboxShape.getMargin();
     return 0;
+}
+}
+
+extern "C" {
+// btCollisionWorld::rayTest from `in6` (from, to; Bullet units) with a ClosestRayResultCallback that
+// ignores car `ignore_id` (0: none), as the vehicle raycaster runs it (test aid): writes hit (0/1),
+// fraction, normal (3), object kind (0 none, 1 static, 2 ball, 3 car) and car id.
+int rsref_debug_ray(void* h, const float* in6, uint32_t ignore_id, float* out7) {
+    RefArena* ra = (RefArena*)h;
+    btVector3 from(in6[0], in6[1], in6[2]), to(in6[3], in6[4], in6[5]);
+    Car* ign = ignore_id ? FindCar(ra, ignore_id) : nullptr;
+    btCollisionWorld::ClosestRayResultCallback cb(from, to, ign ? (const btCollisionObject*)&ign->_rigidBody : nullptr);
+    ra->arena->_bulletWorld.rayTest(from, to, cb);
+    out7[0] = cb.hasHit() ? 1.f : 0.f;
+    out7[1] = cb.m_closestHitFraction;
+    out7[2] = cb.m_hitNormalWorld.x(); out7[3] = cb.m_hitNormalWorld.y(); out7[4] = cb.m_hitNormalWorld.z();
+    out7[5] = 0; out7[6] = 0;
+    if (cb.hasHit()) {
+        const btCollisionObject* o = cb.m_collisionObject;
+        out7[5] = o->isStaticObject() ? 1.f : 0.f;
+        if (o == &ra->arena->ball->_rigidBody) out7[5] = 2.f;
+        for (Car* c : ra->arena->GetCars())
+            if (o == &c->_rigidBody) { out7[5] = 3.f; out7[6] = (float)c->id; }
+    }
+    return 0;
+}
+}
+
+extern "C" {
+// btSubsimplexConvexCast of a point from in6[0:3] to in6[3:6] against the box child of car `car_id`
+// (test aid): writes the fraction and hit (2 floats), then the same loop restated here with the
+// reference's own solver and shapes, traced per iteration (lambda, v, dist2, vertices: 6 floats).
+int rsref_debug_subsimplex(void* h, const float* in6, uint32_t car_id, float* out, int cap) {
+    RefArena* ra = (RefArena*)h;
+    Car* car = FindCar(ra, car_id);
+    if (!car) return -1;
+    btTransform fromT, toT;
+    fromT.setIdentity(); toT.setIdentity();
+    fromT.setOrigin(btVector3(in6[0], in6[1], in6[2]));
+    toT.setOrigin(btVector3(in6[3], in6[4], in6[5]));
+    const btCompoundShape* comp = (const btCompoundShape*)car->_rigidBody.getCollisionShape();
+    const btConvexShape* box = (const btConvexShape*)comp->getChildShape(0);
+    btTransform childW = car->_rigidBody.getWorldTransform() * comp->getChildTransform(0);
+    btSphereShape pointShape(btScalar(0.0));
+    pointShape.setMargin(0.f);
+    {
+        btVoronoiSimplexSolver ss;
+        btSubsimplexConvexCast cc(&pointShape, box, &ss);
+        btConvexCast::CastResult res;
+        res.m_fraction = 1.f;
+        bool ok = cc.calcTimeOfImpact(fromT, toT, childW, childW, res);
+        out[0] = res.m_fraction; out[1] = ok;
+    }
+    btVoronoiSimplexSolver sx;
+    sx.reset();
+    btVector3 r = toT.getOrigin() - fromT.getOrigin();
+    btScalar lambda = 0;
+    btTransform ia = fromT;
+    btVector3 sa = fromT(pointShape.localGetSupportingVertex(-r * fromT.getBasis()));
+    btVector3 sb = childW(box->localGetSupportingVertex(r * childW.getBasis()));
+    btVector3 v = sa - sb, w;
+    btScalar dist2 = v.length2();
+    int maxIter = 32, n = 0;
+    while ((dist2 > btScalar(0.0001)) && maxIter--) {
+        sa = ia(pointShape.localGetSupportingVertex(-v * ia.getBasis()));
+        sb = childW(box->localGetSupportingVertex(v * childW.getBasis()));
+        w = sa - sb;
+        btScalar vdw = v.dot(w);
+        if (lambda > 1) break;
+        if (vdw > 0) {
+            btScalar vdr = v.dot(r);
+            if (vdr >= -(SIMD_EPSILON * SIMD_EPSILON)) break;
+            lambda = lambda - vdw / vdr;
+            ia.getOrigin().setInterpolate3(fromT.getOrigin(), toT.getOrigin(), lambda);
+            w = sa - sb;
+        }
+        if (!sx.inSimplex(w)) sx.addVertex(w, sa, sb);
+        if (sx.closest(v)) dist2 = v.length2(); else dist2 = 0;
+        if (n < cap) {
+            float* o = out + 2 + 6 * n;
+            o[0] = lambda; o[1] = v.x(); o[2] = v.y(); o[3] = v.z(); o[4] = dist2; o[5] = sx.numVertices();
+        }
+        n++;
+    }
+    return n;
 }
 }

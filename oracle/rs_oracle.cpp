@@ -1055,6 +1055,12 @@ void cell_dyn_list(Arena& a, int ci, int cj, int ck, std::vector<int>& out) {
     std::stable_sort(out.begin(), out.end(), [&](int x, int y) { return a.body(x).cell_seq < a.body(y).cell_seq; });
 }
 
+// Ray against a dynamic object the way btCollisionWorld::rayTestSingleInternal casts it
+// (btCollisionWorld.cpp:267-310): btSubsimplexConvexCast of a point against the car's box child
+// (the car's compound has no child tree, Car.cpp:198) or the ball's sphere; defined after Simplex.
+bool ray_cast_box(V3 from, V3 to, const Xf& box_xf, V3 he_margin, float& hit_frac, V3& out_normal);
+bool ray_cast_sphere(V3 from, V3 to, const Xf& xf, float radius, float& hit_frac, V3& out_normal);
+
 RayHit cast_ray(Arena& a, V3 from, V3 to, int self_obj) {
     RayHit r;
     float frac = 1.f;
@@ -1083,13 +1089,13 @@ RayHit cast_ray(Arena& a, V3 from, V3 to, int self_obj) {
         if (frac == 0.f) break;
         V3 n;
         if (o == OBJ_BALL) {
-            if (ray_sphere(from, to, a.ball.xf.o, a.ball_radius, frac, n)) { obj = o; nrm = n; }
+            if (ray_cast_sphere(from, to, a.ball.xf, a.ball_radius, frac, n)) { obj = o; nrm = n; }
         } else {
             Car& c = a.cars[o - OBJ_CAR0];
             Xf bx = c.rb.xf;
             bx.o = xf_apply(c.rb.xf, c.hitbox_off);
             V3 he = c.hitbox_he + V3(c.hitbox_margin, c.hitbox_margin, c.hitbox_margin);
-            if (ray_box(from, to, bx, he, frac, n)) { obj = o; nrm = n; }
+            if (ray_cast_box(from, to, bx, he, frac, n)) { obj = o; nrm = n; }
         }
     }
     if (obj < 0) return r;
@@ -2165,6 +2171,83 @@ struct Simplex {
     }
     void points(V3& p1, V3& p2) { update(); p1 = cP1; p2 = cP2; }
 };
+
+// btSubsimplexConvexCast::calcTimeOfImpact (B/BulletCollision/NarrowPhaseCollision/btSubSimplexConvexCast.cpp:30-141)
+// of a point (btSphereShape of radius and margin 0, btCollisionWorld.cpp:271-273) moving from `from`
+// to `to` against a static convex shape whose world support vertex for a world direction d is
+// `support(d, o)` with the shape's origin at o; then the acceptance of
+// btCollisionWorld::rayTestSingleInternal (btCollisionWorld.cpp:288-310): a normal longer than 0.01
+// and a fraction below the closest hit so far.  The shape's transform is interpolated like the
+// point's (btSubSimplexConvexCast.cpp:93-94), between two equal origins, which moves it by rounding.
+// MAX_CONVEX_CAST_ITERATIONS 32, MAX_CONVEX_CAST_EPSILON 1e-4 (btConvexCast.h:28-29), no allowed
+// penetration; the point's supporting vertex is its origin.
+template <class Sup>
+bool ray_subsimplex(V3 from, V3 to, V3 ob, Sup support, float& hit_frac, V3& out_normal) {
+    Simplex sx;
+    sx.reset();
+    V3 r = to - from;
+    float lambda = 0.f;
+    V3 xa = from, xb = ob;
+    V3 sa = xa, sb = support(r, ob);
+    V3 v = sa - sb;
+    int max_iter = 32;
+    V3 n(0, 0, 0);
+    float dist2 = len2(v);
+    V3 w;
+    while ((dist2 > 0.0001f) && max_iter--) {
+        sa = xa;
+        sb = support(v, xb);
+        w = sa - sb;
+        float vdw = dot(v, w);
+        if (lambda > 1.f) return false;
+        if (vdw > 0.f) {
+            float vdr = dot(v, r);
+            if (vdr >= -(SIMD_EPS * SIMD_EPS)) return false;
+            lambda = lambda - vdw / vdr;
+            xa = lerp(from, to, lambda);
+            xb = lerp(ob, ob, lambda);
+            w = sa - sb;
+            n = v;
+        }
+        if (!sx.in_simplex(w)) sx.add(w, sa, sb);
+        if (sx.closest(v)) dist2 = len2(v);
+        else dist2 = 0.f;
+    }
+    V3 nrm = len2(n) >= (SIMD_EPS * SIMD_EPS) ? normalized(n) : V3(0, 0, 0);
+    if (dot(nrm, r) >= -0.f) return false;
+    if (!(len2(nrm) > 0.0001f)) return false;
+    if (!(lambda < hit_frac)) return false;
+    hit_frac = lambda;
+    out_normal = normalized(nrm);
+    return true;
+}
+
+// btBoxShape::localGetSupportingVertex (btBoxShape.h:47-56), half extents with the margin
+bool ray_cast_box(V3 from, V3 to, const Xf& box_xf, V3 he_margin, float& hit_frac, V3& out_normal) {
+    auto sup = [&](V3 d, V3 o) {
+        V3 l = transpose(box_xf.b) * d;  // d * basis
+        V3 s(l.x >= 0.f ? he_margin.x : -he_margin.x, l.y >= 0.f ? he_margin.y : -he_margin.y,
+             l.z >= 0.f ? he_margin.z : -he_margin.z);
+        Xf t = box_xf;
+        t.o = o;
+        return xf_apply(t, s);
+    };
+    return ray_subsimplex(from, to, box_xf.o, sup, hit_frac, out_normal);
+}
+
+// btSphereShape::localGetSupportingVertex (btSphereShape.cpp:37-49): the margin (the radius) along the
+// normalised direction, (-1,-1,-1) normalised for a vanishing one
+bool ray_cast_sphere(V3 from, V3 to, const Xf& xf, float radius, float& hit_frac, V3& out_normal) {
+    auto sup = [&](V3 d, V3 o) {
+        V3 l = transpose(xf.b) * d;
+        if (len2(l) < (SIMD_EPS * SIMD_EPS)) l = normalized(V3(-1, -1, -1));
+        else l = normalized(l);
+        Xf t = xf;
+        t.o = o;
+        return xf_apply(t, l * radius);
+    };
+    return ray_subsimplex(from, to, xf.o, sup, hit_frac, out_normal);
+}
 
 // ---------------------------------------------------------------- GJK + EPA penetration depth
 // btGjkEpa2 (B/BulletCollision/NarrowPhaseCollision/btGjkEpa2.cpp) as btGjkEpaPenetrationDepthSolver
@@ -3797,6 +3880,9 @@ void solve(Arena& a, std::vector<int>& bodies, std::vector<Manifold*>& mans, flo
             b.sp_total_normal = V3(0, 0, 0);
         }
     }
+    a.counters[7] += s.contacts.size();  // workload statistics: solver rows per tick
+    a.counters[8] += s.frictions.size();
+    a.counters[9] += mans.size();
     const int ITER = 10;
     for (int it = 0; it < ITER; it++) {
         float lsr = 0;
@@ -4505,6 +4591,60 @@ int rsora_wheel_debug(void* h, uint32_t id, float* out) {
         o[15] = w.ground < 0 ? 0.f : (w.ground < OBJ_BALL ? 1.f : 2.f);
     }
     return 0;
+}
+
+// The suspension ray of one wheel at the current state, traced object by object (test aid): writes
+// from (3), to (3), then per hit candidate (kind 0 mesh triangle / 1 plane, index, accepted, fraction)
+// up to `cap` candidates; returns the number of candidates.
+int rsora_debug_wheel_ray(void* h, uint32_t id, int wheel, float* out, int cap) {
+    Arena& a = *(Arena*)h;
+    Car* car = find_car(a, id);
+    if (!car || wheel < 0 || wheel > 3) return -1;
+    Wheel w = car->w[wheel];
+    wheel_transforms_ws(*car, w);
+    float travel = w.travel_cm / 100;
+    float ray_len = w.rest_len + travel + w.radius - RL::BTV::SUSPENSION_SUBTRACTION;
+    V3 src = w.hard_point, dst = src + (w.dir_ws * ray_len);
+    out[0] = src.x; out[1] = src.y; out[2] = src.z; out[3] = dst.x; out[4] = dst.y; out[5] = dst.z;
+    int n = 0;
+    float frac = 1.f;
+    const Mesh& m = *g_mesh;
+    m.query_ray(src, dst, [&](int t) {
+        V3 tv[3];
+        m.tri_verts(t, tv);
+        V3 nn;
+        float f0 = frac;
+        bool ok = ray_triangle(src, dst, tv, frac, nn);
+        if (n < cap) { float* o = out + 6 + 4 * n; o[0] = 0; o[1] = (float)t; o[2] = ok; o[3] = ok ? frac : f0; }
+        n++;
+    });
+    for (int p = 0; p < 4; p++) {
+        V3 nn;
+        bool ok = ray_plane(a.planes[p], src, dst, frac, nn);
+        if (n < cap) { float* o = out + 6 + 4 * n; o[0] = 1; o[1] = (float)p; o[2] = ok; o[3] = frac; }
+        n++;
+    }
+    int ci, cj, ck;
+    g_grid->indices(src, ci, cj, ck);
+    std::vector<int> dyn;
+    cell_dyn_list(a, ci, cj, ck, dyn);
+    for (int o : dyn) {
+        if (o == car->obj) continue;
+        V3 nn;
+        bool ok;
+        if (o == OBJ_BALL) {
+            ok = ray_cast_sphere(src, dst, a.ball.xf, a.ball_radius, frac, nn);
+        } else {
+            Car& c = a.cars[o - OBJ_CAR0];
+            Xf bx = c.rb.xf;
+            bx.o = xf_apply(c.rb.xf, c.hitbox_off);
+            V3 he = c.hitbox_he + V3(c.hitbox_margin, c.hitbox_margin, c.hitbox_margin);
+            ok = ray_cast_box(src, dst, bx, he, frac, nn);
+        }
+        if (n < cap) { float* q = out + 6 + 4 * n; q[0] = 2; q[1] = (float)o; q[2] = ok; q[3] = frac; }
+        n++;
+    }
+    return n;
 }
 
 int rsora_body_debug(void* h, uint32_t id, float* out) {

@@ -582,48 +582,12 @@ RSG_D bool ray_plane(const PlaneC& p, V3 from_w, V3 to_w, float& hit_frac, V3& o
     if (ray_triangle(from, to, tri, hit_frac, n)) { any = true; out_n = n; }
     return any;
 }
-// Rays against the ball / another car's box (the reference runs btSubsimplexConvexCast;
-// both solve the same intersection, this one directly)
-RSG_D bool ray_sphere(V3 from, V3 to, V3 c, float r, float& hit_frac, V3& out_n) {
-    V3 d = to - from, mm = from - c;
-    float a = dot(d, d), b = dot(mm, d), cc = dot(mm, mm) - r * r;
-    if (cc > 0.f && b > 0.f) return false;
-    float disc = b * b - a * cc;
-    if (disc < 0.f) return false;
-    float t = (-b - sqrtf(disc)) / a;
-    if (t < 0.f) t = 0.f;
-    if (!(t < hit_frac)) return false;
-    V3 n = (from + d * t) - c;
-    if (len2(n) <= 0.0001f) return false;
-    hit_frac = t;
-    out_n = normalized(n);
-    return true;
-}
-RSG_D bool ray_box(V3 from_w, V3 to_w, const Xf& bx, V3 he, float& hit_frac, V3& out_n) {
-    V3 from = xf_inv_apply(bx, from_w), to = xf_inv_apply(bx, to_w);
-    V3 d = to - from;
-    float tmin = 0.f, tmax = 1.f, sgn = 1;
-    int axis = -1;
-    for (int k = 0; k < 3; k++) {
-        if (fabsf(d[k]) < 1e-12f) {
-            if (from[k] < -he[k] || from[k] > he[k]) return false;
-            continue;
-        }
-        float inv = 1.f / d[k];
-        float t1 = (-he[k] - from[k]) * inv, t2 = (he[k] - from[k]) * inv;
-        float s = -1;
-        if (t1 > t2) { float tt = t1; t1 = t2; t2 = tt; s = 1; }
-        if (t1 > tmin) { tmin = t1; axis = k; sgn = s; }
-        if (t2 < tmax) tmax = t2;
-        if (tmin > tmax) return false;
-    }
-    if (axis < 0 || !(tmin < hit_frac)) return false;
-    V3 nl(0, 0, 0);
-    nl[axis] = sgn;
-    hit_frac = tmin;
-    out_n = bx.b * nl;
-    return true;
-}
+// Rays against the ball / another car's box the way btCollisionWorld::rayTestSingleInternal casts
+// them (btCollisionWorld.cpp:267-310): btSubsimplexConvexCast of a point against the car's box child
+// (the car's compound keeps no child tree, Car.cpp:198) or the ball's sphere.  Defined after the
+// simplex solver they share with GJK.
+RSG_DN bool ray_cast_box(V3 from, V3 to, const Xf& box_xf, V3 he_margin, float& hit_frac, V3& out_n);
+RSG_DN bool ray_cast_sphere(V3 from, V3 to, const Xf& xf, float radius, float& hit_frac, V3& out_n);
 
 
 // ---------------------------------------------------------------- broadphase helpers
@@ -717,13 +681,13 @@ RSG_DN RayHit cast_ray(const BatchView& bv, Ctx& a, V3 from, V3 to, int self_obj
         if (frac == 0.f) break;
         V3 n;
         if (o == OBJ_BALL) {
-            if (ray_sphere(from, to, a.ball.xf.o, a.ball_r, frac, n)) { obj = o; nrm = n; }
+            if (ray_cast_sphere(from, to, a.ball.xf, a.ball_r, frac, n)) { obj = o; nrm = n; }
         } else {
             Car& c = a.cars[o - OBJ_CAR0];
             Xf bx = c.rb.xf;
             bx.o = xf_apply(c.rb.xf, V3(c.cfg->off[0], c.cfg->off[1], c.cfg->off[2]));
             V3 he = car_he(c) + V3(c.cfg->margin, c.cfg->margin, c.cfg->margin);
-            if (ray_box(from, to, bx, he, frac, n)) { obj = o; nrm = n; }
+            if (ray_cast_box(from, to, bx, he, frac, n)) { obj = o; nrm = n; }
         }
     }
     RSG_CT(34);
@@ -1938,6 +1902,82 @@ struct Simplex {
 }  // namespace rsg
 #include "rsg_epa.cuh"
 namespace rsg {
+
+// btSubsimplexConvexCast::calcTimeOfImpact (B/BulletCollision/NarrowPhaseCollision/btSubSimplexConvexCast.cpp:30-141)
+// of a point (btSphereShape of radius and margin 0, btCollisionWorld.cpp:271-273) moving from `from`
+// to `to` against a static convex shape with world support vertex `support(d, o)` for its origin at o,
+// then the acceptance of btCollisionWorld::rayTestSingleInternal (btCollisionWorld.cpp:288-310): a
+// normal longer than 0.01 and a fraction below the closest hit so far.  The shape's transform is
+// interpolated like the point's (btSubSimplexConvexCast.cpp:93-94), between two equal origins, which
+// moves it by rounding.  32 iterations, epsilon 1e-4 (btConvexCast.h:28-29),
+// no allowed penetration; the point's supporting vertex is its origin.
+template <class Sup>
+RSG_D bool ray_subsimplex(V3 from, V3 to, V3 ob, Sup support, float& hit_frac, V3& out_n) {
+    Simplex sx;
+    sx.reset();
+    V3 r = to - from;
+    float lambda = 0.f;
+    V3 xa = from, xb = ob;
+    V3 sa = xa, sb = support(r, ob);
+    V3 v = sa - sb;
+    int max_iter = 32;
+    V3 n(0, 0, 0);
+    float dist2 = len2(v);
+    V3 w;
+    while ((dist2 > 0.0001f) && max_iter--) {
+        sa = xa;
+        sb = support(v, xb);
+        w = sa - sb;
+        float vdw = dot(v, w);
+        if (lambda > 1.f) return false;
+        if (vdw > 0.f) {
+            float vdr = dot(v, r);
+            if (vdr >= -(SIMD_EPS * SIMD_EPS)) return false;
+            lambda = lambda - vdw / vdr;
+            xa = lerp(from, to, lambda);
+            xb = lerp(ob, ob, lambda);
+            w = sa - sb;
+            n = v;
+        }
+        if (!sx.in_simplex(w)) sx.add(w, sa, sb);
+        if (sx.closest(v)) dist2 = len2(v);
+        else dist2 = 0.f;
+    }
+    V3 nrm = len2(n) >= (SIMD_EPS * SIMD_EPS) ? normalized(n) : V3(0, 0, 0);
+    if (dot(nrm, r) >= -0.f) return false;
+    if (!(len2(nrm) > 0.0001f)) return false;
+    if (!(lambda < hit_frac)) return false;
+    hit_frac = lambda;
+    out_n = normalized(nrm);
+    return true;
+}
+
+// btBoxShape::localGetSupportingVertex (btBoxShape.h:47-56) with the margin in the half extents
+RSG_DN bool ray_cast_box(V3 from, V3 to, const Xf& box_xf, V3 he_margin, float& hit_frac, V3& out_n) {
+    auto sup = [&](V3 d, V3 o) {
+        V3 l = d * box_xf.b;
+        V3 s(l.x >= 0.f ? he_margin.x : -he_margin.x, l.y >= 0.f ? he_margin.y : -he_margin.y,
+             l.z >= 0.f ? he_margin.z : -he_margin.z);
+        Xf t = box_xf;
+        t.o = o;
+        return xf_apply(t, s);
+    };
+    return ray_subsimplex(from, to, box_xf.o, sup, hit_frac, out_n);
+}
+
+// btSphereShape::localGetSupportingVertex (btSphereShape.cpp:37-49): the margin (the radius) along the
+// normalised direction, (-1,-1,-1) normalised for a vanishing one
+RSG_DN bool ray_cast_sphere(V3 from, V3 to, const Xf& xf, float radius, float& hit_frac, V3& out_n) {
+    auto sup = [&](V3 d, V3 o) {
+        V3 l = d * xf.b;
+        if (len2(l) < (SIMD_EPS * SIMD_EPS)) l = normalized(V3(-1, -1, -1));
+        else l = normalized(l);
+        Xf t = xf;
+        t.o = o;
+        return xf_apply(t, l * radius);
+    };
+    return ray_subsimplex(from, to, xf.o, sup, hit_frac, out_n);
+}
 
 struct GjkOut {
     bool valid;

@@ -5,7 +5,9 @@ It builds the reference from its own sources (oracle/Makefile, target ``ref``),
 plays seeded scenarios (tests/scenarios.py) through it and stores, per
 scenario, the starting state, update order and controls, the full car / ball
 state after 1 and 8 ticks, the discrete state (flags, timers, boost, pads)
-after every one of 120 ticks, and the goal / bump events.  The CPU restatement
+after every one of 120 ticks, the ball-hit record (its tick counters bit for bit, its
+positions and velocity as floats) and tickCountSinceUpdate after every tick, and the goal /
+bump events (kind, tick, car ids, demo flag).  The CPU restatement
 is played alongside to record the first tick at which the reference needed
 Bullet's EPA penetration solver (a narrow-phase path the restatement does not
 cover yet); scenarios without one carry epa_tick = -1.
@@ -21,8 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from scenarios import (CONTROLS_DTYPE, cpu_snapshot, discrete_car, discrete_pads, make_carcar_scenario,  # noqa: E402
-                       make_scenario, run_cpu)
+from scenarios import (CONTROLS_DTYPE, cpu_snapshot, discrete_car, discrete_hit, discrete_pads,  # noqa: E402
+                       hit_vec, make_carcar_scenario, make_scenario, run_cpu)
 from rocketsim_gb300 import abi  # noqa: E402
 
 TICKS = 120
@@ -57,6 +59,8 @@ def record(scs, mutators=None, epa=True, config=None):
     cars_t = {1: np.zeros((S, MC), car_dt), 8: np.zeros((S, MC), car_dt)}
     ball_t = {1: np.zeros(S, ball_dt), 8: np.zeros(S, ball_dt)}
     disc_cars = np.zeros((S, TICKS, MC, 28), np.float32)
+    disc_hit = np.zeros((S, TICKS, MC, 4), np.uint64)
+    hit_cont = np.zeros((S, TICKS, MC, 9), np.float32)
     npads = int(config.num_custom_boost_pads) if config is not None and config.use_custom_boost_pads else 34
     disc_pads = np.zeros((S, TICKS, npads, 3), np.float32)
     events = []
@@ -76,6 +80,8 @@ def record(scs, mutators=None, epa=True, config=None):
                 cars_t[t + 1][si, :n] = cars
                 ball_t[t + 1][si] = ball[0]
             disc_cars[si, t, :n] = discrete_car(cars)
+            disc_hit[si, t, :n] = discrete_hit(cars)
+            hit_cont[si, t, :n] = hit_vec(cars)
             disc_pads[si, t] = discrete_pads(pads)
             for e in a.pop_events():
                 events.append((si,) + e)
@@ -92,6 +98,7 @@ def record(scs, mutators=None, epa=True, config=None):
     return dict(seeds=np.array([s.seed for s in scs]), ncars=ncars, presets=presets, teams=teams, order=order,
                 init_cars=init_cars, init_ball=init_ball, controls=controls, cars_t1=cars_t[1], ball_t1=ball_t[1],
                 cars_t8=cars_t[8], ball_t8=ball_t[8], disc_cars=disc_cars, disc_pads=disc_pads,
+                disc_hit=disc_hit, hit_cont=hit_cont,
                 events=np.array(events, np.uint64).reshape(-1, 6), epa_tick=epa_tick, mesh_seed=np.int32(0))
 
 

@@ -284,3 +284,24 @@ def discrete_car(cars: np.ndarray) -> np.ndarray:
 def discrete_pads(pads: np.ndarray) -> np.ndarray:
     return np.stack([pads["is_active"].astype(np.float64), pads["cooldown"].astype(np.float64),
                      pads["prev_locked_car_id"].astype(np.float64)], axis=-1)
+
+
+HIT_COUNTERS = ("is_valid", "tick_count_when_hit", "tick_count_when_extra_impulse_applied")
+
+
+def discrete_hit(cars: np.ndarray) -> np.ndarray:
+    """[n, 4] uint64: ballHitInfo.isValid, tickCountWhenHit, tickCountWhenExtraImpulseApplied and
+    CarState::tickCountSinceUpdate (BallHitInfo.h:9-26, Car.h:17-120), compared bit for bit."""
+    hi = cars["ball_hit_info"]
+    cols = [hi[k].astype(np.uint64) for k in HIT_COUNTERS]
+    cols.append(cars["tick_count_since_update"].astype(np.uint64))
+    return np.stack(cols, axis=-1)
+
+
+def hit_vec(cars: np.ndarray) -> np.ndarray:
+    """[n, 9] float64: ballHitInfo.relativePosOnBall, ballPos and extraHitVel (uu, uu/s)."""
+    hi = cars["ball_hit_info"]
+    parts = []
+    for f in ("relative_pos_on_ball", "ball_pos", "extra_hit_vel"):
+        parts += [hi[f]["x"], hi[f]["y"], hi[f]["z"]]
+    return np.stack(parts, axis=-1).astype(np.float64)

@@ -12,8 +12,8 @@ import numpy as np
 import pytest
 
 from golden_data import TOL, check_continuous
-from scenarios import (CONTROLS_DTYPE, cpu_snapshot, discrete_car, discrete_pads, gpu_controls, gpu_snapshot,
-                       make_scenario, mesh_bytes, run_cpu, setup_gpu)
+from scenarios import (CONTROLS_DTYPE, cpu_snapshot, discrete_car, discrete_hit, discrete_pads, gpu_controls,
+                       gpu_snapshot, make_scenario, mesh_bytes, run_cpu, setup_gpu)
 
 pytestmark = pytest.mark.gpu
 
@@ -32,9 +32,26 @@ def play_gpu(scs, ticks, every_tick=True):
 
 
 def test_gpu_matches_reference_golden(golden):
+    """Continuous state after 1 and 8 ticks; discrete car state, ball-hit counters,
+    tickCountSinceUpdate and pads after every tick; the goal and bump callbacks against the
+    reference's events (tick, kind, car ids / team, demo flag) in order."""
     scs = golden.scenarios
-    batch, snaps = play_gpu(scs, 120)
+    batch, ids = setup_gpu(scs)
+    pos = [{cid: i for i, cid in enumerate(row)} for row in ids]
+    events = [[] for _ in scs]
+    cur = {"t": 0}
+    batch.set_goal_score_callback(lambda a, team: events[a].append((cur["t"], 1, team, 0, 0)))
+    batch.set_car_bump_callback(
+        lambda a, x, y, demo: events[a].append((cur["t"], 2, pos[a][x] + 1, pos[a][y] + 1, int(demo))))
+    snaps = []
+    for t in range(120):
+        cur["t"] = t
+        batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
+        batch.step(1)
+        snaps.append(gpu_snapshot(batch, scs))
+    z = golden.z
     for si in range(golden.S):
+        n = golden.ncars(si)
         for t in (1, 8):
             cars, ball, _ = snaps[t - 1][si]
             check_continuous(cars, ball, golden.cars_at(si, t), golden.ball_at(si, t), t, f"golden scenario {si}")
@@ -42,8 +59,12 @@ def test_gpu_matches_reference_golden(golden):
             cars, ball, pads = snaps[t][si]
             np.testing.assert_array_equal(discrete_car(cars).astype(np.float32), golden.disc_cars(si)[t],
                                           err_msg=f"golden scenario {si} tick {t + 1}: car discrete state")
+            np.testing.assert_array_equal(discrete_hit(cars), z["disc_hit"][si, t, :n],
+                                          err_msg=f"golden scenario {si} tick {t + 1}: ball-hit counters")
             np.testing.assert_array_equal(discrete_pads(pads).astype(np.float32), golden.disc_pads(si)[t],
                                           err_msg=f"golden scenario {si} tick {t + 1}: pads")
+        ref = [(e[1], e[0], e[2], e[3], e[4]) for e in golden.events(si)]
+        assert events[si] == ref, f"golden scenario {si}: events {events[si]} != reference {ref}"
     batch.close()
 
 
