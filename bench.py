@@ -391,11 +391,14 @@ def run_arena_leg(args, dev: int, A: int, mc: int, steps: int, warmup: int, sett
         total_ms = float(t.item())
     value = A * tps * steps * world / (total_ms / 1e3)
     flags = batch.device_flags()
+    shape = batch.tick_shape()
     out = {"value": value, "ms_per_step": total_ms / steps, "times_ms": times_ms, "clocks": clk,
+           "tick_shape": {"arenas_per_block": shape[0], "lanes_per_car": shape[1], "header_cache": shape[2],
+                          "leaf_grid": shape[3], "tuner": batch.tuning_log()},
            "game_tick_first_timed": first_tick, "game_tick_last_timed": ticks_done,
            "ticks_per_s_vs_game_tick": [[t, round(v)] for t, v in settle_curve],
            "warn_flags_any": int(np.bitwise_or.reduce(flags)) if flags.size else 0, "arenas_reset": resets,
-           "gpu_launches": steps}
+           "gpu_launches": 2 * steps}  # per step: the tick kernel and the arena placement kernel
     if e2e:
         # ---- e2e: host buffers (pinned) through the synchronous API: controls in, every car, ball and
         # pad state out, each step
@@ -1006,7 +1009,7 @@ def main():
                                    f"({n} arena-ticks) plus 1 thread for {args.cpu_seconds:.1f} s; "
                                    + reference_kind_note(kind)},
         "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "device_warn_flags": r["warn_flags_any"],
-        "host": platform.machine(),
+        "host": platform.machine(), "tick_shape": r["tick_shape"],
         "steady_state": {"game_tick_first_timed": r["game_tick_first_timed"],
                          "game_tick_last_timed": r["game_tick_last_timed"],
                          "ticks_per_s_vs_game_tick": r["ticks_per_s_vs_game_tick"]},
@@ -1029,7 +1032,7 @@ def main():
             "ms_per_step": c2["ms_per_step"], "steps": args.c2_steps,
             "game_tick_first_timed": c2["game_tick_first_timed"], "arenas_reset": c2["arenas_reset"],
             "ticks_per_s_vs_game_tick": c2["ticks_per_s_vs_game_tick"], "device_warn_flags": c2["warn_flags_any"],
-            "clocks": c2["clocks"]}
+            "clocks": c2["clocks"], "tick_shape": c2["tick_shape"]}
     if "adjoint" in legs:
         adj = run_adjoint(args, dev)
         adj_err, cpu_grads, cpu_el = adjoint_cpu_check(adj["case"], adj["g_gpu"], args.adj_check)

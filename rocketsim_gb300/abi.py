@@ -177,6 +177,8 @@ PROTOTYPES = {
     "rsg_set_bump_callback": (i32, [vp, BUMP_FN, vp]),
     "rsg_set_ball_hit_callback": (i32, [vp, BALL_HIT_FN, vp]),
     "rsg_get_device_flags": (i32, [vp, P(u32)]),
+    "rsg_get_tick_shape": (i32, [vp, P(C.c_int32)]),
+    "rsg_get_tuning_log": (i32, [vp, C.c_char_p, C.c_uint64]),
     "rsg_air_forward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, vp, vp, i32, vp]),
     "rsg_air_backward_workspace_size": (i32, [i32, i32, P(C.c_size_t)]),
     "rsg_air_backward": (i32, [P(CarConfig), f32, i32, i32, vp, vp, i32, vp, vp, vp, vp, C.c_size_t, vp]),

@@ -264,6 +264,17 @@ class ArenaBatch:
         return out
 
     # ---- stepping
+    def tick_shape(self) -> tuple[int, int, int, int]:
+        """Launch shape of the tick kernel (arenas per block, threads per car, header cache, leaf grid)."""
+        out = (C.c_int32 * 4)()
+        check(self.lib.rsg_get_tick_shape(self.h, out), "rsg_get_tick_shape")
+        return tuple(int(x) for x in out)
+
+    def tuning_log(self) -> str:
+        buf = C.create_string_buffer(4096)
+        check(self.lib.rsg_get_tuning_log(self.h, buf, 4096), "rsg_get_tuning_log")
+        return buf.value.decode()
+
     def step(self, ticks: int = 1) -> None:
         check(self.lib.rsg_step(self.h, ticks), "rsg_step")
 

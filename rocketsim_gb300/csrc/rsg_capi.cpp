@@ -13,8 +13,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/rocketsim_gb300.h"
@@ -192,17 +194,11 @@ static_assert(sizeof(DevEventHost) == DEV_EVENT_BYTES, "event record");
 struct rsg_batch {
     int game_mode = 0;
     int device = 0;
-    int warps_per_block = 8;  // arenas per block of the tick kernel
-    // block-shape tuner: candidate arenas-per-block values tried on the first launches, each
-    // timed with a pair of events that is read without blocking on a later launch
-    bool tuning = false;
-    std::vector<int> tune_cand;
-    std::vector<double> tune_ms_per_tick;  // < 0: not measured yet
-    int tune_next = 0;                     // next candidate to launch
-    int tune_pending = -1;                 // candidate whose events are in flight
-    int tune_pending_ticks = 0;
-    int tune_skip = 1;  // launches before the first trial (the first launch also loads the module)
-    cudaEvent_t tune_ev[2] = {nullptr, nullptr};
+    // launch shape of the tick kernel: tuned on the batch's first launch (identical states for every
+    // trial), cached per (device, arenas, car slots, game mode), or fixed by the environment
+    TickShape shape;
+    bool tune_pending = true;
+    std::string tune_log;
     BatchBuffers buf{};
     cudaStream_t stream = nullptr;
     std::vector<CarCfgDev> cfgs;
@@ -515,72 +511,137 @@ int rsg_get_car_config_preset(int preset, rsg_car_config* out) {
 
 namespace {
 
-// Candidate arenas-per-block values for the tick kernel: the ones that reach the fewest waves of
-// blocks over the device's SMs (one block per SM: the tick kernel's shared memory allows no
-// more), largest first.  Arenas never depend on the block they share, so any shape gives the
-// same results and the first real launches can serve as the trials.
-void setup_tuner(rsg_batch* b, int A, int MC) {
-    int sms = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess || sms <= 0) return;
-    const int per_arena = tick_smem_per_arena(MC);
-    int best_waves = 1 << 30;
-    std::vector<std::pair<int, int>> opts;  // (waves, wpb)
-    for (int w = 8; w >= 4; w--) {
-        if (per_arena * w > 227 * 1024) continue;
-        int blocks = (A + w - 1) / w;
-        int waves = (blocks + sms - 1) / sms;
-        opts.push_back({waves, w});
-        best_waves = std::min(best_waves, waves);
+// Block-shape tuner.  Every launch shape gives the same results, so the shapes can be timed on the
+// batch itself: the first launch saves the arena records, runs each candidate shape from the saved
+// state (launch, wait, time), restores the records and launches for real with the fastest.  The
+// candidates are searched one parameter at a time from the default shape: arenas per block (4 to 8,
+// as shared memory allows), threads per car in the vehicle update (1, 2, 4), the BVH subtree headers
+// in shared memory or read through L2, and wheel rays on the leaf grid or walking the BVH.  The
+// choice is cached per (device, arenas, car slots, game mode).
+struct TuneKey {
+    int dev, A, MC, arena;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(dev, A, MC, arena) < std::tie(o.dev, o.A, o.MC, o.arena);
     }
-    for (auto& o : opts)
-        if (o.first == best_waves) b->tune_cand.push_back(o.second);
-    if (b->tune_cand.size() <= 1) {
-        if (!b->tune_cand.empty()) b->warps_per_block = b->tune_cand[0];
-        return;
-    }
-    if (cudaEventCreate(&b->tune_ev[0]) != cudaSuccess || cudaEventCreate(&b->tune_ev[1]) != cudaSuccess) return;
-    b->tune_ms_per_tick.assign(b->tune_cand.size(), -1.0);
-    b->tuning = true;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<TickShape, std::string>> g_tune_cache;
+
+std::string shape_str(const TickShape& s) {
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), "arenas_per_block=%d lanes_per_car=%d header_cache=%d leaf_grid=%d",
+                  s.arenas_per_block, s.lanes_per_car, s.header_cache, s.leaf_grid);
+    return buf;
 }
 
-// Collects a finished trial (without waiting) and chooses the shape of the next launch.
-void tuner_before_launch(rsg_batch* b) {
-    if (!b->tuning) return;
-    if (b->tune_pending >= 0 && cudaEventQuery(b->tune_ev[1]) == cudaSuccess) {
-        float ms = 0;
-        if (cudaEventElapsedTime(&ms, b->tune_ev[0], b->tune_ev[1]) == cudaSuccess && b->tune_pending_ticks > 0)
-            b->tune_ms_per_tick[b->tune_pending] = ms / b->tune_pending_ticks;
-        b->tune_pending = -1;
+cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks) {
+    b->tune_pending = false;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(b->stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+        return cudaSuccess;  // no synchronous trials inside a capture: keep the default shape
+    const TuneKey key{b->device, b->buf.A, b->buf.MC, b->buf.has_arena};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            b->shape = it->second.first;
+            b->tune_log = it->second.second + " (cached)";
+            return cudaSuccess;
+        }
     }
-    bool all = true;
-    for (double v : b->tune_ms_per_tick) all = all && v >= 0;
-    if (all) {
-        size_t best = 0;
-        for (size_t i = 1; i < b->tune_cand.size(); i++)
-            if (b->tune_ms_per_tick[i] < b->tune_ms_per_tick[best]) best = i;
-        b->warps_per_block = b->tune_cand[best];
-        b->tuning = false;
-        return;
-    }
-    if (b->tune_pending < 0 && b->tune_next < (int)b->tune_cand.size())
-        b->warps_per_block = b->tune_cand[b->tune_next];
+    const BatchBuffers& B = b->buf;
+    const size_t rec_b = sizeof(uint32_t) * (size_t)rec_words(B.MC) * B.A, au_b = sizeof(uint32_t) * AU_COUNT * B.A;
+    const size_t pl_b = sizeof(uint32_t) * B.A;
+    char* snap = nullptr;
+    cudaError_t e = cudaMalloc(&snap, rec_b + au_b + 2 * pl_b);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    auto copy_all = [&](bool save) -> cudaError_t {
+        void* dev[4] = {B.rec, B.au, B.place, B.cost};
+        size_t sz[4] = {rec_b, au_b, pl_b, pl_b}, off = 0;
+        for (int i = 0; i < 4; i++) {
+            cudaError_t r = save ? cudaMemcpyAsync(snap + off, dev[i], sz[i], cudaMemcpyDeviceToDevice, b->stream)
+                                 : cudaMemcpyAsync(dev[i], snap + off, sz[i], cudaMemcpyDeviceToDevice, b->stream);
+            if (r != cudaSuccess) return r;
+            off += sz[i];
+        }
+        return cudaSuccess;
+    };
+    auto trial = [&](const TickShape& s, double& ms) -> cudaError_t {
+        cudaError_t r = copy_all(false);
+        if (r == cudaSuccess) r = cudaEventRecord(ev[0], b->stream);
+        if (r == cudaSuccess) r = launch_tick(B, controls, ticks, s, b->stream);
+        if (r == cudaSuccess) r = cudaEventRecord(ev[1], b->stream);
+        if (r == cudaSuccess) r = cudaEventSynchronize(ev[1]);
+        float f = 0;
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&f, ev[0], ev[1]);
+        ms = f;
+        return r;
+    };
+    std::string log;
+    TickShape best = b->shape;
+    do {
+        if ((e = cudaEventCreate(&ev[0])) != cudaSuccess || (e = cudaEventCreate(&ev[1])) != cudaSuccess) break;
+        if ((e = copy_all(true)) != cudaSuccess) break;
+        double ms = 0, best_ms = 0;
+        if ((e = trial(best, ms)) != cudaSuccess) break;  // loads the module and warms the caches
+        if ((e = trial(best, best_ms)) != cudaSuccess) break;
+        log = shape_str(best) + ": " + std::to_string(best_ms / ticks) + " ms/tick";
+        auto consider = [&](TickShape s) -> cudaError_t {
+            double t = 0;
+            cudaError_t r = trial(s, t);
+            if (r != cudaSuccess) return r;
+            log += "; " + shape_str(s) + ": " + std::to_string(t / ticks) + " ms/tick";
+            if (t < best_ms) { best_ms = t; best = s; }
+            return cudaSuccess;
+        };
+        const int per_arena = tick_smem_per_arena(B.MC);
+        for (int w = 8; w >= 4 && e == cudaSuccess; w--) {
+            if (w == best.arenas_per_block || per_arena * w > 227 * 1024) continue;
+            TickShape s = best;
+            s.arenas_per_block = w;
+            e = consider(s);
+        }
+        const TickShape base = best;
+        for (int l : {1, 2, 4}) {
+            if (e != cudaSuccess || l == base.lanes_per_car) continue;
+            TickShape s = base;
+            s.lanes_per_car = l;
+            e = consider(s);
+        }
+        const TickShape base2 = best;
+        for (int h : {0, 1}) {
+            if (e != cudaSuccess || !B.mesh.sub) continue;
+            TickShape s = base2;
+            s.header_cache = h;
+            e = consider(s);
+        }
+        if (e == cudaSuccess && B.mesh.lg_block) {
+            TickShape s = best;
+            s.leaf_grid = 0;
+            e = consider(s);
+        }
+        if (e == cudaSuccess) e = copy_all(false);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    } while (false);
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    cudaFree(snap);
+    if (e != cudaSuccess) return e;
+    b->shape = best;
+    b->tune_log = "chose " + shape_str(best) + " from " + log;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = {best, b->tune_log};
+    return cudaSuccess;
 }
 
-// Launches `ticks` ticks, timing the launch when it is a trial of the tuner.
+// Launches `ticks` ticks (tuning the shape first on the batch's first launch), then re-places the
+// arenas in blocks by the cost of their collision work in that launch.
 cudaError_t tuned_launch(rsg_batch* b, const rsg_car_controls* controls, int ticks) {
-    if (b->tuning && b->tune_skip > 0) {
-        b->tune_skip--;
-        return launch_tick(b->buf, controls, ticks, b->warps_per_block, b->stream);
-    }
-    tuner_before_launch(b);
-    const bool trial = b->tuning && b->tune_pending < 0 && b->tune_next < (int)b->tune_cand.size();
-    if (trial) cudaEventRecord(b->tune_ev[0], b->stream);
-    cudaError_t e = launch_tick(b->buf, controls, ticks, b->warps_per_block, b->stream);
-    if (trial && e == cudaSuccess) {
-        cudaEventRecord(b->tune_ev[1], b->stream);
-        b->tune_pending = b->tune_next++;
-        b->tune_pending_ticks = ticks;
-    }
+    cudaError_t e = cudaSuccess;
+    if (b->tune_pending) e = run_tuner(b, controls, ticks);
+    if (e == cudaSuccess) e = launch_tick(b->buf, controls, ticks, b->shape, b->stream);
+    if (e == cudaSuccess) e = launch_place_arenas(b->buf, b->stream);
     return e;
 }
 
@@ -654,11 +715,15 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         fail(RSG_ERR_STATE, "the mesh was loaded on another device");
         return nullptr;
     }
-    if (const char* w = std::getenv("RSG_TICK_WARPS_PER_BLOCK")) {  // fixed launch shape, no tuning
-        int v = std::atoi(w);
-        if (v >= 1 && v <= 8) b->warps_per_block = v;
-    } else {
-        setup_tuner(b, (int)n_arenas, (int)max_cars_per_arena);
+    if (const char* w = std::getenv("RSG_TICK_SHAPE")) {  // fixed launch shape "w,lanes,header,leafgrid", no tuning
+        int v[4] = {8, 4, -1, 1};
+        std::sscanf(w, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]);
+        b->shape.arenas_per_block = v[0];
+        b->shape.lanes_per_car = v[1];
+        b->shape.header_cache = v[2];
+        b->shape.leaf_grid = v[3];
+        b->tune_pending = false;
+        b->tune_log = "fixed by RSG_TICK_SHAPE: " + shape_str(b->shape);
     }
     BatchBuffers& B = b->buf;
     B.A = (int)n_arenas;
@@ -713,6 +778,8 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
     ok = ok && alloc((void**)&B.rec, sizeof(uint32_t) * (size_t)rec_words((int)MC) * A);
     ok = ok && alloc((void**)&B.au, sizeof(uint32_t) * AU_COUNT * A);
     ok = ok && alloc(&B.events, (size_t)DEV_EVENT_BYTES * MAX_EVENTS_PER_ARENA * A);
+    ok = ok && alloc((void**)&B.place, sizeof(uint32_t) * A);
+    ok = ok && alloc((void**)&B.cost, sizeof(uint32_t) * A);
     if (!ok) {
         rsg_batch_destroy(b);
         return nullptr;
@@ -749,13 +816,11 @@ void rsg_batch_destroy(rsg_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     BatchBuffers& B = b->buf;
-    void* ptrs[] = {B.rec, B.au, B.events, b->d_cfgs, b->d_stage, b->d_pads};
+    void* ptrs[] = {B.rec, B.au, B.events, B.place, B.cost, b->d_cfgs, b->d_stage, b->d_pads};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->h_bounce) cudaFreeHost(b->h_bounce);
     if (b->stream) cudaStreamDestroy(b->stream);
-    for (cudaEvent_t e : b->tune_ev)
-        if (e) cudaEventDestroy(e);
     delete b;
 }
 
@@ -1275,6 +1340,24 @@ int rsg_get_device_flags(rsg_batch* b, uint32_t* out) {
     if ((rc = set_device(b))) return rc;
     RSG_CUDA(cudaMemcpyAsync(out, b->buf.au + au_index(b, AU_ERR, 0), 4 * (size_t)b->buf.A, cudaMemcpyDeviceToHost, b->stream));
     RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+int rsg_get_tick_shape(const rsg_batch* b, int32_t out[4]) {
+    if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
+    out[0] = b->shape.arenas_per_block;
+    out[1] = b->shape.lanes_per_car;
+    out[2] = b->shape.header_cache;
+    out[3] = b->shape.leaf_grid;
+    return RSG_OK;
+}
+
+int rsg_get_tuning_log(const rsg_batch* b, char* buf, uint64_t buf_len) {
+    if (!b || !buf || buf_len == 0) return fail(RSG_ERR_ARG, "null argument");
+    const std::string& s = b->tune_log.empty() ? std::string("not tuned yet") : b->tune_log;
+    size_t n = std::min<size_t>(s.size(), (size_t)buf_len - 1);
+    std::memcpy(buf, s.data(), n);
+    buf[n] = 0;
     return RSG_OK;
 }
 

@@ -29,20 +29,24 @@ RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
 // One warp per arena: the arena's working set is carved out of dynamic shared memory
 // (smem_layout), loaded from its record, advanced `ticks` ticks and stored back.  The warps of a
 // block step through the parts of a tick together (block-wide barriers between parts), which keeps
-// the instruction working set of an SM to one part of the tick at a time.
+// the instruction working set of an SM to one part of the tick at a time.  Warp slot s of the grid
+// advances arena place[s]; lane 0 adds up the cycles of the arena's own collision work into cost[].
 __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
-                                                          int ticks, int hdr_cache) {
+                                                          int ticks, int hdr_cache, const uint32_t* __restrict__ place,
+                                                          uint32_t* __restrict__ cost) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int ar = blockIdx.x * (blockDim.x >> 5) + warp;
-    const bool active = ar < bv.A;  // warp-uniform; idle warps still take part in the barriers
+    const int wpb = blockDim.x >> 5;
+    const int slot0 = blockIdx.x * wpb;
+    const bool active = slot0 + warp < bv.A;  // warp-uniform; idle warps still take part in the barriers
+    const int ar = active ? (int)place[slot0 + warp] : 0;
     const SmemLayout L = smem_layout(bv.MC);
     Ctx& a = bind_ctx(smem + (size_t)warp * L.bytes, L, lane);
     // the BVH subtree headers, read by every narrow-phase query, copied once into the block's
     // shared memory behind the arenas when they fit
     const Subtree* sub = bv.mesh.sub;
     if (hdr_cache) {
-        uint32_t* dst = reinterpret_cast<uint32_t*>(smem + (size_t)(blockDim.x >> 5) * L.bytes);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(smem + (size_t)wpb * L.bytes);
         const uint32_t* src = reinterpret_cast<const uint32_t*>(bv.mesh.sub);
         for (int i = threadIdx.x; i < bv.mesh.nsub * 5; i += blockDim.x) dst[i] = __ldg(src + i);
         sub = reinterpret_cast<const Subtree*>(dst);
@@ -58,17 +62,17 @@ __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rs
         load_pads(bv, ar, a, lane);
         __syncwarp();
     }
-    const int wpb = blockDim.x >> 5;
-    int nact = bv.A - blockIdx.x * wpb;
+    int nact = bv.A - slot0;
     nact = nact < wpb ? nact : wpb;
     const BlockArenas B{smem, L.bytes, nact};
+    unsigned long long busy = 0;
     RSG_PHASE_BEGIN;
     for (int t = 0; t < ticks; t++) {
         if (controls)
             for (int u = threadIdx.x; u < nact * bv.MC; u += blockDim.x) {
                 const int w = u / bv.MC, k = u % bv.MC;
                 Ctx& aw = B(w);
-                if (k < aw.ncars) apply_controls(aw.cars[k], controls[((size_t)t * bv.A + blockIdx.x * wpb + w) * bv.MC + k]);
+                if (k < aw.ncars) apply_controls(aw.cars[k], controls[((size_t)t * bv.A + place[slot0 + w]) * bv.MC + k]);
             }
         __syncthreads();
         block_tick_pre(bv, B, threadIdx.x, blockDim.x);
@@ -76,17 +80,58 @@ __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rs
         if (active) step_bodies_pre(bv, a, lane);
         __syncthreads();
         RSG_PHASE(1);
+        const long long c0 = clock64();
         if (active) step_collide_warp(bv, a, lane);
+        busy += (unsigned long long)(clock64() - c0);
         __syncthreads();
         RSG_PHASE(2);
         block_tick_post(bv, B, threadIdx.x, blockDim.x);
         RSG_PHASE(3);
     }
     if (active) {
-        if (lane == 0) store_arena(bv, ar, a);
+        if (lane == 0) {
+            store_arena(bv, ar, a);
+            cost[ar] = busy > 0xffffffffull ? 0xffffffffu : (uint32_t)busy;
+        }
         if (lane < a.ncars) store_car(bv, ar, a, lane);
         store_pads(bv, ar, a, lane);
     }
+}
+
+// Placement order of the arenas: a counting sort by the cost of their collision work in the last
+// launch, on a log scale with eight steps per octave, most expensive first.  Any order gives the same
+// results (arenas are independent); this one makes the arenas of a block cost about the same.
+__global__ void rsg_place_arenas_kernel(int A, const uint32_t* __restrict__ cost, uint32_t* __restrict__ place) {
+    __shared__ uint32_t start[256];
+    auto key = [](uint32_t c) {
+        c |= 1u;
+        const int l = 31 - __clz(c);
+        const int frac = l >= 3 ? (int)((c >> (l - 3)) & 7u) : 0;
+        return 255 - (l * 8 + frac);
+    };
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) start[i] = 0;
+    __syncthreads();
+    for (int a = threadIdx.x; a < A; a += blockDim.x) atomicAdd(&start[key(cost[a])], 1u);
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive prefix sum of the 256 bucket sizes, 8 per lane
+        uint32_t v[8], s = 0;
+        for (int j = 0; j < 8; j++) { v[j] = start[threadIdx.x * 8 + j]; s += v[j]; }
+        uint32_t incl = s;
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+            if ((int)threadIdx.x >= d) incl += o;
+        }
+        uint32_t run = incl - s;
+        for (int j = 0; j < 8; j++) { start[threadIdx.x * 8 + j] = run; run += v[j]; }
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < A; a += blockDim.x) place[atomicAdd(&start[key(cost[a])], 1u)] = (uint32_t)a;
+}
+
+cudaError_t launch_place_arenas(const BatchBuffers& b, cudaStream_t st) {
+    if (b.A <= 1) return cudaSuccess;
+    rsg_place_arenas_kernel<<<1, 1024, 0, st>>>(b.A, b.cost, b.place);
+    return cudaGetLastError();
 }
 
 int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars).bytes; }
@@ -115,25 +160,34 @@ cudaError_t ensure_epa_pool() {
     return cudaSuccess;
 }
 
-cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int warps_per_block,
+cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, const TickShape& shape,
                         cudaStream_t st) {
     if (b.A <= 0 || ticks <= 0) return cudaSuccess;
-    if (warps_per_block <= 0 || warps_per_block > 8) warps_per_block = 2;
+    int wpb = shape.arenas_per_block;
+    if (wpb <= 0 || wpb > 8) wpb = 8;
     // the block must fit in shared memory
-    while (warps_per_block > 1 && smem_layout(b.MC).bytes * warps_per_block > 227 * 1024) warps_per_block--;
+    while (wpb > 1 && smem_layout(b.MC).bytes * wpb > 227 * 1024) wpb--;
     const int per_arena = smem_layout(b.MC).bytes;
-    int smem = per_arena * warps_per_block;
-    // the header copy is made only when it costs no block per SM (228 KB of shared memory per SM,
-    // 1 KB of it reserved per block)
+    int smem = per_arena * wpb;
+    // the header copy: on request, or (automatic) only when it costs no block per SM (228 KB of
+    // shared memory per SM, 1 KB of it reserved per block)
     const int hdr_bytes = b.mesh.sub ? b.mesh.nsub * (int)sizeof(Subtree) : 0;
     const int sm_smem = 228 * 1024;
     const int blocks_without = sm_smem / (smem + 1024), blocks_with = sm_smem / (smem + hdr_bytes + 1024);
-    const int hdr_cache = (hdr_bytes > 0 && smem + hdr_bytes <= 227 * 1024 && blocks_with >= blocks_without) ? 1 : 0;
+    const bool fits = hdr_bytes > 0 && smem + hdr_bytes <= 227 * 1024;
+    const int hdr_cache = shape.header_cache < 0 ? ((fits && blocks_with >= blocks_without) ? 1 : 0)
+                                                 : ((fits && shape.header_cache) ? 1 : 0);
     if (hdr_cache) smem += hdr_bytes;
     cudaError_t e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    int grid = (b.A + warps_per_block - 1) / warps_per_block;
-    rsg_tick_kernel<<<grid, 32 * warps_per_block, smem, st>>>(make_view(b), controls, ticks, hdr_cache);
+    BatchView v = make_view(b);
+    v.lanes_per_car = (shape.lanes_per_car == 1 || shape.lanes_per_car == 2) ? shape.lanes_per_car : 4;
+    if (!shape.leaf_grid) {
+        v.mesh.lg_block = nullptr;
+        v.mesh.lg_over = nullptr;
+    }
+    int grid = (b.A + wpb - 1) / wpb;
+    rsg_tick_kernel<<<grid, 32 * wpb, smem, st>>>(v, controls, ticks, hdr_cache, b.place, b.cost);
     return cudaGetLastError();
 }
 
@@ -555,9 +609,11 @@ cudaError_t launch_is_scored(const BatchBuffers& b, int* out, cudaStream_t st) {
 
 // ---------------------------------------------------------------- batch bookkeeping kernels
 // Arena::Arena's initial ball, pads and counters (src/Sim/Arena/Arena.cpp:416-540)
-__global__ void rsg_init_arenas_kernel(BatchView bv, uint32_t ball_cell) {
+__global__ void rsg_init_arenas_kernel(BatchView bv, uint32_t ball_cell, uint32_t* place, uint32_t* cost) {
     int ar = blockIdx.x * blockDim.x + threadIdx.x;
     if (ar >= bv.A) return;
+    place[ar] = (uint32_t)ar;
+    cost[ar] = 0;
     SoA s{bv, ar};
     V3 p = V3(0, 0, RL::BALL_REST_Z) * RL::UU_TO_BT;
     for (int f = 0; f < BF_COUNT; f++) s.bf(f) = 0.f;
@@ -628,7 +684,7 @@ __global__ void rsg_demolish_kernel(BatchView bv, uint32_t ar, uint32_t slot, fl
 }
 
 cudaError_t launch_init_arenas(const BatchBuffers& b, uint32_t ball_cell, cudaStream_t st) {
-    rsg_init_arenas_kernel<<<blocks_for(b.A, 128), 128, 0, st>>>(make_view(b), ball_cell);
+    rsg_init_arenas_kernel<<<blocks_for(b.A, 128), 128, 0, st>>>(make_view(b), ball_cell, b.place, b.cost);
     return cudaGetLastError();
 }
 cudaError_t launch_add_car(const BatchBuffers& b, uint32_t arena, uint32_t slot, uint32_t id, uint32_t cfg, uint32_t flags,

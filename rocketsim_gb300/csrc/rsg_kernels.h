@@ -38,15 +38,29 @@ struct BatchBuffers {
     uint32_t event_mask;
     DevMeshPtrs mesh;
     GridSpec grid;
+    uint32_t* place;  // [A] arena advanced by each warp slot of the tick kernel (a permutation of 0..A-1)
+    uint32_t* cost;   // [A] cycles each arena's own collision work took in the last tick launch
 };
 
 constexpr int DEV_EVENT_BYTES = 24;
 
-// Advances every arena by `ticks` ticks, one warp per arena and `warps_per_block`
-// arenas per block.  `controls` (device, may be null) holds [ticks][A][MC]
-// rsg_car_controls applied before each tick.
-cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, int warps_per_block,
+// Launch shape of the tick kernel.  Every shape gives the same results (arenas never depend on the
+// block they share or on how their units are spread); they differ in speed.
+struct TickShape {
+    int arenas_per_block = 8;  // one warp per arena
+    int lanes_per_car = 4;     // threads per car in the vehicle update after the rays: 1, 2 or 4
+    int header_cache = -1;     // BVH subtree headers in shared memory: 1 yes, 0 no, -1 when it costs no block per SM
+    int leaf_grid = 1;         // wheel rays scan the leaf grid (1) or walk the quantized BVH (0)
+};
+
+// Advances every arena by `ticks` ticks, one warp per arena, arenas placed in blocks by b.place.
+// `controls` (device, may be null) holds [ticks][A][MC] rsg_car_controls applied before each tick.
+cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, const TickShape& shape,
                         cudaStream_t st);
+// Re-places the arenas for the next launch: b.place lists them by the cost of their collision work
+// in the last launch, most expensive first, so that the arenas sharing a block (and waiting for each
+// other at its barriers) cost about the same and the cheap blocks fill the last wave.
+cudaError_t launch_place_arenas(const BatchBuffers& b, cudaStream_t st);
 // Shared memory one arena needs in the tick kernel.
 int tick_smem_per_arena(int max_cars);
 

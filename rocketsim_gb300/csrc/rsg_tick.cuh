@@ -106,6 +106,7 @@ struct BatchView {
     const float4* pad_cfg;  // per pad: position (uu) and is_big (ArenaConfig's pads or the soccar ones)
     int npads, custom_pads;  // pad count; custom pads skip BoostPadGrid (Arena.cpp:724-731)
     int no_ball_rot;         // ArenaConfig::noBallRot
+    int lanes_per_car;       // threads per car in the vehicle update after the rays (1, 2 or 4)
     uint32_t* rec;  // A records of rec_words(MC) words
     int rec_words;
     uint32_t* au;   // [AU_COUNT][A]
@@ -1331,7 +1332,7 @@ RSG_DN void car_pre_after_rays_grp(const BatchView& bv, Ctx& a, Car& c, int wl, 
         if (wl == 0)
             for (int j = 0; j < 4; j++)
                 if (on[j]) { c.rb.lin_vel += dv[j]; c.rb.ang_vel += dw[j]; }
-    } else {
+    } else if (wl == 0) {
         apply_suspension(c, dt);
         apply_friction_impulses(c, dt);
     }
@@ -3956,21 +3957,22 @@ RSG_DN void block_tick_pre(const BatchView& bv, const BlockArenas& B, int tid, i
     }
     __syncthreads();
     RSG_SUB(10);
-    {  // four threads per car (one per wheel), cars spread over the warps
-        const int nw = nthreads >> 5, lane = tid & 31, g = lane >> 2, wl = lane & 3;
+    {  // bv.lanes_per_car threads per car (1, 2 or 4; wheels split between them), cars spread over the warps
+        const int LPC = bv.lanes_per_car;
+        const int nw = nthreads >> 5, lane = tid & 31, g = lane / LPC, wl = lane % LPC;
         const int u = g * nw + (tid >> 5);
-        const unsigned gmask = 0xfu << (4 * g);
+        const unsigned gmask = ((1u << LPC) - 1u) << (LPC * g);
         Ctx& a = B(u / MC);
         int k = u % MC;
         if (u < B.nact * MC && !a.serial && k < a.ncars) {
             if (a.on_car) {
                 if (k == 0)
-                    for (int kk = 0; kk < a.ncars; kk++) car_pre_after_rays_grp(bv, a, a.cars[a.order[kk]], wl, 4, gmask);
+                    for (int kk = 0; kk < a.ncars; kk++) car_pre_after_rays_grp(bv, a, a.cars[a.order[kk]], wl, LPC, gmask);
             } else {
 #if defined(RSG_PHASE_TIMERS)
                 long long at0_ = clock64();
 #endif
-                car_pre_after_rays_grp(bv, a, a.cars[k], wl, 4, gmask);
+                car_pre_after_rays_grp(bv, a, a.cars[k], wl, LPC, gmask);
 #if defined(RSG_PHASE_TIMERS)
                 if (wl == 0) {
                     long long dtc = clock64() - at0_;

@@ -18,6 +18,7 @@ inline BatchView make_view(const BatchBuffers& b) {
     v.npads = b.npads;
     v.custom_pads = b.custom_pads;
     v.no_ball_rot = b.no_ball_rot;
+    v.lanes_per_car = 4;
     v.rec = b.rec;
     v.rec_words = rec_words(b.MC);
     v.au = b.au;

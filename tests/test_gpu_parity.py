@@ -259,3 +259,49 @@ def test_the_void_free_flight_matches_restatement():
         assert d <= TOL[8]["pos"], d
     b.close()
     o.close()
+
+
+def test_launch_shapes_give_identical_results(golden, monkeypatch):
+    """Every launch shape the tuner may choose (arenas per block, threads per car, BVH headers in shared
+    memory or not, leaf grid or BVH walk), with the arenas re-placed in blocks by cost after every
+    launch, steps the golden scenarios (each three times in the batch) to bit-identical states."""
+    scs = golden.scenarios * 3
+    results = []
+    for shape in ("8,4,-1,1", "4,1,0,1", "6,2,1,0", "7,4,1,1", "5,1,0,0"):
+        monkeypatch.setenv("RSG_TICK_SHAPE", shape)
+        batch, _ = setup_gpu(scs)
+        assert batch.tick_shape()[:2] == tuple(int(x) for x in shape.split(",")[:2])
+        for t in range(24):
+            batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
+            batch.step(1)
+        cars, balls, pads = batch.get_all_states()
+        results.append((cars.tobytes(), balls.tobytes(), pads.tobytes()))
+        batch.close()
+    assert all(r == results[0] for r in results[1:])
+
+
+def test_tuner_reports_its_trials():
+    """The first launch of a batch runs the shape tuner from one saved state: the log lists the
+    trials, the chosen shape is one of them, and the batch's results equal a fixed-shape batch's."""
+    import os
+    scs = random_scenarios(16, base_seed=4000)
+    assert "RSG_TICK_SHAPE" not in os.environ
+    b1, _ = setup_gpu(scs)
+    for t in range(16):
+        b1.set_controls_all(gpu_controls(scs, t, b1.max_cars))
+        b1.step(1)
+    log = b1.tuning_log()
+    assert log.startswith("chose ") and "ms/tick" in log, log
+    s1 = b1.get_all_states()
+    b1.close()
+    os.environ["RSG_TICK_SHAPE"] = "8,4,-1,1"
+    try:
+        b2, _ = setup_gpu(scs)
+        for t in range(16):
+            b2.set_controls_all(gpu_controls(scs, t, b2.max_cars))
+            b2.step(1)
+        s2 = b2.get_all_states()
+        b2.close()
+    finally:
+        del os.environ["RSG_TICK_SHAPE"]
+    assert s1[0].tobytes() == s2[0].tobytes() and s1[1].tobytes() == s2[1].tobytes()
