@@ -271,6 +271,13 @@ struct Ctx {
     int16_t* hdr_n;    // [MAX_DYN], -1 when the list overflowed
     int nflat;
     uint32_t warn;
+    // the solver batch planned on lane 0 and set up on the warp: solver bodies (object ids in island
+    // order), (manifold, point) of every contact row in row order, bodies with special contacts
+    int solve_nb, solve_nc, solve_nsp;
+    int* solve_bodies;
+    int* solve_plan;
+    int8_t sb_of[MAX_CARS + 1];
+    int8_t solve_special[MAX_CARS + 1];
 
     RSG_D Body& body(int o) { return o == OBJ_BALL ? ball : cars[o - OBJ_CAR0].rb; }
 };
@@ -2991,23 +2998,17 @@ RSG_D float solve_split(Ctx& a, Row& c) {  // gResolveSplitPenetrationImpulse_ss
     return (float)((double)d * (1. / (double)c.jac_inv));
 }
 
-// Solves one batch: `bodies` are dynamic object ids in island order, `mans` manifold indices in
-// sorted island order (btSequentialImpulseConstraintSolver::solveGroup)
-RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, float dt) {
-    RSG_L0_BEGIN;
-    int nc = 0, nf = 0;
-    int sb_of[MAX_DYN];
-    for (int i = 0; i < MAX_DYN; i++) sb_of[i] = -1;
-    for (int i = 0; i < nb; i++) {
-        init_solver_body(a, a.sb[i], bodies[i], dt);
-        sb_of[bodies[i] - OBJ_BALL] = i;
-    }
-    SBody& fixed = a.sb[SB_FIXED];
-    fixed.obj = -1;
-    fixed.xf = xf_identity();
-    fixed.inv_mass = 0;
-    fixed.dlv = fixed.dav = fixed.push = fixed.turn = fixed.lv = fixed.av = fixed.ext_f = fixed.ext_t = V3(0, 0, 0);
-    auto sbi = [&](int o) { return is_static_obj(o) ? SB_FIXED : sb_of[o - OBJ_BALL]; };
+// The solver (btSequentialImpulseConstraintSolver::solveGroup) in three parts: solve_plan (lane 0)
+// fixes the solver bodies and the contact rows in Bullet's order and adds up RocketSim's special
+// contacts per body; solve_setup_warp sets the rows up on the warp's lanes (each row reads only its
+// contact point and the solver bodies' start state); solve_iterate (lane 0) runs the iterations and
+// writes the bodies back.  `bodies` are dynamic object ids in island order, `mans` manifold indices in
+// sorted island order, `plan` room for one word per row.
+RSG_DN void solve_plan(Ctx& a, const int* bodies, int nb, const int* mans, int nm, int* plan) {
+    int nc = 0;
+    for (int i = 0; i < MAX_DYN; i++) a.sb_of[i] = -1;
+    for (int i = 0; i < nb; i++) a.sb_of[bodies[i] - OBJ_BALL] = (int8_t)i;
+    auto sbi = [&](int o) { return is_static_obj(o) ? SB_FIXED : (int)a.sb_of[o - OBJ_BALL]; };
     for (int mi = 0; mi < nm; mi++) {
         Manifold& m = a.man[mans[mi]];
         int ia = sbi(m.body0), ib = sbi(m.body1);
@@ -3016,12 +3017,10 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
             const MPoint& cp = a.pts[m.pt[j]];
             if (!(cp.dist <= BT_LARGE)) continue;
             if (nc >= a.cap_rows) { a.err |= ERR_ROW_OVERFLOW; continue; }
-            Row& r = a.rows_c[nc];
-            V3 rel1 = cp.pos_a - obj_xf(a, m.body0).o;
-            V3 rel2 = cp.pos_b - obj_xf(a, m.body1).o;
-            setup_contact_row(a, r, ia, ib, cp, rel1, rel2, dt);
-            r.friction_index = (int16_t)nf;
-            if (cp.special) {
+            plan[nc++] = (mans[mi] << 2) | j;
+            if (cp.special) {  // the special contact sums, in row order (convertContactSpecial's inputs)
+                V3 rel1 = cp.pos_a - obj_xf(a, m.body0).o;
+                V3 rel2 = cp.pos_b - obj_xf(a, m.body1).o;
                 for (int k = 0; k < 2; k++) {
                     int o = k ? m.body1 : m.body0;
                     if (!is_static_obj(o)) {
@@ -3034,40 +3033,82 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
                     }
                 }
             }
-            int fidx = nc++;
-            add_friction(a, nf, ia, ib, cp.normal, cp.friction, rel1, rel2, fidx);
         }
     }
     // RocketSim's averaged ball-world contact (convertContactSpecial,
-    // btSequentialImpulseConstraintSolver.cpp:1164-1211)
+    // btSequentialImpulseConstraintSolver.cpp:1164-1211): one row per body with special contacts,
+    // in body order after the others
+    int nsp = 0;
     for (int i = 0; i < nb; i++) {
         Body& b = a.body(bodies[i]);
         if (b.n_special > 0) {
-            float dist = b.sp_total_dist / b.n_special;
-            V3 nrm = b.sp_total_normal / (float)b.n_special;
-            MPoint tmp;
-            tmp.dist = dist;
-            tmp.normal = nrm;
-            tmp.friction = b.sp_friction;
-            tmp.restitution = b.sp_restitution;
-            tmp.special = false;
-            if (nc < a.cap_rows) {
-                Row& r = a.rows_c[nc];
-                V3 rel1 = nrm * -dist, rel2(0, 0, 0);
-                setup_contact_row(a, r, i, SB_FIXED, tmp, rel1, rel2, dt);
-                int fidx = nc;
-                r.friction_index = (int16_t)nf;
-                nc++;
-                add_friction(a, nf, i, SB_FIXED, tmp.normal, tmp.friction, rel1, rel2, fidx);
+            if (nc + nsp < a.cap_rows) {
+                a.solve_special[nsp++] = (int8_t)i;
             } else {
                 a.err |= ERR_ROW_OVERFLOW;
+                b.n_special = 0;
+                b.sp_friction = b.sp_restitution = b.sp_total_dist = 0;
+                b.sp_total_normal = V3(0, 0, 0);
             }
-            b.n_special = 0;
-            b.sp_friction = b.sp_restitution = b.sp_total_dist = 0;
-            b.sp_total_normal = V3(0, 0, 0);
         }
     }
-    RSG_L0(19);
+    a.solve_bodies = const_cast<int*>(bodies);
+    a.solve_plan = plan;
+    a.solve_nb = nb;
+    a.solve_nc = nc;
+    a.solve_nsp = nsp;
+}
+
+RSG_D void solve_setup_warp(Ctx& a, int lane, float dt) {
+    const int nb = a.solve_nb, nc = a.solve_nc, nsp = a.solve_nsp;
+    if (lane < nb) init_solver_body(a, a.sb[lane], a.solve_bodies[lane], dt);
+    if (lane == 31) {
+        SBody& fixed = a.sb[SB_FIXED];
+        fixed.obj = -1;
+        fixed.xf = xf_identity();
+        fixed.inv_mass = 0;
+        fixed.dlv = fixed.dav = fixed.push = fixed.turn = fixed.lv = fixed.av = fixed.ext_f = fixed.ext_t = V3(0, 0, 0);
+    }
+    __syncwarp();
+    auto sbi = [&](int o) { return is_static_obj(o) ? SB_FIXED : (int)a.sb_of[o - OBJ_BALL]; };
+    for (int k = lane; k < nc; k += 32) {
+        const int e = a.solve_plan[k];
+        const Manifold& m = a.man[e >> 2];
+        const MPoint& cp = a.pts[m.pt[e & 3]];
+        const int ia = sbi(m.body0), ib = sbi(m.body1);
+        Row& r = a.rows_c[k];
+        V3 rel1 = cp.pos_a - obj_xf(a, m.body0).o;
+        V3 rel2 = cp.pos_b - obj_xf(a, m.body1).o;
+        setup_contact_row(a, r, ia, ib, cp, rel1, rel2, dt);
+        r.friction_index = (int16_t)k;
+        int nf = k;
+        add_friction(a, nf, ia, ib, cp.normal, cp.friction, rel1, rel2, k);
+    }
+    for (int q = lane; q < nsp; q += 32) {
+        const int i = a.solve_special[q], k = nc + q;
+        Body& b = a.body(a.solve_bodies[i]);
+        float dist = b.sp_total_dist / b.n_special;
+        V3 nrm = b.sp_total_normal / (float)b.n_special;
+        MPoint tmp;
+        tmp.dist = dist;
+        tmp.normal = nrm;
+        tmp.friction = b.sp_friction;
+        tmp.restitution = b.sp_restitution;
+        tmp.special = false;
+        Row& r = a.rows_c[k];
+        V3 rel1 = nrm * -dist, rel2(0, 0, 0);
+        setup_contact_row(a, r, i, SB_FIXED, tmp, rel1, rel2, dt);
+        r.friction_index = (int16_t)k;
+        int nf = k;
+        add_friction(a, nf, i, SB_FIXED, tmp.normal, tmp.friction, rel1, rel2, k);
+        b.n_special = 0;
+        b.sp_friction = b.sp_restitution = b.sp_total_dist = 0;
+        b.sp_total_normal = V3(0, 0, 0);
+    }
+}
+
+RSG_DN void solve_iterate(Ctx& a, float dt) {
+    const int nb = a.solve_nb, nc = a.solve_nc + a.solve_nsp, nf = nc;
     const int ITER = 10;
     for (int it = 0; it < ITER; it++) {
         float lsr = 0;
@@ -3078,7 +3119,6 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
         }
         if (lsr <= 0.f || it >= ITER - 1) break;
     }
-    RSG_L0(20);
     for (int it = 0; it < ITER; it++) {
         for (int k = 0; k < nc; k++) {
             if (a.rows_c[k].special) continue;
@@ -3090,7 +3130,6 @@ RSG_DN void solve(Ctx& a, const int* bodies, int nb, const int* mans, int nm, fl
             if (total > 0.f) solve_row(a, f, -(f.friction * total), f.friction * total, false);
         }
     }
-    RSG_L0(21);
     // writeBackBodies (btSequentialImpulseConstraintSolver.cpp:1878-1904)
     for (int i = 0; i < nb; i++) {
         SBody& sb = a.sb[i];
@@ -3692,6 +3731,13 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     }
     RSG_PHASE(6);
     if (lane == 0) step_collide_tail(bv, a);
+    __syncwarp();
+    if (a.solve_nb > 0) {
+        solve_setup_warp(a, lane, bv.dt);
+        __syncwarp();
+        if (lane == 0) solve_iterate(a, bv.dt);
+    }
+    __syncwarp();
     RSG_PHASE(7);
 }
 
@@ -3839,7 +3885,8 @@ RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a) {
         if ((awake >> a.man[island_mans[k]].island) & 1u) solve_mans[nsm++] = island_mans[k];
     a.solver_dt = dt;
     RSG_L0(18);
-    if (nb > 0) solve(a, bodies, nb, solve_mans, nsm, dt);
+    a.solve_nb = 0;
+    if (nb > 0) solve_plan(a, bodies, nb, solve_mans, nsm, bodies + MAX_DYN);
 }
 
 // Phase 3 of a world step, one lane per dynamic object: integration, activation, force reset.
@@ -4449,7 +4496,7 @@ RSG_HD SmemLayout smem_layout(int mc) {
     L.flat_off = o; o = align16(o + 2 * L.caps.pairs);
     L.flat_n = o; o = align16(o + 2 * L.caps.pairs);
     {  // candidate triangles; reused by the island / solver lists after the narrow phase
-        int words = MESH_SEG * (mc + 1), tail = 4 * L.caps.pairs + MAX_DYN;
+        int words = MESH_SEG * (mc + 1), tail = 4 * L.caps.pairs + MAX_DYN + L.caps.rows;
         L.cand_tri = o; o = align16(o + 4 * (words > tail ? words : tail));
     }
     L.cand_n = o; o = align16(o + 2 * (mc + 1));
