@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256, 2) rsg_ball_pred_run_kernel(BatchView bv,
         block_tick_pre(bv, B, threadIdx.x, blockDim.x);
         if (active) step_bodies_pre(bv, a, lane);
         __syncthreads();
-        if (active) step_collide_warp(bv, a, lane);
+        step_collide_block(bv, a, lane, active, false);
         __syncthreads();
         block_tick_post(bv, B, threadIdx.x, blockDim.x);
         if (active && lane == 0 && t < my_steps) {

@@ -528,9 +528,9 @@ std::mutex g_tune_mu;
 std::map<TuneKey, std::pair<TickShape, std::string>> g_tune_cache;
 
 std::string shape_str(const TickShape& s) {
-    char buf[96];
-    std::snprintf(buf, sizeof(buf), "arenas_per_block=%d lanes_per_car=%d header_cache=%d leaf_grid=%d",
-                  s.arenas_per_block, s.lanes_per_car, s.header_cache, s.leaf_grid);
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "arenas_per_block=%d lanes_per_car=%d header_cache=%d leaf_grid=%d collide_sync=%d",
+                  s.arenas_per_block, s.lanes_per_car, s.header_cache, s.leaf_grid, s.collide_sync);
     return buf;
 }
 
@@ -619,6 +619,11 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
         if (e == cudaSuccess && B.mesh.lg_block) {
             TickShape s = best;
             s.leaf_grid = 0;
+            e = consider(s);
+        }
+        if (e == cudaSuccess) {
+            TickShape s = best;
+            s.collide_sync = best.collide_sync ? 0 : 1;
             e = consider(s);
         }
         if (e == cudaSuccess) e = copy_all(false);
@@ -715,13 +720,14 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         fail(RSG_ERR_STATE, "the mesh was loaded on another device");
         return nullptr;
     }
-    if (const char* w = std::getenv("RSG_TICK_SHAPE")) {  // fixed launch shape "w,lanes,header,leafgrid", no tuning
-        int v[4] = {8, 4, -1, 1};
-        std::sscanf(w, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]);
+    if (const char* w = std::getenv("RSG_TICK_SHAPE")) {  // fixed shape "w,lanes,header,leafgrid[,sync]", no tuning
+        int v[5] = {8, 4, -1, 1, 1};
+        std::sscanf(w, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]);
         b->shape.arenas_per_block = v[0];
         b->shape.lanes_per_car = v[1];
         b->shape.header_cache = v[2];
         b->shape.leaf_grid = v[3];
+        b->shape.collide_sync = v[4];
         b->tune_pending = false;
         b->tune_log = "fixed by RSG_TICK_SHAPE: " + shape_str(b->shape);
     }
@@ -1343,12 +1349,13 @@ int rsg_get_device_flags(rsg_batch* b, uint32_t* out) {
     return RSG_OK;
 }
 
-int rsg_get_tick_shape(const rsg_batch* b, int32_t out[4]) {
+int rsg_get_tick_shape(const rsg_batch* b, int32_t out[5]) {
     if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
     out[0] = b->shape.arenas_per_block;
     out[1] = b->shape.lanes_per_car;
     out[2] = b->shape.header_cache;
     out[3] = b->shape.leaf_grid;
+    out[4] = b->shape.collide_sync;
     return RSG_OK;
 }
 

@@ -32,8 +32,8 @@ RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
 // the instruction working set of an SM to one part of the tick at a time.  Warp slot s of the grid
 // advances arena place[s]; lane 0 adds up the cycles of the arena's own collision work into cost[].
 __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
-                                                          int ticks, int hdr_cache, const uint32_t* __restrict__ place,
-                                                          uint32_t* __restrict__ cost) {
+                                                          int ticks, int hdr_cache, int collide_sync,
+                                                          const uint32_t* __restrict__ place, uint32_t* __restrict__ cost) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rs
         __syncthreads();
         RSG_PHASE(1);
         const long long c0 = clock64();
-        if (active) step_collide_warp(bv, a, lane);
+        step_collide_block(bv, a, lane, active, collide_sync != 0);
         busy += (unsigned long long)(clock64() - c0);
         __syncthreads();
         RSG_PHASE(2);
@@ -187,7 +187,8 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
         v.mesh.lg_over = nullptr;
     }
     int grid = (b.A + wpb - 1) / wpb;
-    rsg_tick_kernel<<<grid, 32 * wpb, smem, st>>>(v, controls, ticks, hdr_cache, b.place, b.cost);
+    rsg_tick_kernel<<<grid, 32 * wpb, smem, st>>>(v, controls, ticks, hdr_cache, shape.collide_sync ? 1 : 0, b.place,
+                                                   b.cost);
     return cudaGetLastError();
 }
 

@@ -51,6 +51,7 @@ struct TickShape {
     int lanes_per_car = 4;     // threads per car in the vehicle update after the rays: 1, 2 or 4
     int header_cache = -1;     // BVH subtree headers in shared memory: 1 yes, 0 no, -1 when it costs no block per SM
     int leaf_grid = 1;         // wheel rays scan the leaf grid (1) or walk the quantized BVH (0)
+    int collide_sync = 1;      // block-wide barriers between the parts of the collision work (1) or not (0)
 };
 
 // Advances every arena by `ticks` ticks, one warp per arena, arenas placed in blocks by b.place.

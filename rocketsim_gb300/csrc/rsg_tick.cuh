@@ -2603,7 +2603,13 @@ RSG_DN void contact_added(const BatchView& bv, Ctx& a, Manifold& m, int idx, int
     } else if (ua == 2 && ub == -1) {
         cp.special = true;  // ball-world (src/Sim/Arena/Arena.cpp:298-306)
     }
+#if defined(RSG_PHASE_TIMERS)
+    long long ie_ = clock64();
+#endif
     if (tri >= 0) adjust_internal_edge(bv.mesh, cp, tri);
+#if defined(RSG_PHASE_TIMERS)
+    atomicAdd(&g_phase_cycles[48], (unsigned long long)(clock64() - ie_));
+#endif
 }
 
 // btManifoldResult::calculateCombined{Friction,Restitution} as RocketSim patches them
@@ -2980,8 +2986,23 @@ RSG_D void solve_row(Ctx& a, Row& c, float lo, float hi, bool lower_only) {
     if (B.obj >= 0) { B.dlv += n2 * B.inv_mass * d; B.dav += c.angB * d; }
 }
 
-RSG_D float solve_split(Ctx& a, Row& c) {  // gResolveSplitPenetrationImpulse_sse2
-    if (!c.rhs_pen) return 0.f;
+// Whether the squared split-impulse residual the reference returns, (float)(d * (1. / jac_inv)) computed
+// in double and squared in float, is positive: all the split iterations use it for (their stop test
+// compares the largest square with 0).  Clear cases are decided in float (the double value agrees
+// with |d| / |jac_inv| to a few float ulps, so it squares to at least 2^-120 above 2^-60 and rounds
+// to 0 below 2^-90); the band between, NaN and infinity take the reference's double arithmetic.
+RSG_D bool split_residual_positive(float d, float jac_inv) {
+    if (d == 0.f) return false;
+    const float q = fabsf(d) / fabsf(jac_inv);
+    if (q > 8.673617e-19f) return true;   // 2^-60
+    if (q < 8.077936e-28f) return false;  // 2^-90
+    const float res = (float)((double)d * (1. / (double)jac_inv));
+    return res * res > 0.f;
+}
+
+// gResolveSplitPenetrationImpulse_sse2; returns split_residual_positive of its impulse change
+RSG_D bool solve_split(Ctx& a, Row& c) {
+    if (!c.rhs_pen) return false;
     SBody& A = a.sb[c.ba];
     SBody& B = a.sb[c.bb];
     V3 n2 = row_n2(c);
@@ -2995,7 +3016,7 @@ RSG_D float solve_split(Ctx& a, Row& c) {  // gResolveSplitPenetrationImpulse_ss
     else c.applied_push = sum;
     if (A.obj >= 0) { A.push += c.n1 * A.inv_mass * d; A.turn += c.angA * d; }
     if (B.obj >= 0) { B.push += n2 * B.inv_mass * d; B.turn += c.angB * d; }
-    return (float)((double)d * (1. / (double)c.jac_inv));
+    return split_residual_positive(d, c.jac_inv);
 }
 
 // The solver (btSequentialImpulseConstraintSolver::solveGroup) in three parts: solve_plan (lane 0)
@@ -3111,13 +3132,9 @@ RSG_DN void solve_iterate(Ctx& a, float dt) {
     const int nb = a.solve_nb, nc = a.solve_nc + a.solve_nsp, nf = nc;
     const int ITER = 10;
     for (int it = 0; it < ITER; it++) {
-        float lsr = 0;
-        for (int k = 0; k < nc; k++) {
-            float res = solve_split(a, a.rows_c[k]);
-            float r2 = res * res;
-            lsr = lsr < r2 ? r2 : lsr;
-        }
-        if (lsr <= 0.f || it >= ITER - 1) break;
+        bool any = false;  // the largest squared residual is above 0
+        for (int k = 0; k < nc; k++) any |= solve_split(a, a.rows_c[k]);
+        if (!any || it >= ITER - 1) break;
     }
     for (int it = 0; it < ITER; it++) {
         for (int k = 0; k < nc; k++) {
@@ -3576,26 +3593,30 @@ RSG_DN void commit_sweep(const BatchView& bv, Ctx& a, CommitState& cs, int base,
 
 RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a);
 
-RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
-    RSG_PHASE_BEGIN;
+// The first part of a world step's collision work on one arena's warp: the pair list, the BVH
+// subtree headers and candidate triangles of each mesh pair, and the flattened candidate list.  Every
+// warp of the block calls it, `active` or not (with `bsync` they meet at barriers between the parts).
+RSG_DN void step_collide_gather(const BatchView& bv, Ctx& a, int lane, bool active, bool bsync) {
 #if defined(RSG_PHASE_TIMERS)
     long long rsg_w_ = clock64();
 #define RSG_W(i) do { if (lane == 0) { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - rsg_w_)); rsg_w_ = t_; } } while (0)
 #else
 #define RSG_W(i)
 #endif
-    build_pairs_warp(bv, a, lane);
-    if (lane == 0) {
-        a.nman = 0;
-        a.npts = 0;
-        a.warn = 0;
+    if (active) {
+        build_pairs_warp(bv, a, lane);
+        if (lane == 0) {
+            a.nman = 0;
+            a.npts = 0;
+            a.warn = 0;
+        }
     }
     __syncwarp();
     RSG_W(22);
-    uint32_t warn = 0;
+    if (bsync) __syncthreads();
     // quantized query box of each mesh pair (one lane per pair)
     unsigned qmask = 0;
-    for (int p = lane; p < a.npairs; p += 32) {
+    for (int p = lane; active && p < a.npairs; p += 32) {
         int k = a.pkind[p];
         if (k == PK_BALL_MESH || k == PK_CAR_MESH) {
             int d = a.pair1[p] - OBJ_BALL;
@@ -3613,6 +3634,7 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     qmask = __reduce_or_sync(0xffffffffu, qmask);
     __syncwarp();
     RSG_W(23);
+    if (bsync) __syncthreads();
     // subtree headers against every query box, 32 headers at a time; each query keeps the
     // overlapping headers in header order.  A run of 32 headers is scanned only for the queries
     // that overlap the box around the whole run.
@@ -3661,8 +3683,9 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
     }
     __syncwarp();
     RSG_W(24);
+    if (bsync) __syncthreads();
     // candidate triangles of each mesh pair, one lane per pair, in BVH order
-    for (int p = lane; p < a.npairs; p += 32) {
+    for (int p = lane; active && p < a.npairs; p += 32) {
         int k = a.pkind[p];
         if (k == PK_BALL_MESH || k == PK_CAR_MESH) {
             int o = a.pair1[p];
@@ -3682,8 +3705,8 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
         }
     }
     __syncwarp();
-    RSG_PHASE(4);
-    if (lane == 0) {
+    RSG_W(49);
+    if (active && lane == 0) {
         int total = 0;
         for (int p = 0; p < a.npairs; p++) {
             int n = 0;
@@ -3695,13 +3718,28 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
         a.nflat = total;
     }
     __syncwarp();
+}
+
+// A world step's collision work (pairs, narrow phase, commits, islands, solver) for the arena of each
+// warp of the block.  Every warp of the block calls it, `active` or not; with `bsync` the block's warps
+// also meet at block-wide barriers between its parts (and between the test and commit halves of every
+// round of candidate tests), so that they run the same code at the same time.
+RSG_D void step_collide_block(const BatchView& bv, Ctx& a, int lane, bool active, bool bsync) {
+    RSG_PHASE_BEGIN;
+#if defined(RSG_PHASE_TIMERS)
+    long long rsg_w_ = clock64();
+#endif
+    step_collide_gather(bv, a, lane, active, bsync);
+    RSG_PHASE(4);
+    if (bsync) __syncthreads();
+    uint32_t warn = 0;
     // rounds of 32 candidate tests, then lane 0 commits them in pair order
     CommitState cs;
     cs.p = 0;
     cs.j = 0;
     cs.mi = 0;
-    const int nflat = a.nflat;
-    for (int base = 0; base < nflat; base += 32) {
+    const int nflat = active ? a.nflat : 0;
+    for (int base = 0; bsync ? __syncthreads_or(base < nflat) : (base < nflat); base += 32) {
         const int f = base + lane;
         if (f < nflat) {
             int p = 0;
@@ -3719,24 +3757,29 @@ RSG_D void step_collide_warp(const BatchView& bv, Ctx& a, int lane) {
             }
         }
         __syncwarp();
-        if (lane == 0) commit_sweep(bv, a, cs, base, base + 32 < nflat ? base + 32 : nflat);
+        RSG_W(46);
+        if (bsync) __syncthreads();
+        if (base < nflat && lane == 0) commit_sweep(bv, a, cs, base, base + 32 < nflat ? base + 32 : nflat);
+        __syncwarp();
+        RSG_W(47);
+    }
+    if (active) {
+        if (warn) atomicOr(&a.warn, warn);
+        __syncwarp();
+        RSG_PHASE(5);
+        if (lane == 0) {
+            commit_sweep(bv, a, cs, nflat, nflat);
+            a.err |= a.warn;
+        }
+        RSG_PHASE(6);
+        if (lane == 0) step_collide_tail(bv, a);
         __syncwarp();
     }
-    if (warn) atomicOr(&a.warn, warn);
+    if (bsync) __syncthreads();
+    if (active && a.solve_nb > 0) solve_setup_warp(a, lane, bv.dt);
     __syncwarp();
-    RSG_PHASE(5);
-    if (lane == 0) {
-        commit_sweep(bv, a, cs, nflat, nflat);
-        a.err |= a.warn;
-    }
-    RSG_PHASE(6);
-    if (lane == 0) step_collide_tail(bv, a);
-    __syncwarp();
-    if (a.solve_nb > 0) {
-        solve_setup_warp(a, lane, bv.dt);
-        __syncwarp();
-        if (lane == 0) solve_iterate(a, bv.dt);
-    }
+    if (bsync) __syncthreads();
+    if (active && a.solve_nb > 0 && lane == 0) solve_iterate(a, bv.dt);
     __syncwarp();
     RSG_PHASE(7);
 }

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from game_event_cases import SCRIPTS, TEAMS
+from golden_data import TOL
 from scenarios import mesh_bytes
 
 pytestmark = pytest.mark.gpu
@@ -69,6 +70,9 @@ def test_events_match_the_reference(name):
     auto, script = SCRIPTS[name]
     ev, balls = run_gpu(auto, script)
     ref_ev = z[f"{name}_events"]
-    assert np.abs(balls - z[f"{name}_balls"]).max() < 5.0  # the same game (the events decide, not the bits)
+    # the ball at every update within the 8-tick tolerance of golden_data.TOL (measured: 1.5e-4 uu,
+    # 6.1e-4 uu/s in the longest script), the events equal
+    d = np.abs(balls - z[f"{name}_balls"])
+    assert d[:, :3].max() <= TOL[8]["pos"] and d[:, 3:].max() <= TOL[8]["vel"], d.max(axis=0)
     np.testing.assert_array_equal(ev, ref_ev, err_msg=name)
     assert (ref_ev[:, 0] != 0).any()  # every script has at least one event

@@ -3,12 +3,9 @@ mutators (tests/golden/mutator_rollouts.npz, written by tests/golden/make_mutato
 argument checks of rsg_set_mutator_config.
 
 Continuous state within golden_data.TOL after 1 and 8 ticks; discrete state (flags, timers, boost,
-demolitions, pads) identical over 120 ticks, except in the four car-car scenarios, checked over their
-first 45 ticks: with demolition on contact the bumping car drives on into the demolished car, whose
-box stays where it was, and climbs onto it; whether a wheel ray that grazes that box's edge ends
-inside it then depends on the last float bits, where the reference (SSE reciprocal square root) and
-this code (exact square root) differ (measured: seed 3 diverged at tick 46 after its states had agreed
-to 3.7e-4 uu, seed 8 at tick 73).  The demolitions themselves happen at ticks 11-19.
+demolitions, pads) identical over all 120 ticks, the four car-car scenarios included: there the
+bumping car drives on into the demolished car's box and climbs onto it, and its wheel rays against
+that box follow the reference's subsimplex convex cast.  The demolitions happen at ticks 11-19.
 """
 from __future__ import annotations
 
@@ -43,8 +40,7 @@ def test_gpu_matches_reference_under_mutators():
         for t in (1, 8):
             cars, ball, _ = snaps[t - 1][si]
             check_continuous(cars, ball, g.cars_at(si, t), g.ball_at(si, t), t, f"mutator scenario {si}")
-        carcar = si >= 8
-        for t in range(45 if carcar else 120):
+        for t in range(120):
             cars, ball, pads = snaps[t][si]
             np.testing.assert_array_equal(discrete_car(cars).astype(np.float32), g.disc_cars(si)[t],
                                           err_msg=f"mutator scenario {si} tick {t + 1}: car discrete state")

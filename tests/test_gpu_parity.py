@@ -263,11 +263,12 @@ def test_the_void_free_flight_matches_restatement():
 
 def test_launch_shapes_give_identical_results(golden, monkeypatch):
     """Every launch shape the tuner may choose (arenas per block, threads per car, BVH headers in shared
-    memory or not, leaf grid or BVH walk), with the arenas re-placed in blocks by cost after every
-    launch, steps the golden scenarios (each three times in the batch) to bit-identical states."""
+    memory or not, leaf grid or BVH walk, block-wide barriers in the collision work or not), with the
+    arenas re-placed in blocks by cost after every launch, steps the golden scenarios (each three times
+    in the batch) to bit-identical states."""
     scs = golden.scenarios * 3
     results = []
-    for shape in ("8,4,-1,1", "4,1,0,1", "6,2,1,0", "7,4,1,1", "5,1,0,0"):
+    for shape in ("8,4,-1,1", "4,1,0,1", "6,2,1,0", "7,4,1,1,1", "5,1,0,0,1", "8,2,1,1,1"):
         monkeypatch.setenv("RSG_TICK_SHAPE", shape)
         batch, _ = setup_gpu(scs)
         assert batch.tick_shape()[:2] == tuple(int(x) for x in shape.split(",")[:2])
