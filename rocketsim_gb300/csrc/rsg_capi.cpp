@@ -729,8 +729,14 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         b->shape.leaf_grid = v[3];
         b->shape.collide_sync = v[4];
         b->tune_pending = false;
-        b->tune_log = "fixed by RSG_TICK_SHAPE: " + shape_str(b->shape);
     }
+    {  // at most as many arenas per block as shared memory holds (launch_tick clamps the same way)
+        const int per_arena = tick_smem_per_arena((int)max_cars_per_arena);
+        int& w = b->shape.arenas_per_block;
+        if (w < 1 || w > 8) w = 8;
+        while (w > 1 && per_arena * w > 227 * 1024) w--;
+    }
+    if (!b->tune_pending) b->tune_log = "fixed by RSG_TICK_SHAPE: " + shape_str(b->shape);
     BatchBuffers& B = b->buf;
     B.A = (int)n_arenas;
     B.MC = (int)max_cars_per_arena;

@@ -271,7 +271,8 @@ def test_launch_shapes_give_identical_results(golden, monkeypatch):
     for shape in ("8,4,-1,1", "4,1,0,1", "6,2,1,0", "7,4,1,1,1", "5,1,0,0,1", "8,2,1,1,1"):
         monkeypatch.setenv("RSG_TICK_SHAPE", shape)
         batch, _ = setup_gpu(scs)
-        assert batch.tick_shape()[:2] == tuple(int(x) for x in shape.split(",")[:2])
+        want, got = [int(x) for x in shape.split(",")], batch.tick_shape()
+        assert got[1] == want[1] and 1 <= got[0] <= want[0]  # arenas per block as shared memory allows
         for t in range(24):
             batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
             batch.step(1)
