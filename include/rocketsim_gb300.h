@@ -39,6 +39,7 @@ extern "C" {
 
 /* Game modes: src/Sim/GameMode.h:6-17. Only SOCCAR and THE_VOID are simulated. */
 #define RSG_GAMEMODE_SOCCAR 0
+#define RSG_GAMEMODE_HEATSEEKER 2
 #define RSG_GAMEMODE_THE_VOID 5
 
 /* Teams: src/Sim/Car/Car.h:130-133 */
@@ -135,6 +136,13 @@ typedef struct rsg_ball_state {
     rsg_vec3 ang_vel;
     uint64_t tick_count_since_update;
 } rsg_ball_state;
+
+/* BallState::HeatseekerInfo, src/Sim/Ball/Ball.h:24-32 (heatseeker's seeking ball) */
+typedef struct rsg_heatseeker_info {
+    float y_target_dir;      /* the net the ball seeks: 1 orange (+y), -1 blue, 0 none */
+    float cur_target_speed;  /* uu/s */
+    float time_since_hit;    /* s */
+} rsg_heatseeker_info;
 
 /* BoostPadState, src/Sim/BoostPad/BoostPad.h:23-35 */
 typedef struct rsg_pad_state {
@@ -328,6 +336,11 @@ int rsg_demolish_car(rsg_batch* batch, uint32_t arena, uint32_t car_id, float re
 /* Ball::GetState / Ball::SetState (Ball.cpp:27-51) */
 int rsg_get_ball_state(rsg_batch* batch, uint32_t arena, rsg_ball_state* out);
 int rsg_set_ball_state(rsg_batch* batch, uint32_t arena, const rsg_ball_state* state);
+/* BallState::hsInfo (Ball.h:24-32), the heatseeker part of GetState / SetState: rsg_set_ball_state
+ * resets it to a default BallState's (no target, 2900 uu/s, 0 s), as Ball::SetState does with a
+ * fresh state; set it afterwards to carry it over.  Soccar arenas keep the default. */
+int rsg_get_ball_heatseeker(rsg_batch* batch, uint32_t arena, rsg_heatseeker_info* out);
+int rsg_set_ball_heatseeker(rsg_batch* batch, uint32_t arena, const rsg_heatseeker_info* in);
 /* BoostPad::GetState / SetState (BoostPad.h:44-45); pad order of Arena.cpp:514-531 */
 int rsg_get_pad_state(rsg_batch* batch, uint32_t arena, uint32_t pad, rsg_pad_state* out);
 int rsg_set_pad_state(rsg_batch* batch, uint32_t arena, uint32_t pad, const rsg_pad_state* state);

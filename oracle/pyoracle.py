@@ -301,6 +301,20 @@ class SimArena:
         self.lib[self.p + "wheel_debug"](self.h, car_id, buf)
         return [list(buf[i * 16:(i + 1) * 16]) for i in range(4)]
 
+    def ball_heatseeker(self) -> tuple[float, float, float]:
+        """BallState::hsInfo (yTargetDir, curTargetSpeed, timeSinceHit); reference library only."""
+        fn = self.lib[self.p + "get_ball_hs"]
+        fn.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+        out = (C.c_float * 3)()
+        assert fn(self.h, out) == 0
+        return tuple(float(x) for x in out)
+
+    def set_ball_heatseeker(self, hs) -> None:
+        """Ball::SetState with the ball's state and the given hsInfo; reference library only."""
+        fn = self.lib[self.p + "set_ball_hs"]
+        fn.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+        assert fn(self.h, (C.c_float * 3)(*hs)) == 0
+
     def serialize(self) -> bytes:
         """Arena::Serialize (reference library only)."""
         fn = self.lib[self.p + "serialize"]

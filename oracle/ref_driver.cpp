@@ -143,6 +143,7 @@ int rsref_init(const uint8_t* cmf, uint64_t len) {
     std::map<GameMode, std::vector<FileData>> m;
     FileData fd(cmf, cmf + len);
     m[GameMode::SOCCAR].push_back(fd);
+    m[GameMode::HEATSEEKER].push_back(fd);  // heatseeker plays in the soccar arena
     try {
         RocketSim::InitFromMem(m, true);
     } catch (...) {
@@ -694,5 +695,29 @@ int rsref_debug_subsimplex(void* h, const float* in6, uint32_t car_id, float* ou
         n++;
     }
     return n;
+}
+}
+
+extern "C" {
+// BallState::hsInfo of the arena's ball: yTargetDir, curTargetSpeed, timeSinceHit (test aid).
+int rsref_get_ball_hs(void* h, float* out3) {
+    BallState st = ((RefArena*)h)->arena->ball->GetState();
+    out3[0] = st.hsInfo.yTargetDir;
+    out3[1] = st.hsInfo.curTargetSpeed;
+    out3[2] = st.hsInfo.timeSinceHit;
+    return 0;
+}
+}
+
+extern "C" {
+// Sets BallState::hsInfo through Ball::SetState with the ball's current state (test aid).
+int rsref_set_ball_hs(void* h, const float* in3) {
+    Ball* ball = ((RefArena*)h)->arena->ball;
+    BallState st = ball->GetState();
+    st.hsInfo.yTargetDir = in3[0];
+    st.hsInfo.curTargetSpeed = in3[1];
+    st.hsInfo.timeSinceHit = in3[2];
+    ball->SetState(st);
+    return 0;
 }
 }

@@ -14,7 +14,7 @@ from . import build as _build
 
 OK = 0
 ERR_ARG, ERR_STATE, ERR_CUDA, ERR_MESH, ERR_DEVICE = -1, -2, -3, -4, -5
-GAMEMODE_SOCCAR, GAMEMODE_THE_VOID = 0, 5
+GAMEMODE_SOCCAR, GAMEMODE_HEATSEEKER, GAMEMODE_THE_VOID = 0, 2, 5
 TEAM_BLUE, TEAM_ORANGE = 0, 1
 CAR_OCTANE, CAR_DOMINUS, CAR_PLANK, CAR_BREAKOUT, CAR_HYBRID, CAR_MERC = range(6)
 MAX_CARS_PER_ARENA = 8
@@ -65,6 +65,10 @@ class CarState(C.Structure):
         ("is_demoed", C.c_uint8), ("_pad5", C.c_uint8 * 3), ("demo_respawn_timer", C.c_float),
         ("ball_hit_info", BallHitInfo), ("last_controls", CarControls),
     ]
+
+
+class HeatseekerInfo(C.Structure):
+    _fields_ = [("y_target_dir", C.c_float), ("cur_target_speed", C.c_float), ("time_since_hit", C.c_float)]
 
 
 class BallState(C.Structure):
@@ -161,6 +165,8 @@ PROTOTYPES = {
     "rsg_demolish_car": (i32, [vp, u32, u32, f32]),
     "rsg_get_ball_state": (i32, [vp, u32, P(BallState)]),
     "rsg_set_ball_state": (i32, [vp, u32, P(BallState)]),
+    "rsg_get_ball_heatseeker": (i32, [vp, u32, P(HeatseekerInfo)]),
+    "rsg_set_ball_heatseeker": (i32, [vp, u32, P(HeatseekerInfo)]),
     "rsg_get_pad_state": (i32, [vp, u32, u32, P(PadState)]),
     "rsg_set_pad_state": (i32, [vp, u32, u32, P(PadState)]),
     "rsg_get_pad_config": (i32, [vp, u32, P(Vec3), P(i32)]),

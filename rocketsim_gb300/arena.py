@@ -213,6 +213,15 @@ class ArenaBatch:
     def set_ball_state(self, arena: int, state: BallState) -> None:
         check(self.lib.rsg_set_ball_state(self.h, arena, C.byref(state)), "rsg_set_ball_state")
 
+    def get_ball_heatseeker(self, arena: int) -> "abi.HeatseekerInfo":
+        """BallState::hsInfo: (y_target_dir, cur_target_speed, time_since_hit)."""
+        s = abi.HeatseekerInfo()
+        check(self.lib.rsg_get_ball_heatseeker(self.h, arena, C.byref(s)), "rsg_get_ball_heatseeker")
+        return s
+
+    def set_ball_heatseeker(self, arena: int, info: "abi.HeatseekerInfo") -> None:
+        check(self.lib.rsg_set_ball_heatseeker(self.h, arena, C.byref(info)), "rsg_set_ball_heatseeker")
+
     def get_pad_state(self, arena: int, pad: int) -> PadState:
         s = PadState()
         check(self.lib.rsg_get_pad_state(self.h, arena, pad, C.byref(s)), "rsg_get_pad_state")

@@ -381,7 +381,8 @@ CarCfgDev car_config_derived(const rsg_car_config& c) { return derive_config(c);
 
 // MutatorConfig(GameMode) (src/Sim/MutatorConfig/MutatorConfig.cpp:5-40, defaults in MutatorConfig.h:16-79)
 // for the game modes the batch supports (soccar and THE_VOID share them).
-rsg_mutator_config default_mutators(int /*game_mode*/) {
+// MutatorConfig(gameMode) (src/Sim/MutatorConfig/MutatorConfig.cpp:5-40)
+rsg_mutator_config default_mutators(int game_mode) {
     rsg_mutator_config m;
     std::memset(&m, 0, sizeof(m));
     m.gravity = rsg_vec3{0, 0, RL::GRAVITY_Z};
@@ -410,6 +411,10 @@ rsg_mutator_config default_mutators(int /*game_mode*/) {
     m.recharge_boost_delay = RL::RECHARGE_BOOST_DELAY;
     m.demo_mode = 0;
     m.goal_base_threshold_y = RL::SOCCAR_GOAL_SCORE_BASE_THRESHOLD_Y;
+    if (game_mode == RSG_GAMEMODE_HEATSEEKER) {  // infinite boost
+        m.car_spawn_boost_amount = 100;
+        m.boost_used_per_second = 0;
+    }
     return m;
 }
 
@@ -689,7 +694,7 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         }
         cfg = c;
     }
-    if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_THE_VOID) {
+    if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_HEATSEEKER && game_mode != RSG_GAMEMODE_THE_VOID) {
         fail(RSG_ERR_ARG, "game mode not supported (soccar and the void only)");
         return nullptr;
     }
@@ -702,7 +707,8 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         fail(RSG_ERR_ARG, "tick rate must be 15..120");
         return nullptr;
     }
-    bool arena = game_mode == RSG_GAMEMODE_SOCCAR;
+    // heatseeker plays in the soccar arena (the same collision meshes, pads and goals)
+    bool arena = game_mode == RSG_GAMEMODE_SOCCAR || game_mode == RSG_GAMEMODE_HEATSEEKER;
     if (arena && !g_soccar.ready) {
         fail(RSG_ERR_STATE, "no soccar mesh loaded (rsg_init_from_mem)");
         return nullptr;
@@ -741,6 +747,7 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
     B.A = (int)n_arenas;
     B.MC = (int)max_cars_per_arena;
     B.has_arena = arena ? 1 : 0;
+    B.heatseeker = game_mode == RSG_GAMEMODE_HEATSEEKER ? 1 : 0;
     B.dt = 1.f / tick_rate;
     b->mutators = default_mutators(game_mode);
     B.mut = mutators_dev(b->mutators);
@@ -852,7 +859,7 @@ static_assert(sizeof(rsg_mutator_config) == 116, "rsg_mutator_config layout");
 
 int rsg_get_default_mutator_config(int game_mode, rsg_mutator_config* out) {
     if (!out) return fail(RSG_ERR_ARG, "null output");
-    if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_THE_VOID)
+    if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_HEATSEEKER && game_mode != RSG_GAMEMODE_THE_VOID)
         return fail(RSG_ERR_ARG, "game mode not supported (soccar and THE_VOID are)");
     *out = default_mutators(game_mode);
     return RSG_OK;
@@ -1119,6 +1126,34 @@ int rsg_set_ball_state(rsg_batch* b, uint32_t arena, const rsg_ball_state* in) {
     RSG_CUDA(cudaMemcpyAsync(st + sizeof(rsg_ball_state), &arena, 4, cudaMemcpyHostToDevice, b->stream));
     RSG_CUDA(launch_set_balls(b->buf, (const uint32_t*)(st + sizeof(rsg_ball_state)), 1, (const rsg_ball_state*)st,
                               b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return RSG_OK;
+}
+
+// BallState::hsInfo (src/Sim/Ball/Ball.h:24-32) of one arena: the three floats of its record.
+int rsg_get_ball_heatseeker(rsg_batch* b, uint32_t arena, rsg_heatseeker_info* out) {
+    int rc;
+    if ((rc = check_arena(b, arena))) return rc;
+    if (!out) return fail(RSG_ERR_ARG, "null output");
+    if ((rc = set_device(b))) return rc;
+    const uint32_t* src = b->buf.rec + (size_t)arena * rec_words(b->buf.MC) + rec_ball_f(BF_HS_DIR);
+    float v[3];
+    RSG_CUDA(cudaMemcpyAsync(v, src, sizeof(v), cudaMemcpyDeviceToHost, b->stream));
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    out->y_target_dir = v[0];
+    out->cur_target_speed = v[1];
+    out->time_since_hit = v[2];
+    return RSG_OK;
+}
+
+int rsg_set_ball_heatseeker(rsg_batch* b, uint32_t arena, const rsg_heatseeker_info* in) {
+    int rc;
+    if ((rc = check_arena(b, arena))) return rc;
+    if (!in) return fail(RSG_ERR_ARG, "null input");
+    if ((rc = set_device(b))) return rc;
+    uint32_t* dst = b->buf.rec + (size_t)arena * rec_words(b->buf.MC) + rec_ball_f(BF_HS_DIR);
+    const float v[3] = {in->y_target_dir, in->cur_target_speed, in->time_since_hit};
+    RSG_CUDA(cudaMemcpyAsync(dst, v, sizeof(v), cudaMemcpyHostToDevice, b->stream));
     RSG_CUDA(cudaStreamSynchronize(b->stream));
     return RSG_OK;
 }
@@ -1561,9 +1596,11 @@ int rsg_serialize_arena(rsg_batch* b, uint32_t arena, uint8_t* out, uint64_t cap
     }
     rsg_ball_state bs;
     if ((rc = rsg_get_ball_state(b, arena, &bs))) return rc;
-    o.group(12);  // BallState::Serialize (Ball.cpp:19-21): soccar has no heatseeker / dropshot state
+    rsg_heatseeker_info hs;
+    if ((rc = rsg_get_ball_heatseeker(b, arena, &hs))) return rc;
+    o.group(12);  // BallState::Serialize (Ball.cpp:19-21); no dropshot state here
     o.vec(bs.pos); o.rot(bs.rot_mat); o.vec(bs.vel); o.vec(bs.ang_vel);
-    o.w(0.f); o.w(2900.f); o.w(0.f);        // hsInfo: yTargetDir, curTargetSpeed (INITIAL_TARGET_SPEED), timeSinceHit
+    o.w(hs.y_target_dir); o.w(hs.cur_target_speed); o.w(hs.time_since_hit);  // hsInfo
     o.w<int32_t>(1); o.w(0.f); o.w(0.f);    // dsInfo: chargeLevel, accumulatedHitForce, yTargetDir
     o.u8(0); o.w<uint64_t>(0);              // dsInfo: hasDamaged, lastDamageTick
     put_mutators(o, b->mutators);
@@ -1683,9 +1720,11 @@ static int deserialize_impl(rsg_batch* b, uint32_t arena, const uint8_t* data, u
         }
     }
     rsg_ball_state bs{};
+    rsg_heatseeker_info hs{0.f, RL::HS::INITIAL_TARGET_SPEED, 0.f};
     if (in.group(12)) {
         bs.pos = in.vec(); bs.rot_mat = in.rot(); bs.vel = in.vec(); bs.ang_vel = in.vec();
-        in.r<float>(); in.r<float>(); in.r<float>(); in.r<int32_t>(); in.r<float>(); in.r<float>(); in.u8();
+        hs.y_target_dir = in.r<float>(); hs.cur_target_speed = in.r<float>(); hs.time_since_hit = in.r<float>();
+        in.r<int32_t>(); in.r<float>(); in.r<float>(); in.u8();
         in.r<uint64_t>();
     }
     rsg_mutator_config mut;
@@ -1709,6 +1748,7 @@ static int deserialize_impl(rsg_batch* b, uint32_t arena, const uint8_t* data, u
     for (size_t i = 0; i < pad_states.size(); i++)
         if ((rc = rsg_set_pad_state(b, arena, (uint32_t)i, &pad_states[i]))) return rc;
     if ((rc = rsg_set_ball_state(b, arena, &bs))) return rc;
+    if ((rc = rsg_set_ball_heatseeker(b, arena, &hs))) return rc;
     return rsg_set_tick_count(b, arena, tick);
 }
 
@@ -1732,11 +1772,14 @@ int rsg_clone_arena(rsg_batch* dst, uint32_t dst_arena, rsg_batch* src, uint32_t
     for (size_t k = 0; k < ids.size(); k++)
         if ((rc = rsg_get_car_state(src, src_arena, ids[k], &states[k]))) return rc;
     rsg_ball_state bs;
+    rsg_heatseeker_info hs;
     if ((rc = rsg_get_ball_state(src, src_arena, &bs))) return rc;
+    if ((rc = rsg_get_ball_heatseeker(src, src_arena, &hs))) return rc;
     if ((rc = deserialize_impl(dst, dst_arena, buf.data(), n, false))) return rc;
     for (size_t k = 0; k < ids.size(); k++)
         if ((rc = rsg_set_car_state(dst, dst_arena, ids[k], &states[k]))) return rc;
-    return rsg_set_ball_state(dst, dst_arena, &bs);
+    if ((rc = rsg_set_ball_state(dst, dst_arena, &bs))) return rc;
+    return rsg_set_ball_heatseeker(dst, dst_arena, &hs);
 }
 
 }  // extern "C"
@@ -1790,12 +1833,18 @@ extern "C" {
 // orange cars mirrored; the ball at rest at the centre and every pad reset.
 int rsg_reset_to_random_kickoff_many(rsg_batch* b, const uint32_t* arenas, const int32_t* seeds, uint32_t n) {
     if (!b || (n && !arenas)) return fail(RSG_ERR_ARG, "null batch or arena list");
-    if (b->game_mode != RSG_GAMEMODE_SOCCAR) return fail(RSG_ERR_STATE, "kickoffs need the soccar arena");
+    const bool hs = b->game_mode == RSG_GAMEMODE_HEATSEEKER;
+    if (b->game_mode != RSG_GAMEMODE_SOCCAR && !hs) return fail(RSG_ERR_STATE, "kickoffs need the soccar arena");
     static const float SPAWN[5][3] = {{-2048, -2560, (float)(M_PI_4 * 1)}, {2048, -2560, (float)(M_PI_4 * 3)},
                                       {-256, -3840, (float)(M_PI_4 * 2)}, {256, -3840, (float)(M_PI_4 * 2)},
                                       {0, -4608, (float)(M_PI_4 * 2)}};
     static const float RESPAWN[4][3] = {{-2304, -4608, (float)(M_PI / 2)}, {-2688, -4608, (float)(M_PI / 2)},
                                         {2304, -4608, (float)(M_PI / 2)}, {2688, -4608, (float)(M_PI / 2)}};
+    // CAR_SPAWN_LOCATIONS_HEATSEEKER (src/RLConst.h:364-370): four spots, the soccar respawn spots past them
+    static const float SPAWN_HS[4][3] = {{-1000, -4620, (float)(M_PI / 2)}, {1000, -4620, (float)(M_PI / 2)},
+                                         {-2000, -4620, (float)(M_PI / 2)}, {2000, -4620, (float)(M_PI / 2)}};
+    const int nloc = hs ? 4 : 5;
+    std::vector<float> ball_side(n, 1.f);
     const int MC = b->buf.MC;
     std::vector<uint32_t> idx;
     std::vector<rsg_car_state> cars;
@@ -1805,12 +1854,11 @@ int rsg_reset_to_random_kickoff_many(rsg_batch* b, const uint32_t* arenas, const
         if (rc) return rc;
         int order[5] = {0, 1, 2, 3, 4};
         const int32_t seed = seeds ? seeds[k] : -1;
-        if (seed == -1) {
-            shuffle5(order, 5, process_engine());
-        } else {
-            MinStd0 g((int64_t)seed);
-            shuffle5(order, 5, g);
-        }
+        MinStd0 local((int64_t)(seed == -1 ? 1 : seed));
+        MinStd0& g = seed == -1 ? process_engine() : local;
+        shuffle5(order, nloc, g);
+        // heatseeker's ball starts on the side of the next draw of the same engine (Arena.cpp:200-204)
+        if (hs) ball_side[k] = ((int)g() % 2) ? 1.f : -1.f;
         std::vector<int> team_slots[2];
         for (uint32_t p = 0; p < b->ncars[ar]; p++) {
             const int slot = b->order[(size_t)ar * MC + p];
@@ -1820,11 +1868,11 @@ int rsg_reset_to_random_kickoff_many(rsg_batch* b, const uint32_t* arenas, const
         const int npos = (int)std::max(team_slots[0].size(), team_slots[1].size());
         for (int i = 0; i < npos; i++) {
             float x, y, yaw;
-            if (i < 5) {
-                const float* sp = SPAWN[std::min(order[i], 4)];
+            if (i < nloc) {
+                const float* sp = hs ? SPAWN_HS[std::min(order[i], nloc - 1)] : SPAWN[std::min(order[i], nloc - 1)];
                 x = sp[0]; y = sp[1]; yaw = sp[2];
             } else {
-                const int r = (i - 5) % 5;
+                const int r = (i - nloc) % nloc;
                 const float* sp = RESPAWN[r < 4 ? r : 3];
                 x = sp[0]; y = sp[1]; yaw = sp[2];
                 if (r < 4) y += 250.f * at_respawn[r]++;
@@ -1853,10 +1901,17 @@ int rsg_reset_to_random_kickoff_many(rsg_batch* b, const uint32_t* arenas, const
     int rc;
     if ((rc = set_device(b))) return rc;
     std::vector<rsg_ball_state> balls(n);
-    for (auto& bs : balls) {
+    for (uint32_t k = 0; k < n; k++) {
+        rsg_ball_state& bs = balls[k];
         std::memset(&bs, 0, sizeof(bs));
         bs.pos.z = RL::BALL_REST_Z;
         bs.rot_mat.forward.x = bs.rot_mat.right.y = bs.rot_mat.up.z = 1;
+        if (hs) {  // Heatseeker::BALL_START_POS / BALL_START_VEL (RLConst.h:186-188), y flipped by the side
+            const float* p = RL::HS::BALL_START_POS;
+            const float* v = RL::HS::BALL_START_VEL;
+            bs.pos = rsg_vec3{p[0] * 1, p[1] * ball_side[k], p[2] * 1};
+            bs.vel = rsg_vec3{v[0] * 1, v[1] * ball_side[k], v[2] * 1};
+        }
     }
     std::vector<rsg_pad_state> pads((size_t)n * b->buf.npads);
     for (auto& ps : pads) {
@@ -2055,6 +2110,10 @@ extern "C" {
 
 rsg_ball_pred* rsg_ball_pred_create(rsg_batch* src, uint32_t num_pred_ticks) {
     if (!src) { fail(RSG_ERR_ARG, "null batch"); return nullptr; }
+    if (src->game_mode == RSG_GAMEMODE_HEATSEEKER) {  // the prediction inputs carry no heatseeker state
+        fail(RSG_ERR_STATE, "ball prediction supports soccar and the void");
+        return nullptr;
+    }
     if (num_pred_ticks == 0 || num_pred_ticks > (1u << 20)) {
         fail(RSG_ERR_ARG, "num_pred_ticks must be 1..1048576");
         return nullptr;

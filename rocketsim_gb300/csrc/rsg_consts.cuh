@@ -27,6 +27,17 @@ constexpr float BOOST_ACCEL_GROUND = 2975 / 3.f, BOOST_ACCEL_AIR = 3175 / 3.f, B
 constexpr float CAR_MAX_ANG_SPEED = 5.5f;
 constexpr float SUPERSONIC_START_SPEED = 2200.f, SUPERSONIC_MAINTAIN_MIN_SPEED = SUPERSONIC_START_SPEED - 100.f;
 constexpr float SUPERSONIC_MAINTAIN_MAX_TIME = 1.f;
+constexpr float ARENA_EXTENT_Y = 5120;
+// Heatseeker (src/RLConst.h:168-190)
+namespace HS {
+constexpr float INITIAL_TARGET_SPEED = 2900, TARGET_SPEED_INCREMENT = 85, MIN_SPEEDUP_INTERVAL = 1;
+constexpr float TARGET_Y = 5120, TARGET_Z = 320, HORIZONTAL_BLEND = 1.45f, VERTICAL_BLEND = 0.78f,
+                SPEED_BLEND = 0.3f;
+constexpr float MAX_TURN_PITCH = (float)(7000 * 3.14159265358979323846 / (1 << 15)), MAX_SPEED = 4600;
+constexpr float WALL_BOUNCE_CHANGE_Y_THRESH = 300, WALL_BOUNCE_CHANGE_Y_NORMAL = 0.5f,
+                WALL_BOUNCE_FORCE_SCALE = 1 / 3.f, WALL_BOUNCE_UP_FRAC = 0.3f;
+constexpr float BALL_START_POS[3] = {-1000, -2220, 92.75f}, BALL_START_VEL[3] = {0, -65, 650};
+}  // namespace HS
 constexpr float POWERSLIDE_RISE_RATE = 5, POWERSLIDE_FALL_RATE = 2;
 constexpr float THROTTLE_TORQUE_AMOUNT = CAR_MASS_BT * 400.f;
 constexpr float BRAKE_TORQUE_AMOUNT = CAR_MASS_BT * (14.25f + (1.f / 3.f));

@@ -618,6 +618,7 @@ __global__ void rsg_init_arenas_kernel(BatchView bv, uint32_t ball_cell, uint32_
     SoA s{bv, ar};
     V3 p = V3(0, 0, RL::BALL_REST_Z) * RL::UU_TO_BT;
     for (int f = 0; f < BF_COUNT; f++) s.bf(f) = 0.f;
+    s.bf(BF_HS_SPEED) = RL::HS::INITIAL_TARGET_SPEED;
     s.bf(BF_POS) = p.x; s.bf(BF_POS + 1) = p.y; s.bf(BF_POS + 2) = p.z;
     s.bf(BF_BASIS + 0) = 1.f; s.bf(BF_BASIS + 4) = 1.f; s.bf(BF_BASIS + 8) = 1.f;
     s.bu(BU_CELL) = ball_cell;

@@ -31,6 +31,7 @@ struct BatchBuffers {
     MutatorsDev mut;
     const float4* pad_cfg;  // [npads] position (uu), is_big
     int npads, custom_pads, no_ball_rot;
+    int heatseeker;  // GameMode::HEATSEEKER: the ball seeks a goal (Ball::_PreTickUpdate)
     uint32_t* rec;  // A records of rec_words(MC) 32-bit words
     uint32_t* au;   // [AU_COUNT][A]
     const CarCfgDev* cfgs;

@@ -97,7 +97,9 @@ enum CarU : int {
 };
 
 // ---- ball (per arena)
-enum BallF : int { BF_POS = 0, BF_BASIS = 3, BF_VEL = 12, BF_ANG = 15, BF_COUNT = 18 };
+// BF_HS_*: BallState::HeatseekerInfo (src/Sim/Ball/Ball.h:24-32): yTargetDir, curTargetSpeed, timeSinceHit
+enum BallF : int { BF_POS = 0, BF_BASIS = 3, BF_VEL = 12, BF_ANG = 15, BF_HS_DIR = 18, BF_HS_SPEED = 19, BF_HS_TIME = 20,
+                   BF_COUNT = 21 };
 enum BallU : int { BU_CELL = 0, BU_CELL_SEQ = 1, BU_TICKS_LO = 2, BU_TICKS_HI = 3, BU_COUNT = 4 };
 
 // ---- pads (per arena and pad)
@@ -137,7 +139,7 @@ constexpr int PAD_WORDS = 4;   // cooldown (f32), then PadU fields
 constexpr int CAR_WORDS = 96;  // CarF floats, then CarU words, one spare
 constexpr int REC_BALL = 0;
 constexpr int REC_PADS = REC_BALL + BF_COUNT + BU_COUNT;
-constexpr int REC_CARS = 160;
+constexpr int REC_CARS = 168;
 static_assert(REC_PADS + NUM_PADS * PAD_WORDS <= REC_CARS, "record layout");
 static_assert(CF_COUNT + CU_COUNT <= CAR_WORDS, "car block");
 RSG_LAYOUT_FN int rec_words(int max_cars) { return REC_CARS + CAR_WORDS * max_cars; }

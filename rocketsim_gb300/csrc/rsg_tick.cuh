@@ -106,6 +106,7 @@ struct BatchView {
     const float4* pad_cfg;  // per pad: position (uu) and is_big (ArenaConfig's pads or the soccar ones)
     int npads, custom_pads;  // pad count; custom pads skip BoostPadGrid (Arena.cpp:724-731)
     int no_ball_rot;         // ArenaConfig::noBallRot
+    int heatseeker;          // GameMode::HEATSEEKER
     int lanes_per_car;       // threads per car in the vehicle update after the rays (1, 2 or 4)
     uint32_t* rec;  // A records of rec_words(MC) words
     int rec_words;
@@ -236,6 +237,7 @@ struct Ctx {
     Car* cars;
     Body ball;
     V3 ball_cache;
+    float hs_dir, hs_speed, hs_time;  // BallState::hsInfo (heatseeker)
     Pad* pads;
     uint64_t tick;
     uint32_t seq;
@@ -2548,6 +2550,15 @@ RSG_DN void contact_added(const BatchView& bv, Ctx& a, Manifold& m, int idx, int
                     car.bhi_extra = added;
                     a.ball_cache += added * RL::UU_TO_BT;
                 }
+                if (bv.heatseeker) {  // Ball.cpp:291-299: the touching car's team sets the target net
+                    bool can_increase = (a.hs_time > RL::HS::MIN_SPEEDUP_INTERVAL) || (a.hs_dir == 0);
+                    float new_dir = car.f(F_TEAM_ORANGE) ? -1.f : 1.f;
+                    if (can_increase && (new_dir != a.hs_dir)) {
+                        a.hs_time = 0;
+                        a.hs_speed = rs_minf(a.hs_speed + RL::HS::TARGET_SPEED_INCREMENT, RL::HS::MAX_SPEED);
+                    }
+                    a.hs_dir = new_dir;
+                }
             }
         } else if (ub == 1) {
             // car-car: Arena::_BtCallback_OnCarCarCollision (src/Sim/Arena/Arena.cpp:323-405)
@@ -2601,7 +2612,22 @@ RSG_DN void contact_added(const BatchView& bv, Ctx& a, Manifold& m, int idx, int
             cp.restitution = bv.mut.car_world_restitution;
         }
     } else if (ua == 2 && ub == -1) {
-        cp.special = true;  // ball-world (src/Sim/Arena/Arena.cpp:298-306)
+        // ball-world (src/Sim/Arena/Arena.cpp:298-306): Ball::_OnWorldCollision, then special
+        if (bv.heatseeker && a.hs_dir != 0) {  // Ball.cpp:326-357: a back-wall bounce turns the target around
+            const V3 pos = a.ball.xf.o * RL::BT_TO_UU;
+            const float rel_normal_y = cp.normal.y * a.hs_dir, rel_y = pos.y * a.hs_dir;
+            if (rel_normal_y <= -RL::HS::WALL_BOUNCE_CHANGE_Y_NORMAL &&
+                rel_y >= RL::ARENA_EXTENT_Y - RL::HS::WALL_BOUNCE_CHANGE_Y_THRESH) {
+                a.hs_dir *= -1;
+                const V3 vel = a.ball.lin_vel * RL::BT_TO_UU;
+                const V3 goal(0, RL::HS::TARGET_Y * a.hs_dir, RL::HS::TARGET_Z);
+                const V3 to_goal = rs_normalized(goal - pos);
+                const V3 dir = to_goal * (1 - RL::HS::WALL_BOUNCE_UP_FRAC) + V3(0, 0, 1) * RL::HS::WALL_BOUNCE_UP_FRAC;
+                const V3 imp = dir * rs_len(vel) * RL::HS::WALL_BOUNCE_FORCE_SCALE;
+                a.ball_cache += imp * RL::UU_TO_BT;
+            }
+        }
+        cp.special = true;
     }
 #if defined(RSG_PHASE_TIMERS)
     long long ie_ = clock64();
@@ -3193,9 +3219,72 @@ RSG_D Manifold& new_manifold(Ctx& a, int b0, int b1, float breaking) {
 // Phase 1 of a world step, one lane per dynamic object (ball = lane 0, cars = lanes 1..): gravity,
 // damping and predicted transform, broadphase AABB and voxel cell.  Cell changes take their sequence
 // numbers in object order (a ballot prefix count), like the reference's serial AABB update.
+// Angle::FromVec (src/Math/MathTypes/MathTypes.cpp:80-100): yaw and pitch of a direction
+RSG_D void angle_from_vec(V3 f, float& yaw, float& pitch) {
+    if (fabsf(f.y) > FLT_EPSILON || fabsf(f.x) > FLT_EPSILON) {
+        yaw = atan2f(f.y, f.x);
+        float dist2d = sqrtf(f.x * f.x + f.y * f.y);
+        pitch = -atan2f(-f.z, dist2d);
+    } else {
+        yaw = 0;
+        if (f.z > FLT_EPSILON) pitch = (float)(3.14159265358979323846 / 2);
+        else if (f.z < -FLT_EPSILON) pitch = (float)(-3.14159265358979323846 / 2);
+        else pitch = 0;
+    }
+}
+// Math::WrapNormalizeFloat (src/Math/Math.cpp:66-73)
+RSG_D float wrap_normalize(float val, float minmax) {
+    float r = fmodf(val, minmax * 2);
+    if (r > minmax) r -= minmax * 2;
+    else if (r < -minmax) r += minmax * 2;
+    return r;
+}
+// Math::RoundAngleUE3 (src/Math/Math.cpp:75-91): to UE3 rotator units, the low two bits dropped
+RSG_D float round_angle_ue3(float ang) {
+    const float TO_INTS = (float)((float)(1 << 15) / 3.14159265358979323846);
+    const float BACK_TO_RADIANS = (1.f / TO_INTS) * 4.f;
+    int r = ((int)(ang * TO_INTS) >> 2) & (0x4000 - 1);
+    return r * BACK_TO_RADIANS;
+}
+
+// Ball::_PreTickUpdate for heatseeker (src/Sim/Ball/Ball.cpp:161-207): once a touch has given the
+// ball a target net, it turns towards it and blends its speed towards the target speed.
+RSG_D void ball_pre_tick_heatseeker(const BatchView& bv, Ctx& a) {
+    if (a.hs_dir == 0) return;
+    Body& b = a.ball;
+    const V3 pos = b.xf.o * RL::BT_TO_UU, vel = b.lin_vel * RL::BT_TO_UU;
+    float vyaw, vpitch, gyaw, gpitch;
+    angle_from_vec(vel, vyaw, vpitch);
+    const V3 goal(0, RL::HS::TARGET_Y * a.hs_dir, RL::HS::TARGET_Z);
+    angle_from_vec(goal - pos, gyaw, gpitch);
+    // Angle::operator- is GetDeltaTo, which wraps the delta too (MathTypes.h:306-320)
+    const float dyaw = wrap_normalize(gyaw - vyaw, (float)3.14159265358979323846);
+    const float dpitch = wrap_normalize(gpitch - vpitch, (float)(3.14159265358979323846 / 2));
+    const float cur_speed = rs_len(vel);
+    const float speed_ratio = cur_speed / RL::HS::MAX_SPEED;
+    const float base = speed_ratio * bv.dt;
+    float yaw = vyaw + dyaw * base * RL::HS::HORIZONTAL_BLEND;
+    float pitch = vpitch + dpitch * base * RL::HS::VERTICAL_BLEND;
+    yaw = wrap_normalize(yaw, (float)3.14159265358979323846);  // Angle::NormalizeFix
+    pitch = wrap_normalize(pitch, (float)(3.14159265358979323846 / 2));
+    pitch = rs_clampf(pitch, -RL::HS::MAX_TURN_PITCH, RL::HS::MAX_TURN_PITCH);
+    yaw = round_angle_ue3(yaw);
+    pitch = round_angle_ue3(pitch);
+    const float new_speed = cur_speed + ((a.hs_speed - cur_speed) * RL::HS::SPEED_BLEND);
+    // Angle::GetForwardVec (MathTypes.cpp:102-110)
+    const float cp = cosf(-pitch), cy = cosf(yaw), sy = sinf(yaw), sp = sinf(-pitch);
+    const V3 dir(cp * cy, cp * sy, -sp);
+    b.lin_vel = (dir * new_speed) * RL::UU_TO_BT;
+    a.hs_time += bv.dt;
+}
+
 RSG_D void step_bodies_pre(const BatchView& bv, Ctx& a, int lane) {
     const float dt = bv.dt;
     const int nd = 1 + a.ncars;
+    if (bv.heatseeker) {  // Ball::_PreTickUpdate runs after the cars' and pads' (Arena.cpp:705-716)
+        if (lane == 0) ball_pre_tick_heatseeker(bv, a);
+        __syncwarp();
+    }
     bool changed = false;
     if (lane < nd) {
         Body& b = a.body(OBJ_BALL + lane);
@@ -4349,6 +4438,9 @@ RSG_DN void load_arena(const BatchView& bv, int ar, Ctx& a) {  // scalars and ba
     body_common(b);
     a.ball_ticks = (uint64_t)s.bu(BU_TICKS_LO) | ((uint64_t)s.bu(BU_TICKS_HI) << 32);
     a.ball_cache = V3(0, 0, 0);
+    a.hs_dir = s.bf(BF_HS_DIR);
+    a.hs_speed = s.bf(BF_HS_SPEED);
+    a.hs_time = s.bf(BF_HS_TIME);
     // cars (Car::_BulletSetup, src/Sim/Car/Car.cpp:195-292, derived per config on the host)
 }
 
@@ -4447,6 +4539,9 @@ RSG_DN void store_arena(const BatchView& bv, int ar, Ctx& a) {
     s.bu(BU_CELL_SEQ) = b.cell_seq;
     s.bu(BU_TICKS_LO) = (uint32_t)a.ball_ticks;
     s.bu(BU_TICKS_HI) = (uint32_t)(a.ball_ticks >> 32);
+    s.bf(BF_HS_DIR) = a.hs_dir;
+    s.bf(BF_HS_SPEED) = a.hs_speed;
+    s.bf(BF_HS_TIME) = a.hs_time;
 }
 
 RSG_DN void store_car(const BatchView& bv, int ar, Ctx& a, int i) {

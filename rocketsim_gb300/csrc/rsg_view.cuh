@@ -18,6 +18,7 @@ inline BatchView make_view(const BatchBuffers& b) {
     v.npads = b.npads;
     v.custom_pads = b.custom_pads;
     v.no_ball_rot = b.no_ball_rot;
+    v.heatseeker = b.heatseeker;
     v.lanes_per_car = 4;
     v.rec = b.rec;
     v.rec_words = rec_words(b.MC);
@@ -93,6 +94,10 @@ RSG_D void ball_set(const SoA& s, const rsg_ball_state& st) {
     }
     s.bf(BF_VEL) = v.x; s.bf(BF_VEL + 1) = v.y; s.bf(BF_VEL + 2) = v.z;
     s.bf(BF_ANG) = st.ang_vel.x; s.bf(BF_ANG + 1) = st.ang_vel.y; s.bf(BF_ANG + 2) = st.ang_vel.z;
+    // a default BallState's HeatseekerInfo (Ball.h:24-32)
+    s.bf(BF_HS_DIR) = 0.f;
+    s.bf(BF_HS_SPEED) = RL::HS::INITIAL_TARGET_SPEED;
+    s.bf(BF_HS_TIME) = 0.f;
     s.bu(BU_TICKS_LO) = 0;
     s.bu(BU_TICKS_HI) = 0;
 }

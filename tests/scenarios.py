@@ -161,12 +161,12 @@ def _controls_struct(row) -> abi.CarControls:
 
 
 # ---------------------------------------------------------------- CPU checkers
-def setup_cpu(kind: str, sc: Scenario, mutators=None, config=None):
+def setup_cpu(kind: str, sc: Scenario, mutators=None, config=None, game_mode: int = 0):
     """Builds the scenario on a SimArena of `kind` ('ref', 'oracle', 'oracle_sse'); `mutators` (an
     abi.MutatorConfig) is set before the cars are added and `config` (an abi.ArenaConfig) passed
     to Arena::Create, both for the reference only."""
     from oracle.pyoracle import SimArena, CarState as OCarState, BallState as OBallState, CarControls as OCtl
-    a = SimArena(kind, mesh_bytes(), config=config)
+    a = SimArena(kind, mesh_bytes(), game_mode=game_mode, config=config)
     if mutators is not None:
         a.set_mutator_config(mutators)
     ids = [a.add_car(t, p) for t, p in zip(sc.teams, sc.presets)]
@@ -206,13 +206,14 @@ def cpu_snapshot(a, ids):
 
 
 # ---------------------------------------------------------------- GPU
-def setup_gpu(scs: list[Scenario], max_cars: int | None = None, mutators=None, config=None):
+def setup_gpu(scs: list[Scenario], max_cars: int | None = None, mutators=None, config=None,
+              game_mode: int = abi.GAMEMODE_SOCCAR):
     """One ArenaBatch holding one arena per scenario (`mutators` set before the cars are added,
     `config` an abi.ArenaConfig for the batch)."""
     import rocketsim_gb300 as rsg
     rsg.init_from_mem([mesh_bytes()])
     mc = max_cars or max(len(s.cars) for s in scs)
-    batch = rsg.ArenaBatch(abi.GAMEMODE_SOCCAR, len(scs), mc, 120.0, config)
+    batch = rsg.ArenaBatch(game_mode, len(scs), mc, 120.0, config)
     if mutators is not None:
         batch.set_mutator_config(mutators)
     all_ids = []

@@ -38,7 +38,8 @@ def test_struct_layouts_match_header():
         pytest.skip("gcc not available")
     structs = {"rsg_car_state": abi.CarState, "rsg_ball_state": abi.BallState, "rsg_pad_state": abi.PadState,
                "rsg_car_controls": abi.CarControls, "rsg_car_config": abi.CarConfig,
-               "rsg_ball_hit_info": abi.BallHitInfo, "rsg_rotmat": abi.RotMat}
+               "rsg_ball_hit_info": abi.BallHitInfo, "rsg_rotmat": abi.RotMat,
+               "rsg_heatseeker_info": abi.HeatseekerInfo}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', 'int main(void) {']
     for cname, ct in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')

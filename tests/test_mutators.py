@@ -41,5 +41,6 @@ def test_default_mutators_match_the_reference():
     import rocketsim_gb300 as rsg
     ref = C.CDLL(REF_SO)
     m = abi.MutatorConfig()
-    assert ref.rsref_default_mutator_config(abi.GAMEMODE_SOCCAR, C.byref(m)) == 0
-    assert fields(m) == fields(rsg.default_mutator_config(abi.GAMEMODE_SOCCAR))
+    for mode in (abi.GAMEMODE_SOCCAR, abi.GAMEMODE_HEATSEEKER):
+        assert ref.rsref_default_mutator_config(mode, C.byref(m)) == 0
+        assert fields(m) == fields(rsg.default_mutator_config(mode)), mode
