@@ -394,7 +394,8 @@ def run_arena_leg(args, dev: int, A: int, mc: int, steps: int, warmup: int, sett
     shape = batch.tick_shape()
     out = {"value": value, "ms_per_step": total_ms / steps, "times_ms": times_ms, "clocks": clk,
            "tick_shape": {"arenas_per_block": shape[0], "lanes_per_car": shape[1], "header_cache": shape[2],
-                          "leaf_grid": shape[3], "collide_sync": shape[4], "tuner": batch.tuning_log()},
+                          "leaf_grid": shape[3], "collide_sync": shape[4], "persistent": shape[5],
+                          "tuner": batch.tuning_log()},
            "game_tick_first_timed": first_tick, "game_tick_last_timed": ticks_done,
            "ticks_per_s_vs_game_tick": [[t, round(v)] for t, v in settle_curve],
            "warn_flags_any": int(np.bitwise_or.reduce(flags)) if flags.size else 0, "arenas_reset": resets,

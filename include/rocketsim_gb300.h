@@ -594,11 +594,12 @@ int rsg_get_device_flags(rsg_batch* batch, uint32_t* out);
  * per car in the vehicle update, out[2] BVH subtree headers in shared memory (1) or
  * read through L2 (0; -1 automatic), out[3] wheel rays on the leaf grid (1) or
  * walking the BVH (0), out[4] block-wide barriers between the parts of the collision
- * work (1) or not (0).  Chosen by the tuner on the batch's first launch (every shape
- * gives the same results) or fixed by the environment variable RSG_TICK_SHAPE
- * (the numbers comma separated, the last one optional).  No counterpart in the
- * reference. */
-int rsg_get_tick_shape(const rsg_batch* batch, int32_t out[5]);
+ * work (1) or not (0), out[5] a persistent launch (as many blocks as are resident,
+ * each taking groups of arenas from a device counter, 1) or one block per group (0).
+ * Chosen by the tuner on the batch's first launch (every shape gives the same
+ * results) or fixed by the environment variable RSG_TICK_SHAPE (the numbers comma
+ * separated, the last two optional).  No counterpart in the reference. */
+int rsg_get_tick_shape(const rsg_batch* batch, int32_t out[6]);
 /* The tuner's trials as text (shapes and milliseconds per tick), NUL-terminated and
  * cut to buf_len.  No counterpart in the reference. */
 int rsg_get_tuning_log(const rsg_batch* batch, char* buf, uint64_t buf_len);

@@ -273,10 +273,10 @@ class ArenaBatch:
         return out
 
     # ---- stepping
-    def tick_shape(self) -> tuple[int, int, int, int, int]:
+    def tick_shape(self) -> tuple[int, int, int, int, int, int]:
         """Launch shape of the tick kernel (arenas per block, threads per car, header cache, leaf grid,
-        collision barriers)."""
-        out = (C.c_int32 * 5)()
+        collision barriers, persistent launch)."""
+        out = (C.c_int32 * 6)()
         check(self.lib.rsg_get_tick_shape(self.h, out), "rsg_get_tick_shape")
         return tuple(int(x) for x in out)
 

@@ -533,9 +533,10 @@ std::mutex g_tune_mu;
 std::map<TuneKey, std::pair<TickShape, std::string>> g_tune_cache;
 
 std::string shape_str(const TickShape& s) {
-    char buf[128];
-    std::snprintf(buf, sizeof(buf), "arenas_per_block=%d lanes_per_car=%d header_cache=%d leaf_grid=%d collide_sync=%d",
-                  s.arenas_per_block, s.lanes_per_car, s.header_cache, s.leaf_grid, s.collide_sync);
+    char buf[160];
+    std::snprintf(buf, sizeof(buf),
+                  "arenas_per_block=%d lanes_per_car=%d header_cache=%d leaf_grid=%d collide_sync=%d persistent=%d",
+                  s.arenas_per_block, s.lanes_per_car, s.header_cache, s.leaf_grid, s.collide_sync, s.persistent);
     return buf;
 }
 
@@ -601,8 +602,8 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
             return cudaSuccess;
         };
         const int per_arena = tick_smem_per_arena(B.MC);
-        for (int w = 8; w >= 4 && e == cudaSuccess; w--) {
-            if (w == best.arenas_per_block || per_arena * w > 227 * 1024) continue;
+        for (int w = TICK_MAX_ARENAS_PER_BLOCK; w >= 4 && e == cudaSuccess; w--) {
+            if (w == best.arenas_per_block || per_arena * w + 16 > 227 * 1024) continue;
             TickShape s = best;
             s.arenas_per_block = w;
             e = consider(s);
@@ -629,6 +630,11 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
         if (e == cudaSuccess) {
             TickShape s = best;
             s.collide_sync = best.collide_sync ? 0 : 1;
+            e = consider(s);
+        }
+        if (e == cudaSuccess) {
+            TickShape s = best;
+            s.persistent = best.persistent ? 0 : 1;
             e = consider(s);
         }
         if (e == cudaSuccess) e = copy_all(false);
@@ -695,7 +701,7 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         cfg = c;
     }
     if (game_mode != RSG_GAMEMODE_SOCCAR && game_mode != RSG_GAMEMODE_HEATSEEKER && game_mode != RSG_GAMEMODE_THE_VOID) {
-        fail(RSG_ERR_ARG, "game mode not supported (soccar and the void only)");
+        fail(RSG_ERR_ARG, "game mode not supported (soccar, heatseeker and the void only)");
         return nullptr;
     }
     if (n_arenas == 0 || n_arenas > (1u << 24)) { fail(RSG_ERR_ARG, "n_arenas out of range"); return nullptr; }
@@ -726,21 +732,22 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         fail(RSG_ERR_STATE, "the mesh was loaded on another device");
         return nullptr;
     }
-    if (const char* w = std::getenv("RSG_TICK_SHAPE")) {  // fixed shape "w,lanes,header,leafgrid[,sync]", no tuning
-        int v[5] = {8, 4, -1, 1, 1};
-        std::sscanf(w, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]);
+    if (const char* w = std::getenv("RSG_TICK_SHAPE")) {  // fixed shape "w,lanes,header,leafgrid[,sync[,persistent]]"
+        int v[6] = {TICK_MAX_ARENAS_PER_BLOCK, 4, -1, 1, 1, 0};
+        std::sscanf(w, "%d,%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5]);
         b->shape.arenas_per_block = v[0];
         b->shape.lanes_per_car = v[1];
         b->shape.header_cache = v[2];
         b->shape.leaf_grid = v[3];
         b->shape.collide_sync = v[4];
+        b->shape.persistent = v[5] ? 1 : 0;
         b->tune_pending = false;
     }
     {  // at most as many arenas per block as shared memory holds (launch_tick clamps the same way)
         const int per_arena = tick_smem_per_arena((int)max_cars_per_arena);
         int& w = b->shape.arenas_per_block;
-        if (w < 1 || w > 8) w = 8;
-        while (w > 1 && per_arena * w > 227 * 1024) w--;
+        if (w < 1 || w > TICK_MAX_ARENAS_PER_BLOCK) w = TICK_MAX_ARENAS_PER_BLOCK;
+        while (w > 1 && per_arena * w + 16 > 227 * 1024) w--;
     }
     if (!b->tune_pending) b->tune_log = "fixed by RSG_TICK_SHAPE: " + shape_str(b->shape);
     BatchBuffers& B = b->buf;
@@ -799,6 +806,8 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
     ok = ok && alloc(&B.events, (size_t)DEV_EVENT_BYTES * MAX_EVENTS_PER_ARENA * A);
     ok = ok && alloc((void**)&B.place, sizeof(uint32_t) * A);
     ok = ok && alloc((void**)&B.cost, sizeof(uint32_t) * A);
+    ok = ok && alloc((void**)&B.group_next, sizeof(uint32_t));
+    if (const size_t ts = tick_scratch_bytes((int)A, (int)MC)) ok = ok && alloc((void**)&B.tick_scratch, ts);
     if (!ok) {
         rsg_batch_destroy(b);
         return nullptr;
@@ -835,7 +844,8 @@ void rsg_batch_destroy(rsg_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     BatchBuffers& B = b->buf;
-    void* ptrs[] = {B.rec, B.au, B.events, B.place, B.cost, b->d_cfgs, b->d_stage, b->d_pads};
+    void* ptrs[] = {B.rec, B.au, B.events, B.place, B.cost, B.group_next, B.tick_scratch, b->d_cfgs, b->d_stage,
+                    b->d_pads};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->h_bounce) cudaFreeHost(b->h_bounce);
@@ -1390,13 +1400,14 @@ int rsg_get_device_flags(rsg_batch* b, uint32_t* out) {
     return RSG_OK;
 }
 
-int rsg_get_tick_shape(const rsg_batch* b, int32_t out[5]) {
+int rsg_get_tick_shape(const rsg_batch* b, int32_t out[6]) {
     if (!b || !out) return fail(RSG_ERR_ARG, "null argument");
     out[0] = b->shape.arenas_per_block;
     out[1] = b->shape.lanes_per_car;
     out[2] = b->shape.header_cache;
     out[3] = b->shape.leaf_grid;
     out[4] = b->shape.collide_sync;
+    out[5] = b->shape.persistent;
     return RSG_OK;
 }
 

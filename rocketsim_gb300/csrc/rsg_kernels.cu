@@ -3,8 +3,9 @@
 //
 // rsg_tick_kernel: one warp advances one arena by `ticks` ticks (its record is
 // loaded into the warp's shared-memory region, the ticks run there in block-wide
-// parts, and the record is stored back).  Arenas are independent, so the grid is
-// simply ceil(A / arenas per block) blocks.
+// parts, and the record is stored back).  Arenas are independent; a block advances
+// one group of arenas per block of the grid, or, in a persistent launch, groups
+// taken from a counter until none is left.
 #include <mutex>
 
 #include "rsg_kernels.h"
@@ -14,6 +15,12 @@
 namespace rsg {
 
 static_assert(sizeof(DevEvent) == DEV_EVENT_BYTES, "event record size");
+
+// The tick kernel keeps its manifold points and solver rows in a global scratch per warp slot
+// (L1-cached; only the rows and points a tick uses are touched), so that more arenas fit an SM's
+// shared memory.
+constexpr bool kRowsInSmem = false;
+constexpr bool kPtsInSmem = false;
 
 RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
     c.ctrl[0] = k.throttle;
@@ -29,29 +36,40 @@ RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
 // One warp per arena: the arena's working set is carved out of dynamic shared memory
 // (smem_layout), loaded from its record, advanced `ticks` ticks and stored back.  The warps of a
 // block step through the parts of a tick together (block-wide barriers between parts), which keeps
-// the instruction working set of an SM to one part of the tick at a time.  Warp slot s of the grid
-// advances arena place[s]; lane 0 adds up the cycles of the arena's own collision work into cost[].
-__global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
+// the instruction working set of an SM to one part of the tick at a time.  Group g of the launch
+// (warp slots g * wpb ...) advances arenas place[g * wpb + warp]; lane 0 adds up the cycles of the
+// arena's own collision work into cost[].  Block b takes group b; a persistent launch (as many blocks
+// as are resident at once) then takes the next groups from the counter *group_next, in group order,
+// so that the dearest groups (placed first) start first and the cheapest fill in at the end.
+__global__ void __launch_bounds__(32 * TICK_MAX_ARENAS_PER_BLOCK, 1) rsg_tick_kernel(BatchView bv, const rsg_car_controls* __restrict__ controls,
                                                           int ticks, int hdr_cache, int collide_sync,
-                                                          const uint32_t* __restrict__ place, uint32_t* __restrict__ cost) {
+                                                          const uint32_t* __restrict__ place, uint32_t* __restrict__ cost,
+                                                          uint32_t* group_next) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
-    const int slot0 = blockIdx.x * wpb;
-    const bool active = slot0 + warp < bv.A;  // warp-uniform; idle warps still take part in the barriers
-    const int ar = active ? (int)place[slot0 + warp] : 0;
-    const SmemLayout L = smem_layout(bv.MC);
-    Ctx& a = bind_ctx(smem + (size_t)warp * L.bytes, L, lane);
+    const int ngroups = (bv.A + wpb - 1) / wpb;
+    const SmemLayout L = smem_layout(bv.MC, kRowsInSmem, kPtsInSmem);
+    unsigned char* const gscr = bv.tick_scratch + ((size_t)blockIdx.x * wpb + warp) * L.g_bytes;
     // the BVH subtree headers, read by every narrow-phase query, copied once into the block's
     // shared memory behind the arenas when they fit
+    const size_t hdr_off = (size_t)wpb * L.bytes;
     const Subtree* sub = bv.mesh.sub;
     if (hdr_cache) {
-        uint32_t* dst = reinterpret_cast<uint32_t*>(smem + (size_t)wpb * L.bytes);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(smem + hdr_off);
         const uint32_t* src = reinterpret_cast<const uint32_t*>(bv.mesh.sub);
         for (int i = threadIdx.x; i < bv.mesh.nsub * 5; i += blockDim.x) dst[i] = __ldg(src + i);
         sub = reinterpret_cast<const Subtree*>(dst);
         __syncthreads();
     }
+    // the next group's number, broadcast to the block through the word behind the arenas and headers
+    volatile int* next_slot =
+        reinterpret_cast<volatile int*>(smem + hdr_off + (hdr_cache ? (size_t)bv.mesh.nsub * sizeof(Subtree) : 0));
+    for (int grp = blockIdx.x; grp < ngroups;) {
+    const int slot0 = grp * wpb;
+    const bool active = slot0 + warp < bv.A;  // warp-uniform; idle warps still take part in the barriers
+    const int ar = active ? (int)place[slot0 + warp] : 0;
+    Ctx& a = bind_ctx(smem + (size_t)warp * L.bytes, L, lane, gscr);
     if (active) {
         if (lane == 0) {
             load_arena(bv, ar, a);
@@ -96,6 +114,12 @@ __global__ void __launch_bounds__(256, 1) rsg_tick_kernel(BatchView bv, const rs
         if (lane < a.ncars) store_car(bv, ar, a, lane);
         store_pads(bv, ar, a, lane);
     }
+    if (!group_next) break;
+    __syncthreads();  // every warp is done with its working set (and has read next_slot)
+    if (threadIdx.x == 0) *next_slot = (int)gridDim.x + (int)atomicAdd(group_next, 1u);
+    __syncthreads();
+    grp = *next_slot;
+    }
 }
 
 // Placement order of the arenas: a counting sort by the cost of their collision work in the last
@@ -134,7 +158,10 @@ cudaError_t launch_place_arenas(const BatchBuffers& b, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars).bytes; }
+int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars, kRowsInSmem, kPtsInSmem).bytes; }
+size_t tick_scratch_bytes(int A, int max_cars) {  // a slot per warp of the grid: at most A + arenas per block - 1
+    return (size_t)(A + TICK_MAX_ARENAS_PER_BLOCK) * smem_layout(max_cars, kRowsInSmem, kPtsInSmem).g_bytes;
+}
 
 // The EPA work-slot pool of the current device, made once per device for the process.
 cudaError_t ensure_epa_pool() {
@@ -164,31 +191,48 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
                         cudaStream_t st) {
     if (b.A <= 0 || ticks <= 0) return cudaSuccess;
     int wpb = shape.arenas_per_block;
-    if (wpb <= 0 || wpb > 8) wpb = 8;
+    if (wpb <= 0 || wpb > TICK_MAX_ARENAS_PER_BLOCK) wpb = TICK_MAX_ARENAS_PER_BLOCK;
     // the block must fit in shared memory
-    while (wpb > 1 && smem_layout(b.MC).bytes * wpb > 227 * 1024) wpb--;
-    const int per_arena = smem_layout(b.MC).bytes;
+    const int per_arena = tick_smem_per_arena(b.MC);
+    while (wpb > 1 && per_arena * wpb + 16 > 227 * 1024) wpb--;
     int smem = per_arena * wpb;
     // the header copy: on request, or (automatic) only when it costs no block per SM (228 KB of
     // shared memory per SM, 1 KB of it reserved per block)
     const int hdr_bytes = b.mesh.sub ? b.mesh.nsub * (int)sizeof(Subtree) : 0;
     const int sm_smem = 228 * 1024;
     const int blocks_without = sm_smem / (smem + 1024), blocks_with = sm_smem / (smem + hdr_bytes + 1024);
-    const bool fits = hdr_bytes > 0 && smem + hdr_bytes <= 227 * 1024;
+    const bool fits = hdr_bytes > 0 && smem + hdr_bytes + 16 <= 227 * 1024;
     const int hdr_cache = shape.header_cache < 0 ? ((fits && blocks_with >= blocks_without) ? 1 : 0)
                                                  : ((fits && shape.header_cache) ? 1 : 0);
     if (hdr_cache) smem += hdr_bytes;
-    cudaError_t e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
     BatchView v = make_view(b);
     v.lanes_per_car = (shape.lanes_per_car == 1 || shape.lanes_per_car == 2) ? shape.lanes_per_car : 4;
     if (!shape.leaf_grid) {
         v.mesh.lg_block = nullptr;
         v.mesh.lg_over = nullptr;
     }
-    int grid = (b.A + wpb - 1) / wpb;
+    smem += 16;  // the next group's number (persistent launches)
+    e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int ngroups = (b.A + wpb - 1) / wpb;
+    int grid = ngroups;
+    uint32_t* group_next = nullptr;
+    if (shape.persistent && b.group_next) {
+        int dev = 0, nsm = 0, per_sm = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsg_tick_kernel, 32 * wpb, smem)) != cudaSuccess)
+            return e;
+        const int resident = nsm * (per_sm > 0 ? per_sm : 1);
+        if (resident < ngroups) {
+            grid = resident;
+            group_next = b.group_next;
+            if ((e = cudaMemsetAsync(group_next, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+        }
+    }
     rsg_tick_kernel<<<grid, 32 * wpb, smem, st>>>(v, controls, ticks, hdr_cache, shape.collide_sync ? 1 : 0, b.place,
-                                                   b.cost);
+                                                   b.cost, group_next);
     return cudaGetLastError();
 }
 

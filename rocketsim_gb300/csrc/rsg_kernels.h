@@ -41,18 +41,28 @@ struct BatchBuffers {
     GridSpec grid;
     uint32_t* place;  // [A] arena advanced by each warp slot of the tick kernel (a permutation of 0..A-1)
     uint32_t* cost;   // [A] cycles each arena's own collision work took in the last tick launch
+    uint32_t* group_next;  // [1] groups taken so far by the blocks of a persistent tick launch
+    unsigned char* tick_scratch;  // tick_scratch_bytes: per warp slot, the working set kept out of shared memory
 };
 
 constexpr int DEV_EVENT_BYTES = 24;
 
 // Launch shape of the tick kernel.  Every shape gives the same results (arenas never depend on the
 // block they share or on how their units are spread); they differ in speed.
+#ifndef RSG_TICK_MAX_WARPS
+#define RSG_TICK_MAX_WARPS 16
+#endif
+// Most arenas (warps) per block of the tick kernel; its register budget per thread follows from it
+// (16 warps: 128 registers, so that 16 warps of one or more blocks fit an SM's register file).
+constexpr int TICK_MAX_ARENAS_PER_BLOCK = RSG_TICK_MAX_WARPS;
+
 struct TickShape {
-    int arenas_per_block = 8;  // one warp per arena
+    int arenas_per_block = TICK_MAX_ARENAS_PER_BLOCK;  // one warp per arena (as many as shared memory holds)
     int lanes_per_car = 4;     // threads per car in the vehicle update after the rays: 1, 2 or 4
     int header_cache = -1;     // BVH subtree headers in shared memory: 1 yes, 0 no, -1 when it costs no block per SM
     int leaf_grid = 1;         // wheel rays scan the leaf grid (1) or walk the quantized BVH (0)
     int collide_sync = 1;      // block-wide barriers between the parts of the collision work (1) or not (0)
+    int persistent = 0;        // one block per resident slot taking arena groups from a counter (1), or a block per group (0)
 };
 
 // Advances every arena by `ticks` ticks, one warp per arena, arenas placed in blocks by b.place.
@@ -65,6 +75,8 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
 cudaError_t launch_place_arenas(const BatchBuffers& b, cudaStream_t st);
 // Shared memory one arena needs in the tick kernel.
 int tick_smem_per_arena(int max_cars);
+// Bytes of the tick kernel's global scratch (a working-set slot per warp of its grid).
+size_t tick_scratch_bytes(int A, int max_cars);
 
 // Allocates the current device's pool of EPA work slots (once per device; about 14 MB).
 cudaError_t ensure_epa_pool();

@@ -116,6 +116,7 @@ struct BatchView {
     uint32_t event_mask;
     DevMesh mesh;
     DevGrid grid;
+    unsigned char* tick_scratch;  // per warp slot: the working-set parts the tick kernel keeps out of shared memory
 };
 
 constexpr int OBJ_MESH = 0, OBJ_PLANE0 = 1, OBJ_BALL = 5, OBJ_CAR0 = 6;
@@ -4614,22 +4615,43 @@ RSG_D void store_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
 struct SmemLayout {
     int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, qbox,
         hdr_list, hdr_n, bytes;
+    int g_pts, g_rows, g_bytes;  // parts kept in a per-warp global scratch instead (offsets there, -1: in shared)
     ArenaCaps caps;
 };
 RSG_HD int align16(int x) { return (x + 15) & ~15; }
-RSG_HD SmemLayout smem_layout(int mc) {
+// The manifold points and the solver rows live only within a tick's collision work; either can be
+// kept in a global scratch of the warp (L1-cached) instead of shared memory.
+RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem = true) {
     SmemLayout L;
     L.caps = arena_caps(mc);
+    L.g_pts = L.g_rows = -1;
+    L.g_bytes = 0;
+    if (!pts_in_smem) {
+        L.g_pts = L.g_bytes;
+        L.g_bytes = align16(L.g_bytes + (int)sizeof(MPoint) * L.caps.points);
+    }
+    if (!rows_in_smem) {
+        L.g_rows = L.g_bytes;
+        L.g_bytes = align16(L.g_bytes + 2 * (int)sizeof(Row) * L.caps.rows);
+    }
     int o = align16((int)sizeof(Ctx));
     L.cars = o;   o = align16(o + (int)sizeof(Car) * mc);
     L.pads = o;   o = align16(o + (int)sizeof(Pad) * NUM_PADS);
     L.pair0 = o;  o = align16(o + L.caps.pairs);
     L.pair1 = o;  o = align16(o + L.caps.pairs);
     L.man = o;    o = align16(o + (int)sizeof(Manifold) * L.caps.pairs);
-    L.pts = o;    o = align16(o + (int)sizeof(MPoint) * L.caps.points);
+    if (pts_in_smem) {
+        L.pts = o; o = align16(o + (int)sizeof(MPoint) * L.caps.points);
+    } else {
+        L.pts = -1;
+    }
     L.sb = o;     o = align16(o + (int)sizeof(SBody) * (MAX_DYN + 1));
-    L.rows_c = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
-    L.rows_f = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
+    if (rows_in_smem) {
+        L.rows_c = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
+        L.rows_f = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
+    } else {
+        L.rows_c = L.rows_f = -1;
+    }
     L.pkind = o;  o = align16(o + L.caps.pairs);
     L.flat_off = o; o = align16(o + 2 * L.caps.pairs);
     L.flat_n = o; o = align16(o + 2 * L.caps.pairs);
@@ -4646,7 +4668,8 @@ RSG_HD SmemLayout smem_layout(int mc) {
     return L;
 }
 // Lane 0 writes the carve-out pointers; the caller synchronises the warp before use.
-RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane) {
+// `gscr` is the warp's global scratch (L.g_bytes) for the parts the layout keeps out of shared memory.
+RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane, unsigned char* gscr = nullptr) {
     Ctx& a = *reinterpret_cast<Ctx*>(base);
     if (lane != 0) return a;
     a.cars = reinterpret_cast<Car*>(base + L.cars);
@@ -4654,10 +4677,10 @@ RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane) {
     a.pair0 = reinterpret_cast<int8_t*>(base + L.pair0);
     a.pair1 = reinterpret_cast<int8_t*>(base + L.pair1);
     a.man = reinterpret_cast<Manifold*>(base + L.man);
-    a.pts = reinterpret_cast<MPoint*>(base + L.pts);
+    a.pts = reinterpret_cast<MPoint*>(L.pts >= 0 ? base + L.pts : gscr + L.g_pts);
     a.sb = reinterpret_cast<SBody*>(base + L.sb);
-    a.rows_c = reinterpret_cast<Row*>(base + L.rows_c);
-    a.rows_f = reinterpret_cast<Row*>(base + L.rows_f);
+    a.rows_c = reinterpret_cast<Row*>(L.rows_c >= 0 ? base + L.rows_c : gscr + L.g_rows);
+    a.rows_f = L.rows_c >= 0 ? reinterpret_cast<Row*>(base + L.rows_f) : a.rows_c + L.caps.rows;
     a.pkind = reinterpret_cast<int8_t*>(base + L.pkind);
     a.flat_off = reinterpret_cast<int16_t*>(base + L.flat_off);
     a.flat_n = reinterpret_cast<int16_t*>(base + L.flat_n);

@@ -125,17 +125,40 @@ def test_gpu_matches_restatement_random():
     batch.close()
 
 
-def test_full_size_batch_is_deterministic_and_independent():
-    """4096 arenas holding 8 scenarios 512 times each: every copy of a scenario
-    must end bit-identical after 8 ticks, and all states stay finite."""
+@pytest.fixture(scope="module")
+def full_size_runs():
+    """4096 arenas holding 8 scenarios 512 times each, stepped 8 ticks with one block per group of 6
+    arenas and with a persistent launch (683 groups, more than the blocks resident at once, so its
+    blocks take further groups from the counter)."""
+    import os
     base = random_scenarios(8, base_seed=2000)
     scs = [base[k % 8] for k in range(4096)]
-    batch, ids = setup_gpu(scs, max_cars=6)
-    for t in range(8):
-        batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
-        batch.step(1)
-    cars, balls, pads = batch.get_all_states()
-    mc = batch.max_cars
+    out = {}
+    old = os.environ.get("RSG_TICK_SHAPE")
+    try:
+        for persistent in (0, 1):
+            os.environ["RSG_TICK_SHAPE"] = f"6,4,-1,1,1,{persistent}"
+            batch, ids = setup_gpu(scs, max_cars=6)
+            assert batch.tick_shape()[5] == persistent
+            for t in range(8):
+                batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
+                batch.step(1)
+            out[persistent] = (batch.get_all_states(), batch.max_cars)
+            batch.close()
+    finally:
+        if old is None:
+            os.environ.pop("RSG_TICK_SHAPE", None)
+        else:
+            os.environ["RSG_TICK_SHAPE"] = old
+    return base, out
+
+
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_full_size_batch_is_deterministic_and_independent(full_size_runs, persistent):
+    """Every copy of a scenario ends bit-identical after 8 ticks, all states stay finite, and the
+    persistent launch gives the same bytes as one block per group."""
+    base, out = full_size_runs
+    (cars, balls, pads), mc = out[persistent]
     for k in range(8):
         n = len(base[k].cars)
         rows = [cars[a * mc:a * mc + n].tobytes() for a in range(k, 4096, 8)]
@@ -145,7 +168,8 @@ def test_full_size_batch_is_deterministic_and_independent():
     for f in ("pos", "vel", "ang_vel"):
         for c in "xyz":
             assert np.isfinite(cars[f][c]).all() and np.isfinite(balls[f][c]).all()
-    batch.close()
+    (c0, b0, p0), _ = out[0]
+    assert cars.tobytes() == c0.tobytes() and balls.tobytes() == b0.tobytes() and pads.tobytes() == p0.tobytes()
 
 
 def test_state_round_trip_and_ids():
@@ -263,12 +287,14 @@ def test_the_void_free_flight_matches_restatement():
 
 def test_launch_shapes_give_identical_results(golden, monkeypatch):
     """Every launch shape the tuner may choose (arenas per block, threads per car, BVH headers in shared
-    memory or not, leaf grid or BVH walk, block-wide barriers in the collision work or not), with the
+    memory or not, leaf grid or BVH walk, block-wide barriers in the collision work or not, a persistent
+    launch or not: at this size a persistent launch has a block per group), with the
     arenas re-placed in blocks by cost after every launch, steps the golden scenarios (each three times
     in the batch) to bit-identical states."""
     scs = golden.scenarios * 3
     results = []
-    for shape in ("8,4,-1,1", "4,1,0,1", "6,2,1,0", "7,4,1,1,1", "5,1,0,0,1", "8,2,1,1,1"):
+    for shape in ("8,4,-1,1", "4,1,0,1", "6,2,1,0", "7,4,1,1,1", "5,1,0,0,1", "8,2,1,1,1", "8,4,0,1,1,1", "5,2,1,0,0,1",
+                  "16,4,0,1,1,0", "12,1,1,1,0,1"):
         monkeypatch.setenv("RSG_TICK_SHAPE", shape)
         batch, _ = setup_gpu(scs)
         want, got = [int(x) for x in shape.split(",")], batch.tick_shape()
