@@ -10,9 +10,9 @@ handbrake Bernoulli(0.3), each car re-drawing after a hold of 2..60 ticks).
 
 A step is 8 ticks of every arena.  ``value`` runs each step as one
 rsg_step_async launch whose per-tick controls are already in device memory;
-``e2e`` runs it through the synchronous host API: controls from pinned host
-memory (rsg_set_controls_all), rsg_step(8), and every car, ball and pad state
-read back to host memory (rsg_get_all_states).  The L2 cache is flushed
+``e2e`` runs it through the synchronous host API: the step's per-tick controls
+from pinned host memory (rsg_step_controls, 8 ticks), and every car, ball and
+pad state read back to host memory (rsg_get_all_states).  The L2 cache is flushed
 (a 256 MiB device write) between timed steps.
 
 The same line carries ``adjoint``: gradient steps (forward with checkpoints,
@@ -383,13 +383,7 @@ def run_arena_leg(args, dev: int, A: int, mc: int, steps: int, warmup: int, sett
         dist.barrier()
     clk = clocks.stop()
     times_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(times_ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=d)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = A * tps * steps * world / (total_ms / 1e3)
+    value, total_ms = replica_rate(A * tps * steps, sum(times_ms), world, d)
     flags = batch.device_flags()
     shape = batch.tick_shape()
     out = {"value": value, "ms_per_step": total_ms / steps, "times_ms": times_ms, "clocks": clk,
@@ -403,18 +397,16 @@ def run_arena_leg(args, dev: int, A: int, mc: int, steps: int, warmup: int, sett
     if e2e:
         # ---- e2e: host buffers (pinned) through the synchronous API: controls in, every car, ball and
         # pad state out, each step
-        ctl_h = torch.empty(n_ctl * rsg.CONTROLS_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
-        ctl_np = ctl_h.numpy().view(rsg.CONTROLS_DTYPE)
         pin = lambda dt, n: torch.empty(n * dt.itemsize, dtype=torch.uint8).pin_memory().numpy().view(dt)  # noqa
+        ctl_np = pin(rsg.CONTROLS_DTYPE, n_ctl * tps).reshape(tps, n_ctl)
         out_cars = pin(rsg.CAR_STATE_DTYPE, A * mc)
         out_balls = pin(rsg.BALL_STATE_DTYPE, A)
         out_pads = pin(rsg.PAD_STATE_DTYPE, A * batch.num_pads)
         e2e_steps = max(3, min(steps, 20))
-        seq_h = np.stack([proc.tick() for _ in range(e2e_steps + 2)])
+        seq_h = np.stack([proc.tick() for _ in range((e2e_steps + 2) * tps)]).reshape(e2e_steps + 2, tps, n_ctl)
         for s in range(2):
             ctl_np[:] = seq_h[s]
-            batch.set_controls_all(ctl_np)
-            batch.step(tps)
+            batch.step_controls(ctl_np, tps)
             batch.get_all_states(out_cars, out_balls, out_pads)
         e2e_time = 0.0
         for s in range(e2e_steps):
@@ -423,16 +415,31 @@ def run_arena_leg(args, dev: int, A: int, mc: int, steps: int, warmup: int, sett
                 flush.fill_(s & 0xff)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            batch.set_controls_all(ctl_np)
-            batch.step(tps)
+            batch.step_controls(ctl_np, tps)
             batch.get_all_states(out_cars, out_balls, out_pads)
             e2e_time += time.perf_counter() - t0
         out["e2e"] = {"value": A * tps * e2e_steps * world / e2e_time, "unit": "arena-ticks/s",
                       "h2d_bytes_per_step": int(ctl_np.nbytes),
                       "d2h_bytes_per_step": int(out_cars.nbytes + out_balls.nbytes + out_pads.nbytes),
-                      "host_buffers": "pinned", "controls": "the same control for all 8 ticks of a step"}
+                      "host_buffers": "pinned",
+                      "controls": "a control per car and tick from the same input process as the device-resident steps "
+                                  "(rsg_step_controls)"}
     batch.close()
     return out
+
+
+def replica_rate(units_per_rank: float, rank_ms: float, world: int, device) -> tuple[float, float]:
+    """Whole-job rate of `world` independent replicas: every rank's units over the slowest rank's time
+    (the maximum over the ranks, one all_reduce on the initialised process group).  Returns the rate
+    per second and that time in ms."""
+    total_ms = rank_ms
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([rank_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return units_per_rank * world / (total_ms / 1e3), total_ms
 
 
 def load_counters() -> dict:
@@ -497,8 +504,8 @@ def run_gpu(args, rank: int, world: int):
 
 def run_config0(args, dev: int):
     """One arena, 2v2 Octane: the reference's own benchmark shape, a bounded sample of its 1M ticks."""
-    return run_arena_leg(args, dev, 1, CARS, args.c0_steps, 3, 240, e2e=False, flush_l2=False, curve=False,
-                         tps=120)
+    return run_arena_leg(args, dev, 1, CARS, args.c0_steps, 3, args.settle_ticks, e2e=False, flush_l2=False,
+                         curve=False, tps=120)
 
 
 def run_config2(args, dev: int):
@@ -955,6 +962,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    # the launch-shape tuner's second round runs on a batch's first launch after 1024 ticks: keep it
+    # in the settle ticks, out of the timed steps
+    args.settle_ticks = max(args.settle_ticks, 1080)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     threads = os.cpu_count() or 1

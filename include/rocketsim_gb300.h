@@ -366,6 +366,12 @@ int rsg_set_all_states(rsg_batch* batch, const rsg_car_state* cars, const rsg_ba
  * callbacks have run. */
 int rsg_step(rsg_batch* batch, int ticks);
 
+/* Arena::Step one tick at a time with each car's controls set before every
+ * tick (Car::controls, Car.h:149, read by Car::_PreTickUpdate), for every arena
+ * of the batch: controls (host memory, pinned or not) holds [ticks][arena][slot]
+ * controls, copied to the device at the call.  Synchronous like rsg_step. */
+int rsg_step_controls(rsg_batch* batch, const rsg_car_controls* controls, int ticks);
+
 /* Asynchronous variant on the batch's own stream for callers that keep
  * inputs resident in device memory: d_controls (device pointer, may be NULL
  * to keep the current controls) holds [ticks][arena][slot] controls.  Events

@@ -176,6 +176,7 @@ PROTOTYPES = {
     "rsg_get_all_states": (i32, [vp, vp, vp, vp]),
     "rsg_set_all_states": (i32, [vp, vp, vp, vp]),
     "rsg_step": (i32, [vp, i32]),
+    "rsg_step_controls": (i32, [vp, vp, i32]),
     "rsg_step_async": (i32, [vp, vp, i32]),
     "rsg_sync": (i32, [vp]),
     "rsg_batch_stream": (vp, [vp]),

@@ -281,12 +281,19 @@ class ArenaBatch:
         return tuple(int(x) for x in out)
 
     def tuning_log(self) -> str:
-        buf = C.create_string_buffer(4096)
-        check(self.lib.rsg_get_tuning_log(self.h, buf, 4096), "rsg_get_tuning_log")
+        buf = C.create_string_buffer(65536)
+        check(self.lib.rsg_get_tuning_log(self.h, buf, 65536), "rsg_get_tuning_log")
         return buf.value.decode()
 
     def step(self, ticks: int = 1) -> None:
         check(self.lib.rsg_step(self.h, ticks), "rsg_step")
+
+    def step_controls(self, controls: np.ndarray, ticks: int) -> None:
+        """Steps `ticks` ticks with host controls for every tick ([ticks][arena][slot] CONTROLS_DTYPE)."""
+        if controls.dtype != CONTROLS_DTYPE or controls.size != ticks * self.n_arenas * self.max_cars:
+            raise ValueError("controls must be ticks * n_arenas * max_cars CONTROLS_DTYPE entries")
+        c = np.ascontiguousarray(controls)
+        check(self.lib.rsg_step_controls(self.h, c.ctypes.data, ticks), "rsg_step_controls")
 
     def step_async(self, d_controls_ptr: int | None, ticks: int) -> None:
         check(self.lib.rsg_step_async(self.h, d_controls_ptr, ticks), "rsg_step_async")

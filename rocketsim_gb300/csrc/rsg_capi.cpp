@@ -194,10 +194,14 @@ static_assert(sizeof(DevEventHost) == DEV_EVENT_BYTES, "event record");
 struct rsg_batch {
     int game_mode = 0;
     int device = 0;
-    // launch shape of the tick kernel: tuned on the batch's first launch (identical states for every
-    // trial), cached per (device, arenas, car slots, game mode), or fixed by the environment
+    // launch shape of the tick kernel: tuned on the batch's first launch and again once it has run
+    // RETUNE_TICKS ticks (identical states for every trial), cached per (device, arenas, car slots,
+    // game mode, round), or fixed by the environment
     TickShape shape;
     bool tune_pending = true;
+    bool shape_fixed = false;
+    int tune_round = 0;
+    uint64_t ticks_launched = 0;
     std::string tune_log;
     BatchBuffers buf{};
     cudaStream_t stream = nullptr;
@@ -213,6 +217,8 @@ struct rsg_batch {
     // staging
     void* d_stage = nullptr;
     size_t stage_bytes = 0;
+    void* d_ctl = nullptr;  // rsg_step_controls' per-tick controls (apart from d_stage: callbacks may use that)
+    size_t ctl_bytes = 0;
     void* h_bounce = nullptr;  // pinned host buffer of the bulk getter (batches with empty car slots)
     size_t bounce_bytes = 0;
     std::vector<uint32_t> h_counts;
@@ -517,16 +523,21 @@ int rsg_get_car_config_preset(int preset, rsg_car_config* out) {
 namespace {
 
 // Block-shape tuner.  Every launch shape gives the same results, so the shapes can be timed on the
-// batch itself: the first launch saves the arena records, runs each candidate shape from the saved
+// batch itself: a tuning launch saves the arena records, runs each candidate shape from the saved
 // state (launch, wait, time), restores the records and launches for real with the fastest.  The
-// candidates are searched one parameter at a time from the default shape: arenas per block (4 to 8,
-// as shared memory allows), threads per car in the vehicle update (1, 2, 4), the BVH subtree headers
-// in shared memory or read through L2, and wheel rays on the leaf grid or walking the BVH.  The
-// choice is cached per (device, arenas, car slots, game mode).
+// candidates are searched one parameter at a time: barriers in the collision work, arenas per block
+// (16 to 4, as shared memory allows), threads per car in the vehicle update (1, 2, 4), the BVH subtree
+// headers in shared memory or read through L2, wheel rays on the leaf grid or walking the BVH, a
+// persistent launch.  It runs on the batch's first launch and again, from the default shape and with
+// a second look at the barriers and the arenas per block, on the first launch after RETUNE_TICKS
+// ticks, when the arenas have left the start of the game (cars landed, on walls, in contact: the
+// collision work that decides the best shape has grown).  The choice of each round is cached per
+// (device, arenas, car slots, game mode).
+constexpr uint64_t RETUNE_TICKS = 1024;
 struct TuneKey {
-    int dev, A, MC, arena;
+    int dev, A, MC, arena, round;
     bool operator<(const TuneKey& o) const {
-        return std::tie(dev, A, MC, arena) < std::tie(o.dev, o.A, o.MC, o.arena);
+        return std::tie(dev, A, MC, arena, round) < std::tie(o.dev, o.A, o.MC, o.arena, o.round);
     }
 };
 std::mutex g_tune_mu;
@@ -544,14 +555,16 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
     b->tune_pending = false;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(b->stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
-        return cudaSuccess;  // no synchronous trials inside a capture: keep the default shape
-    const TuneKey key{b->device, b->buf.A, b->buf.MC, b->buf.has_arena};
+        return cudaSuccess;  // no synchronous trials inside a capture: keep the current shape
+    const int round = b->tune_round++;
+    const std::string prefix = round == 0 ? "" : b->tune_log + " | after " + std::to_string(RETUNE_TICKS) + " ticks: ";
+    const TuneKey key{b->device, b->buf.A, b->buf.MC, b->buf.has_arena, round};
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
             b->shape = it->second.first;
-            b->tune_log = it->second.second + " (cached)";
+            b->tune_log = prefix + it->second.second + " (cached)";
             return cudaSuccess;
         }
     }
@@ -573,19 +586,27 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
         }
         return cudaSuccess;
     };
-    auto trial = [&](const TickShape& s, double& ms) -> cudaError_t {
-        cudaError_t r = copy_all(false);
-        if (r == cudaSuccess) r = cudaEventRecord(ev[0], b->stream);
-        if (r == cudaSuccess) r = launch_tick(B, controls, ticks, s, b->stream);
-        if (r == cudaSuccess) r = cudaEventRecord(ev[1], b->stream);
-        if (r == cudaSuccess) r = cudaEventSynchronize(ev[1]);
-        float f = 0;
-        if (r == cudaSuccess) r = cudaEventElapsedTime(&f, ev[0], ev[1]);
-        ms = f;
+    auto trial = [&](const TickShape& s, double& ms) -> cudaError_t {  // the faster of two launches
+        cudaError_t r = cudaSuccess;
+        ms = 1e30;
+        for (int rep = 0; rep < 2 && r == cudaSuccess; rep++) {
+            r = copy_all(false);
+            if (r == cudaSuccess) r = cudaEventRecord(ev[0], b->stream);
+            if (r == cudaSuccess) r = launch_tick(B, controls, ticks, s, b->stream);
+            if (r == cudaSuccess) r = cudaEventRecord(ev[1], b->stream);
+            if (r == cudaSuccess) r = cudaEventSynchronize(ev[1]);
+            float f = 0;
+            if (r == cudaSuccess) r = cudaEventElapsedTime(&f, ev[0], ev[1]);
+            if (r == cudaSuccess && f < ms) ms = f;
+        }
         return r;
     };
     std::string log;
-    TickShape best = b->shape;
+    const int per_arena = tick_smem_per_arena(B.MC);
+    // round 0 starts from the batch's shape, later rounds from the default one (the first round's
+    // choice was made for the start of a game)
+    TickShape best = round == 0 ? b->shape : TickShape{};
+    while (best.arenas_per_block > 1 && per_arena * best.arenas_per_block + 16 > 227 * 1024) best.arenas_per_block--;
     do {
         if ((e = cudaEventCreate(&ev[0])) != cudaSuccess || (e = cudaEventCreate(&ev[1])) != cudaSuccess) break;
         if ((e = copy_all(true)) != cudaSuccess) break;
@@ -601,13 +622,26 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
             if (t < best_ms) { best_ms = t; best = s; }
             return cudaSuccess;
         };
-        const int per_arena = tick_smem_per_arena(B.MC);
-        for (int w = TICK_MAX_ARENAS_PER_BLOCK; w >= 4 && e == cudaSuccess; w--) {
-            if (w == best.arenas_per_block || per_arena * w + 16 > 227 * 1024) continue;
+        auto toggle_sync = [&]() -> cudaError_t {
             TickShape s = best;
-            s.arenas_per_block = w;
-            e = consider(s);
-        }
+            s.collide_sync = best.collide_sync ? 0 : 1;
+            return consider(s);
+        };
+        auto widths = [&]() -> cudaError_t {
+            const TickShape base = best;
+            for (int w = TICK_MAX_ARENAS_PER_BLOCK; w >= 4; w--) {
+                if (w == base.arenas_per_block || per_arena * w + 16 > 227 * 1024) continue;
+                TickShape s = base;
+                s.arenas_per_block = w;
+                cudaError_t r = consider(s);
+                if (r != cudaSuccess) return r;
+            }
+            return cudaSuccess;
+        };
+        // one parameter at a time from the best shape so far; the collision barriers first (at a
+        // game's steady state they change the cost of everything else)
+        if ((e = toggle_sync()) != cudaSuccess) break;
+        if ((e = widths()) != cudaSuccess) break;
         const TickShape base = best;
         for (int l : {1, 2, 4}) {
             if (e != cudaSuccess || l == base.lanes_per_car) continue;
@@ -617,19 +651,14 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
         }
         const TickShape base2 = best;
         for (int h : {0, 1}) {
-            if (e != cudaSuccess || !B.mesh.sub) continue;
+            if (e != cudaSuccess || !B.mesh.sub || h == base2.header_cache) continue;
             TickShape s = base2;
             s.header_cache = h;
             e = consider(s);
         }
         if (e == cudaSuccess && B.mesh.lg_block) {
             TickShape s = best;
-            s.leaf_grid = 0;
-            e = consider(s);
-        }
-        if (e == cudaSuccess) {
-            TickShape s = best;
-            s.collide_sync = best.collide_sync ? 0 : 1;
+            s.leaf_grid = best.leaf_grid ? 0 : 1;
             e = consider(s);
         }
         if (e == cudaSuccess) {
@@ -637,6 +666,9 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
             s.persistent = best.persistent ? 0 : 1;
             e = consider(s);
         }
+        // after the start of a game, a second look at the two parameters that matter most
+        if (e == cudaSuccess && round > 0) e = toggle_sync();
+        if (e == cudaSuccess && round > 0) e = widths();
         if (e == cudaSuccess) e = copy_all(false);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     } while (false);
@@ -645,16 +677,20 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
     cudaFree(snap);
     if (e != cudaSuccess) return e;
     b->shape = best;
-    b->tune_log = "chose " + shape_str(best) + " from " + log;
+    const std::string mine = "chose " + shape_str(best) + " from " + log;
+    b->tune_log = prefix + mine;
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tune_cache[key] = {best, b->tune_log};
+    g_tune_cache[key] = {best, mine};
     return cudaSuccess;
 }
 
-// Launches `ticks` ticks (tuning the shape first on the batch's first launch), then re-places the
-// arenas in blocks by the cost of their collision work in that launch.
+// Launches `ticks` ticks (tuning the shape first on the batch's first launch and on its first launch
+// after RETUNE_TICKS ticks), then re-places the arenas in blocks by the cost of their collision work
+// in that launch.
 cudaError_t tuned_launch(rsg_batch* b, const rsg_car_controls* controls, int ticks) {
     cudaError_t e = cudaSuccess;
+    if (!b->shape_fixed && b->tune_round == 1 && b->ticks_launched >= RETUNE_TICKS) b->tune_pending = true;
+    b->ticks_launched += (uint64_t)ticks;
     if (b->tune_pending) e = run_tuner(b, controls, ticks);
     if (e == cudaSuccess) e = launch_tick(b->buf, controls, ticks, b->shape, b->stream);
     if (e == cudaSuccess) e = launch_place_arenas(b->buf, b->stream);
@@ -742,6 +778,7 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
         b->shape.collide_sync = v[4];
         b->shape.persistent = v[5] ? 1 : 0;
         b->tune_pending = false;
+        b->shape_fixed = true;
     }
     {  // at most as many arenas per block as shared memory holds (launch_tick clamps the same way)
         const int per_arena = tick_smem_per_arena((int)max_cars_per_arena);
@@ -845,7 +882,7 @@ void rsg_batch_destroy(rsg_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     BatchBuffers& B = b->buf;
     void* ptrs[] = {B.rec, B.au, B.events, B.place, B.cost, B.group_next, B.tick_scratch, b->d_cfgs, b->d_stage,
-                    b->d_pads};
+                    b->d_pads, b->d_ctl};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->h_bounce) cudaFreeHost(b->h_bounce);
@@ -1340,6 +1377,37 @@ int rsg_step(rsg_batch* b, int ticks) {
     for (int done = 0; done < ticks;) {
         int n = std::min(chunk, ticks - done);
         RSG_CUDA(tuned_launch(b, nullptr, n));
+        done += n;
+        if (b->buf.event_mask && (rc = drain_events(b))) return rc;
+    }
+    RSG_CUDA(cudaStreamSynchronize(b->stream));
+    return check_device_errors(b);
+}
+
+int rsg_step_controls(rsg_batch* b, const rsg_car_controls* controls, int ticks) {
+    if (!b || !controls) return fail(RSG_ERR_ARG, "null argument");
+    if (ticks < 0) return fail(RSG_ERR_ARG, "negative tick count");
+    int rc;
+    if ((rc = set_device(b))) return rc;
+    if (ticks == 0) return RSG_OK;
+    const size_t per_tick = (size_t)b->buf.A * b->buf.MC, bytes = per_tick * sizeof(rsg_car_controls) * (size_t)ticks;
+    if (b->ctl_bytes < bytes) {
+        if (b->d_ctl) {
+            RSG_CUDA(cudaStreamSynchronize(b->stream));
+            cudaFree(b->d_ctl);
+        }
+        b->d_ctl = nullptr;
+        b->ctl_bytes = 0;
+        RSG_CUDA(cudaMalloc(&b->d_ctl, bytes));
+        b->ctl_bytes = bytes;
+    }
+    const rsg_car_controls* d = (const rsg_car_controls*)b->d_ctl;
+    RSG_CUDA(cudaMemcpyAsync(b->d_ctl, controls, bytes, cudaMemcpyHostToDevice, b->stream));
+    int chunk = b->buf.event_mask ? 32 : ticks;  // as rsg_step: events drained at least every 32 ticks
+    RSG_CUDA(cudaMemsetAsync(b->buf.au + au_index(b, AU_ERR, 0), 0, 4 * (size_t)b->buf.A, b->stream));
+    for (int done = 0; done < ticks;) {
+        int n = std::min(chunk, ticks - done);
+        RSG_CUDA(tuned_launch(b, d + (size_t)done * per_tick, n));
         done += n;
         if (b->buf.event_mask && (rc = drain_events(b))) return rc;
     }

@@ -6,7 +6,9 @@
 // parts, and the record is stored back).  Arenas are independent; a block advances
 // one group of arenas per block of the grid, or, in a persistent launch, groups
 // taken from a counter until none is left.
+#include <map>
 #include <mutex>
+#include <tuple>
 
 #include "rsg_kernels.h"
 #include "rsg_tick.cuh"
@@ -16,11 +18,13 @@ namespace rsg {
 
 static_assert(sizeof(DevEvent) == DEV_EVENT_BYTES, "event record size");
 
-// The tick kernel keeps its manifold points and solver rows in a global scratch per warp slot
-// (L1-cached; only the rows and points a tick uses are touched), so that more arenas fit an SM's
-// shared memory.
+// The tick kernel keeps the parts of an arena's working set that live only within a tick's collision
+// work — manifold points, solver rows, solver bodies, candidate and island lists — in a global scratch
+// per warp slot (L1-cached; only what a tick uses is touched), so that more arenas fit an SM's shared
+// memory.
 constexpr bool kRowsInSmem = false;
 constexpr bool kPtsInSmem = false;
+constexpr bool kMoreInSmem = false;
 
 RSG_D void apply_controls(Car& c, const rsg_car_controls& k) {
     c.ctrl[0] = k.throttle;
@@ -49,7 +53,7 @@ __global__ void __launch_bounds__(32 * TICK_MAX_ARENAS_PER_BLOCK, 1) rsg_tick_ke
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
     const int ngroups = (bv.A + wpb - 1) / wpb;
-    const SmemLayout L = smem_layout(bv.MC, kRowsInSmem, kPtsInSmem);
+    const SmemLayout L = smem_layout(bv.MC, kRowsInSmem, kPtsInSmem, kMoreInSmem);
     unsigned char* const gscr = bv.tick_scratch + ((size_t)blockIdx.x * wpb + warp) * L.g_bytes;
     // the BVH subtree headers, read by every narrow-phase query, copied once into the block's
     // shared memory behind the arenas when they fit
@@ -158,9 +162,9 @@ cudaError_t launch_place_arenas(const BatchBuffers& b, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars, kRowsInSmem, kPtsInSmem).bytes; }
+int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars, kRowsInSmem, kPtsInSmem, kMoreInSmem).bytes; }
 size_t tick_scratch_bytes(int A, int max_cars) {  // a slot per warp of the grid: at most A + arenas per block - 1
-    return (size_t)(A + TICK_MAX_ARENAS_PER_BLOCK) * smem_layout(max_cars, kRowsInSmem, kPtsInSmem).g_bytes;
+    return (size_t)(A + TICK_MAX_ARENAS_PER_BLOCK) * smem_layout(max_cars, kRowsInSmem, kPtsInSmem, kMoreInSmem).g_bytes;
 }
 
 // The EPA work-slot pool of the current device, made once per device for the process.
@@ -187,9 +191,25 @@ cudaError_t ensure_epa_pool() {
     return cudaSuccess;
 }
 
+// Per device: the tick kernel's shared-memory limit raised once, and the blocks an SM holds for each
+// (arenas per block, shared memory) a persistent launch asks about.
+struct TickLaunchCache {
+    std::mutex mu;
+    std::map<int, bool> smem_set;
+    std::map<std::tuple<int, int, int>, int> resident;
+};
+TickLaunchCache& tick_launch_cache() {
+    static TickLaunchCache c;
+    return c;
+}
+
 cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls, int ticks, const TickShape& shape,
                         cudaStream_t st) {
     if (b.A <= 0 || ticks <= 0) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    TickLaunchCache& tc = tick_launch_cache();
     int wpb = shape.arenas_per_block;
     if (wpb <= 0 || wpb > TICK_MAX_ARENAS_PER_BLOCK) wpb = TICK_MAX_ARENAS_PER_BLOCK;
     // the block must fit in shared memory
@@ -205,7 +225,6 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
     const int hdr_cache = shape.header_cache < 0 ? ((fits && blocks_with >= blocks_without) ? 1 : 0)
                                                  : ((fits && shape.header_cache) ? 1 : 0);
     if (hdr_cache) smem += hdr_bytes;
-    cudaError_t e = cudaSuccess;
     BatchView v = make_view(b);
     v.lanes_per_car = (shape.lanes_per_car == 1 || shape.lanes_per_car == 2) ? shape.lanes_per_car : 4;
     if (!shape.leaf_grid) {
@@ -213,18 +232,34 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
         v.mesh.lg_over = nullptr;
     }
     smem += 16;  // the next group's number (persistent launches)
-    e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lock(tc.mu);
+        if (!tc.smem_set[dev]) {
+            e = cudaFuncSetAttribute(rsg_tick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            if (e != cudaSuccess) return e;
+            tc.smem_set[dev] = true;
+        }
+    }
     const int ngroups = (b.A + wpb - 1) / wpb;
     int grid = ngroups;
     uint32_t* group_next = nullptr;
     if (shape.persistent && b.group_next) {
-        int dev = 0, nsm = 0, per_sm = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsg_tick_kernel, 32 * wpb, smem)) != cudaSuccess)
-            return e;
-        const int resident = nsm * (per_sm > 0 ? per_sm : 1);
+        int resident = 0;
+        {
+            std::lock_guard<std::mutex> lock(tc.mu);
+            auto it = tc.resident.find(std::make_tuple(dev, wpb, smem));
+            if (it != tc.resident.end()) resident = it->second;
+        }
+        if (resident == 0) {
+            int nsm = 0, per_sm = 0;
+            if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsg_tick_kernel, 32 * wpb, smem)) !=
+                cudaSuccess)
+                return e;
+            resident = nsm * (per_sm > 0 ? per_sm : 1);
+            std::lock_guard<std::mutex> lock(tc.mu);
+            tc.resident[std::make_tuple(dev, wpb, smem)] = resident;
+        }
         if (resident < ngroups) {
             grid = resident;
             group_next = b.group_next;

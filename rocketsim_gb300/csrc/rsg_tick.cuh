@@ -227,8 +227,9 @@ struct Row;
 struct SBody;
 
 // One arena's working state during a launch.  It lives in shared memory (one
-// region per warp); the arrays are carved out of the same region with sizes
-// from arena_caps(MC).
+// region per warp); the arrays are carved out of the same region, or (the parts
+// the tick kernel's layout keeps out of shared memory) out of the warp's global
+// scratch, with sizes from arena_caps(MC).
 struct Ctx {
     DevEvent* ev;         // this arena's event slots
     uint32_t event_mask;  // bit k set: record events of kind k
@@ -4615,17 +4616,26 @@ RSG_D void store_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
 struct SmemLayout {
     int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, qbox,
         hdr_list, hdr_n, bytes;
-    int g_pts, g_rows, g_bytes;  // parts kept in a per-warp global scratch instead (offsets there, -1: in shared)
+    int g_pts, g_rows, g_sb, g_cand, g_bytes;  // parts kept in a per-warp global scratch (offsets, -1: in shared)
     ArenaCaps caps;
 };
 RSG_HD int align16(int x) { return (x + 15) & ~15; }
 // The manifold points and the solver rows live only within a tick's collision work; either can be
 // kept in a global scratch of the warp (L1-cached) instead of shared memory.
-RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem = true) {
+RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem = true, bool more_in_smem = true) {
     SmemLayout L;
     L.caps = arena_caps(mc);
-    L.g_pts = L.g_rows = -1;
+    L.g_pts = L.g_rows = L.g_sb = L.g_cand = -1;
     L.g_bytes = 0;
+    const int cand_words = MESH_SEG * (mc + 1) > 4 * L.caps.pairs + MAX_DYN + L.caps.rows
+                               ? MESH_SEG * (mc + 1)
+                               : 4 * L.caps.pairs + MAX_DYN + L.caps.rows;
+    if (!more_in_smem) {
+        L.g_sb = L.g_bytes;
+        L.g_bytes = align16(L.g_bytes + (int)sizeof(SBody) * (MAX_DYN + 1));
+        L.g_cand = L.g_bytes;
+        L.g_bytes = align16(L.g_bytes + 4 * cand_words);
+    }
     if (!pts_in_smem) {
         L.g_pts = L.g_bytes;
         L.g_bytes = align16(L.g_bytes + (int)sizeof(MPoint) * L.caps.points);
@@ -4645,7 +4655,11 @@ RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem
     } else {
         L.pts = -1;
     }
-    L.sb = o;     o = align16(o + (int)sizeof(SBody) * (MAX_DYN + 1));
+    if (more_in_smem) {
+        L.sb = o; o = align16(o + (int)sizeof(SBody) * (MAX_DYN + 1));
+    } else {
+        L.sb = -1;
+    }
     if (rows_in_smem) {
         L.rows_c = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
         L.rows_f = o; o = align16(o + (int)sizeof(Row) * L.caps.rows);
@@ -4655,9 +4669,11 @@ RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem
     L.pkind = o;  o = align16(o + L.caps.pairs);
     L.flat_off = o; o = align16(o + 2 * L.caps.pairs);
     L.flat_n = o; o = align16(o + 2 * L.caps.pairs);
-    {  // candidate triangles; reused by the island / solver lists after the narrow phase
-        int words = MESH_SEG * (mc + 1), tail = 4 * L.caps.pairs + MAX_DYN + L.caps.rows;
-        L.cand_tri = o; o = align16(o + 4 * (words > tail ? words : tail));
+    // candidate triangles; reused by the island / solver lists after the narrow phase
+    if (more_in_smem) {
+        L.cand_tri = o; o = align16(o + 4 * cand_words);
+    } else {
+        L.cand_tri = -1;
     }
     L.cand_n = o; o = align16(o + 2 * (mc + 1));
     L.cand_res = o; o = align16(o + (int)sizeof(CandRes) * 32);
@@ -4678,13 +4694,13 @@ RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane, unsigned
     a.pair1 = reinterpret_cast<int8_t*>(base + L.pair1);
     a.man = reinterpret_cast<Manifold*>(base + L.man);
     a.pts = reinterpret_cast<MPoint*>(L.pts >= 0 ? base + L.pts : gscr + L.g_pts);
-    a.sb = reinterpret_cast<SBody*>(base + L.sb);
+    a.sb = reinterpret_cast<SBody*>(L.sb >= 0 ? base + L.sb : gscr + L.g_sb);
     a.rows_c = reinterpret_cast<Row*>(L.rows_c >= 0 ? base + L.rows_c : gscr + L.g_rows);
     a.rows_f = L.rows_c >= 0 ? reinterpret_cast<Row*>(base + L.rows_f) : a.rows_c + L.caps.rows;
     a.pkind = reinterpret_cast<int8_t*>(base + L.pkind);
     a.flat_off = reinterpret_cast<int16_t*>(base + L.flat_off);
     a.flat_n = reinterpret_cast<int16_t*>(base + L.flat_n);
-    a.cand_tri = reinterpret_cast<int*>(base + L.cand_tri);
+    a.cand_tri = reinterpret_cast<int*>(L.cand_tri >= 0 ? base + L.cand_tri : gscr + L.g_cand);
     a.cand_n = reinterpret_cast<int16_t*>(base + L.cand_n);
     a.cand_res = reinterpret_cast<CandRes*>(base + L.cand_res);
     a.qbox = reinterpret_cast<uint16_t*>(base + L.qbox);

@@ -189,6 +189,8 @@ def test_state_round_trip_and_ids():
 
 
 def test_async_device_controls_match_host_controls():
+    """Per-tick controls three ways give the same bytes: set before each one-tick step (the reference's
+    pattern), as a device array for an asynchronous step, and as a host array for rsg_step_controls."""
     import torch
     scs = random_scenarios(6, base_seed=3000)
     b1, _ = setup_gpu(scs)
@@ -204,8 +206,17 @@ def test_async_device_controls_match_host_controls():
     b2.sync()
     s2 = b2.get_all_states()
     assert s1[0].tobytes() == s2[0].tobytes() and s1[1].tobytes() == s2[1].tobytes()
+    # host controls for every tick in one synchronous call (rsg_step_controls), with the goal and
+    # bump callbacks registered so that the ticks run in event-draining chunks
+    b3, _ = setup_gpu(scs)
+    b3.set_goal_score_callback(lambda arena, team: None)
+    b3.set_car_bump_callback(lambda arena, a, b, demo: None)
+    b3.step_controls(seq, 8)
+    s3 = b3.get_all_states()
+    assert all(x.tobytes() == y.tobytes() for x, y in zip(s1, s3))
     b1.close()
     b2.close()
+    b3.close()
 
 
 def test_goal_event_matches_restatement():
