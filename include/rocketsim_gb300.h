@@ -590,7 +590,9 @@ int rsg_ball_pred_device_buffers(rsg_ball_pred* tracker, const rsg_ball_state** 
 int rsg_ball_pred_device_flags(rsg_ball_pred* tracker, uint32_t* out);
 
 /* Device flags of every arena after the last step ([n_arenas] words).  Bits 0-7
- * are capacity overflows (the step also returns RSG_ERR_DEVICE); bit 8 marks a
+ * are errors (the step also returns RSG_ERR_DEVICE): bits 0-3 capacity
+ * overflows, bit 4 a non-finite state, bit 5 a tick launch wider than the
+ * batch's scratch (the arena was not stepped; the host never launches one); bit 8 marks a
  * box contact deeper than GJK resolves and bit 9 overlapping car boxes, two
  * contact kinds the restated narrow phase does not produce yet.  No counterpart
  * in the reference. */

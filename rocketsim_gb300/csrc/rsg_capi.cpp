@@ -366,7 +366,7 @@ int check_device_errors(rsg_batch* b) {
         uint32_t e = b->h_counts[a] & 0xffu;
         if (e) {
             char msg[160];
-            std::snprintf(msg, sizeof(msg), "arena %d reported device error flags 0x%x (capacity overflow)", a, e);
+            std::snprintf(msg, sizeof(msg), "arena %d reported device error flags 0x%x (capacity overflow or launch error)", a, e);
             return fail(RSG_ERR_DEVICE, msg);
         }
     }
@@ -525,13 +525,13 @@ namespace {
 // Block-shape tuner.  Every launch shape gives the same results, so the shapes can be timed on the
 // batch itself: a tuning launch saves the arena records, runs each candidate shape from the saved
 // state (launch, wait, time), restores the records and launches for real with the fastest.  The
-// candidates are searched one parameter at a time: barriers in the collision work, arenas per block
-// (16 to 4, as shared memory allows), threads per car in the vehicle update (1, 2, 4), the BVH subtree
-// headers in shared memory or read through L2, wheel rays on the leaf grid or walking the BVH, a
-// persistent launch.  It runs on the batch's first launch and again, from the default shape and with
-// a second look at the barriers and the arenas per block, on the first launch after RETUNE_TICKS
-// ticks, when the arenas have left the start of the game (cars landed, on walls, in contact: the
-// collision work that decides the best shape has grown).  The choice of each round is cached per
+// candidates are searched one parameter at a time: barriers in the collision work (not in the first
+// round), arenas per block (16 to 4, as shared memory allows), threads per car in the vehicle update
+// (1, 2, 4), the BVH subtree headers in shared memory or read through L2, wheel rays on the leaf grid
+// or walking the BVH, a persistent launch.  It runs on the batch's first launch and again, from the
+// default shape and with a second look at the barriers and the arenas per block, on the first launch
+// after RETUNE_TICKS ticks, when the arenas have left the start of the game (cars landed, on walls, in
+// contact: the collision work that decides the best shape has grown).  The choice of each round is cached per
 // (device, arenas, car slots, game mode).
 constexpr uint64_t RETUNE_TICKS = 1024;
 struct TuneKey {
@@ -639,8 +639,9 @@ cudaError_t run_tuner(rsg_batch* b, const rsg_car_controls* controls, int ticks)
             return cudaSuccess;
         };
         // one parameter at a time from the best shape so far; the collision barriers first (at a
-        // game's steady state they change the cost of everything else)
-        if ((e = toggle_sync()) != cudaSuccess) break;
+        // game's steady state they change the cost of everything else).  The first round keeps them:
+        // at a batch's first launch the arenas have barely any collision work to measure them on.
+        if (round > 0 && (e = toggle_sync()) != cudaSuccess) break;
         if ((e = widths()) != cudaSuccess) break;
         const TickShape base = best;
         for (int l : {1, 2, 4}) {
@@ -844,7 +845,12 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
     ok = ok && alloc((void**)&B.place, sizeof(uint32_t) * A);
     ok = ok && alloc((void**)&B.cost, sizeof(uint32_t) * A);
     ok = ok && alloc((void**)&B.group_next, sizeof(uint32_t));
-    if (const size_t ts = tick_scratch_bytes((int)A, (int)MC)) ok = ok && alloc((void**)&B.tick_scratch, ts);
+    {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess) sms = 0;
+        B.scratch_slots = tick_scratch_slots((int)A, sms);
+        if (const size_t ts = tick_scratch_bytes(B.scratch_slots, (int)MC)) ok = ok && alloc((void**)&B.tick_scratch, ts);
+    }
     if (!ok) {
         rsg_batch_destroy(b);
         return nullptr;

@@ -53,6 +53,12 @@ __global__ void __launch_bounds__(32 * TICK_MAX_ARENAS_PER_BLOCK, 1) rsg_tick_ke
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
     const int ngroups = (bv.A + wpb - 1) / wpb;
+    if ((long long)(blockIdx.x + 1) * wpb > bv.scratch_slots) {  // launch_tick keeps the grid within the slots
+        for (int g = blockIdx.x; g < ngroups; g += gridDim.x)
+            if (threadIdx.x < wpb && g * wpb + (int)threadIdx.x < bv.A)
+                atomicOr(&bv.au[(size_t)AU_ERR * bv.A + place[g * wpb + threadIdx.x]], (uint32_t)ERR_LAUNCH);
+        return;
+    }
     const SmemLayout L = smem_layout(bv.MC, kRowsInSmem, kPtsInSmem, kMoreInSmem);
     unsigned char* const gscr = bv.tick_scratch + ((size_t)blockIdx.x * wpb + warp) * L.g_bytes;
     // the BVH subtree headers, read by every narrow-phase query, copied once into the block's
@@ -163,8 +169,13 @@ cudaError_t launch_place_arenas(const BatchBuffers& b, cudaStream_t st) {
 }
 
 int tick_smem_per_arena(int max_cars) { return smem_layout(max_cars, kRowsInSmem, kPtsInSmem, kMoreInSmem).bytes; }
-size_t tick_scratch_bytes(int A, int max_cars) {  // a slot per warp of the grid: at most A + arenas per block - 1
-    return (size_t)(A + TICK_MAX_ARENAS_PER_BLOCK) * smem_layout(max_cars, kRowsInSmem, kPtsInSmem, kMoreInSmem).g_bytes;
+int tick_scratch_slots(int A, int sms) {
+    const long long per_grid = (long long)A + TICK_MAX_ARENAS_PER_BLOCK;  // ngroups * arenas per block < A + that
+    const long long cap = 2LL * (sms > 0 ? sms : 1) * TICK_MAX_ARENAS_PER_BLOCK;
+    return (int)(per_grid < cap ? per_grid : cap);
+}
+size_t tick_scratch_bytes(int slots, int max_cars) {
+    return (size_t)slots * smem_layout(max_cars, kRowsInSmem, kPtsInSmem, kMoreInSmem).g_bytes;
 }
 
 // The EPA work-slot pool of the current device, made once per device for the process.
@@ -243,7 +254,8 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
     const int ngroups = (b.A + wpb - 1) / wpb;
     int grid = ngroups;
     uint32_t* group_next = nullptr;
-    if (shape.persistent && b.group_next) {
+    // a grid wider than the scratch's slots runs as a persistent launch of resident blocks
+    if ((shape.persistent || (long long)ngroups * wpb > b.scratch_slots) && b.group_next) {
         int resident = 0;
         {
             std::lock_guard<std::mutex> lock(tc.mu);

@@ -43,6 +43,7 @@ struct BatchBuffers {
     uint32_t* cost;   // [A] cycles each arena's own collision work took in the last tick launch
     uint32_t* group_next;  // [1] groups taken so far by the blocks of a persistent tick launch
     unsigned char* tick_scratch;  // tick_scratch_bytes: per warp slot, the working set kept out of shared memory
+    int scratch_slots;            // warp slots in tick_scratch: a launch's grid * arenas per block stays within
 };
 
 constexpr int DEV_EVENT_BYTES = 24;
@@ -75,8 +76,11 @@ cudaError_t launch_tick(const BatchBuffers& b, const rsg_car_controls* controls,
 cudaError_t launch_place_arenas(const BatchBuffers& b, cudaStream_t st);
 // Shared memory one arena needs in the tick kernel.
 int tick_smem_per_arena(int max_cars);
-// Bytes of the tick kernel's global scratch (a working-set slot per warp of its grid).
-size_t tick_scratch_bytes(int A, int max_cars);
+// Warp slots of the tick kernel's global scratch for a batch of A arenas on a GPU of `sms` SMs: a slot
+// per warp of a grid of a block per arena group, at most 2 slots per warp an SM holds (larger batches
+// run persistent launches of resident blocks), and the scratch's bytes.
+int tick_scratch_slots(int A, int sms);
+size_t tick_scratch_bytes(int slots, int max_cars);
 
 // Allocates the current device's pool of EPA work slots (once per device; about 14 MB).
 cudaError_t ensure_epa_pool();

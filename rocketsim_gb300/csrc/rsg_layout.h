@@ -125,6 +125,7 @@ enum DeviceError : uint32_t {
     ERR_PAIR_OVERFLOW = 1u << 2,
     ERR_EVENT_OVERFLOW = 1u << 3,
     ERR_NAN = 1u << 4,
+    ERR_LAUNCH = 1u << 5,  // the tick kernel's grid exceeded its scratch slots; the arena was not stepped
     // not errors: contacts that the restated narrow phase does not produce yet
     WARN_EPA_SKIPPED = 1u << 8,     // box-triangle / box-sphere penetration deeper than GJK resolves
     WARN_CARCAR_SKIPPED = 1u << 9,  // overlapping car boxes (box-box detector)

@@ -117,6 +117,7 @@ struct BatchView {
     DevMesh mesh;
     DevGrid grid;
     unsigned char* tick_scratch;  // per warp slot: the working-set parts the tick kernel keeps out of shared memory
+    int scratch_slots;            // warp slots in tick_scratch
 };
 
 constexpr int OBJ_MESH = 0, OBJ_PLANE0 = 1, OBJ_BALL = 5, OBJ_CAR0 = 6;

@@ -27,6 +27,7 @@ inline BatchView make_view(const BatchBuffers& b) {
     v.events = (DevEvent*)b.events;
     v.event_mask = b.event_mask;
     v.tick_scratch = b.tick_scratch;
+    v.scratch_slots = b.scratch_slots;
     v.mesh.tv = b.mesh.tv;
     v.mesh.nodes = b.mesh.nodes;
     v.mesh.sub = b.mesh.sub;

@@ -172,6 +172,25 @@ def test_full_size_batch_is_deterministic_and_independent(full_size_runs, persis
     assert cars.tobytes() == c0.tobytes() and balls.tobytes() == b0.tobytes() and pads.tobytes() == p0.tobytes()
 
 
+def test_batch_wider_than_the_scratch_runs_persistent(monkeypatch):
+    """8192 arenas in blocks of 16 need more warp slots than the tick scratch holds (two per warp an
+    SM holds), so even a launch shape without the persistent launch runs as one: the same bytes as the
+    persistent shape, and no arena flagged as not stepped."""
+    base = random_scenarios(8, base_seed=2100)
+    scs = [base[k % 8] for k in range(8192)]
+    out = []
+    for persistent in (0, 1):
+        monkeypatch.setenv("RSG_TICK_SHAPE", f"16,4,-1,1,1,{persistent}")
+        batch, _ = setup_gpu(scs)
+        for t in range(8):
+            batch.set_controls_all(gpu_controls(scs, t, batch.max_cars))
+            batch.step(1)
+        assert not (batch.device_flags() & 0xff).any()
+        out.append(tuple(x.tobytes() for x in batch.get_all_states()))
+        batch.close()
+    assert out[0] == out[1]
+
+
 def test_state_round_trip_and_ids():
     """Get after Set returns what the reference returns: the state converted to Bullet
     units and back (pos * (1/50) * 50 is not the identity in float), other fields as set."""
