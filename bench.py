@@ -1030,9 +1030,9 @@ def main():
         line["config0_one_arena"] = {
             "metric": "2v2 ticks/s of one arena", "value": c0["value"], "unit": "ticks/s",
             "workload": "1 arena x (4 Octane + ball), procedural soccar mesh, the same input process; "
-                        f"{args.c0_steps} timed launches of 120 ticks after 240 + 360 ticks (a bounded sample of "
-                        "the 1M-tick run)",
-            "ms_per_launch": c0["ms_per_step"], "cpu_single_thread": single}
+                        f"{args.c0_steps} timed launches of 120 ticks after {args.settle_ticks} + 360 ticks (a bounded "
+                        "sample of the 1M-tick run)",
+            "ms_per_launch": c0["ms_per_step"], "cpu_single_thread": single, "tick_shape": c0["tick_shape"]}
     if "c2" in legs:
         c2 = run_config2(args, dev)
         line["config2_uneven"] = {
