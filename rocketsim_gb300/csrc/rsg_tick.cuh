@@ -281,6 +281,8 @@ struct Ctx {
     int solve_nb, solve_nc, solve_nsp;
     int* solve_bodies;
     int* solve_plan;
+    int16_t* solve_perm;  // rows by solver-body component: contact rows, friction rows, their two start lists
+    int solve_ncomp;
     int8_t sb_of[MAX_CARS + 1];
     int8_t solve_special[MAX_CARS + 1];
 
@@ -3051,8 +3053,8 @@ RSG_D bool solve_split(Ctx& a, Row& c) {
 // The solver (btSequentialImpulseConstraintSolver::solveGroup) in three parts: solve_plan (lane 0)
 // fixes the solver bodies and the contact rows in Bullet's order and adds up RocketSim's special
 // contacts per body; solve_setup_warp sets the rows up on the warp's lanes (each row reads only its
-// contact point and the solver bodies' start state); solve_iterate (lane 0) runs the iterations and
-// writes the bodies back.  `bodies` are dynamic object ids in island order, `mans` manifold indices in
+// contact point and the solver bodies' start state); solve_iterate_warp runs the iterations, a lane
+// per component of solver bodies joined by rows, and writes the bodies back.  `bodies` are dynamic object ids in island order, `mans` manifold indices in
 // sorted island order, `plan` room for one word per row.
 RSG_DN void solve_plan(Ctx& a, const int* bodies, int nb, const int* mans, int nm, int* plan) {
     int nc = 0;
@@ -3157,27 +3159,81 @@ RSG_D void solve_setup_warp(Ctx& a, int lane, float dt) {
     }
 }
 
-RSG_DN void solve_iterate(Ctx& a, float dt) {
+// Solver bodies joined by a row form a component; rows of different components touch different bodies
+// (the fixed body takes no impulse), so each component's rows can run on their own lane, in their order,
+// and every body sees the same operations as in the reference's single pass over all rows.  Lane 0
+// lists the rows by component (a stable counting sort: contact rows, then friction rows).
+RSG_DN void solve_components(Ctx& a) {
     const int nb = a.solve_nb, nc = a.solve_nc + a.solve_nsp, nf = nc;
+    int par[MAX_DYN + 1], cid[MAX_DYN + 1];
+    for (int i = 0; i <= MAX_DYN; i++) { par[i] = i; cid[i] = -1; }
+    auto find = [&](int x) {
+        while (par[x] != x) x = par[x];
+        return x;
+    };
+    for (int k = 0; k < nc; k++) {
+        const Row& r = a.rows_c[k];
+        if (r.ba != SB_FIXED && r.bb != SB_FIXED) {
+            const int x = find(r.ba), y = find(r.bb);
+            if (x != y) par[x > y ? x : y] = x < y ? x : y;
+        }
+    }
+    int ncomp = 0;
+    auto comp = [&](const Row& r) {
+        const int root = find(r.ba != SB_FIXED ? r.ba : r.bb);
+        if (cid[root] < 0) cid[root] = ncomp++;
+        return cid[root];
+    };
+    int16_t* pc = a.solve_perm;
+    int16_t* pf = pc + a.cap_rows;
+    int16_t* sc = pf + a.cap_rows;
+    int16_t* sf = sc + (MAX_DYN + 2);
+    for (int i = 0; i < MAX_DYN + 2; i++) sc[i] = sf[i] = 0;
+    for (int k = 0; k < nc; k++) sc[comp(a.rows_c[k]) + 1]++;
+    for (int k = 0; k < nf; k++) sf[comp(a.rows_f[k]) + 1]++;
+    for (int i = 0; i < ncomp; i++) { sc[i + 1] += sc[i]; sf[i + 1] += sf[i]; }
+    int16_t fc[MAX_DYN + 1], ff[MAX_DYN + 1];
+    for (int i = 0; i < ncomp; i++) { fc[i] = sc[i]; ff[i] = sf[i]; }
+    for (int k = 0; k < nc; k++) pc[fc[comp(a.rows_c[k])]++] = (int16_t)k;
+    for (int k = 0; k < nf; k++) pf[ff[comp(a.rows_f[k])]++] = (int16_t)k;
+    a.solve_ncomp = ncomp;
+}
+
+// The split-impulse and the ten solver iterations with a lane per component (the split iterations'
+// stop test is one vote of the warp: whether any row's residual is positive), then the bodies written
+// back, a lane per body.
+RSG_D void solve_iterate_warp(Ctx& a, int lane, float dt) {
+    if (lane == 0) solve_components(a);
+    __syncwarp();
+    const int nb = a.solve_nb, ncomp = a.solve_ncomp;
+    const int16_t* pc = a.solve_perm;
+    const int16_t* pf = pc + a.cap_rows;
+    const int16_t* sc = pf + a.cap_rows;
+    const int16_t* sf = sc + (MAX_DYN + 2);
     const int ITER = 10;
+    const bool mine = lane < ncomp;
+    const int c0 = mine ? sc[lane] : 0, c1 = mine ? sc[lane + 1] : 0;
+    const int f0 = mine ? sf[lane] : 0, f1 = mine ? sf[lane + 1] : 0;
     for (int it = 0; it < ITER; it++) {
-        bool any = false;  // the largest squared residual is above 0
-        for (int k = 0; k < nc; k++) any |= solve_split(a, a.rows_c[k]);
-        if (!any || it >= ITER - 1) break;
+        bool any = false;
+        for (int j = c0; j < c1; j++) any |= solve_split(a, a.rows_c[pc[j]]);
+        if (!__any_sync(0xffffffffu, any) || it >= ITER - 1) break;
     }
     for (int it = 0; it < ITER; it++) {
-        for (int k = 0; k < nc; k++) {
-            if (a.rows_c[k].special) continue;
-            solve_row(a, a.rows_c[k], 0.f, 1e10f, true);
+        for (int j = c0; j < c1; j++) {
+            Row& r = a.rows_c[pc[j]];
+            if (r.special) continue;
+            solve_row(a, r, 0.f, 1e10f, true);
         }
-        for (int k = 0; k < nf; k++) {
-            Row& f = a.rows_f[k];
+        for (int j = f0; j < f1; j++) {
+            Row& f = a.rows_f[pf[j]];
             float total = a.rows_c[f.friction_index].applied;
             if (total > 0.f) solve_row(a, f, -(f.friction * total), f.friction * total, false);
         }
     }
+    __syncwarp();
     // writeBackBodies (btSequentialImpulseConstraintSolver.cpp:1878-1904)
-    for (int i = 0; i < nb; i++) {
+    for (int i = lane; i < nb; i += 32) {
         SBody& sb = a.sb[i];
         Body& b = a.body(sb.obj);
         sb.lv += sb.dlv;
@@ -3191,6 +3247,7 @@ RSG_DN void solve_iterate(Ctx& a, float dt) {
         b.ang_vel = sb.av + sb.ext_t;
         b.xf = sb.xf;
     }
+    __syncwarp();
 }
 
 // ---------------------------------------------------------------- world step
@@ -3871,7 +3928,7 @@ RSG_D void step_collide_block(const BatchView& bv, Ctx& a, int lane, bool active
     if (active && a.solve_nb > 0) solve_setup_warp(a, lane, bv.dt);
     __syncwarp();
     if (bsync) __syncthreads();
-    if (active && a.solve_nb > 0 && lane == 0) solve_iterate(a, bv.dt);
+    if (active && a.solve_nb > 0) solve_iterate_warp(a, lane, bv.dt);
     __syncwarp();
     RSG_PHASE(7);
 }
@@ -4617,7 +4674,8 @@ RSG_D void store_pads(const BatchView& bv, int ar, Ctx& a, int lane) {
 struct SmemLayout {
     int cars, pads, pair0, pair1, man, pts, sb, rows_c, rows_f, pkind, flat_off, flat_n, cand_tri, cand_n, cand_res, qbox,
         hdr_list, hdr_n, bytes;
-    int g_pts, g_rows, g_sb, g_cand, g_bytes;  // parts kept in a per-warp global scratch (offsets, -1: in shared)
+    int g_pts, g_rows, g_sb, g_cand, g_perm, g_bytes;  // parts in a per-warp global scratch (offsets, -1: shared)
+    int perm;
     ArenaCaps caps;
 };
 RSG_HD int align16(int x) { return (x + 15) & ~15; }
@@ -4626,7 +4684,8 @@ RSG_HD int align16(int x) { return (x + 15) & ~15; }
 RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem = true, bool more_in_smem = true) {
     SmemLayout L;
     L.caps = arena_caps(mc);
-    L.g_pts = L.g_rows = L.g_sb = L.g_cand = -1;
+    L.g_pts = L.g_rows = L.g_sb = L.g_cand = L.g_perm = -1;
+    const int perm_bytes = 2 * (2 * L.caps.rows + 2 * (MAX_DYN + 2));
     L.g_bytes = 0;
     const int cand_words = MESH_SEG * (mc + 1) > 4 * L.caps.pairs + MAX_DYN + L.caps.rows
                                ? MESH_SEG * (mc + 1)
@@ -4636,6 +4695,8 @@ RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem
         L.g_bytes = align16(L.g_bytes + (int)sizeof(SBody) * (MAX_DYN + 1));
         L.g_cand = L.g_bytes;
         L.g_bytes = align16(L.g_bytes + 4 * cand_words);
+        L.g_perm = L.g_bytes;
+        L.g_bytes = align16(L.g_bytes + perm_bytes);
     }
     if (!pts_in_smem) {
         L.g_pts = L.g_bytes;
@@ -4673,8 +4734,9 @@ RSG_HD SmemLayout smem_layout(int mc, bool rows_in_smem = true, bool pts_in_smem
     // candidate triangles; reused by the island / solver lists after the narrow phase
     if (more_in_smem) {
         L.cand_tri = o; o = align16(o + 4 * cand_words);
+        L.perm = o; o = align16(o + perm_bytes);
     } else {
-        L.cand_tri = -1;
+        L.cand_tri = L.perm = -1;
     }
     L.cand_n = o; o = align16(o + 2 * (mc + 1));
     L.cand_res = o; o = align16(o + (int)sizeof(CandRes) * 32);
@@ -4702,6 +4764,7 @@ RSG_D Ctx& bind_ctx(unsigned char* base, const SmemLayout& L, int lane, unsigned
     a.flat_off = reinterpret_cast<int16_t*>(base + L.flat_off);
     a.flat_n = reinterpret_cast<int16_t*>(base + L.flat_n);
     a.cand_tri = reinterpret_cast<int*>(L.cand_tri >= 0 ? base + L.cand_tri : gscr + L.g_cand);
+    a.solve_perm = reinterpret_cast<int16_t*>(L.perm >= 0 ? base + L.perm : gscr + L.g_perm);
     a.cand_n = reinterpret_cast<int16_t*>(base + L.cand_n);
     a.cand_res = reinterpret_cast<CandRes*>(base + L.cand_res);
     a.qbox = reinterpret_cast<uint16_t*>(base + L.qbox);
