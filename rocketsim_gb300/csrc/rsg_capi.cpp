@@ -816,10 +816,10 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
     B.mesh = mesh_ptrs(g_soccar);
     B.grid = default_grid();
     size_t A = n_arenas, MC = max_cars_per_arena;
-    auto alloc = [&](void** p, size_t bytes) -> bool {
+    auto alloc = [&](void** p, size_t bytes) -> bool {  // zeroed on the batch's stream, ahead of its kernels
         cudaError_t e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, bytes, b->stream);
         if (e != cudaSuccess) { cuda_fail(e, "cudaMalloc(batch)"); return false; }
-        cudaMemset(*p, 0, bytes);
         return true;
     };
     if (cudaError_t pe = ensure_epa_pool(); pe != cudaSuccess) {
@@ -836,8 +836,9 @@ rsg_batch* rsg_batch_create_ex(int game_mode, uint32_t n_arenas, uint32_t max_ca
     }
     bool ok = alloc((void**)&b->d_pads, sizeof(float4) * NUM_PADS);
     if (ok && !b->pads.empty())
-        ok = cudaMemcpy(b->d_pads, b->pads.data(), sizeof(float4) * b->pads.size(), cudaMemcpyHostToDevice) ==
-             cudaSuccess;
+        ok = cudaMemcpyAsync(b->d_pads, b->pads.data(), sizeof(float4) * b->pads.size(), cudaMemcpyHostToDevice,
+                             b->stream) == cudaSuccess &&
+             cudaStreamSynchronize(b->stream) == cudaSuccess;  // after the buffer's zeroing, on the same stream
     B.pad_cfg = b->d_pads;
     ok = ok && alloc((void**)&B.rec, sizeof(uint32_t) * (size_t)rec_words((int)MC) * A);
     ok = ok && alloc((void**)&B.au, sizeof(uint32_t) * AU_COUNT * A);
@@ -2095,6 +2096,7 @@ rsg_game_event_tracker* rsg_game_event_tracker_create(rsg_batch* b, const rsg_ga
     alloc((void**)&t->d.scored_last, 4 * A);
     alloc((void**)&t->d.last_update, 8 * A);
     alloc((void**)&t->d_ev, sizeof(rsg_game_event) * A);
+    if (ok && cudaDeviceSynchronize() != cudaSuccess) ok = false;  // the zeroing done before any stream uses them
     if (ok && cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) ok = false;
     if (ok && cudaEventCreateWithFlags(&t->src_done, cudaEventDisableTiming) != cudaSuccess) ok = false;
     if (!ok) {
@@ -2229,6 +2231,7 @@ rsg_ball_pred* rsg_ball_pred_create(rsg_batch* src, uint32_t num_pred_ticks) {
     alloc((void**)&p->d.steps, sizeof(int) * A);
     alloc((void**)&p->d.base, sizeof(uint32_t) * A);
     alloc(&p->d_in, in_bytes((int)A));
+    if (ok && cudaDeviceSynchronize() != cudaSuccess) ok = false;  // the zeroing done before any stream uses them
     if (ok && cudaEventCreateWithFlags(&p->src_done, cudaEventDisableTiming) != cudaSuccess) {
         fail(RSG_ERR_CUDA, "cudaEventCreate");
         ok = false;

@@ -88,8 +88,10 @@ __global__ void __launch_bounds__(32 * TICK_MAX_ARENAS_PER_BLOCK, 1) rsg_tick_ke
         __syncwarp();
         if (lane < a.ncars) load_car(bv, ar, a, lane);
         load_pads(bv, ar, a, lane);
-        __syncwarp();
     }
+    // every warp's arena loaded (and its working-set pointers bound) before any thread of the block
+    // touches another warp's arena (the controls below, the block-wide parts of the tick)
+    __syncthreads();
     int nact = bv.A - slot0;
     nact = nact < wpb ? nact : wpb;
     const BlockArenas B{smem, L.bytes, nact};

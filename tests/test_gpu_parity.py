@@ -238,6 +238,43 @@ def test_async_device_controls_match_host_controls():
     b3.close()
 
 
+def _device_controls_run(scs, ticks, first_launch):
+    """Steps `scs` with device-resident per-tick controls: one launch of `first_launch` ticks, then
+    one-tick launches; returns the bytes of every state."""
+    import torch
+    b, _ = setup_gpu(scs)
+    mc = b.max_cars
+    n = len(scs) * mc * CONTROLS_DTYPE.itemsize
+    seq = np.concatenate([gpu_controls(scs, t, mc) for t in range(ticks)])
+    dev = torch.from_numpy(seq.view(np.uint8).copy()).cuda()
+    torch.cuda.synchronize()
+    b.step_async(dev.data_ptr(), first_launch)
+    b.sync()
+    for t in range(first_launch, ticks):
+        b.step_async(dev[t * n:].data_ptr(), 1)
+        b.sync()
+    out = b"".join(x.tobytes() for x in b.get_all_states())
+    b.close()
+    return out
+
+
+def test_device_controls_are_deterministic():
+    """Device-resident controls are applied by the block's threads to every arena of the block, after
+    every warp has loaded its arena: the same batch gives the same bytes on every run (40 arenas in
+    three blocks, an 8-tick launch then one-tick launches), and a batch stepped while another batch
+    exists gives the same bytes as alone."""
+    scs = random_scenarios(40, base_seed=2000)
+    runs = {_device_controls_run(scs, 24, 8) for _ in range(3)}
+    assert len(runs) == 1
+    small = random_scenarios(6, base_seed=3001)
+    alone = _device_controls_run(small, 8, 8)
+    other, _ = setup_gpu(random_scenarios(6, base_seed=3000))
+    try:
+        assert _device_controls_run(small, 8, 8) == alone
+    finally:
+        other.close()
+
+
 def test_goal_event_matches_restatement():
     from rocketsim_gb300 import abi
     sc = make_scenario(11, ncars=2, air_frac=0.0)
