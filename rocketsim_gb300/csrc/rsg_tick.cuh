@@ -3746,8 +3746,9 @@ RSG_DN void step_collide_tail(const BatchView& bv, Ctx& a);
 
 // The first part of a world step's collision work on one arena's warp: the pair list, the BVH
 // subtree headers and candidate triangles of each mesh pair, and the flattened candidate list.  Every
-// warp of the block calls it, `active` or not (with `bsync` they meet at barriers between the parts).
-RSG_DN void step_collide_gather(const BatchView& bv, Ctx& a, int lane, bool active, bool bsync) {
+// warp of the block calls it, `active` or not; its parts are warp-local (block barriers between them
+// measured 1-2 % slower).
+RSG_DN void step_collide_gather(const BatchView& bv, Ctx& a, int lane, bool active) {
 #if defined(RSG_PHASE_TIMERS)
     long long rsg_w_ = clock64();
 #define RSG_W(i) do { if (lane == 0) { long long t_ = clock64(); atomicAdd(&g_phase_cycles[i], (unsigned long long)(t_ - rsg_w_)); rsg_w_ = t_; } } while (0)
@@ -3764,7 +3765,6 @@ RSG_DN void step_collide_gather(const BatchView& bv, Ctx& a, int lane, bool acti
     }
     __syncwarp();
     RSG_W(22);
-    if (bsync) __syncthreads();
     // quantized query box of each mesh pair (one lane per pair)
     unsigned qmask = 0;
     for (int p = lane; active && p < a.npairs; p += 32) {
@@ -3785,7 +3785,6 @@ RSG_DN void step_collide_gather(const BatchView& bv, Ctx& a, int lane, bool acti
     qmask = __reduce_or_sync(0xffffffffu, qmask);
     __syncwarp();
     RSG_W(23);
-    if (bsync) __syncthreads();
     // subtree headers against every query box, 32 headers at a time; each query keeps the
     // overlapping headers in header order.  A run of 32 headers is scanned only for the queries
     // that overlap the box around the whole run.
@@ -3834,7 +3833,6 @@ RSG_DN void step_collide_gather(const BatchView& bv, Ctx& a, int lane, bool acti
     }
     __syncwarp();
     RSG_W(24);
-    if (bsync) __syncthreads();
     // candidate triangles of each mesh pair, one lane per pair, in BVH order
     for (int p = lane; active && p < a.npairs; p += 32) {
         int k = a.pkind[p];
@@ -3880,7 +3878,7 @@ RSG_D void step_collide_block(const BatchView& bv, Ctx& a, int lane, bool active
 #if defined(RSG_PHASE_TIMERS)
     long long rsg_w_ = clock64();
 #endif
-    step_collide_gather(bv, a, lane, active, bsync);
+    step_collide_gather(bv, a, lane, active);
     RSG_PHASE(4);
     if (bsync) __syncthreads();
     uint32_t warn = 0;
